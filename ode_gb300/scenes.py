@@ -1,0 +1,280 @@
+"""Seeded synthetic scenes for the rigid-body step.
+
+Headless restatements of the scene recipes the reference's demos use
+(ode/demo/demo_boxstack.cpp:130-170 for the near callback and stack,
+ode/demo/demo_crash.cpp:119-150 for a wall of boxes), sized to the two
+single-world workloads this package measures:
+
+* ``box_stack``   -- 10 unit boxes (1 m, density 1) stacked on the plane z=0,
+  x/y jitter U(+-0.01 m), yaw U(+-5 deg); gravity -9.81, dt 0.01, 20 SOR
+  iterations, W 1.3, mu 0.5, dContactApprox1, <= 4 contacts per pair,
+  ERP 0.2, CFM 1e-5.
+* ``pile``        -- N bodies (default 32,768) dropped into an open box made of
+  5 static planes: 50 % spheres r~U[0.05,0.25] m, 50 % boxes sides
+  ~U[0.1,0.5] m, density ~U[500,2000] kg/m^3, on a jittered 3-D grid with
+  random unit quaternions; dt 1/120, 30 iterations, mu 0.6.
+
+Every array is float32 / int32 so that the same bytes feed the reference,
+the CPU restatement and the GPU path.
+
+Layouts (shared with tests/golden/gen_golden.cpp):
+  bodies  float32 [nb, 20]: pos(3) q(4, w first) lvel(3) avel(3) mass(1)
+                            I11 I22 I33 I12 I13 I23 (body frame, about the COM)
+  geoms   cls int32 [ng]  (0 sphere, 1 box, 2 capsule, 4 plane: ODE class ids)
+          body int32 [ng] (-1 = static geom)
+          pos float32 [ng,3], R float32 [ng,12] (3x4 row-major, only for static
+          geoms), dims float32 [ng,4] (sphere r | box lx ly lz | capsule r len |
+          plane a b c d)
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+SPHERE, BOX, CAPSULE, PLANE = 0, 1, 2, 4
+
+# dSurfaceParameters.mode bits (include/ode/contact.h:28-52)
+dContactMu2 = 0x001
+dContactAxisDep = 0x001
+dContactFDir1 = 0x002
+dContactBounce = 0x004
+dContactSoftERP = 0x008
+dContactSoftCFM = 0x010
+dContactMotion1 = 0x020
+dContactMotion2 = 0x040
+dContactMotionN = 0x080
+dContactSlip1 = 0x100
+dContactSlip2 = 0x200
+dContactRolling = 0x400
+dContactApprox1_1 = 0x1000
+dContactApprox1_2 = 0x2000
+dContactApprox1_N = 0x4000
+dContactApprox1 = 0x7000
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    bodies: np.ndarray          # float32 [nb, 20]
+    geom_cls: np.ndarray        # int32 [ng]
+    geom_body: np.ndarray       # int32 [ng]
+    geom_pos: np.ndarray        # float32 [ng, 3]
+    geom_R: np.ndarray          # float32 [ng, 12]
+    geom_dims: np.ndarray       # float32 [ng, 4]
+    dt: float = 0.01
+    gravity: tuple = (0.0, 0.0, -9.81)
+    erp: float = 0.2
+    cfm: float = 1e-5
+    w: float = 1.3
+    iterations: int = 20
+    max_vel: float = float("inf")
+    min_depth: float = 0.0
+    mu: float = 0.5
+    mu2: float = 0.0
+    bounce: float = 0.0
+    bounce_vel: float = 0.0
+    soft_erp: float = 0.0
+    soft_cfm: float = 0.0
+    surface_mode: int = dContactApprox1
+    maxc: int = 4
+    hash_levels: tuple = (-3, 10)
+
+    @property
+    def nb(self) -> int:
+        return int(self.bodies.shape[0])
+
+    @property
+    def ng(self) -> int:
+        return int(self.geom_cls.shape[0])
+
+    def world_params(self) -> np.ndarray:
+        """dt, g(3), erp, cfm, w, max_vel, min_depth as float32[9]."""
+        return np.array([self.dt, *self.gravity, self.erp, self.cfm, self.w,
+                         self.max_vel, self.min_depth], dtype=np.float32)
+
+    def surface(self) -> np.ndarray:
+        """mu, mu2, bounce, bounce_vel, soft_erp, soft_cfm, 0, 0 as float32[8]."""
+        return np.array([self.mu, self.mu2, self.bounce, self.bounce_vel,
+                         self.soft_erp, self.soft_cfm, 0, 0], dtype=np.float32)
+
+
+def quat_to_R(q: np.ndarray) -> np.ndarray:
+    """Rotation matrix (3x4 row-major, float32) from unit quaternions [...,4]
+    (w,x,y,z), by the same formula as dRfromQ (ode/src/rotation.cpp:236-254),
+    evaluated in float32 term by term."""
+    q = np.asarray(q, dtype=np.float32)
+    two = np.float32(2)
+    one = np.float32(1)
+    q0, q1, q2, q3 = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    qq1 = two * q1 * q1
+    qq2 = two * q2 * q2
+    qq3 = two * q3 * q3
+    R = np.zeros(q.shape[:-1] + (12,), dtype=np.float32)
+    R[..., 0] = one - qq2 - qq3
+    R[..., 1] = two * (q1 * q2 - q0 * q3)
+    R[..., 2] = two * (q1 * q3 + q0 * q2)
+    R[..., 4] = two * (q1 * q2 + q0 * q3)
+    R[..., 5] = one - qq1 - qq3
+    R[..., 6] = two * (q2 * q3 - q0 * q1)
+    R[..., 8] = two * (q1 * q3 - q0 * q2)
+    R[..., 9] = two * (q2 * q3 + q0 * q1)
+    R[..., 10] = one - qq1 - qq2
+    return R
+
+
+def random_quats(rng: np.random.Generator, n: int) -> np.ndarray:
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.astype(np.float32)
+
+
+def mass_box(density, lx, ly, lz):
+    """dMassSetBox (ode/src/mass.cpp:182-196): mass and body-frame inertia."""
+    density = np.float32(density)
+    lx, ly, lz = np.float32(lx), np.float32(ly), np.float32(lz)
+    m = lx * ly * lz * density
+    k = m / np.float32(12.0)
+    return m, k * (ly * ly + lz * lz), k * (lx * lx + lz * lz), k * (lx * lx + ly * ly)
+
+
+def mass_sphere(density, r):
+    """dMassSetSphere (ode/src/mass.cpp:118-130)."""
+    r = np.float32(r)
+    m = np.float32(4.0) / np.float32(3.0) * np.float32(math.pi) * r * r * r * np.float32(density)
+    ii = np.float32(0.4) * m * r * r
+    return m, ii, ii, ii
+
+
+def _body_rows(pos, q, mass, I3):
+    n = pos.shape[0]
+    b = np.zeros((n, 20), dtype=np.float32)
+    b[:, 0:3] = pos
+    b[:, 3:7] = q
+    b[:, 13] = mass
+    b[:, 14:17] = I3
+    return b
+
+
+def box_stack(seed: int = 0, n: int = 10) -> Scene:
+    rng = np.random.default_rng(seed)
+    pos = np.zeros((n, 3), dtype=np.float32)
+    pos[:, 0:2] = rng.uniform(-0.01, 0.01, size=(n, 2))
+    pos[:, 2] = 0.5 + np.arange(n, dtype=np.float32)
+    yaw = np.deg2rad(rng.uniform(-5.0, 5.0, size=n))
+    q = np.zeros((n, 4), dtype=np.float32)
+    q[:, 0] = np.cos(yaw / 2)
+    q[:, 3] = np.sin(yaw / 2)
+    m, i1, i2, i3 = mass_box(1.0, 1.0, 1.0, 1.0)
+    bodies = _body_rows(pos, q, m, np.array([i1, i2, i3], dtype=np.float32))
+    ng = n + 1
+    cls = np.full(ng, BOX, dtype=np.int32)
+    cls[-1] = PLANE
+    gbody = np.arange(ng, dtype=np.int32)
+    gbody[-1] = -1
+    gdims = np.zeros((ng, 4), dtype=np.float32)
+    gdims[:n, 0:3] = 1.0
+    gdims[-1] = (0, 0, 1, 0)
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene("box_stack", bodies, cls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
+                 dt=0.01, iterations=20, mu=0.5, maxc=4)
+
+
+def pile(n: int = 32768, seed: int = 1, spacing: float = 0.6, jitter: float = 0.05) -> Scene:
+    """Open-box pile: n bodies on a jittered grid of side ceil(cbrt(n)), walls
+    at x,y = 0 and x,y = L (L = side*spacing), floor z = 0."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(round(n ** (1.0 / 3.0), 6)))
+    L = side * spacing
+    idx = np.arange(n)
+    gx, gy, gz = idx % side, (idx // side) % side, idx // (side * side)
+    pos = np.stack([(gx + 0.5) * spacing, (gy + 0.5) * spacing, (gz + 0.5) * spacing + 0.3], axis=1)
+    pos = (pos + rng.uniform(-jitter, jitter, size=(n, 3))).astype(np.float32)
+    q = random_quats(rng, n)
+    is_sphere = rng.random(n) < 0.5
+    radius = rng.uniform(0.05, 0.25, size=n).astype(np.float32)
+    sides = rng.uniform(0.1, 0.5, size=(n, 3)).astype(np.float32)
+    density = rng.uniform(500.0, 2000.0, size=n).astype(np.float32)
+    mass = np.zeros(n, np.float32)
+    I3 = np.zeros((n, 3), np.float32)
+    for i in range(n):
+        if is_sphere[i]:
+            r = mass_sphere(density[i], radius[i])
+        else:
+            r = mass_box(density[i], *sides[i])
+        mass[i] = r[0]
+        I3[i] = r[1:]
+    bodies = _body_rows(pos, q, mass, I3)
+    ng = n + 5
+    cls = np.where(is_sphere, SPHERE, BOX).astype(np.int32)
+    cls = np.concatenate([cls, np.full(5, PLANE, np.int32)])
+    gbody = np.concatenate([np.arange(n, dtype=np.int32), np.full(5, -1, np.int32)])
+    gdims = np.zeros((ng, 4), dtype=np.float32)
+    gdims[:n, 0] = np.where(is_sphere, radius, sides[:, 0])
+    gdims[:n, 1] = np.where(is_sphere, 0, sides[:, 1])
+    gdims[:n, 2] = np.where(is_sphere, 0, sides[:, 2])
+    gdims[n:] = np.array([[0, 0, 1, 0], [1, 0, 0, 0], [-1, 0, 0, -L], [0, 1, 0, 0], [0, -1, 0, -L]],
+                         dtype=np.float32)
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene(f"pile{n}", bodies, cls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
+                 dt=1.0 / 120.0, iterations=30, mu=0.6, maxc=4)
+
+
+def capsule_pile(n: int = 96, seed: int = 2, spacing: float = 0.7) -> Scene:
+    """Small mixed pile with capsules (r 0.05-0.2, length 0.1-0.6), spheres and
+    boxes, so every pair type of the narrow phase occurs in the loop."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(round(n ** (1.0 / 3.0), 6)))
+    L = side * spacing
+    idx = np.arange(n)
+    gx, gy, gz = idx % side, (idx // side) % side, idx // (side * side)
+    pos = np.stack([(gx + 0.5) * spacing, (gy + 0.5) * spacing, (gz + 0.5) * spacing + 0.3], axis=1)
+    pos = (pos + rng.uniform(-0.05, 0.05, size=(n, 3))).astype(np.float32)
+    q = random_quats(rng, n)
+    kind = rng.integers(0, 3, size=n)
+    bodies = np.zeros((n, 20), np.float32)
+    dims = np.zeros((n, 4), np.float32)
+    cls = np.zeros(n, np.int32)
+    for i in range(n):
+        dens = rng.uniform(500, 2000)
+        if kind[i] == 0:
+            r = rng.uniform(0.05, 0.25)
+            m = mass_sphere(dens, r)
+            cls[i] = SPHERE
+            dims[i, 0] = r
+        elif kind[i] == 1:
+            s = rng.uniform(0.1, 0.5, size=3)
+            m = mass_box(dens, *s)
+            cls[i] = BOX
+            dims[i, :3] = s
+        else:
+            r = rng.uniform(0.05, 0.2)
+            ln = rng.uniform(0.1, 0.6)
+            # dMassSetCapsule (ode/src/mass.cpp:144-170), axis along z
+            r32, l32 = np.float32(r), np.float32(ln)
+            M1 = np.float32(math.pi) * r32 * r32 * l32 * np.float32(dens)
+            M2 = np.float32(4.0 / 3.0) * np.float32(math.pi) * r32 * r32 * r32 * np.float32(dens)
+            mt = M1 + M2
+            Ia = M1 * (np.float32(0.25) * r32 * r32 + np.float32(1.0 / 12.0) * l32 * l32) + \
+                M2 * (np.float32(0.4) * r32 * r32 + np.float32(0.375) * r32 * l32 + np.float32(0.25) * l32 * l32)
+            Iz = (np.float32(0.5) * M1 + np.float32(0.4) * M2) * r32 * r32
+            m = (mt, Ia, Ia, Iz)
+            cls[i] = CAPSULE
+            dims[i, 0] = r
+            dims[i, 1] = ln
+        bodies[i, 13] = m[0]
+        bodies[i, 14:17] = m[1:]
+    bodies[:, 0:3] = pos
+    bodies[:, 3:7] = q
+    ng = n + 5
+    gcls = np.concatenate([cls, np.full(5, PLANE, np.int32)])
+    gbody = np.concatenate([np.arange(n, dtype=np.int32), np.full(5, -1, np.int32)])
+    gdims = np.concatenate([dims, np.array([[0, 0, 1, 0], [1, 0, 0, 0], [-1, 0, 0, -L], [0, 1, 0, 0],
+                                            [0, -1, 0, -L]], dtype=np.float32)])
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene(f"capsule_pile{n}", bodies, gcls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
+                 dt=1.0 / 120.0, iterations=20, mu=0.6, maxc=4)
