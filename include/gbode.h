@@ -1,0 +1,298 @@
+/* gbode -- GB300-native rigid-body step behind ODE's C API.
+ *
+ * libgbode.so exports the subset of the Open Dynamics Engine 0.16 C API that
+ * the rigid-body hot path uses (hash-space broad phase -> dCollide contact
+ * generation for sphere/box/capsule/plane -> contact joints -> dWorldQuickStep
+ * -> body integration), with ODE's exact names, argument meanings, struct
+ * layouts and return conventions (dReal = float, i.e. ODE's dSINGLE build), so
+ * an ODE program that uses only this subset links against it unchanged.  The
+ * numerical work runs in hand-written CUDA kernels on one GPU; host code keeps
+ * only handles, parameters and the near-callback loop.
+ *
+ * Each declaration cites the reference declaration it replaces
+ * (include/ode/<file>:<line> in the reference tree).  The gbode* functions at
+ * the end have no ODE counterpart: they expose the fused GPU path (contacts
+ * that never leave the device) and GPU-only controls.
+ */
+#ifndef GBODE_H
+#define GBODE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- scalar and vector types: include/ode/common.h:270-275, odeconfig.h */
+typedef float dReal;
+typedef dReal dVector3[4];
+typedef dReal dVector4[4];
+typedef dReal dMatrix3[4 * 3];
+typedef dReal dQuaternion[4];
+
+/* ---- opaque handles: include/ode/common.h:330-345 */
+typedef struct dxWorld *dWorldID;
+typedef struct dxSpace *dSpaceID;
+typedef struct dxBody *dBodyID;
+typedef struct dxGeom *dGeomID;
+typedef struct dxJoint *dJointID;
+typedef struct dxJointGroup *dJointGroupID;
+
+/* ---- geom classes: include/ode/collision.h:881-905 */
+enum { dSphereClass = 0, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass };
+
+/* ---- contact records: include/ode/contact.h:28-103 (identical layout) */
+enum {
+    dContactMu2 = 0x001, dContactAxisDep = 0x001, dContactFDir1 = 0x002, dContactBounce = 0x004,
+    dContactSoftERP = 0x008, dContactSoftCFM = 0x010, dContactMotion1 = 0x020, dContactMotion2 = 0x040,
+    dContactMotionN = 0x080, dContactSlip1 = 0x100, dContactSlip2 = 0x200, dContactRolling = 0x400,
+    dContactApprox0 = 0x0000, dContactApprox1_1 = 0x1000, dContactApprox1_2 = 0x2000,
+    dContactApprox1_N = 0x4000, dContactApprox1 = 0x7000
+};
+typedef struct dSurfaceParameters {
+    int mode;
+    dReal mu, mu2, rho, rho2, rhoN, bounce, bounce_vel, soft_erp, soft_cfm;
+    dReal motion1, motion2, motionN, slip1, slip2;
+} dSurfaceParameters;
+typedef struct dContactGeom {
+    dVector3 pos;
+    dVector3 normal;
+    dReal depth;
+    dGeomID g1, g2;
+    int side1, side2;
+} dContactGeom;
+typedef struct dContact {
+    dSurfaceParameters surface;
+    dContactGeom geom;
+    dVector3 fdir1;
+} dContact;
+
+/* ---- mass: include/ode/mass.h:31-96 */
+typedef struct dMass {
+    dReal mass;
+    dVector3 c;
+    dMatrix3 I;
+} dMass;
+
+/* ---- joint feedback: include/ode/common.h:389-396 */
+typedef struct dJointFeedback {
+    dVector3 f1, t1, f2, t2;
+} dJointFeedback;
+
+/* near callback: include/ode/collision_space.h:49 */
+typedef void dNearCallback(void *data, dGeomID o1, dGeomID o2);
+
+/* ---- init: include/ode/odeinit.h:119, :177, :227 */
+int dInitODE2(unsigned int uiInitFlags);
+void dInitODE(void);
+int dAllocateODEDataForThread(unsigned int uiAllocateFlags);
+void dCloseODE(void);
+
+/* ---- world: include/ode/objects.h:77-560 */
+dWorldID dWorldCreate(void);
+void dWorldDestroy(dWorldID w);
+void dWorldSetGravity(dWorldID w, dReal x, dReal y, dReal z);
+void dWorldGetGravity(dWorldID w, dVector3 gravity);
+void dWorldSetERP(dWorldID w, dReal erp);
+dReal dWorldGetERP(dWorldID w);
+void dWorldSetCFM(dWorldID w, dReal cfm);
+dReal dWorldGetCFM(dWorldID w);
+int dWorldQuickStep(dWorldID w, dReal stepsize);
+int dWorldStep(dWorldID w, dReal stepsize);
+void dWorldSetQuickStepNumIterations(dWorldID w, int num);
+int dWorldGetQuickStepNumIterations(dWorldID w);
+void dWorldSetQuickStepW(dWorldID w, dReal over_relaxation);
+dReal dWorldGetQuickStepW(dWorldID w);
+void dWorldSetQuickStepDynamicIterationParameters(dWorldID w, const dReal *ptr_iteration_premature_exit_delta,
+                                                  const dReal *ptr_max_num_extra_factor,
+                                                  const dReal *ptr_extra_iteration_requirement_delta);
+void dWorldGetQuickStepDynamicIterationParameters(dWorldID w, dReal *out_iteration_premature_exit_delta,
+                                                  dReal *out_max_num_extra_factor,
+                                                  dReal *out_extra_iteration_requirement_delta);
+void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal vel);
+dReal dWorldGetContactMaxCorrectingVel(dWorldID w);
+void dWorldSetContactSurfaceLayer(dWorldID w, dReal depth);
+dReal dWorldGetContactSurfaceLayer(dWorldID w);
+
+/* ---- bodies: include/ode/objects.h:700-1400 */
+dBodyID dBodyCreate(dWorldID w);
+void dBodyDestroy(dBodyID b);
+void dBodySetData(dBodyID b, void *data);
+void *dBodyGetData(dBodyID b);
+void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z);
+void dBodySetRotation(dBodyID b, const dMatrix3 R);
+void dBodySetQuaternion(dBodyID b, const dQuaternion q);
+void dBodySetLinearVel(dBodyID b, dReal x, dReal y, dReal z);
+void dBodySetAngularVel(dBodyID b, dReal x, dReal y, dReal z);
+const dReal *dBodyGetPosition(dBodyID b);
+const dReal *dBodyGetRotation(dBodyID b);
+const dReal *dBodyGetQuaternion(dBodyID b);
+const dReal *dBodyGetLinearVel(dBodyID b);
+const dReal *dBodyGetAngularVel(dBodyID b);
+void dBodySetMass(dBodyID b, const dMass *mass);
+void dBodyGetMass(dBodyID b, dMass *mass);
+void dBodyAddForce(dBodyID b, dReal fx, dReal fy, dReal fz);
+void dBodyAddTorque(dBodyID b, dReal fx, dReal fy, dReal fz);
+const dReal *dBodyGetForce(dBodyID b);
+const dReal *dBodyGetTorque(dBodyID b);
+void dBodySetGyroscopicMode(dBodyID b, int enabled);
+int dBodyGetGyroscopicMode(dBodyID b);
+int dBodyGetNumJoints(dBodyID b);
+
+/* ---- mass helpers: include/ode/mass.h:40-96 */
+void dMassSetZero(dMass *m);
+void dMassSetParameters(dMass *m, dReal themass, dReal cgx, dReal cgy, dReal cgz, dReal I11, dReal I22,
+                        dReal I33, dReal I12, dReal I13, dReal I23);
+void dMassSetSphere(dMass *m, dReal density, dReal radius);
+void dMassSetSphereTotal(dMass *m, dReal total_mass, dReal radius);
+void dMassSetCapsule(dMass *m, dReal density, int direction, dReal radius, dReal length);
+void dMassSetBox(dMass *m, dReal density, dReal lx, dReal ly, dReal lz);
+void dMassSetBoxTotal(dMass *m, dReal total_mass, dReal lx, dReal ly, dReal lz);
+
+/* ---- spaces: include/ode/collision_space.h:60-120 */
+dSpaceID dHashSpaceCreate(dSpaceID space);
+void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel);
+void dHashSpaceGetLevels(dSpaceID space, int *minlevel, int *maxlevel);
+void dSpaceDestroy(dSpaceID space);
+void dSpaceSetCleanup(dSpaceID space, int mode);
+int dSpaceGetNumGeoms(dSpaceID space);
+/* include/ode/collision.h:822 */
+void dSpaceCollide(dSpaceID space, void *data, dNearCallback *callback);
+
+/* ---- geoms: include/ode/collision.h:100-1000 */
+dGeomID dCreateSphere(dSpaceID space, dReal radius);
+dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);
+dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length);
+dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d);
+void dGeomDestroy(dGeomID geom);
+void dGeomSetData(dGeomID geom, void *data);
+void *dGeomGetData(dGeomID geom);
+void dGeomSetBody(dGeomID geom, dBodyID body);
+dBodyID dGeomGetBody(dGeomID geom);
+void dGeomSetPosition(dGeomID geom, dReal x, dReal y, dReal z);
+void dGeomSetRotation(dGeomID geom, const dMatrix3 R);
+const dReal *dGeomGetPosition(dGeomID geom);
+const dReal *dGeomGetRotation(dGeomID geom);
+int dGeomGetClass(dGeomID geom);
+void dGeomGetAABB(dGeomID geom, dReal aabb[6]);
+/* include/ode/collision.h:792 */
+int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom *contact, int skip);
+/* include/ode/collision.h:1478 */
+int dBoxBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2, const dMatrix3 R2,
+            const dVector3 side2, dVector3 normal, dReal *depth, int *return_code, int flags,
+            dContactGeom *contact, int skip);
+
+/* ---- joints: include/ode/objects.h:1500-1700 */
+dJointGroupID dJointGroupCreate(int max_size);
+void dJointGroupDestroy(dJointGroupID group);
+void dJointGroupEmpty(dJointGroupID group);
+dJointID dJointCreateContact(dWorldID w, dJointGroupID group, const dContact *c);
+void dJointAttach(dJointID j, dBodyID body1, dBodyID body2);
+void dJointDestroy(dJointID j);
+void dJointSetFeedback(dJointID j, dJointFeedback *fb);
+dJointFeedback *dJointGetFeedback(dJointID j);
+dBodyID dJointGetBody(dJointID j, int index);
+int dAreConnectedExcluding(dBodyID body1, dBodyID body2, int joint_type);
+
+/* ---- misc: include/ode/misc.h:35-50, rotation.h:40-70 */
+unsigned long dRand(void);
+int dRandInt(int n);
+void dRandSetSeed(unsigned long s);
+unsigned long dRandGetSeed(void);
+int dTestRand(void);
+void dRSetIdentity(dMatrix3 R);
+void dRFromAxisAndAngle(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal angle);
+void dRfromQ(dMatrix3 R, const dQuaternion q);
+void dQFromAxisAndAngle(dQuaternion q, dReal ax, dReal ay, dReal az, dReal angle);
+
+/* ======================================================================
+ * gbode extensions (no ODE counterpart)
+ * ====================================================================== */
+
+/* Solver schedule used by dWorldQuickStep. */
+enum {
+    /* Graph-coloured projected Gauss-Seidel over all rows of the world: rows of
+     * one colour share no body and are relaxed in parallel; colours run in
+     * sequence.  The default. */
+    GBODE_SOLVER_COLOURED = 0,
+    /* The reference's own row order: islands built as ODE builds them, rows in
+     * joint order with findex<0 rows first, one island per thread block, rows
+     * relaxed one after another (ODE with row reordering disabled). */
+    GBODE_SOLVER_REFERENCE_ORDER = 1,
+};
+void gbodeWorldSetSolver(dWorldID w, int solver);
+int gbodeWorldGetSolver(dWorldID w);
+
+/* Iterate until the LCP residual (projected natural map, FP32, relative to
+ * max(1, max|lambda|)) is <= target, checking every check_every iterations,
+ * up to max_iterations.  target <= 0 restores the fixed iteration count. */
+void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int max_iterations);
+
+/* Warm start: 0 = cold (lambda = 0, the reference default), 1 = previous-step
+ * lambda of the same (geom pair, contact slot) scaled by `scale`. */
+void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale);
+
+/* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
+ * creation without leaving the device.  Equivalent to dSpaceCollide with a near
+ * callback that calls dCollide(o1, o2, maxc, ...) and makes one contact joint
+ * per point with surface *s (fdir1 unused), attached to the geoms' bodies.
+ * The contacts belong to `group` and are cleared by dJointGroupEmpty.  Runs
+ * asynchronously on the world's stream.  Returns 1, or 0 on a bad argument. */
+int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, const dSurfaceParameters *s,
+                              int maxc);
+
+/* CUDA stream (cudaStream_t) the world enqueues its work on; NULL = the
+ * library's own stream. */
+void gbodeWorldSetStream(dWorldID w, void *stream);
+void *gbodeWorldGetStream(dWorldID w);
+/* Wait for the world's stream. Returns 1, or 0 if a device error was recorded. */
+int gbodeWorldSynchronize(dWorldID w);
+
+/* Statistics of the last dWorldQuickStep (synchronises the stream). */
+typedef struct gbodeStepStats {
+    int contacts;          /* contact joints stepped */
+    int rows;              /* constraint rows */
+    int colours;           /* colours (coloured solver) */
+    int iterations;        /* PGS sweeps performed */
+    float residual;        /* final FP32 relative residual (0 if not computed) */
+    int pairs;             /* candidate pairs of the last broad phase */
+    float solve_ms;        /* device time of the PGS sweeps, if timing is on */
+    float step_ms;         /* device time of the whole dWorldQuickStep, if timing is on */
+} gbodeStepStats;
+void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
+/* Record CUDA events around the solver and the step (adds no host syncs). */
+void gbodeWorldSetTiming(dWorldID w, int enabled);
+
+/* FP64 LCP residual and complementarity error of the last step's solution,
+ * evaluated on the device from the step's FP32 rows (unscaled) and lambda:
+ * max_i |lambda_i - proj_[lo,hi](lambda_i - (A lambda - b)_i / A_ii)|, not
+ * normalised; *max_lambda receives max|lambda|.  Synchronises the stream. */
+double gbodeWorldLastResidual(dWorldID w, double *complementarity, double *max_lambda);
+
+/* Copies of the last step's rows and lambda for checking: rows [nrows][20]
+ * (J1(6) J2(6) rhs cfm lo hi b1 b2 findex lambda, world body indices), in the
+ * solver's row order.  Returns nrows (writes at most cap rows). */
+int gbodeWorldGetLastRows(dWorldID w, float *rows, int cap);
+
+/* Copies of the contacts the last gbodeSpaceCollideContacts (or the host
+ * contact joints of the last step) produced: [n][12] pos(3) normal(3) depth
+ * g1 g2 b1 b2 slot (geom indices are positions in the space's geom list,
+ * body indices creation order among live bodies).  Returns n (writes at most
+ * cap).  Synchronises the stream. */
+int gbodeWorldGetContacts(dWorldID w, float *out, int cap);
+
+/* Last error message ("" if none) and clear. */
+const char *gbodeGetLastError(void);
+/* Number of kernel launches the library has issued since load. */
+long long gbodeKernelLaunchCount(void);
+
+/* Bulk state access for batched drivers: [nb][25] pos q R lvel avel in body
+ * creation order (index = order of dBodyCreate among live bodies). */
+int gbodeWorldGetBodyCount(dWorldID w);
+void gbodeWorldGetState(dWorldID w, float *out);
+void gbodeWorldSetState(dWorldID w, const float *in);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1267 @@
+// The C-ABI layer: ODE's public functions for the rigid-body hot path, backed
+// by the device pipeline in collide.cu / solve.cu.
+//
+// Host objects keep only what ODE's API exposes (handles, parameters, user
+// data, the bodies' host-visible state) and a dirty/valid protocol against the
+// device copy: setters mark the world's device state dirty and it is uploaded
+// whole before the next device step; getters download the whole body state
+// once after a step.  Argument checking follows ODE's release build: invalid
+// handles are the caller's responsibility, device failures are reported
+// through the return value (0) and gbodeGetLastError(), never by aborting.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gbode.h"
+#include "gbode_internal.h"
+
+using namespace gb;
+
+// ------------------------------------------------------------------ infrastructure
+namespace gb {
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches += n; }
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+bool DBuf::ensure(size_t want) {
+    if (want <= bytes && p) return true;
+    size_t nb = bytes ? bytes : 256;
+    while (nb < want) nb = nb + nb / 2 + 256;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&p, nb) != cudaSuccess) { p = nullptr; return false; }
+    bytes = nb;
+    return true;
+}
+void DBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+void Workspace::release() {
+    DBuf *all[] = {&g_cls, &g_body, &g_dims, &g_spos, &g_sR, &g_pos, &g_R, &g_amin, &g_amax, &g_level, &g_dblo, &g_dbhi,
+                   &g_big, &h_keys, &h_count, &h_start, &h_fill, &h_members, &h_entry, &p_count, &p_start, &pairs,
+                   &c_slots, &c_count, &c_start, &contacts, &surfaces, &c_mcount, &c_rstart, &c_code, &b_pos, &b_q,
+                   &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
+                   &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
+                   &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
+                   &col_fill, &col_list, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
+    for (DBuf *b : all) b->release();
+    if (dc) cudaFree(dc);
+    if (hc) cudaFreeHost(hc);
+    dc = nullptr;
+    hc = nullptr;
+}
+}  // namespace gb
+
+static thread_local std::string g_err;
+static void set_error(const char *where, cudaError_t e = cudaSuccess) {
+    char buf[256];
+    if (e != cudaSuccess) snprintf(buf, sizeof buf, "%s: %s", where, cudaGetErrorString(e));
+    else snprintf(buf, sizeof buf, "%s", where);
+    g_err = buf;
+}
+
+// ------------------------------------------------------------------ objects
+struct dxJoint;
+struct dxGeom;
+
+struct dxBody {
+    dxWorld *world;
+    int index;
+    void *data = nullptr;
+    float pos[4] = {0, 0, 0, 0}, q[4] = {1, 0, 0, 0}, R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    float lvel[4] = {0, 0, 0, 0}, avel[4] = {0, 0, 0, 0}, facc[4] = {0, 0, 0, 0}, tacc[4] = {0, 0, 0, 0};
+    dMass mass;
+    float invI[12];
+    float invMass = 1;
+    int gyro = 1;  // ode.cpp:283 -- dBodyCreate enables the implicit gyroscopic term
+    int njoints = 0;
+};
+
+struct dxSpace;
+struct dxGeom {
+    int cls;
+    dxSpace *space = nullptr;
+    dxBody *body = nullptr;
+    void *data = nullptr;
+    float dims[4] = {0, 0, 0, 0};
+    float pos[4] = {0, 0, 0, 0};
+    float R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    int index = -1;  // position in its space
+};
+
+struct dxSpace {
+    std::vector<dxGeom *> geoms;
+    int minlevel = -3, maxlevel = 10;  // collision_space.cpp:371-376
+    int cleanup = 1;
+    bool dirty = true;                 // geom set or static poses changed since the last upload
+};
+
+struct dxJointGroup {
+    std::vector<dxJoint *> joints;
+    dxWorld *device_world = nullptr;   // world holding this group's device-resident contacts
+};
+
+struct dxJoint {
+    dxWorld *world;
+    dxJointGroup *group;
+    dContact contact;
+    dxBody *b1 = nullptr, *b2 = nullptr;
+    bool attached = false;
+    dJointFeedback *feedback = nullptr;
+};
+
+struct dxWorld {
+    Workspace ws;
+    SolverParams P;
+    std::vector<dxBody *> bodies;
+    std::vector<dxJoint *> joints;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool dev_dirty = true;    // host body state newer than device
+    bool host_valid = true;   // host body state equals device
+    dxSpace *uploaded_space = nullptr;
+    bool device_contacts = false;
+    int device_surfaces = 0;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gbodeStepStats stats{};
+    bool stats_pending = false;
+    int last_host_contacts = 0;
+    std::vector<dxJoint *> last_fb_joints;
+};
+
+static dxWorld *g_default_world = nullptr;
+static std::vector<dxWorld *> g_worlds;
+
+// ------------------------------------------------------------------ small math (host)
+// rotation.cpp:236-254 dRfromQ
+static void r_from_q(float *R, const float *q) {
+    float qq1 = 2 * q[1] * q[1], qq2 = 2 * q[2] * q[2], qq3 = 2 * q[3] * q[3];
+    R[0] = 1 - qq2 - qq3; R[1] = 2 * (q[1] * q[2] - q[0] * q[3]); R[2] = 2 * (q[1] * q[3] + q[0] * q[2]); R[3] = 0;
+    R[4] = 2 * (q[1] * q[2] + q[0] * q[3]); R[5] = 1 - qq1 - qq3; R[6] = 2 * (q[2] * q[3] - q[0] * q[1]); R[7] = 0;
+    R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2; R[11] = 0;
+}
+// odemath.cpp:200-218 dxSafeNormalize4 with the dxNormalize4 fallback
+static void normalize4(float *a) {
+    float l = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3];
+    if (l > 0) { l = 1.0f / sqrtf(l); a[0] *= l; a[1] *= l; a[2] *= l; a[3] *= l; }
+    else { a[0] = 1; a[1] = a[2] = a[3] = 0; }
+}
+// rotation.cpp:257-307 dQfromR
+static void q_from_r(float *q, const float *Rm) {
+#define RR(i, j) Rm[(i) * 4 + (j)]
+    float tr = RR(0, 0) + RR(1, 1) + RR(2, 2), s;
+    if (tr >= 0) {
+        s = sqrtf(tr + 1); q[0] = 0.5f * s; s = 0.5f * (1.0f / s);
+        q[1] = (RR(2, 1) - RR(1, 2)) * s; q[2] = (RR(0, 2) - RR(2, 0)) * s; q[3] = (RR(1, 0) - RR(0, 1)) * s;
+    } else if (RR(1, 1) > RR(0, 0) && !(RR(2, 2) > RR(1, 1))) {
+        s = sqrtf((RR(1, 1) - (RR(2, 2) + RR(0, 0))) + 1); q[2] = 0.5f * s; s = 0.5f * (1.0f / s);
+        q[3] = (RR(1, 2) + RR(2, 1)) * s; q[1] = (RR(0, 1) + RR(1, 0)) * s; q[0] = (RR(0, 2) - RR(2, 0)) * s;
+    } else if ((RR(1, 1) > RR(0, 0) && RR(2, 2) > RR(1, 1)) || (!(RR(1, 1) > RR(0, 0)) && RR(2, 2) > RR(0, 0))) {
+        s = sqrtf((RR(2, 2) - (RR(0, 0) + RR(1, 1))) + 1); q[3] = 0.5f * s; s = 0.5f * (1.0f / s);
+        q[1] = (RR(2, 0) + RR(0, 2)) * s; q[2] = (RR(1, 2) + RR(2, 1)) * s; q[0] = (RR(1, 0) - RR(0, 1)) * s;
+    } else {
+        s = sqrtf((RR(0, 0) - (RR(1, 1) + RR(2, 2))) + 1); q[1] = 0.5f * s; s = 0.5f * (1.0f / s);
+        q[2] = (RR(0, 1) + RR(1, 0)) * s; q[3] = (RR(2, 0) + RR(0, 2)) * s; q[0] = (RR(2, 1) - RR(1, 2)) * s;
+    }
+#undef RR
+}
+// matrix.cpp dxFactorCholesky + dxSolveCholesky + dxInvertPDMatrix for n = 3
+// (row stride 4), the inversion dBodySetMass uses (ode.cpp:488-505).
+static int invert_pd3(const float *A, float *Ainv) {
+    float L[12], recip[3], X[3], y[3];
+    memcpy(L, A, sizeof L);
+    for (int i = 0; i < 3; i++) {
+        float *aa = L + 4 * i;
+        for (int j = 0; j < i; j++) {
+            float sum = aa[j];
+            const float *bb = L + 4 * j;
+            for (int k = 0; k < j; k++) sum -= aa[k] * bb[k];
+            aa[j] = sum * recip[j];
+        }
+        float sum = aa[i];
+        for (int k = 0; k < i; k++) sum -= aa[k] * aa[k];
+        if (sum <= 0.0f) return 0;
+        float sq = sqrtf(sum);
+        aa[i] = sq;
+        recip[i] = 1.0f / sq;
+    }
+    memset(Ainv, 0, 12 * sizeof(float));
+    for (int c = 0; c < 3; c++) {
+        X[0] = X[1] = X[2] = 0; X[c] = 1.0f;
+        for (int i = 0; i < 3; i++) {
+            float sum = 0.0f;
+            for (int k = 0; k < i; k++) sum += L[4 * i + k] * y[k];
+            y[i] = (X[i] - sum) / L[4 * i + i];
+        }
+        for (int i = 2; i >= 0; i--) {
+            float sum = 0.0f;
+            for (int k = i + 1; k < 3; k++) sum += L[4 * k + i] * X[k];
+            X[i] = (y[i] - sum) / L[4 * i + i];
+        }
+        for (int k = 0; k < 3; k++) Ainv[4 * k + c] = X[k];
+    }
+    return 1;
+}
+
+// ------------------------------------------------------------------ world plumbing
+static bool world_init_device(dxWorld *w) {
+    if (w->ws.dc) return true;
+    cudaError_t e = cudaMalloc(&w->ws.dc, sizeof(DevCounters));
+    if (e != cudaSuccess) { set_error("cudaMalloc(counters)", e); return false; }
+    cudaMemset(w->ws.dc, 0, sizeof(DevCounters));
+    e = cudaMallocHost(&w->ws.hc, sizeof(DevCounters));
+    if (e != cudaSuccess) { set_error("cudaMallocHost", e); return false; }
+    memset(w->ws.hc, 0, sizeof(DevCounters));
+    if (!w->stream) {
+        e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { set_error("cudaStreamCreate", e); return false; }
+        w->own_stream = true;
+    }
+    for (int i = 0; i < 4; i++) cudaEventCreate(&w->ev[i]);
+    return true;
+}
+
+static void world_download(dxWorld *w) {
+    if (w->host_valid) return;
+    int nb = (int)w->bodies.size();
+    if (nb > 0) {
+        std::vector<float4> pos(nb), q(nb), R(3 * nb), lv(nb), av(nb);
+        cudaStream_t s = w->stream;
+        cudaMemcpyAsync(pos.data(), w->ws.b_pos.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(q.data(), w->ws.b_q.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(R.data(), w->ws.b_R.p, 48 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(lv.data(), w->ws.b_lvel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(av.data(), w->ws.b_avel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { set_error("download bodies", e); return; }
+        for (int i = 0; i < nb; i++) {
+            dxBody *b = w->bodies[i];
+            b->pos[0] = pos[i].x; b->pos[1] = pos[i].y; b->pos[2] = pos[i].z;
+            b->q[0] = q[i].x; b->q[1] = q[i].y; b->q[2] = q[i].z; b->q[3] = q[i].w;
+            for (int r = 0; r < 3; r++) {
+                b->R[4 * r] = R[3 * i + r].x; b->R[4 * r + 1] = R[3 * i + r].y; b->R[4 * r + 2] = R[3 * i + r].z; b->R[4 * r + 3] = 0;
+            }
+            b->lvel[0] = lv[i].x; b->lvel[1] = lv[i].y; b->lvel[2] = lv[i].z;
+            b->avel[0] = av[i].x; b->avel[1] = av[i].y; b->avel[2] = av[i].z;
+            // the device consumed the force accumulators
+            b->facc[0] = b->facc[1] = b->facc[2] = 0;
+            b->tacc[0] = b->tacc[1] = b->tacc[2] = 0;
+        }
+    }
+    w->host_valid = true;
+}
+
+static void mark_host_changed(dxBody *b) {
+    dxWorld *w = b->world;
+    world_download(w);  // keep the other bodies' device state
+    w->dev_dirty = true;
+}
+
+static bool world_upload(dxWorld *w) {
+    if (!world_init_device(w)) return false;
+    int nb = (int)w->bodies.size();
+    if (!ensure_bodies(w->ws, nb)) { set_error("device allocation (bodies)"); return false; }
+    if (!w->dev_dirty) return true;
+    std::vector<float4> pos(nb), q(nb), R(3 * nb), lv(nb), av(nb), fa(nb), ta(nb), Ib(3 * nb), iIb(3 * nb);
+    for (int i = 0; i < nb; i++) {
+        dxBody *b = w->bodies[i];
+        b->index = i;
+        pos[i] = make_float4(b->pos[0], b->pos[1], b->pos[2], b->invMass);
+        q[i] = make_float4(b->q[0], b->q[1], b->q[2], b->q[3]);
+        for (int r = 0; r < 3; r++) {
+            R[3 * i + r] = make_float4(b->R[4 * r], b->R[4 * r + 1], b->R[4 * r + 2], 0.f);
+            Ib[3 * i + r] = make_float4(b->mass.I[4 * r], b->mass.I[4 * r + 1], b->mass.I[4 * r + 2], 0.f);
+            iIb[3 * i + r] = make_float4(b->invI[4 * r], b->invI[4 * r + 1], b->invI[4 * r + 2], 0.f);
+        }
+        lv[i] = make_float4(b->lvel[0], b->lvel[1], b->lvel[2], b->mass.mass);
+        int flags = b->gyro ? 1 : 0;
+        float ff;
+        memcpy(&ff, &flags, 4);
+        av[i] = make_float4(b->avel[0], b->avel[1], b->avel[2], ff);
+        fa[i] = make_float4(b->facc[0], b->facc[1], b->facc[2], 0.f);
+        ta[i] = make_float4(b->tacc[0], b->tacc[1], b->tacc[2], 0.f);
+    }
+    if (nb > 0) {
+        cudaStream_t s = w->stream;
+        cudaMemcpyAsync(w->ws.b_pos.p, pos.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_q.p, q.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_R.p, R.data(), 48 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_lvel.p, lv.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_avel.p, av.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_facc.p, fa.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_tacc.p, ta.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_Ib.p, Ib.data(), 48 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_invIb.p, iIb.data(), 48 * nb, cudaMemcpyHostToDevice, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { set_error("upload bodies", e); return false; }
+    }
+    w->dev_dirty = false;
+    w->host_valid = true;
+    return true;
+}
+
+static dxWorld *space_world(dxSpace *sp) {
+    for (dxGeom *g : sp->geoms)
+        if (g->body) return g->body->world;
+    if (!g_default_world) g_default_world = dWorldCreate();
+    return g_default_world;
+}
+
+static bool space_upload(dxSpace *sp, dxWorld *w) {
+    if (!world_upload(w)) return false;
+    if (w->uploaded_space == sp && !sp->dirty) return true;
+    std::vector<GeomHost> gh(sp->geoms.size());
+    for (size_t i = 0; i < sp->geoms.size(); i++) {
+        dxGeom *g = sp->geoms[i];
+        g->index = (int)i;
+        gh[i].cls = g->cls;
+        gh[i].body = g->body ? g->body->index : -1;
+        memcpy(gh[i].dims, g->dims, sizeof g->dims);
+        memcpy(gh[i].pos, g->pos, sizeof g->pos);
+        memcpy(gh[i].R, g->R, sizeof g->R);
+    }
+    if (!upload_geoms(w->ws, gh, w->stream)) { set_error("upload geoms"); return false; }
+    w->uploaded_space = sp;
+    sp->dirty = false;
+    return true;
+}
+
+// ------------------------------------------------------------------ init / misc
+extern "C" {
+
+int dInitODE2(unsigned int) { return 1; }
+void dInitODE(void) {}
+int dAllocateODEDataForThread(unsigned int) { return 1; }
+void dCloseODE(void) {}
+
+const char *gbodeGetLastError(void) { return g_err.c_str(); }
+long long gbodeKernelLaunchCount(void) { return g_launches.load(); }
+
+// misc.cpp:35-135 dRand / dRandInt
+static uint32_t g_seed = 0;
+unsigned long dRand(void) {
+    g_seed = (uint32_t)(1664525u * g_seed + 1013904223u);
+    return g_seed;
+}
+unsigned long dRandGetSeed(void) { return g_seed; }
+void dRandSetSeed(unsigned long s) { g_seed = (uint32_t)s; }
+int dTestRand(void) {
+    uint32_t old = g_seed;
+    int ok = 1;
+    g_seed = 0;
+    if (dRand() != 0x3c6ef35f || dRand() != 0x47502932 || dRand() != 0xd1ccf6e9 || dRand() != 0xaaf95334 ||
+        dRand() != 0x6252e503)
+        ok = 0;
+    g_seed = old;
+    return ok;
+}
+int dRandInt(int n) {
+    uint32_t r = (uint32_t)dRand(), un = (uint32_t)n;
+    if (un <= 0x10u) {
+        r ^= (r >> 16); r ^= (r >> 8); r ^= (r >> 4);
+        if (un <= 0x2u) { r ^= (r >> 2); r ^= (r >> 1); return (int)(r & (un >> 1)); }
+        if (un <= 0x4u) { r ^= (r >> 2); return (int)(((r & 0x3u) * un) >> 2); }
+        return (int)(((r & 0xFu) * un) >> 4);
+    }
+    if (un <= 0x100u) { r ^= (r >> 16); r ^= (r >> 8); return (int)(((r & 0xFFu) * un) >> 8); }
+    if (un <= 0x10000u) { r ^= (r >> 16); return (int)(((r & 0xFFFFu) * un) >> 16); }
+    return (int)(((uint64_t)r * un) >> 32);
+}
+void dRSetIdentity(dMatrix3 R) {
+    memset(R, 0, sizeof(dMatrix3));
+    R[0] = R[5] = R[10] = 1;
+}
+void dRfromQ(dMatrix3 R, const dQuaternion q) { r_from_q(R, q); }
+// rotation.cpp:160-175 dQFromAxisAndAngle
+void dQFromAxisAndAngle(dQuaternion q, dReal ax, dReal ay, dReal az, dReal angle) {
+    float l = ax * ax + ay * ay + az * az;
+    if (l > 0) {
+        angle *= 0.5f;
+        q[0] = cosf(angle);
+        l = sinf(angle) * (1.0f / sqrtf(l));
+        q[1] = ax * l; q[2] = ay * l; q[3] = az * l;
+    } else {
+        q[0] = 1; q[1] = q[2] = q[3] = 0;
+    }
+}
+void dRFromAxisAndAngle(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal angle) {
+    dQuaternion q;
+    dQFromAxisAndAngle(q, ax, ay, az, angle);
+    r_from_q(R, q);
+}
+
+// ------------------------------------------------------------------ mass
+void dMassSetZero(dMass *m) { memset(m, 0, sizeof(dMass)); }
+void dMassSetParameters(dMass *m, dReal themass, dReal cgx, dReal cgy, dReal cgz, dReal I11, dReal I22, dReal I33,
+                        dReal I12, dReal I13, dReal I23) {
+    dMassSetZero(m);
+    m->mass = themass;
+    m->c[0] = cgx; m->c[1] = cgy; m->c[2] = cgz;
+    m->I[0] = I11; m->I[5] = I22; m->I[10] = I33;
+    m->I[1] = I12; m->I[2] = I13; m->I[6] = I23;
+    m->I[4] = I12; m->I[8] = I13; m->I[9] = I23;
+}
+// mass.cpp:118-210
+void dMassSetSphereTotal(dMass *m, dReal total_mass, dReal radius) {
+    dMassSetZero(m);
+    m->mass = total_mass;
+    float II = 0.4f * total_mass * radius * radius;
+    m->I[0] = II; m->I[5] = II; m->I[10] = II;
+}
+void dMassSetSphere(dMass *m, dReal density, dReal radius) {
+    dMassSetSphereTotal(m, (dReal)((4.0f / 3.0f) * M_PI * radius * radius * radius * density), radius);
+}
+void dMassSetCapsule(dMass *m, dReal density, int direction, dReal radius, dReal length) {
+    dMassSetZero(m);
+    float M1 = (float)(M_PI * radius * radius * length * density);
+    float M2 = (float)((4.0f / 3.0f) * M_PI * radius * radius * radius * density);
+    m->mass = M1 + M2;
+    float Ia = M1 * (0.25f * radius * radius + (1.0f / 12.0f) * length * length) +
+               M2 * (0.4f * radius * radius + 0.375f * radius * length + 0.25f * length * length);
+    float Ib = (M1 * 0.5f + M2 * 0.4f) * radius * radius;
+    m->I[0] = Ia; m->I[5] = Ia; m->I[10] = Ia;
+    int d = direction - 1;
+    if (d >= 0 && d < 3) m->I[5 * d] = Ib;
+}
+void dMassSetBoxTotal(dMass *m, dReal total_mass, dReal lx, dReal ly, dReal lz) {
+    dMassSetZero(m);
+    m->mass = total_mass;
+    m->I[0] = total_mass / 12.0f * (ly * ly + lz * lz);
+    m->I[5] = total_mass / 12.0f * (lx * lx + lz * lz);
+    m->I[10] = total_mass / 12.0f * (lx * lx + ly * ly);
+}
+void dMassSetBox(dMass *m, dReal density, dReal lx, dReal ly, dReal lz) {
+    dMassSetBoxTotal(m, lx * ly * lz * density, lx, ly, lz);
+}
+
+// ------------------------------------------------------------------ world
+dWorldID dWorldCreate(void) {
+    dxWorld *w = new dxWorld();
+    SolverParams &P = w->P;
+    memset(&P, 0, sizeof P);
+    P.erp = 0.2f;     // objects.cpp:37
+    P.cfm = 1e-5f;    // objects.cpp:40 (single precision)
+    P.w = 1.3f;       // objects.cpp:83
+    P.iterations = 20;  // objects.h:451
+    P.max_vel = INFINITY;
+    P.min_depth = 0;
+    P.premature_delta = 1e-8f;  // objects.h:473-475
+    P.extra_factor = 1.0f;
+    P.extra_delta = 1e-2f;
+    P.residual_target = 0;
+    P.check_every = 10;
+    P.max_iterations = 0;
+    P.warm_scale = 1.0f;
+    P.solver = GBODE_SOLVER_COLOURED;
+    g_worlds.push_back(w);
+    return w;
+}
+void dWorldDestroy(dWorldID w) {
+    if (!w) return;
+    for (dxBody *b : w->bodies) delete b;
+    for (dxJoint *j : w->joints) {
+        if (j->group) {
+            auto &v = j->group->joints;
+            for (size_t k = 0; k < v.size(); k++) if (v[k] == j) { v.erase(v.begin() + k); break; }
+        }
+        delete j;
+    }
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (int i = 0; i < 4; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+    w->ws.release();
+    if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
+    for (size_t k = 0; k < g_worlds.size(); k++) if (g_worlds[k] == w) { g_worlds.erase(g_worlds.begin() + k); break; }
+    if (g_default_world == w) g_default_world = nullptr;
+    delete w;
+}
+void dWorldSetGravity(dWorldID w, dReal x, dReal y, dReal z) { w->P.gravity[0] = x; w->P.gravity[1] = y; w->P.gravity[2] = z; }
+void dWorldGetGravity(dWorldID w, dVector3 g) { g[0] = w->P.gravity[0]; g[1] = w->P.gravity[1]; g[2] = w->P.gravity[2]; }
+void dWorldSetERP(dWorldID w, dReal erp) { w->P.erp = erp; }
+dReal dWorldGetERP(dWorldID w) { return w->P.erp; }
+void dWorldSetCFM(dWorldID w, dReal cfm) { w->P.cfm = cfm; }
+dReal dWorldGetCFM(dWorldID w) { return w->P.cfm; }
+void dWorldSetQuickStepNumIterations(dWorldID w, int num) { w->P.iterations = num > 0 ? num : 1; }
+int dWorldGetQuickStepNumIterations(dWorldID w) { return w->P.iterations; }
+void dWorldSetQuickStepW(dWorldID w, dReal over_relaxation) { w->P.w = over_relaxation; }
+dReal dWorldGetQuickStepW(dWorldID w) { return w->P.w; }
+void dWorldSetQuickStepDynamicIterationParameters(dWorldID w, const dReal *pe, const dReal *mf, const dReal *ed) {
+    if (pe) w->P.premature_delta = *pe > 0 ? *pe : 0;
+    if (ed) w->P.extra_delta = *ed > 0 ? *ed : 0;
+    if (mf) w->P.extra_factor = *mf > 0 ? *mf : 0;
+}
+void dWorldGetQuickStepDynamicIterationParameters(dWorldID w, dReal *pe, dReal *mf, dReal *ed) {
+    if (pe) *pe = w->P.premature_delta;
+    if (mf) *mf = w->P.extra_factor;
+    if (ed) *ed = w->P.extra_delta;
+}
+void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal vel) { w->P.max_vel = vel; }
+dReal dWorldGetContactMaxCorrectingVel(dWorldID w) { return w->P.max_vel; }
+void dWorldSetContactSurfaceLayer(dWorldID w, dReal depth) { w->P.min_depth = depth; }
+dReal dWorldGetContactSurfaceLayer(dWorldID w) { return w->P.min_depth; }
+
+void gbodeWorldSetSolver(dWorldID w, int solver) { w->P.solver = solver; }
+int gbodeWorldGetSolver(dWorldID w) { return w->P.solver; }
+void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int max_iterations) {
+    w->P.residual_target = target > 0 ? target : 0;
+    w->P.check_every = check_every > 0 ? check_every : 10;
+    w->P.max_iterations = max_iterations;
+}
+void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode = mode; w->P.warm_scale = scale; }
+void gbodeWorldSetStream(dWorldID w, void *stream) {
+    if (w->own_stream && w->stream) { cudaStreamSynchronize(w->stream); cudaStreamDestroy(w->stream); }
+    w->stream = (cudaStream_t)stream;
+    w->own_stream = false;
+    if (!w->stream) {
+        cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+        w->own_stream = true;
+    }
+}
+void *gbodeWorldGetStream(dWorldID w) {
+    world_init_device(w);
+    return (void *)w->stream;
+}
+int gbodeWorldSynchronize(dWorldID w) {
+    if (!world_init_device(w)) return 0;
+    cudaError_t e = cudaStreamSynchronize(w->stream);
+    if (e != cudaSuccess) { set_error("stream", e); return 0; }
+    unsigned err = 0;
+    cudaMemcpy(&err, &w->ws.dc->err, 4, cudaMemcpyDeviceToHost);
+    if (err) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "device error bits 0x%x", err);
+        set_error(buf);
+        cudaMemset(&w->ws.dc->err, 0, 4);
+        return 0;
+    }
+    return 1;
+}
+void gbodeWorldSetTiming(dWorldID w, int enabled) { w->timing = enabled != 0; }
+
+// ------------------------------------------------------------------ bodies
+dBodyID dBodyCreate(dWorldID w) {
+    world_download(w);
+    dxBody *b = new dxBody();
+    b->world = w;
+    b->index = (int)w->bodies.size();
+    dMassSetParameters(&b->mass, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0);  // ode.cpp:249-254
+    memset(b->invI, 0, sizeof b->invI);
+    b->invI[0] = b->invI[5] = b->invI[10] = 1;
+    w->bodies.push_back(b);
+    w->dev_dirty = true;
+    return b;
+}
+void dBodyDestroy(dBodyID b) {
+    dxWorld *w = b->world;
+    world_download(w);
+    for (dxJoint *j : w->joints) {
+        if (j->b1 == b) j->b1 = nullptr;
+        if (j->b2 == b) j->b2 = nullptr;
+    }
+    for (dxWorld *ww : g_worlds) (void)ww;
+    auto &v = w->bodies;
+    for (size_t k = 0; k < v.size(); k++) if (v[k] == b) { v.erase(v.begin() + k); break; }
+    for (size_t k = 0; k < v.size(); k++) v[k]->index = (int)k;
+    w->dev_dirty = true;
+    w->uploaded_space = nullptr;  // geoms refer to body indices
+    delete b;
+}
+void dBodySetData(dBodyID b, void *data) { b->data = data; }
+void *dBodyGetData(dBodyID b) { return b->data; }
+void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z) {
+    mark_host_changed(b);
+    b->pos[0] = x; b->pos[1] = y; b->pos[2] = z;
+}
+void dBodySetRotation(dBodyID b, const dMatrix3 R) {
+    mark_host_changed(b);
+    memcpy(b->R, R, sizeof(dMatrix3));
+    q_from_r(b->q, R);
+    normalize4(b->q);
+}
+void dBodySetQuaternion(dBodyID b, const dQuaternion q) {
+    mark_host_changed(b);
+    for (int i = 0; i < 4; i++) b->q[i] = q[i];
+    normalize4(b->q);
+    r_from_q(b->R, b->q);
+}
+void dBodySetLinearVel(dBodyID b, dReal x, dReal y, dReal z) {
+    mark_host_changed(b);
+    b->lvel[0] = x; b->lvel[1] = y; b->lvel[2] = z;
+}
+void dBodySetAngularVel(dBodyID b, dReal x, dReal y, dReal z) {
+    mark_host_changed(b);
+    b->avel[0] = x; b->avel[1] = y; b->avel[2] = z;
+}
+const dReal *dBodyGetPosition(dBodyID b) { world_download(b->world); return b->pos; }
+const dReal *dBodyGetRotation(dBodyID b) { world_download(b->world); return b->R; }
+const dReal *dBodyGetQuaternion(dBodyID b) { world_download(b->world); return b->q; }
+const dReal *dBodyGetLinearVel(dBodyID b) { world_download(b->world); return b->lvel; }
+const dReal *dBodyGetAngularVel(dBodyID b) { world_download(b->world); return b->avel; }
+void dBodySetMass(dBodyID b, const dMass *mass) {
+    mark_host_changed(b);
+    b->mass = *mass;
+    if (!invert_pd3(b->mass.I, b->invI)) {
+        memset(b->invI, 0, sizeof b->invI);
+        b->invI[0] = b->invI[5] = b->invI[10] = 1;
+    }
+    b->invMass = 1.0f / b->mass.mass;
+}
+void dBodyGetMass(dBodyID b, dMass *mass) { *mass = b->mass; }
+void dBodyAddForce(dBodyID b, dReal fx, dReal fy, dReal fz) {
+    mark_host_changed(b);
+    b->facc[0] += fx; b->facc[1] += fy; b->facc[2] += fz;
+}
+void dBodyAddTorque(dBodyID b, dReal fx, dReal fy, dReal fz) {
+    mark_host_changed(b);
+    b->tacc[0] += fx; b->tacc[1] += fy; b->tacc[2] += fz;
+}
+const dReal *dBodyGetForce(dBodyID b) { world_download(b->world); return b->facc; }
+const dReal *dBodyGetTorque(dBodyID b) { world_download(b->world); return b->tacc; }
+void dBodySetGyroscopicMode(dBodyID b, int enabled) { mark_host_changed(b); b->gyro = enabled != 0; }
+int dBodyGetGyroscopicMode(dBodyID b) { return b->gyro; }
+int dBodyGetNumJoints(dBodyID b) {
+    int n = 0;
+    for (dxJoint *j : b->world->joints) if (j->attached && (j->b1 == b || j->b2 == b)) n++;
+    return n;
+}
+
+int gbodeWorldGetBodyCount(dWorldID w) { return (int)w->bodies.size(); }
+void gbodeWorldGetState(dWorldID w, float *out) {
+    world_download(w);
+    for (size_t i = 0; i < w->bodies.size(); i++) {
+        dxBody *b = w->bodies[i];
+        float *o = out + 25 * i;
+        memcpy(o, b->pos, 12); memcpy(o + 3, b->q, 16); memcpy(o + 7, b->R, 48);
+        memcpy(o + 19, b->lvel, 12); memcpy(o + 22, b->avel, 12);
+    }
+}
+void gbodeWorldSetState(dWorldID w, const float *in) {
+    world_download(w);
+    for (size_t i = 0; i < w->bodies.size(); i++) {
+        dxBody *b = w->bodies[i];
+        const float *o = in + 25 * i;
+        memcpy(b->pos, o, 12); memcpy(b->q, o + 3, 16); memcpy(b->R, o + 7, 48);
+        memcpy(b->lvel, o + 19, 12); memcpy(b->avel, o + 22, 12);
+    }
+    w->dev_dirty = true;
+}
+
+// ------------------------------------------------------------------ spaces and geoms
+dSpaceID dHashSpaceCreate(dSpaceID parent) {
+    (void)parent;  // nested spaces are outside the supported subset
+    return new dxSpace();
+}
+void dHashSpaceSetLevels(dSpaceID s, int minlevel, int maxlevel) { s->minlevel = minlevel; s->maxlevel = maxlevel; s->dirty = true; }
+void dHashSpaceGetLevels(dSpaceID s, int *minlevel, int *maxlevel) {
+    if (minlevel) *minlevel = s->minlevel;
+    if (maxlevel) *maxlevel = s->maxlevel;
+}
+void dSpaceSetCleanup(dSpaceID s, int mode) { s->cleanup = mode; }
+int dSpaceGetNumGeoms(dSpaceID s) { return (int)s->geoms.size(); }
+void dSpaceDestroy(dSpaceID s) {
+    for (dxGeom *g : s->geoms) {
+        g->space = nullptr;
+        if (s->cleanup) delete g;
+    }
+    for (dxWorld *w : g_worlds) if (w->uploaded_space == s) w->uploaded_space = nullptr;
+    delete s;
+}
+static dxGeom *geom_new(dSpaceID space, int cls) {
+    dxGeom *g = new dxGeom();
+    g->cls = cls;
+    if (space) {
+        g->space = space;
+        // dSpaceAdd puts new geoms at the head of the space list (collision_space.cpp:160-176)
+        space->geoms.insert(space->geoms.begin(), g);
+        space->dirty = true;
+    }
+    return g;
+}
+dGeomID dCreateSphere(dSpaceID space, dReal radius) {
+    dxGeom *g = geom_new(space, dSphereClass);
+    g->dims[0] = radius;
+    return g;
+}
+dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz) {
+    dxGeom *g = geom_new(space, dBoxClass);
+    g->dims[0] = lx; g->dims[1] = ly; g->dims[2] = lz;
+    return g;
+}
+dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length) {
+    dxGeom *g = geom_new(space, dCapsuleClass);
+    g->dims[0] = radius; g->dims[1] = length;
+    return g;
+}
+// plane.cpp:48-66 normalises the plane equation on creation
+dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d) {
+    dxGeom *g = geom_new(space, dPlaneClass);
+    float l = a * a + b * b + c * c;
+    if (l > 0) {
+        l = 1.0f / sqrtf(l);
+        g->dims[0] = a * l; g->dims[1] = b * l; g->dims[2] = c * l; g->dims[3] = d * l;
+    } else {
+        g->dims[0] = 1; g->dims[1] = 0; g->dims[2] = 0; g->dims[3] = 0;
+    }
+    return g;
+}
+void dGeomDestroy(dGeomID g) {
+    if (g->space) {
+        auto &v = g->space->geoms;
+        for (size_t k = 0; k < v.size(); k++) if (v[k] == g) { v.erase(v.begin() + k); break; }
+        g->space->dirty = true;
+    }
+    delete g;
+}
+void dGeomSetData(dGeomID g, void *data) { g->data = data; }
+void *dGeomGetData(dGeomID g) { return g->data; }
+void dGeomSetBody(dGeomID g, dBodyID b) {
+    g->body = b;
+    if (g->space) g->space->dirty = true;
+}
+dBodyID dGeomGetBody(dGeomID g) { return g->body; }
+void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z) {
+    if (g->body) { dBodySetPosition(g->body, x, y, z); return; }
+    g->pos[0] = x; g->pos[1] = y; g->pos[2] = z;
+    if (g->space) g->space->dirty = true;
+}
+void dGeomSetRotation(dGeomID g, const dMatrix3 R) {
+    if (g->body) { dBodySetRotation(g->body, R); return; }
+    memcpy(g->R, R, sizeof(dMatrix3));
+    if (g->space) g->space->dirty = true;
+}
+const dReal *dGeomGetPosition(dGeomID g) { return g->body ? dBodyGetPosition(g->body) : g->pos; }
+const dReal *dGeomGetRotation(dGeomID g) { return g->body ? dBodyGetRotation(g->body) : g->R; }
+int dGeomGetClass(dGeomID g) { return g->cls; }
+void dGeomGetAABB(dGeomID g, dReal aabb[6]) {
+    const float *p = dGeomGetPosition(g), *R = dGeomGetRotation(g), *d = g->dims;
+    float r[3];
+    if (g->cls == dSphereClass) { r[0] = r[1] = r[2] = d[0]; }
+    else if (g->cls == dBoxClass) {
+        for (int i = 0; i < 3; i++) r[i] = 0.5f * (fabsf(R[4 * i] * d[0]) + fabsf(R[4 * i + 1] * d[1]) + fabsf(R[4 * i + 2] * d[2]));
+    } else if (g->cls == dCapsuleClass) {
+        for (int i = 0; i < 3; i++) r[i] = fabsf(R[4 * i + 2] * d[1]) * 0.5f + d[0];
+    } else {
+        for (int i = 0; i < 6; i++) aabb[i] = (i & 1) ? INFINITY : -INFINITY;
+        return;
+    }
+    for (int i = 0; i < 3; i++) { aabb[2 * i] = p[i] - r[i]; aabb[2 * i + 1] = p[i] + r[i]; }
+}
+
+// ------------------------------------------------------------------ collide
+struct CollideBatch {
+    dxSpace *space = nullptr;
+    dxWorld *world = nullptr;
+    std::vector<int> pairs;  // 2 per pair
+    std::unordered_map<long long, int> index;  // (a,b) -> pair
+    int maxc = -1;
+    std::vector<float> out;
+    std::vector<int> counts;
+};
+static thread_local CollideBatch *g_batch = nullptr;
+
+static void fill_contact_geoms(const float *src, int n, dGeomID o1, dGeomID o2, dContactGeom *contact, int skip, bool negate) {
+    for (int i = 0; i < n; i++) {
+        dContactGeom *c = (dContactGeom *)((char *)contact + (size_t)i * skip);
+        const float *o = src + 8 * i;
+        c->pos[0] = o[0]; c->pos[1] = o[1]; c->pos[2] = o[2]; c->pos[3] = 0;
+        float sg = negate ? -1.f : 1.f;
+        c->normal[0] = sg * o[3]; c->normal[1] = sg * o[4]; c->normal[2] = sg * o[5]; c->normal[3] = 0;
+        c->depth = o[6];
+        c->g1 = o1; c->g2 = o2;
+        c->side1 = -1; c->side2 = -1;
+    }
+}
+
+// A one-off pair outside a dSpaceCollide batch: both geoms are posed on the
+// host from their current state and collided on the device.
+static int collide_single(dxGeom *o1, dxGeom *o2, int flags, dContactGeom *contact, int skip) {
+    if (!g_default_world) g_default_world = dWorldCreate();
+    dxWorld *w = g_default_world;
+    if (!world_init_device(w)) return 0;
+    std::vector<GeomHost> gh(2);
+    dxGeom *gg[2] = {o1, o2};
+    for (int k = 0; k < 2; k++) {
+        gh[k].cls = gg[k]->cls;
+        gh[k].body = -1;
+        memcpy(gh[k].dims, gg[k]->dims, sizeof gh[k].dims);
+        const float *p = dGeomGetPosition(gg[k]), *R = dGeomGetRotation(gg[k]);
+        memcpy(gh[k].pos, p, 16);
+        memcpy(gh[k].R, R, 48);
+    }
+    if (!ensure_bodies(w->ws, 1) || !upload_geoms(w->ws, gh, w->stream)) { set_error("dCollide upload"); return 0; }
+    w->uploaded_space = nullptr;
+    launch_pose_aabb(w->ws, bodies_view(w->ws, 0), 2, -1000, 1000, w->stream);
+    int pr[2] = {0, 1};
+    std::vector<float> out;
+    std::vector<int> counts;
+    if (narrow_pairs_host(w->ws, pr, 1, flags & 0xffff, out, counts, w->stream) < 0) { set_error("dCollide"); return 0; }
+    int n = counts.empty() ? 0 : counts[0];
+    fill_contact_geoms(out.data(), n, o1, o2, contact, skip, false);
+    return n;
+}
+
+// collision_kernel.cpp:292-338 dCollide
+int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom *contact, int skip) {
+    if ((flags & 0xffff) == 0) return 0;
+    if (o1 == o2) return 0;
+    if (o1->body == o2->body && o1->body) return 0;
+    CollideBatch *B = g_batch;
+    if (B && o1->space == B->space && o2->space == B->space) {
+        auto it = B->index.find(((long long)o1->index << 32) | (unsigned)o2->index);
+        if (it != B->index.end()) {
+            int maxc = flags & 0xffff;
+            if (maxc > 8) maxc = 8;
+            if (B->maxc != maxc) {
+                // one device launch serves every pair of this dSpaceCollide
+                int np = (int)B->pairs.size() / 2;
+                if (narrow_pairs_host(B->world->ws, B->pairs.data(), np, maxc, B->out, B->counts, B->world->stream) < 0) {
+                    set_error("dCollide batch");
+                    return 0;
+                }
+                B->maxc = maxc;
+            }
+            int p = it->second;
+            int n = B->counts[p];
+            fill_contact_geoms(&B->out[(size_t)p * 64], n, o1, o2, contact, skip, false);
+            return n;
+        }
+    }
+    return collide_single(o1, o2, flags, contact, skip);
+}
+
+// box.cpp:356-737 dBoxBox as a public function: evaluated on the device.
+int dBoxBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2, const dMatrix3 R2,
+            const dVector3 side2, dVector3 normal, dReal *depth, int *return_code, int flags, dContactGeom *contact,
+            int skip);
+
+void dSpaceCollide(dSpaceID space, void *data, dNearCallback *callback) {
+    if (!space || !callback || space->geoms.size() < 2) return;
+    dxWorld *w = space_world(space);
+    if (!space_upload(space, w)) return;
+    int ng = (int)space->geoms.size();
+    cudaStream_t s = w->stream;
+    launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
+    if (!launch_broadphase(w->ws, ng, space->maxlevel, s)) { set_error("broad phase"); return; }
+    int np = 0;
+    cudaMemcpyAsync(&np, &w->ws.dc->npairs, 4, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { set_error("broad phase", e); return; }
+    CollideBatch batch;
+    batch.space = space;
+    batch.world = w;
+    batch.pairs.resize((size_t)np * 2);
+    if (np > 0) {
+        cudaMemcpyAsync(batch.pairs.data(), w->ws.pairs.p, (size_t)np * 8, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+    }
+    batch.index.reserve((size_t)np * 2);
+    for (int p = 0; p < np; p++) batch.index[((long long)batch.pairs[2 * p] << 32) | (unsigned)batch.pairs[2 * p + 1]] = p;
+    w->stats.pairs = np;
+    CollideBatch *prev = g_batch;
+    g_batch = &batch;
+    for (int p = 0; p < np; p++) callback(data, space->geoms[batch.pairs[2 * p]], space->geoms[batch.pairs[2 * p + 1]]);
+    g_batch = prev;
+}
+
+int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, const dSurfaceParameters *sp, int maxc) {
+    if (!space || !w || !group || !sp || maxc < 1) { set_error("gbodeSpaceCollideContacts: bad argument"); return 0; }
+    if (!space_upload(space, w)) return 0;
+    int ng = (int)space->geoms.size();
+    cudaStream_t s = w->stream;
+    Surface surf;
+    memset(&surf, 0, sizeof surf);
+    surf.mode = sp->mode; surf.mu = sp->mu; surf.mu2 = sp->mu2; surf.rho = sp->rho; surf.rho2 = sp->rho2; surf.rhoN = sp->rhoN;
+    surf.bounce = sp->bounce; surf.bounce_vel = sp->bounce_vel; surf.soft_erp = sp->soft_erp; surf.soft_cfm = sp->soft_cfm;
+    surf.motion1 = sp->motion1; surf.motion2 = sp->motion2; surf.motionN = sp->motionN; surf.slip1 = sp->slip1; surf.slip2 = sp->slip2;
+    if (!w->ws.surfaces.ensure(sizeof(Surface))) { set_error("device allocation (surfaces)"); return 0; }
+    static thread_local Surface staged;  // pageable source kept alive past the async copy
+    staged = surf;
+    cudaMemcpyAsync(w->ws.surfaces.p, &staged, sizeof(Surface), cudaMemcpyHostToDevice, s);
+    launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
+    if (!launch_broadphase(w->ws, ng, space->maxlevel, s)) { set_error("broad phase"); return 0; }
+    if (!launch_narrowphase(w->ws, maxc, 0, false, s)) { set_error("narrow phase"); return 0; }
+    w->device_contacts = true;
+    w->device_surfaces = 1;
+    group->device_world = w;
+    return 1;
+}
+
+// ------------------------------------------------------------------ joints
+dJointGroupID dJointGroupCreate(int) { return new dxJointGroup(); }
+void dJointGroupEmpty(dJointGroupID g) {
+    for (dxJoint *j : g->joints) {
+        dxWorld *w = j->world;
+        auto &v = w->joints;
+        for (size_t k = v.size(); k-- > 0;) if (v[k] == j) { v.erase(v.begin() + k); break; }
+        delete j;
+    }
+    g->joints.clear();
+    if (g->device_world) {
+        dxWorld *w = g->device_world;
+        w->device_contacts = false;
+        cudaMemsetAsync(&w->ws.dc->ncontacts, 0, 4, w->stream);
+        g->device_world = nullptr;
+    }
+}
+void dJointGroupDestroy(dJointGroupID g) {
+    dJointGroupEmpty(g);
+    delete g;
+}
+dJointID dJointCreateContact(dWorldID w, dJointGroupID group, const dContact *c) {
+    dxJoint *j = new dxJoint();
+    j->world = w;
+    j->group = group;
+    j->contact = *c;  // ode.cpp:1198 copies the contact
+    w->joints.push_back(j);
+    if (group) group->joints.push_back(j);
+    return j;
+}
+void dJointAttach(dJointID j, dBodyID body1, dBodyID body2) {
+    j->b1 = body1;
+    j->b2 = body2;
+    j->attached = body1 || body2;
+}
+void dJointDestroy(dJointID j) {
+    dxWorld *w = j->world;
+    auto &v = w->joints;
+    for (size_t k = 0; k < v.size(); k++) if (v[k] == j) { v.erase(v.begin() + k); break; }
+    if (j->group) {
+        auto &gv = j->group->joints;
+        for (size_t k = 0; k < gv.size(); k++) if (gv[k] == j) { gv.erase(gv.begin() + k); break; }
+    }
+    delete j;
+}
+void dJointSetFeedback(dJointID j, dJointFeedback *fb) { j->feedback = fb; }
+dJointFeedback *dJointGetFeedback(dJointID j) { return j->feedback; }
+dBodyID dJointGetBody(dJointID j, int index) {
+    // a joint attached with a null first body reports its only body as body 0 (ode.cpp:1403-1411)
+    dxBody *n0 = j->b1 ? j->b1 : j->b2, *n1 = j->b1 ? j->b2 : nullptr;
+    return index == 0 ? n0 : (index == 1 ? n1 : nullptr);
+}
+// ode.cpp dAreConnectedExcluding: contact joints are dJointTypeContact (4),
+// the only joint type of this subset
+int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type) {
+    if (!b1 || !b2 || joint_type == 4) return 0;
+    for (dxJoint *j : b1->world->joints)
+        if (j->attached && ((j->b1 == b1 && j->b2 == b2) || (j->b1 == b2 && j->b2 == b1))) return 1;
+    return 0;
+}
+
+// ------------------------------------------------------------------ stepping
+// joints/contact.cpp:49-122 getInfo1 on the host, for the island schedule
+static int host_contact_m(const dSurfaceParameters &s) {
+    int m = 1;
+    if (s.mode & dContactAxisDep) {
+        if (s.mu > 0) m++;
+        if (s.mu2 > 0) m++;
+        if (s.mode & dContactRolling) { if (!(s.rho < 0)) m++; if (!(s.rho2 < 0)) m++; if (!(s.rhoN < 0)) m++; }
+    } else {
+        if (s.mu > 0) m += 2;
+        if (s.mode & dContactRolling) { if (!(s.rho < 0)) m += 3; }
+    }
+    return m;
+}
+
+// util.cpp:724-860: islands by depth-first search from the newest body over
+// each body's joint list (newest attached first), as the reference orders
+// them, giving the row order of the reference-order solver.
+static void build_islands(dxWorld *w, const std::vector<dxJoint *> &js, const std::vector<int> &rstart,
+                          const std::vector<int> &mrows, IslandSchedule &sch) {
+    int nb = (int)w->bodies.size(), nj = (int)js.size();
+    std::vector<int> cnt(nb + 1, 0);
+    std::vector<int> n0(nj), n1(nj);
+    for (int k = 0; k < nj; k++) {
+        dxJoint *j = js[k];
+        int a = j->b1 ? j->b1->index : (j->b2 ? j->b2->index : -1);
+        int b = j->b1 ? (j->b2 ? j->b2->index : -1) : -1;
+        n0[k] = a; n1[k] = b;
+        if (a >= 0) cnt[a]++;
+        if (b >= 0) cnt[b]++;
+    }
+    std::vector<int> start(nb + 1, 0);
+    for (int i = 0; i < nb; i++) start[i + 1] = start[i] + cnt[i];
+    std::vector<int> lj(start[nb] + 1), lb(start[nb] + 1), fill(nb, 0);
+    for (int k = nj - 1; k >= 0; k--) {
+        int a = n0[k], b = n1[k];
+        if (a >= 0) { int p = start[a] + fill[a]++; lj[p] = k; lb[p] = b; }
+        if (b >= 0) { int p = start[b] + fill[b]++; lj[p] = k; lb[p] = a; }
+    }
+    std::vector<char> btag(nb, 0), jtag(nj, 0);
+    std::vector<int> stack, ib, ij;
+    sch.start.assign(1, 0);
+    sch.bstart.assign(1, 0);
+    for (int bb = nb - 1; bb >= 0; bb--) {
+        if (btag[bb]) continue;
+        btag[bb] = 1;
+        ib.assign(1, bb);
+        ij.clear();
+        stack.clear();
+        int b = bb;
+        for (;;) {
+            for (int p = start[b]; p < start[b + 1]; p++) {
+                int k = lj[p];
+                if (!jtag[k]) {
+                    jtag[k] = 1;
+                    ij.push_back(k);
+                    int nbody = lb[p];
+                    if (nbody >= 0 && !btag[nbody]) { btag[nbody] = 1; stack.push_back(nbody); }
+                }
+            }
+            if (stack.empty()) break;
+            b = stack.back();
+            stack.pop_back();
+            ib.push_back(b);
+        }
+        if (ij.empty()) continue;  // a lone body has no rows; it is integrated by the body pass
+        // ReorderPrep (quickstep.cpp:2329-2355): findex<0 rows first, each group in row order
+        std::vector<int> normals, frictions;
+        for (int k : ij) {
+            int r0 = rstart[k];
+            const dSurfaceParameters &s = js[k]->contact.surface;
+            for (int r = 0; r < mrows[k]; r++) {
+                bool fr = false;
+                if (r >= 1) {
+                    // friction rows carry findex under dContactApprox1_1/_2 (contact.cpp:257-293)
+                    int row = 1;
+                    float mu = s.mu > 0 ? s.mu : 0;
+                    float mu2 = (s.mode & dContactMu2) ? (s.mu2 > 0 ? s.mu2 : 0) : mu;
+                    int which = -1;
+                    if (mu > 0) { if (r == row) which = 1; row++; }
+                    if (mu2 > 0) { if (r == row) which = 2; row++; }
+                    if (which == 1) fr = (s.mode & dContactApprox1_1) != 0;
+                    else if (which == 2) fr = (s.mode & dContactApprox1_2) != 0;
+                    else if (s.mode & dContactRolling) {
+                        const int bits[3] = {dContactApprox1_1, dContactApprox1_2, dContactApprox1_N};
+                        float rho[3] = {s.rho, (s.mode & dContactAxisDep) ? s.rho2 : s.rho, (s.mode & dContactAxisDep) ? s.rhoN : s.rho};
+                        for (int q = 0; q < 3; q++)
+                            if (rho[q] > 0) { if (r == row) { fr = (s.mode & bits[q]) != 0; } row++; }
+                    }
+                }
+                (fr ? frictions : normals).push_back(r0 + r);
+            }
+        }
+        sch.order.insert(sch.order.end(), normals.begin(), normals.end());
+        sch.order.insert(sch.order.end(), frictions.begin(), frictions.end());
+        sch.start.push_back((int)sch.order.size());
+        sch.bodies.insert(sch.bodies.end(), ib.begin(), ib.end());
+        sch.bstart.push_back((int)sch.bodies.size());
+    }
+}
+
+static bool upload_host_contacts(dxWorld *w, const std::vector<dxJoint *> &js) {
+    int nc = (int)js.size();
+    Workspace &ws = w->ws;
+    if (ws.contact_cap < nc) {
+        if (!ws.contacts.ensure((size_t)nc * sizeof(Contact))) return false;
+        ws.contact_cap = nc;
+    }
+    if (!ws.surfaces.ensure((size_t)(nc > 0 ? nc : 1) * sizeof(Surface))) return false;
+    std::vector<Contact> C(nc);
+    std::vector<Surface> S(nc);
+    for (int k = 0; k < nc; k++) {
+        const dContact &c = js[k]->contact;
+        Contact &o = C[k];
+        o.pos_depth = make_float4(c.geom.pos[0], c.geom.pos[1], c.geom.pos[2], c.geom.depth);
+        o.normal = make_float4(c.geom.normal[0], c.geom.normal[1], c.geom.normal[2], 0.f);
+        o.b1 = js[k]->b1 ? js[k]->b1->index : -1;
+        o.b2 = js[k]->b2 ? js[k]->b2->index : -1;
+        o.surf = k;
+        o.slot = 0;
+        o.g1 = c.geom.g1 ? c.geom.g1->index : -1;
+        o.g2 = c.geom.g2 ? c.geom.g2->index : -1;
+        o.pad0 = o.pad1 = 0;
+        Surface &s = S[k];
+        memset(&s, 0, sizeof s);
+        const dSurfaceParameters &sp = c.surface;
+        s.mode = sp.mode; s.mu = sp.mu; s.mu2 = sp.mu2; s.rho = sp.rho; s.rho2 = sp.rho2; s.rhoN = sp.rhoN;
+        s.bounce = sp.bounce; s.bounce_vel = sp.bounce_vel; s.soft_erp = sp.soft_erp; s.soft_cfm = sp.soft_cfm;
+        s.motion1 = sp.motion1; s.motion2 = sp.motion2; s.motionN = sp.motionN; s.slip1 = sp.slip1; s.slip2 = sp.slip2;
+        s.fdir1[0] = c.fdir1[0]; s.fdir1[1] = c.fdir1[1]; s.fdir1[2] = c.fdir1[2];
+    }
+    cudaStream_t s = w->stream;
+    if (nc > 0) {
+        cudaMemcpyAsync(ws.contacts.p, C.data(), (size_t)nc * sizeof(Contact), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ws.surfaces.p, S.data(), (size_t)nc * sizeof(Surface), cudaMemcpyHostToDevice, s);
+    }
+    cudaMemcpyAsync(&ws.dc->ncontacts, &nc, 4, cudaMemcpyHostToDevice, s);
+    return cudaStreamSynchronize(s) == cudaSuccess;
+}
+
+int dWorldQuickStep(dWorldID w, dReal stepsize) {
+    if (!world_upload(w)) return 0;
+    Workspace &ws = w->ws;
+    SolverParams P = w->P;
+    P.dt = stepsize;
+    cudaStream_t s = w->stream;
+    // host-created contact joints (attached) in creation order
+    std::vector<dxJoint *> js;
+    js.reserve(w->joints.size());
+    for (dxJoint *j : w->joints) if (j->attached) js.push_back(j);
+    int nb = (int)w->bodies.size();
+    if (w->timing) cudaEventRecord(w->ev[2], s);
+    bool ok;
+    if (!js.empty() && w->device_contacts) {
+        set_error("dWorldQuickStep: a step mixes dJointCreateContact joints with gbodeSpaceCollideContacts contacts");
+        return 0;
+    }
+    if (!w->device_contacts) {
+        if (!upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
+    } else if (ws.contact_cap <= 0) {
+        ws.contacts.ensure(sizeof(Contact));
+        ws.contact_cap = 1;
+    }
+    if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
+    if (P.solver == GBODE_SOLVER_REFERENCE_ORDER && !w->device_contacts) {
+        int nc = (int)js.size();
+        std::vector<int> mrows(nc), rstart(nc + 1, 0);
+        for (int k = 0; k < nc; k++) {
+            mrows[k] = host_contact_m(js[k]->contact.surface);
+            rstart[k + 1] = rstart[k] + mrows[k];
+        }
+        IslandSchedule sch;
+        build_islands(w, js, rstart, mrows, sch);
+        ok = launch_quickstep_islands(ws, nb, P, sch, s, w->timing ? w->ev[0] : nullptr, w->timing ? w->ev[1] : nullptr);
+    } else {
+        ok = launch_quickstep(ws, nb, 1, P, s, w->timing ? w->ev[0] : nullptr, w->timing ? w->ev[1] : nullptr);
+    }
+    if (w->timing) cudaEventRecord(w->ev[3], s);
+    if (!ok) { set_error("dWorldQuickStep launch", cudaGetLastError()); return 0; }
+    w->host_valid = false;
+    w->stats_pending = true;
+    w->last_host_contacts = (int)js.size();
+    // joint feedback (quickstep.cpp:3108-3181): F = J^T lambda per contact
+    bool any_fb = false;
+    for (dxJoint *j : js) if (j->feedback) { any_fb = true; break; }
+    if (any_fb) {
+        std::vector<float> fb;
+        contact_feedback(ws, (int)js.size(), fb, s);
+        for (size_t k = 0; k < js.size(); k++) {
+            dJointFeedback *f = js[k]->feedback;
+            if (!f) continue;
+            const float *o = &fb[16 * k];
+            for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
+            f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
+        }
+    }
+    return 1;
+}
+
+// dWorldStep (the Dantzig LCP stepper, ode.cpp:1828-1845) is outside this
+// library's path; it runs the quickstep solver with a large iteration count.
+int dWorldStep(dWorldID w, dReal stepsize) {
+    int it = w->P.iterations;
+    w->P.iterations = 200;
+    int r = dWorldQuickStep(w, stepsize);
+    w->P.iterations = it;
+    return r;
+}
+
+void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
+    if (w->stats_pending) {
+        cudaMemcpyAsync(w->ws.hc, w->ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream);
+        cudaStreamSynchronize(w->stream);
+        const DevCounters &h = *w->ws.hc;
+        w->stats.contacts = h.ncontacts;
+        w->stats.rows = h.nrows;
+        w->stats.colours = h.ncolours;
+        w->stats.iterations = h.iterations;
+        w->stats.residual = h.resid;
+        w->stats.solve_ms = 0;
+        w->stats.step_ms = 0;
+        if (w->timing) {
+            cudaEventElapsedTime(&w->stats.solve_ms, w->ev[0], w->ev[1]);
+            cudaEventElapsedTime(&w->stats.step_ms, w->ev[2], w->ev[3]);
+        }
+        w->stats_pending = false;
+    }
+    *out = w->stats;
+}
+
+double gbodeWorldLastResidual(dWorldID w, double *complementarity, double *max_lambda) {
+    return last_residual(w->ws, (int)w->bodies.size(), complementarity, max_lambda, w->stream);
+}
+
+int gbodeWorldGetLastRows(dWorldID w, float *rows, int cap) { return copy_last_rows(w->ws, rows, cap, w->stream); }
+
+int gbodeWorldGetContacts(dWorldID w, float *out, int cap) {
+    if (!w->ws.dc) return 0;
+    int n = 0;
+    cudaMemcpyAsync(&n, &w->ws.dc->ncontacts, 4, cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    if (!out || cap <= 0 || n <= 0) return n;
+    int k = n < cap ? n : cap;
+    std::vector<Contact> C(k);
+    cudaMemcpyAsync(C.data(), w->ws.contacts.p, (size_t)k * sizeof(Contact), cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    for (int i = 0; i < k; i++) {
+        float *o = out + 12 * i;
+        o[0] = C[i].pos_depth.x; o[1] = C[i].pos_depth.y; o[2] = C[i].pos_depth.z;
+        o[3] = C[i].normal.x; o[4] = C[i].normal.y; o[5] = C[i].normal.z;
+        o[6] = C[i].pos_depth.w;
+        o[7] = (float)C[i].g1; o[8] = (float)C[i].g2; o[9] = (float)C[i].b1; o[10] = (float)C[i].b2;
+        o[11] = (float)C[i].slot;
+    }
+    return n;
+}
+
+}  // extern "C"
+
+// dBoxBox on the device through a one-pair narrow phase of two boxes
+extern "C" int dBoxBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2, const dMatrix3 R2,
+                       const dVector3 side2, dVector3 normal, dReal *depth, int *return_code, int flags,
+                       dContactGeom *contact, int skip) {
+    if (!g_default_world) g_default_world = dWorldCreate();
+    dxWorld *w = g_default_world;
+    if (!world_init_device(w)) return 0;
+    std::vector<GeomHost> gh(2);
+    const float *pp[2] = {p1, p2}, *RR[2] = {R1, R2}, *ss[2] = {side1, side2};
+    for (int k = 0; k < 2; k++) {
+        gh[k].cls = dBoxClass;
+        gh[k].body = -1;
+        gh[k].dims[0] = ss[k][0]; gh[k].dims[1] = ss[k][1]; gh[k].dims[2] = ss[k][2]; gh[k].dims[3] = 0;
+        memcpy(gh[k].pos, pp[k], 12);
+        gh[k].pos[3] = 0;
+        memcpy(gh[k].R, RR[k], 48);
+    }
+    if (!ensure_bodies(w->ws, 1) || !upload_geoms(w->ws, gh, w->stream)) return 0;
+    w->uploaded_space = nullptr;
+    launch_pose_aabb(w->ws, bodies_view(w->ws, 0), 2, -1000, 1000, w->stream);
+    int pr[2] = {0, 1};
+    std::vector<float> out;
+    std::vector<int> counts;
+    if (narrow_pairs_host(w->ws, pr, 1, flags & 0xffff, out, counts, w->stream) < 0) return 0;
+    int n = counts.empty() ? 0 : counts[0];
+    int code = 0;
+    cudaMemcpy(&code, w->ws.c_code.p, 4, cudaMemcpyDeviceToHost);
+    // dCollideBoxBox negates dBoxBox's normal (box.cpp:758-760); undo it here
+    for (int i = 0; i < n; i++) {
+        dContactGeom *c = (dContactGeom *)((char *)contact + (size_t)i * skip);
+        const float *o = &out[8 * i];
+        c->pos[0] = o[0]; c->pos[1] = o[1]; c->pos[2] = o[2];
+        c->depth = o[6];
+    }
+    if (n > 0) {
+        normal[0] = -out[3]; normal[1] = -out[4]; normal[2] = -out[5];
+        *depth = 0;
+        for (int i = 0; i < n; i++) if (out[8 * i + 6] > *depth) *depth = out[8 * i + 6];
+        *return_code = code;
+    }
+    return n;
+}

@@ -1,0 +1,140 @@
+// Host-side context shared by the C-ABI layer (api.cpp) and the kernel
+// launchers (collide.cu, solve.cu).  Device buffers are owned here and grown
+// on demand; every launcher enqueues on the world's stream without host syncs
+// unless its comment says otherwise.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "gbode_device.cuh"
+
+namespace gb {
+
+// Grow-only device buffer.
+struct DBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    bool ensure(size_t want);  // false on allocation failure
+    template <class T> T *as() const { return (T *)p; }
+    void release();
+};
+
+struct SolverParams {
+    float dt;
+    float gravity[3];
+    float erp, cfm, w;
+    float max_vel, min_depth;
+    int iterations;
+    // ODE dynamic iteration parameters (objects.h:451-475)
+    float premature_delta, extra_factor, extra_delta;
+    // residual-target mode
+    float residual_target;
+    int check_every, max_iterations;
+    int warm_mode;
+    float warm_scale;
+    int solver;  // GBODE_SOLVER_*
+};
+
+// Device-side scalars the kernels read and write (one pinned/device block).
+struct DevCounters {
+    int npairs;        // candidate pairs of the broad phase
+    int ncontacts;     // contacts
+    int nrows;         // constraint rows
+    int nmanifolds;    // contact groups
+    int ncolours;      // colours used
+    int iterations;    // sweeps performed
+    unsigned err;      // ERR_* bits
+    int uncoloured;    // colouring progress
+    float resid;       // last FP32 relative residual
+    float maxlam;      // last max |lambda|
+    int nbig;          // geoms in the big-box list
+    int maxlevel;      // coarsest hash level in use
+    int narrow_total;  // contacts produced by the last narrow phase
+    int cells_total;   // scan scratch (hash cells)
+    int colour_total;  // scan scratch (colours)
+    float racc[4];     // residual / max|lambda| accumulators, two parities
+    GridSync gsync;    // grid barrier state (zeroed before cooperative launches)
+};
+
+struct Workspace {
+    // geoms
+    DBuf g_cls, g_body, g_dims, g_spos, g_sR, g_pos, g_R, g_amin, g_amax, g_level, g_dblo, g_dbhi, g_big;
+    // broad phase
+    DBuf h_keys, h_count, h_start, h_fill, h_members, h_entry, p_count, p_start, pairs;
+    // narrow phase
+    DBuf c_slots, c_count, c_start, contacts, surfaces, c_mcount, c_rstart, c_code;
+    // bodies
+    DBuf b_pos, b_q, b_R, b_lvel, b_avel, b_facc, b_tacc, b_Ib, b_invIb, b_invIw, b_fc, b_rt, b_fa;
+    // rows
+    DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
+    // colouring / schedule
+    DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list;
+    // reference-order schedule
+    DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
+    // warm start cache (previous step)
+    DBuf w_keys, w_lambda, w_keys_prev, w_lambda_prev;
+    // residual
+    DBuf res_f, res_v;
+    // scan scratch
+    DBuf scan_tmp;
+    DevCounters *dc = nullptr;   // device counters
+    DevCounters *hc = nullptr;   // pinned host mirror
+    int pair_cap = 0, contact_cap = 0, row_cap = 0;
+    void release();
+};
+
+// ---- scan (scan.cu): exclusive prefix sum of n ints (n read from *n_dev if
+// non-null, else n_host), writing the total to *total_dev.
+void scan_exclusive(const int *in, int *out, const int *n_dev, int n_cap, int *total_dev, Workspace &ws,
+                    cudaStream_t s);
+
+// ---- collide.cu
+struct GeomHost {
+    int cls, body;
+    float dims[4];
+    float pos[4];
+    float R[12];
+};
+// upload geoms (class/body/dims/static pose) into the workspace
+bool upload_geoms(Workspace &ws, const std::vector<GeomHost> &g, cudaStream_t s);
+// pose geoms from bodies, AABBs, levels (one launch)
+void launch_pose_aabb(Workspace &ws, const Bodies &b, int ng, int minlevel, int maxlevel, cudaStream_t s);
+// hash-space broad phase into ws.pairs (device count in dc->npairs)
+bool launch_broadphase(Workspace &ws, int ng, int maxlevel_hint, cudaStream_t s);
+// narrow phase on the pair list; contacts compacted into ws.contacts with
+// surface index `surf`; codes (dBoxBox return_code, -1 n/a) optional per slot
+bool launch_narrowphase(Workspace &ws, int maxc, int surf, bool append, cudaStream_t s);
+// narrow phase on an explicit host pair list; results copied back (syncs)
+int narrow_pairs_host(Workspace &ws, const int *pairs, int np, int maxc, std::vector<float> &out,
+                      std::vector<int> &counts, cudaStream_t s);
+
+// ---- solve.cu
+Bodies bodies_view(Workspace &ws, int nb);
+bool ensure_bodies(Workspace &ws, int nb);
+bool ensure_rows(Workspace &ws, int ncontacts_cap);
+// full quickstep on the device contact list (count in dc->ncontacts)
+bool launch_quickstep(Workspace &ws, int nb, int nsurf, const SolverParams &P, cudaStream_t s,
+                      cudaEvent_t ev_solve0, cudaEvent_t ev_solve1);
+// reference-order quickstep with a host-built island schedule
+struct IslandSchedule {
+    std::vector<int> order;       // rows in island order, findex<0 rows first per island
+    std::vector<int> start;       // island row ranges [nisl+1]
+    std::vector<int> bodies;      // bodies per island in DFS order
+    std::vector<int> bstart;      // [nisl+1]
+    std::vector<int> normals;     // per island: count of findex<0 rows
+};
+bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, const IslandSchedule &sch,
+                              cudaStream_t s, cudaEvent_t ev_solve0, cudaEvent_t ev_solve1);
+// FP64 residual of the last step's rows (syncs)
+double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s);
+int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s);
+// per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
+void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
+
+// launch bookkeeping
+void count_launch(int n = 1);
+int num_sms();
+
+}  // namespace gb

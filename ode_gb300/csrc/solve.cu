@@ -1,0 +1,1061 @@
+// dWorldQuickStep on the device.
+//
+// Pipeline (reference stages in quickstep.cpp in brackets):
+//   k_bodies      gravity, world-frame inverse inertia, implicit gyroscopic
+//                 torque, rhs_tmp, fc = 0                  [Stage0_Bodies, 2b]
+//   k_contact_m   rows per contact                           [Stage0_Joints]
+//   k_rows        contact rows J/rhs/cfm/lo/hi/findex, J*rhs_tmp, invM J^T,
+//                 Ad scaling, lambda init -- one pass       [2a, 2c, 4a, iMJ, Ad]
+//   colouring     manifolds (runs of contacts on one body pair) get colours
+//                 such that no two of a colour share a body
+//   k_pgs         projected Gauss-Seidel: colours in sequence, the
+//                 manifolds of a colour in parallel; one persistent
+//                 cooperative launch with bounded grid barriers [4LCP]
+//   k_islands     the same relaxation in the reference's own row order, one
+//                 island per block (for lambda parity)      [4LCP, serial]
+//   k_integrate   v += h fc; v += h invM f_ext; x, q update; AABB-ready pose
+//                                                           [4b, 6a, 6b, util.cpp:583-692]
+#include <cooperative_groups.h>
+#include <math.h>
+
+#include "gbode_internal.h"
+
+namespace gb {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ void load_rows3(const float4 *R3, float *m) {
+    for (int r = 0; r < 3; r++) {
+        float4 v = R3[r];
+        m[4 * r] = v.x; m[4 * r + 1] = v.y; m[4 * r + 2] = v.z; m[4 * r + 3] = 0;
+    }
+}
+__device__ __forceinline__ void store_rows3(float4 *R3, const float *m) {
+    for (int r = 0; r < 3; r++) R3[r] = make_float4(m[4 * r], m[4 * r + 1], m[4 * r + 2], 0.f);
+}
+__device__ __forceinline__ float d41(const float *a, const float *b) { return a[0] * b[0] + a[4] * b[1] + a[8] * b[2]; }
+// dMultiply0_331
+__device__ __forceinline__ void mul0_331(float *r, const float *a, const float *b) {
+    float r0 = dot3(a, b), r1 = dot3(a + 4, b), r2 = dot3(a + 8, b);
+    r[0] = r0; r[1] = r1; r[2] = r2;
+}
+// dMultiply0_333: row i of a times b
+__device__ __forceinline__ void mul0_333(float *r, const float *a, const float *b) {
+    for (int i = 0; i < 3; i++) {
+        float t0 = d41(b, a + 4 * i), t1 = d41(b + 1, a + 4 * i), t2 = d41(b + 2, a + 4 * i);
+        r[4 * i] = t0; r[4 * i + 1] = t1; r[4 * i + 2] = t2; r[4 * i + 3] = 0;
+    }
+}
+// dMultiply2_333: a * b^T
+__device__ __forceinline__ void mul2_333(float *r, const float *a, const float *b) {
+    for (int i = 0; i < 3; i++) {
+        float t0 = dot3(b, a + 4 * i), t1 = dot3(b + 4, a + 4 * i), t2 = dot3(b + 8, a + 4 * i);
+        r[4 * i] = t0; r[4 * i + 1] = t1; r[4 * i + 2] = t2; r[4 * i + 3] = 0;
+    }
+}
+__device__ __forceinline__ void cross3(float *r, const float *a, const float *b) {
+    float r0 = a[1] * b[2] - a[2] * b[1], r1 = a[2] * b[0] - a[0] * b[2], r2 = a[0] * b[1] - a[1] * b[0];
+    r[0] = r0; r[1] = r1; r[2] = r2;
+}
+
+// ------------------------------------------------------------------ bodies
+// quickstep.cpp:1176-1306 (Stage0_Bodies) and :1644-1690 (Stage2b)
+__global__ void k_bodies(Bodies B, SolverParams P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.n) return;
+    const float h = P.dt;
+    float4 lv = B.lvel[i], av = B.avel[i], fa = B.facc[i], ta = B.tacc[i], ps = B.pos[i];
+    const float mass = lv.w, invMass = ps.w;
+    int flags = __float_as_int(av.w);
+    float facc[3] = {fa.x, fa.y, fa.z}, tacc[3] = {ta.x, ta.y, ta.z};
+    // gravity: added per axis only when that component is non-zero
+    if (P.gravity[0]) facc[0] += mass * P.gravity[0];
+    if (P.gravity[1]) facc[1] += mass * P.gravity[1];
+    if (P.gravity[2]) facc[2] += mass * P.gravity[2];
+    float R[12], invIb[12], tmp[12], invIw[12];
+    load_rows3(B.R + 3 * i, R);
+    load_rows3(B.invIb + 3 * i, invIb);
+    mul2_333(tmp, invIb, R);
+    mul0_333(invIw, R, tmp);
+    float avel[3] = {av.x, av.y, av.z};
+    if ((flags & 1) && invMass > 0) {
+        float Ib[12], I[12];
+        load_rows3(B.Ib + 3 * i, Ib);
+        mul2_333(tmp, Ib, R);
+        mul0_333(I, R, tmp);
+        float L[3];
+        mul0_331(L, I, avel);
+        float It[12] = {0, L[2], -L[1], 0, -L[2], 0, L[0], 0, L[1], -L[0], 0, 0};
+        for (int k = 0; k < 12; ++k) It[k] = It[k] * h + I[k];
+        float rh = 1.0f / h;
+        L[0] *= rh; L[1] *= rh; L[2] *= rh;
+        // dInvertMatrix3 (odemath.h:463-500)
+        float det = It[0] * (It[5] * It[10] - It[9] * It[6]) - It[1] * (It[4] * It[10] - It[8] * It[6]) +
+                    It[2] * (It[4] * It[9] - It[8] * It[5]);
+        if (det != 0) {
+            float r = 1.0f / det, iv[12];
+            iv[0] = (It[5] * It[10] - It[6] * It[9]) * r;
+            iv[1] = (It[9] * It[2] - It[1] * It[10]) * r;
+            iv[2] = (It[1] * It[6] - It[5] * It[2]) * r;
+            iv[4] = (It[6] * It[8] - It[4] * It[10]) * r;
+            iv[5] = (It[0] * It[10] - It[8] * It[2]) * r;
+            iv[6] = (It[4] * It[2] - It[0] * It[6]) * r;
+            iv[8] = (It[4] * It[9] - It[8] * It[5]) * r;
+            iv[9] = (It[8] * It[1] - It[0] * It[9]) * r;
+            iv[10] = (It[0] * It[5] - It[1] * It[4]) * r;
+            iv[3] = iv[7] = iv[11] = 0;
+            mul0_333(It, I, iv);
+            It[0] -= 1; It[5] -= 1; It[10] -= 1;
+            float tau[3];
+            mul0_331(tau, It, L);
+            tacc[0] = tacc[0] + tau[0]; tacc[1] = tacc[1] + tau[1]; tacc[2] = tacc[2] + tau[2];
+        }
+    }
+    B.facc[i] = make_float4(facc[0], facc[1], facc[2], 0.f);
+    B.tacc[i] = make_float4(tacc[0], tacc[1], tacc[2], 0.f);
+    store_rows3(B.invIw + 3 * i, invIw);
+    const float rh = 1.0f / h;
+    float rl[3], ra[3];
+    rl[0] = -(facc[0] * invMass + lv.x * rh);
+    rl[1] = -(facc[1] * invMass + lv.y * rh);
+    rl[2] = -(facc[2] * invMass + lv.z * rh);
+    mul0_331(ra, invIw, tacc);
+    ra[0] = -(avel[0] * rh) - ra[0];
+    ra[1] = -(avel[1] * rh) - ra[1];
+    ra[2] = -(avel[2] * rh) - ra[2];
+    B.rt[2 * i] = make_float4(rl[0], rl[1], rl[2], 0.f);
+    B.rt[2 * i + 1] = make_float4(ra[0], ra[1], ra[2], 0.f);
+    B.fc[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    B.fc[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------------------------------ rows
+// joints/contact.cpp:49-122 getInfo1 (mu < 0 is treated as 0)
+__device__ __forceinline__ int contact_m(const Surface &s) {
+    int m = 1;
+    if (s.mode & 0x001) {
+        if (s.mu > 0) m++;
+        if (s.mu2 > 0) m++;
+        if (s.mode & 0x400) { if (!(s.rho < 0)) m++; if (!(s.rho2 < 0)) m++; if (!(s.rhoN < 0)) m++; }
+    } else {
+        if (s.mu > 0) m += 2;
+        if (s.mode & 0x400) { if (!(s.rho < 0)) m += 3; }
+    }
+    return m;
+}
+
+__global__ void k_contact_m(const Contact *C, const Surface *S, const int *nc_dev, int *mcount) {
+    int nc = *nc_dev;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        mcount[c] = contact_m(S[C[c].surf]);
+    }
+}
+
+__global__ void k_rows_total(DevCounters *dc, int row_cap) {
+    if (dc->nrows > row_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); dc->nrows = row_cap; }
+}
+
+// Contact rows: getInfo2 (contact.cpp:126-347) + Stage2a scaling (quickstep.cpp
+// :1555-1561) + Stage2c J*rhs_tmp (:1022-1055) + compute_invM_JT (:858-897) +
+// Ad scaling (:2251-2316) for each of the contact's rows.
+__global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, const int *rstart, Bodies B,
+                       Rows Rw, SolverParams P, int dyn_maxabs, const float *warm, DevCounters *dc) {
+    const int nc = *nc_dev;
+    const float h = P.dt, rh = 1.0f / h;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const Contact k = C[c];
+        Surface s = S[k.surf];
+        const int m = contact_m(s);
+        int r0 = rstart[c];
+        if (r0 + m > Rw.n_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); continue; }
+        // dJointAttach: a missing first body moves the second into slot 0
+        int n0 = k.b1, n1 = k.b2, reverse = 0;
+        if (n0 < 0) { n0 = k.b2; n1 = -1; reverse = 1; }
+        float J[6][16];
+        int findex[6];
+        for (int r = 0; r < m; r++) {
+            for (int q = 0; q < 16; q++) J[r][q] = 0.f;
+            J[r][7] = P.cfm; J[r][14] = -INFINITY; J[r][15] = INFINITY;
+            findex[r] = -1;
+        }
+        const int mode = s.mode;
+        float erp = (mode & 0x008) ? s.soft_erp : P.erp;
+        float kk = rh * erp;
+        float depth = k.pos_depth.w - P.min_depth;
+        if (depth < 0) depth = 0;
+        float motionN = (mode & 0x080) ? s.motionN : 0.0f;
+        const float pushout = kk * depth + motionN;
+        bool bounce = (mode & 0x004) != 0 && s.bounce_vel >= 0;
+        float outgoing = 0;
+        float cval = pushout > P.max_vel ? P.max_vel : pushout;
+        float normal[3] = {k.normal.x, k.normal.y, k.normal.z};
+        if (reverse) { normal[0] = -normal[0]; normal[1] = -normal[1]; normal[2] = -normal[2]; }
+        float cpos[3] = {k.pos_depth.x, k.pos_depth.y, k.pos_depth.z};
+        float c1[3], c2[3] = {0, 0, 0};
+        if (n1 >= 0) {
+            float4 p1 = B.pos[n1];
+            c2[0] = cpos[0] - p1.x; c2[1] = cpos[1] - p1.y; c2[2] = cpos[2] - p1.z;
+            J[0][8] = -normal[0]; J[0][9] = -normal[1]; J[0][10] = -normal[2];
+            cross3(&J[0][11], normal, c2);
+            if (bounce) {
+                float4 av = B.avel[n1], lv = B.lvel[n1];
+                float a3[3] = {av.x, av.y, av.z}, l3[3] = {lv.x, lv.y, lv.z};
+                outgoing = dot3(&J[0][11], a3) - dot3(normal, l3);
+            }
+        }
+        {
+            float4 p0 = B.pos[n0];
+            c1[0] = cpos[0] - p0.x; c1[1] = cpos[1] - p0.y; c1[2] = cpos[2] - p0.z;
+            J[0][0] = normal[0]; J[0][1] = normal[1]; J[0][2] = normal[2];
+            cross3(&J[0][3], c1, normal);
+            if (bounce) {
+                float4 av = B.avel[n0], lv = B.lvel[n0];
+                float a3[3] = {av.x, av.y, av.z}, l3[3] = {lv.x, lv.y, lv.z};
+                outgoing += dot3(&J[0][3], a3) + dot3(normal, l3);
+            }
+        }
+        if (bounce) {
+            float neg = motionN - outgoing;
+            if (neg > s.bounce_vel) {
+                float newc = s.bounce * neg + motionN;
+                if (newc > cval) cval = newc;
+            }
+        }
+        J[0][6] = cval;
+        if (mode & 0x010) J[0][7] = s.soft_cfm;
+        J[0][14] = 0; J[0][15] = INFINITY;
+        if (m > 1) {
+            float t1[3], t2[3];
+            if (mode & 0x002) {
+                t1[0] = s.fdir1[0]; t1[1] = s.fdir1[1]; t1[2] = s.fdir1[2];
+                cross3(t2, normal, t1);
+            } else if (fabsf(normal[2]) > 0.7071067811865476f) {
+                // odemath.cpp:224-251 dxPlaneSpace
+                float a = normal[1] * normal[1] + normal[2] * normal[2];
+                float kq = 1.0f / sqrtf(a);
+                t1[0] = 0; t1[1] = -normal[2] * kq; t1[2] = normal[1] * kq;
+                t2[0] = a * kq; t2[1] = -normal[0] * t1[2]; t2[2] = normal[0] * t1[1];
+            } else {
+                float a = normal[0] * normal[0] + normal[1] * normal[1];
+                float kq = 1.0f / sqrtf(a);
+                t1[0] = -normal[1] * kq; t1[1] = normal[0] * kq; t1[2] = 0;
+                t2[0] = -normal[2] * t1[1]; t2[1] = normal[2] * t1[0]; t2[2] = a * kq;
+            }
+            int row = 1;
+            const float mu = s.mu > 0 ? s.mu : 0.f;
+            if (mu > 0) {
+                float *r = J[row];
+                r[0] = t1[0]; r[1] = t1[1]; r[2] = t1[2];
+                cross3(r + 3, c1, t1);
+                if (n1 >= 0) { r[8] = -t1[0]; r[9] = -t1[1]; r[10] = -t1[2]; cross3(r + 11, t1, c2); }
+                if (mode & 0x020) r[6] = s.motion1;
+                if (mode & 0x100) r[7] = s.slip1;
+                r[14] = -mu; r[15] = mu;
+                if (mode & 0x1000) findex[row] = 0;
+                ++row;
+            }
+            const float mu2 = (mode & 0x001) ? (s.mu2 > 0 ? s.mu2 : 0.f) : mu;
+            if (mu2 > 0) {
+                float *r = J[row];
+                r[0] = t2[0]; r[1] = t2[1]; r[2] = t2[2];
+                cross3(r + 3, c1, t2);
+                if (n1 >= 0) { r[8] = -t2[0]; r[9] = -t2[1]; r[10] = -t2[2]; cross3(r + 11, t2, c2); }
+                if (mode & 0x040) r[6] = s.motion2;
+                if (mode & 0x200) r[7] = s.slip2;
+                r[14] = -mu2; r[15] = mu2;
+                if (mode & 0x2000) findex[row] = 0;
+                ++row;
+            }
+            if (mode & 0x400) {
+                float rho[3] = {s.rho, (mode & 0x001) ? s.rho2 : s.rho, (mode & 0x001) ? s.rhoN : s.rho};
+                const int bits[3] = {0x1000, 0x2000, 0x4000};
+                const float *ax[3] = {t1, t2, normal};
+                for (int q = 0; q < 3 && row < m; q++) {
+                    if (rho[q] > 0) {
+                        float *r = J[row];
+                        r[3] = ax[q][0]; r[4] = ax[q][1]; r[5] = ax[q][2];
+                        if (n1 >= 0) { r[11] = -ax[q][0]; r[12] = -ax[q][1]; r[13] = -ax[q][2]; }
+                        r[14] = -rho[q]; r[15] = rho[q];
+                        if (mode & bits[q]) findex[row] = 0;
+                        ++row;
+                    }
+                    // rho == 0 is counted by getInfo1 but not written by getInfo2: the
+                    // row stays as initialised (zero J, unbounded) at the end of the block
+                }
+            }
+        }
+        // per-row finishing
+        float4 rt0l = B.rt[2 * n0], rt0a = B.rt[2 * n0 + 1];
+        float4 rt1l = make_float4(0, 0, 0, 0), rt1a = rt1l;
+        if (n1 >= 0) { rt1l = B.rt[2 * n1]; rt1a = B.rt[2 * n1 + 1]; }
+        float I0[12], I1[12];
+        load_rows3(B.invIw + 3 * n0, I0);
+        const float im0 = B.pos[n0].w;
+        float im1 = 0.f;
+        if (n1 >= 0) { load_rows3(B.invIw + 3 * n1, I1); im1 = B.pos[n1].w; }
+        for (int r = 0; r < m; r++) {
+            float *j = J[r];
+            j[6] *= rh; j[7] *= rh;
+            float in0[6] = {rt0l.x, rt0l.y, rt0l.z, rt0a.x, rt0a.y, rt0a.z};
+            float sum = 0.f;
+            for (int q = 0; q < 6; q++) sum += j[q] * in0[q];
+            if (n1 >= 0) {
+                float in1[6] = {rt1l.x, rt1l.y, rt1l.z, rt1a.x, rt1a.y, rt1a.z};
+                for (int q = 0; q < 6; q++) sum += j[8 + q] * in1[q];
+            }
+            j[6] += sum;
+            float M1[7], M2[7] = {0, 0, 0, 0, 0, 0, 0};
+            M1[0] = im0 * j[0]; M1[1] = im0 * j[1]; M1[2] = im0 * j[2];
+            mul0_331(M1 + 3, I0, j + 3);
+            M1[6] = 0;
+            if (dyn_maxabs) { float mx = fabsf(M1[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M1[q])); M1[6] = mx; }
+            if (n1 >= 0) {
+                M2[0] = im1 * j[8]; M2[1] = im1 * j[9]; M2[2] = im1 * j[10];
+                mul0_331(M2 + 3, I1, j + 11);
+                if (dyn_maxabs) { float mx = fabsf(M2[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M2[q])); M2[6] = mx; }
+            }
+            float sumA = 0.f;
+            for (int q = 0; q < 6; q++) sumA += M1[q] * j[q];
+            if (n1 >= 0) for (int q = 0; q < 6; q++) sumA += M2[q] * j[8 + q];
+            const float cfm_i = j[7];
+            const float Ad = P.w / (sumA + cfm_i);
+            const int gr = r0 + r;
+            Rw.Ad[gr] = Ad;
+            float jc = cfm_i * Ad, jr = j[6] * Ad;
+            float s1[6], s2[6];
+            for (int q = 0; q < 6; q++) s1[q] = j[q] * Ad;
+            for (int q = 0; q < 6; q++) s2[q] = (n1 >= 0) ? j[8 + q] * Ad : j[8 + q];
+            Rw.J1l[gr] = make_float4(s1[0], s1[1], s1[2], jr);
+            Rw.J1a[gr] = make_float4(s1[3], s1[4], s1[5], jc);
+            Rw.J2l[gr] = make_float4(s2[0], s2[1], s2[2], j[14]);
+            Rw.J2a[gr] = make_float4(s2[3], s2[4], s2[5], j[15]);
+            Rw.M1l[gr] = make_float4(M1[0], M1[1], M1[2], M1[6]);
+            Rw.M1a[gr] = make_float4(M1[3], M1[4], M1[5], 0.f);
+            Rw.M2l[gr] = make_float4(M2[0], M2[1], M2[2], M2[6]);
+            Rw.M2a[gr] = make_float4(M2[3], M2[4], M2[5], 0.f);
+            Rw.findex[gr] = findex[r] >= 0 ? r0 + findex[r] : -1;
+            Rw.body[gr] = make_int2(n0, n1);
+            Rw.contact[gr] = c;
+            Rw.lambda[gr] = warm ? warm[gr] : 0.f;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ manifolds + colouring
+// A manifold is a maximal run of consecutive contacts on the same body pair;
+// its rows are relaxed by one thread in sequence, so manifolds, not rows, are
+// what the colouring separates.
+__global__ void k_manifold_heads(const Contact *C, const int *nc_dev, int *head) {
+    int nc = *nc_dev;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        int h = 1;
+        if (c > 0) {
+            const Contact a = C[c - 1], b = C[c];
+            int a0 = a.b1 >= 0 ? a.b1 : a.b2, a1 = a.b1 >= 0 ? a.b2 : -1;
+            int b0 = b.b1 >= 0 ? b.b1 : b.b2, b1 = b.b1 >= 0 ? b.b2 : -1;
+            h = !(a0 == b0 && a1 == b1);
+        }
+        head[c] = h;
+    }
+}
+__global__ void k_manifold_starts(const int *nc_dev, const int *head, const int *mid, int *mstart, DevCounters *dc) {
+    int nc = *nc_dev;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        if (head[c]) mstart[mid[c]] = c;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) mstart[dc->nmanifolds] = nc;
+}
+
+#define GB_MAX_COLOURS 128
+// Speculative first-fit colouring (rounds of: pick the lowest colour free at
+// both bodies; per (body, colour) the lowest manifold index wins; losers
+// retry).  One cooperative launch; every barrier is bounded.
+__global__ void k_colour(const Contact *C, const int *mstart, DevCounters *dc, unsigned long long *mask, int *claim,
+                         int *colour, int *tent, int nb) {
+    unsigned gen = 0;
+    const int nm = dc->nmanifolds;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (int e = tid; e < nm; e += nth) colour[e] = -1;
+    for (int round = 0; round < 4 * GB_MAX_COLOURS; round++) {
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        if (tid == 0) dc->uncoloured = 0;
+        // phase A: tentative colour + claim
+        for (int e = tid; e < nm; e += nth) {
+            if (colour[e] >= 0) continue;
+            const Contact k = C[mstart[e]];
+            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            unsigned long long m0 = __ldcg(&mask[2 * n0]), m0b = __ldcg(&mask[2 * n0 + 1]);
+            unsigned long long m1 = 0, m1b = 0;
+            if (n1 >= 0) { m1 = __ldcg(&mask[2 * n1]); m1b = __ldcg(&mask[2 * n1 + 1]); }
+            unsigned long long lo = m0 | m1, hi = m0b | m1b;
+            int c;
+            if (~lo) c = __ffsll(~lo) - 1;
+            else if (~hi) c = 64 + __ffsll(~hi) - 1;
+            else { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); c = GB_MAX_COLOURS - 1; }
+            tent[e] = c;
+            atomicMin(&claim[n0 * GB_MAX_COLOURS + c], e);
+            if (n1 >= 0) atomicMin(&claim[n1 * GB_MAX_COLOURS + c], e);
+        }
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        // phase B: winners commit
+        for (int e = tid; e < nm; e += nth) {
+            if (colour[e] >= 0) continue;
+            const Contact k = C[mstart[e]];
+            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            int c = tent[e];
+            bool win = __ldcg(&claim[n0 * GB_MAX_COLOURS + c]) == e &&
+                       (n1 < 0 || __ldcg(&claim[n1 * GB_MAX_COLOURS + c]) == e);
+            if (win) {
+                colour[e] = c;
+                unsigned long long bit = 1ull << (c & 63);
+                atomicOr(&mask[2 * n0 + (c >> 6)], bit);
+                if (n1 >= 0) atomicOr(&mask[2 * n1 + (c >> 6)], bit);
+                atomicMax(&dc->ncolours, c + 1);
+            }
+        }
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        // phase C: losers release claims they still hold
+        for (int e = tid; e < nm; e += nth) {
+            if (colour[e] >= 0) continue;
+            const Contact k = C[mstart[e]];
+            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            int c = tent[e];
+            atomicCAS(&claim[n0 * GB_MAX_COLOURS + c], e, 0x7fffffff);
+            if (n1 >= 0) atomicCAS(&claim[n1 * GB_MAX_COLOURS + c], e, 0x7fffffff);
+            atomicAdd(&dc->uncoloured, 1);
+        }
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        if (__ldcg(&dc->uncoloured) == 0) break;
+        if (round == 4 * GB_MAX_COLOURS - 1 && tid == 0) atomicOr(&dc->err, ERR_COLOUR_OVERFLOW);
+    }
+}
+
+__global__ void k_colour_count(const int *colour, DevCounters *dc, int *ccount) {
+    int nm = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nm; e += gridDim.x * blockDim.x) {
+        int c = colour[e];
+        if (c >= 0) atomicAdd(&ccount[c], 1);
+    }
+}
+__global__ void k_colour_fill(const int *colour, DevCounters *dc, const int *cstart, int *cfill, int *list) {
+    int nm = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nm; e += gridDim.x * blockDim.x) {
+        int c = colour[e];
+        if (c < 0) continue;
+        list[cstart[c] + atomicAdd(&cfill[c], 1)] = e;
+    }
+}
+
+// ------------------------------------------------------------------ PGS row update
+// quickstep.cpp:2917-3033 Stage4LCP_IterationStep for one row, with the body
+// accumulators held by the caller.
+__device__ __forceinline__ void relax_row(const Rows &Rw, int r, float4 &f1l, float4 &f1a, float4 &f2l, float4 &f2a,
+                                          bool two) {
+    const float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
+    const float old = Rw.lambda[r];
+    float delta = j1l.w - old * j1a.w;
+    delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
+    if (two) delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
+    float lo, hi;
+    const int fi = Rw.findex[r];
+    if (fi >= 0) { hi = fabsf(j2a.w * Rw.lambda[fi]); lo = -hi; }
+    else { hi = j2a.w; lo = j2l.w; }
+    float nl = old + delta;
+    if (nl < lo) { delta = lo - old; nl = lo; }
+    else if (nl > hi) { delta = hi - old; nl = hi; }
+    Rw.lambda[r] = nl;
+    if (delta != 0) {
+        const float4 m1l = Rw.M1l[r], m1a = Rw.M1a[r];
+        f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
+        f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
+        if (two) {
+            const float4 m2l = Rw.M2l[r], m2a = Rw.M2a[r];
+            f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
+            f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
+        }
+    }
+}
+
+// natural-map residual of one row at the current fc (no update)
+__device__ __forceinline__ float row_residual(const Rows &Rw, const float4 *fc, int r, float w_sor) {
+    const float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
+    const int2 b = Rw.body[r];
+    const float lam = Rw.lambda[r];
+    const float4 f1l = ldcg4(&fc[2 * b.x]), f1a = ldcg4(&fc[2 * b.x + 1]);
+    float delta = j1l.w - lam * j1a.w;
+    delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
+    if (b.y >= 0) {
+        const float4 f2l = ldcg4(&fc[2 * b.y]), f2a = ldcg4(&fc[2 * b.y + 1]);
+        delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
+    }
+    float lo, hi;
+    const int fi = Rw.findex[r];
+    if (fi >= 0) { hi = fabsf(j2a.w * Rw.lambda[fi]); lo = -hi; }
+    else { hi = j2a.w; lo = j2l.w; }
+    float t = lam + delta / w_sor;
+    t = fminf(fmaxf(t, lo), hi);
+    return fabsf(lam - t);
+}
+
+struct PgsArgs {
+    Rows Rw;
+    float4 *fc;
+    const Contact *C;
+    const int *rstart, *mcount, *mstart, *clist, *cstart, *ccount;
+    DevCounters *dc;
+    int iterations, max_iterations, check_every;
+    float target, w_sor;
+};
+
+__device__ __forceinline__ float atomic_max_pos(float *addr, float v) {
+    return __int_as_float(atomicMax((int *)addr, __float_as_int(v)));
+}
+
+// One manifold: normal (findex < 0) rows of all its contacts first, then the
+// friction rows, mirroring the reference's findex partition.
+__device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
+    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
+    const int r0 = A.rstart[c0];
+    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
+    const int2 b = A.Rw.body[r0];
+    const bool two = b.y >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * b.x]), f1a = ldcg4(&A.fc[2 * b.x + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (two) { f2l = ldcg4(&A.fc[2 * b.y]); f2a = ldcg4(&A.fc[2 * b.y + 1]); }
+    for (int r = r0; r < r1; r++)
+        if (A.Rw.findex[r] < 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+    for (int r = r0; r < r1; r++)
+        if (A.Rw.findex[r] >= 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+    stcg4(&A.fc[2 * b.x], f1l); stcg4(&A.fc[2 * b.x + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * b.y], f2l); stcg4(&A.fc[2 * b.y + 1], f2a); }
+}
+
+__global__ void k_pgs(PgsArgs A) {
+    unsigned gen = 0;
+    DevCounters *dc = A.dc;
+    const int ncol = dc->ncolours;
+    const int nrows = dc->nrows;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const bool residual_mode = A.target > 0;
+    const int itmax = residual_mode ? A.max_iterations : A.iterations;
+    int it = 0, check = 0;
+    float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
+    for (; it < itmax;) {
+        for (int c = 0; c < ncol; c++) {
+            const int s = A.cstart[c], n = A.ccount[c];
+            for (int k = tid; k < n; k += nth) relax_manifold(A, A.clist[s + k]);
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        }
+        ++it;
+        if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
+            float *acc = slots + 2 * (check & 1);
+            float rmax = 0.f, lmax = 0.f;
+            for (int r = tid; r < nrows; r += nth) {
+                rmax = fmaxf(rmax, row_residual(A.Rw, A.fc, r, A.w_sor));
+                lmax = fmaxf(lmax, fabsf(A.Rw.lambda[r]));
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+                lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            }
+            if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
+            const float rel = rr / fmaxf(1.0f, ll);
+            if (tid == 0) {
+                float *other = slots + 2 * ((check + 1) & 1);
+                other[0] = 0.f; other[1] = 0.f;
+                dc->resid = rel; dc->maxlam = ll;
+            }
+            ++check;
+            if (rel <= A.target) break;
+        }
+    }
+    if (tid == 0) dc->iterations = it;
+}
+
+// ------------------------------------------------------------------ reference-order islands
+// One block per island, rows relaxed by thread 0 in the reference's order
+// (island joint order, findex<0 rows first: quickstep.cpp:2329-2355), with
+// the reference's dynamic iteration rule per island (quickstep.cpp:1823-1856,
+// :3253-3285) when enabled.
+struct IslandArgs {
+    Rows Rw;
+    float4 *fc;
+    float *fa;  // [2*nb] force max adjustments (negative, positive)
+    const int *order, *start, *bodies, *bstart;
+    int iterations;
+    unsigned max_extra;
+    float premature, extra_delta;
+    int dyn;
+    DevCounters *dc;
+};
+
+__global__ void k_islands(IslandArgs A) {
+    const int isl = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    const int r0 = A.start[isl], r1 = A.start[isl + 1];
+    const int b0 = A.bstart[isl], b1 = A.bstart[isl + 1];
+    if (r1 == r0) return;
+    for (int k = b0; k < b1; k++) { int bd = A.bodies[k]; A.fa[2 * bd] = 0.f; A.fa[2 * bd + 1] = 0.f; }
+    float premature = A.premature;
+    unsigned iteration = 0, extra = 0;
+    for (;;) {
+        for (int k = r0; k < r1; k++) {
+            const int r = A.order[k];
+            const int2 b = A.Rw.body[r];
+            const bool two = b.y >= 0;
+            float4 f1l = A.fc[2 * b.x], f1a = A.fc[2 * b.x + 1];
+            float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+            if (two) { f2l = A.fc[2 * b.y]; f2a = A.fc[2 * b.y + 1]; }
+            const float old = A.Rw.lambda[r];
+            const float4 j1l = A.Rw.J1l[r], j1a = A.Rw.J1a[r], j2l = A.Rw.J2l[r], j2a = A.Rw.J2a[r];
+            float delta = j1l.w - old * j1a.w;
+            delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
+            if (two) delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
+            float lo, hi;
+            const int fi = A.Rw.findex[r];
+            if (fi >= 0) { hi = fabsf(j2a.w * A.Rw.lambda[fi]); lo = -hi; }
+            else { hi = j2a.w; lo = j2l.w; }
+            float nl = old + delta;
+            if (nl < lo) { delta = lo - old; nl = lo; }
+            else if (nl > hi) { delta = hi - old; nl = hi; }
+            A.Rw.lambda[r] = nl;
+            if (delta != 0) {
+                const float4 m1l = A.Rw.M1l[r], m1a = A.Rw.M1a[r];
+                const int pos = delta > 0;
+                f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
+                f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
+                A.fc[2 * b.x] = f1l; A.fc[2 * b.x + 1] = f1a;
+                A.fa[2 * b.x + pos] += delta * m1l.w;
+                if (two) {
+                    const float4 m2l = A.Rw.M2l[r], m2a = A.Rw.M2a[r];
+                    A.fa[2 * b.y + pos] += delta * m2l.w;
+                    f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
+                    f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
+                    A.fc[2 * b.y] = f2l; A.fc[2 * b.y + 1] = f2a;
+                }
+            }
+        }
+        ++iteration;
+        if (iteration - extra == (unsigned)A.iterations) {
+            if (extra != 0 || A.max_extra == 0) break;
+            extra = A.max_extra;
+            premature = A.extra_delta;
+        }
+        if (A.dyn) {
+            bool hit = false;
+            if (premature == 0) {
+                for (int k = b0; k < b1; k++) { int bd = A.bodies[k]; A.fa[2 * bd] = 0; A.fa[2 * bd + 1] = 0; }
+                hit = true;
+            } else {
+                for (int k = b0; k < b1; k++) {
+                    int bd = A.bodies[k];
+                    if (!(A.fa[2 * bd + 1] < premature) || !(-A.fa[2 * bd] < premature)) {
+                        for (int q = k; q < b1; q++) { int bq = A.bodies[q]; A.fa[2 * bq] = 0; A.fa[2 * bq + 1] = 0; }
+                        hit = true;
+                        break;
+                    }
+                    A.fa[2 * bd] = 0; A.fa[2 * bd + 1] = 0;
+                }
+            }
+            if (!hit) break;
+        }
+        if (iteration > 100000u) break;
+    }
+    atomicMax(&A.dc->iterations, (int)iteration);
+}
+
+// ------------------------------------------------------------------ integration
+// quickstep.cpp:3082-3182 (Stage4b velocity), :3299-3337 (Stage6a),
+// :3409-3439 + util.cpp:583-692 (Stage6b, dxStepBody)
+__global__ void k_integrate(Bodies B, SolverParams P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.n) return;
+    const float h = P.dt;
+    float4 lv = B.lvel[i], av = B.avel[i], ps = B.pos[i], q4 = B.q[i];
+    const float4 fl = B.fc[2 * i], fa = B.fc[2 * i + 1], facc = B.facc[i], tacc4 = B.tacc[i];
+    float lvel[3] = {lv.x, lv.y, lv.z}, avel[3] = {av.x, av.y, av.z};
+    lvel[0] += h * fl.x; lvel[1] += h * fl.y; lvel[2] += h * fl.z;
+    avel[0] += h * fa.x; avel[1] += h * fa.y; avel[2] += h * fa.z;
+    const float ims = h * ps.w;
+    float tacc[3];
+    lvel[0] += ims * facc.x; tacc[0] = tacc4.x * h;
+    lvel[1] += ims * facc.y; tacc[1] = tacc4.y * h;
+    lvel[2] += ims * facc.z; tacc[2] = tacc4.z * h;
+    float invIw[12], tmp[3];
+    load_rows3(B.invIw + 3 * i, invIw);
+    mul0_331(tmp, invIw, tacc);
+    avel[0] = avel[0] + tmp[0]; avel[1] = avel[1] + tmp[1]; avel[2] = avel[2] + tmp[2];
+    // dxStepBody (infinitesimal rotation; no finite-rotation, damping or speed cap)
+    float pos[3] = {ps.x + h * lvel[0], ps.y + h * lvel[1], ps.z + h * lvel[2]};
+    float q[4] = {q4.x, q4.y, q4.z, q4.w};
+    const float *w = avel;
+    float dq[4];
+    dq[0] = 0.5f * (-w[0] * q[1] - w[1] * q[2] - w[2] * q[3]);
+    dq[1] = 0.5f * (w[0] * q[0] + w[1] * q[3] - w[2] * q[2]);
+    dq[2] = 0.5f * (-w[0] * q[3] + w[1] * q[0] + w[2] * q[1]);
+    dq[3] = 0.5f * (w[0] * q[2] - w[1] * q[1] + w[2] * q[0]);
+    for (int j = 0; j < 4; j++) q[j] += h * dq[j];
+    float l = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (l > 0) { l = 1.0f / sqrtf(l); q[0] *= l; q[1] *= l; q[2] *= l; q[3] *= l; }
+    else { q[0] = 1; q[1] = q[2] = q[3] = 0; }
+    float R[12];
+    float qq1 = 2 * q[1] * q[1], qq2 = 2 * q[2] * q[2], qq3 = 2 * q[3] * q[3];
+    R[0] = 1 - qq2 - qq3; R[1] = 2 * (q[1] * q[2] - q[0] * q[3]); R[2] = 2 * (q[1] * q[3] + q[0] * q[2]);
+    R[4] = 2 * (q[1] * q[2] + q[0] * q[3]); R[5] = 1 - qq1 - qq3; R[6] = 2 * (q[2] * q[3] - q[0] * q[1]);
+    R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2;
+    R[3] = R[7] = R[11] = 0;
+    B.pos[i] = make_float4(pos[0], pos[1], pos[2], ps.w);
+    B.q[i] = make_float4(q[0], q[1], q[2], q[3]);
+    store_rows3(B.R + 3 * i, R);
+    B.lvel[i] = make_float4(lvel[0], lvel[1], lvel[2], lv.w);
+    B.avel[i] = make_float4(avel[0], avel[1], avel[2], av.w);
+    B.facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    B.tacc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------------------------------ FP64 residual
+// A = J M^-1 J^T + diag(cfm), b = rhs, both as formed before Ad scaling
+// (unscaled here by the stored Ad); bounds per quickstep.cpp:2972-2978.
+__global__ void k_res_force(Rows Rw, const int *nrows_dev, double *f) {
+    int n = *nrows_dev;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int2 b = Rw.body[r];
+        const double ad = (double)Rw.Ad[r];
+        const double l = (double)Rw.lambda[r] / ad;  // unscaled J = J'/Ad, so J^T lambda = J'^T lambda / Ad
+        float4 a = Rw.J1l[r], c = Rw.J1a[r];
+        atomicAdd(&f[6 * b.x + 0], a.x * l); atomicAdd(&f[6 * b.x + 1], a.y * l); atomicAdd(&f[6 * b.x + 2], a.z * l);
+        atomicAdd(&f[6 * b.x + 3], c.x * l); atomicAdd(&f[6 * b.x + 4], c.y * l); atomicAdd(&f[6 * b.x + 5], c.z * l);
+        if (b.y >= 0) {
+            a = Rw.J2l[r]; c = Rw.J2a[r];
+            atomicAdd(&f[6 * b.y + 0], a.x * l); atomicAdd(&f[6 * b.y + 1], a.y * l); atomicAdd(&f[6 * b.y + 2], a.z * l);
+            atomicAdd(&f[6 * b.y + 3], c.x * l); atomicAdd(&f[6 * b.y + 4], c.y * l); atomicAdd(&f[6 * b.y + 5], c.z * l);
+        }
+    }
+}
+__global__ void k_res_vel(Bodies B, const double *f, double *v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.n) return;
+    double im = B.pos[i].w;
+    for (int k = 0; k < 3; k++) v[6 * i + k] = im * f[6 * i + k];
+    for (int k = 0; k < 3; k++) {
+        float4 row = B.invIw[3 * i + k];
+        v[6 * i + 3 + k] = (double)row.x * f[6 * i + 3] + (double)row.y * f[6 * i + 4] + (double)row.z * f[6 * i + 5];
+    }
+}
+__device__ __forceinline__ void atomic_max_d(double *addr, double v) {
+    unsigned long long *a = (unsigned long long *)addr;
+    unsigned long long nv = __double_as_longlong(v);
+    atomicMax(a, nv);  // v >= 0: bit order equals value order
+}
+__global__ void k_res_rows(Rows Rw, Bodies B, const int *nrows_dev, const double *v, double *out) {
+    int n = *nrows_dev;
+    double rmax = 0, cmax = 0, lmax = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int2 b = Rw.body[r];
+        const double ad = (double)Rw.Ad[r];
+        float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
+        double J[12] = {j1l.x / ad, j1l.y / ad, j1l.z / ad, j1a.x / ad, j1a.y / ad, j1a.z / ad,
+                        j2l.x / ad, j2l.y / ad, j2l.z / ad, j2a.x / ad, j2a.y / ad, j2a.z / ad};
+        double rhs = j1l.w / ad, cfm = j1a.w / ad;
+        double lam = Rw.lambda[r];
+        double Av = 0, D = 0;
+        for (int k = 0; k < 6; k++) Av += J[k] * v[6 * b.x + k];
+        double im = B.pos[b.x].w;
+        float I[12];
+        load_rows3(B.invIw + 3 * b.x, I);
+        for (int k = 0; k < 3; k++) D += J[k] * J[k] * im;
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) D += J[3 + a] * (double)I[4 * a + c] * J[3 + c];
+        if (b.y >= 0) {
+            for (int k = 0; k < 6; k++) Av += J[6 + k] * v[6 * b.y + k];
+            double im2 = B.pos[b.y].w;
+            load_rows3(B.invIw + 3 * b.y, I);
+            for (int k = 0; k < 3; k++) D += J[6 + k] * J[6 + k] * im2;
+            for (int a = 0; a < 3; a++)
+                for (int c = 0; c < 3; c++) D += J[9 + a] * (double)I[4 * a + c] * J[9 + c];
+        }
+        double w = Av + cfm * lam - rhs;
+        D += cfm;
+        double lo, hi;
+        int fi = Rw.findex[r];
+        if (fi >= 0) { hi = fabs((double)j2a.w * (double)Rw.lambda[fi]); lo = -hi; }
+        else { lo = j2l.w; hi = j2a.w; }
+        double t = lam - w / D;
+        t = fmin(fmax(t, lo), hi);
+        rmax = fmax(rmax, fabs(lam - t));
+        double c;
+        if (lam <= lo) c = w < 0 ? -w : 0;
+        else if (lam >= hi) c = w > 0 ? w : 0;
+        else c = fabs(w);
+        cmax = fmax(cmax, c);
+        lmax = fmax(lmax, fabs(lam));
+    }
+    atomic_max_d(&out[0], rmax);
+    atomic_max_d(&out[1], cmax);
+    atomic_max_d(&out[2], lmax);
+}
+
+// joint feedback per contact: f = J^T lambda with the unscaled rows
+__global__ void k_feedback(Rows Rw, const int *nrows_dev, float *fb) {
+    int n = *nrows_dev;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int c = Rw.contact[r];
+        const int2 b = Rw.body[r];
+        const float l = Rw.lambda[r] / Rw.Ad[r];
+        float4 a = Rw.J1l[r], d = Rw.J1a[r];
+        float *o = fb + 16 * c;
+        atomicAdd(&o[0], a.x * l); atomicAdd(&o[1], a.y * l); atomicAdd(&o[2], a.z * l);
+        atomicAdd(&o[4], d.x * l); atomicAdd(&o[5], d.y * l); atomicAdd(&o[6], d.z * l);
+        if (b.y >= 0) {
+            a = Rw.J2l[r]; d = Rw.J2a[r];
+            atomicAdd(&o[8], a.x * l); atomicAdd(&o[9], a.y * l); atomicAdd(&o[10], a.z * l);
+            atomicAdd(&o[12], d.x * l); atomicAdd(&o[13], d.y * l); atomicAdd(&o[14], d.z * l);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+static int grid_for(int n, int block) { return n <= 0 ? 1 : (n + block - 1) / block; }
+
+Bodies bodies_view(Workspace &ws, int nb) {
+    Bodies B;
+    B.pos = ws.b_pos.as<float4>(); B.q = ws.b_q.as<float4>(); B.R = ws.b_R.as<float4>();
+    B.lvel = ws.b_lvel.as<float4>(); B.avel = ws.b_avel.as<float4>(); B.facc = ws.b_facc.as<float4>();
+    B.tacc = ws.b_tacc.as<float4>(); B.Ib = ws.b_Ib.as<float4>(); B.invIb = ws.b_invIb.as<float4>();
+    B.invIw = ws.b_invIw.as<float4>(); B.fc = ws.b_fc.as<float4>(); B.rt = ws.b_rt.as<float4>();
+    B.n = nb;
+    return B;
+}
+
+bool ensure_bodies(Workspace &ws, int nb) {
+    size_t n = nb > 0 ? nb : 1;
+    return ws.b_pos.ensure(n * 16) && ws.b_q.ensure(n * 16) && ws.b_R.ensure(n * 48) && ws.b_lvel.ensure(n * 16) &&
+           ws.b_avel.ensure(n * 16) && ws.b_facc.ensure(n * 16) && ws.b_tacc.ensure(n * 16) && ws.b_Ib.ensure(n * 48) &&
+           ws.b_invIb.ensure(n * 48) && ws.b_invIw.ensure(n * 48) && ws.b_fc.ensure(n * 32) && ws.b_rt.ensure(n * 32) &&
+           ws.b_fa.ensure(n * 8) && ws.m_mask.ensure(n * 16) && ws.m_claim.ensure(n * GB_MAX_COLOURS * 4) &&
+           ws.res_f.ensure(n * 48) && ws.res_v.ensure(n * 48);
+}
+
+bool ensure_rows(Workspace &ws, int ncap) {
+    size_t nc = ncap > 0 ? ncap : 1;
+    size_t rows = nc * 6;
+    bool ok = ws.c_mcount.ensure((nc + 1) * 4) && ws.c_rstart.ensure((nc + 1) * 4) && ws.m_head.ensure((nc + 1) * 4) &&
+              ws.m_id.ensure((nc + 1) * 4) && ws.m_start.ensure((nc + 2) * 4) && ws.m_colour.ensure((nc + 1) * 4) &&
+              ws.m_tent.ensure((nc + 1) * 4) && ws.col_count.ensure(GB_MAX_COLOURS * 4 + 4) &&
+              ws.col_start.ensure(GB_MAX_COLOURS * 4 + 4) && ws.col_fill.ensure(GB_MAX_COLOURS * 4 + 4) &&
+              ws.col_list.ensure((nc + 1) * 4);
+    if (!ok) return false;
+    if (ws.row_cap < (int)rows) {
+        ok = ws.r_J1l.ensure(rows * 16) && ws.r_J1a.ensure(rows * 16) && ws.r_J2l.ensure(rows * 16) &&
+             ws.r_J2a.ensure(rows * 16) && ws.r_M1l.ensure(rows * 16) && ws.r_M1a.ensure(rows * 16) &&
+             ws.r_M2l.ensure(rows * 16) && ws.r_M2a.ensure(rows * 16) && ws.r_lambda.ensure(rows * 4) &&
+             ws.r_Ad.ensure(rows * 4) && ws.r_findex.ensure(rows * 4) && ws.r_contact.ensure(rows * 4) &&
+             ws.r_body.ensure(rows * 8);
+        if (!ok) return false;
+        ws.row_cap = (int)rows;
+    }
+    return true;
+}
+
+static Rows rows_view(Workspace &ws) {
+    Rows R;
+    R.J1l = ws.r_J1l.as<float4>(); R.J1a = ws.r_J1a.as<float4>(); R.J2l = ws.r_J2l.as<float4>();
+    R.J2a = ws.r_J2a.as<float4>(); R.M1l = ws.r_M1l.as<float4>(); R.M1a = ws.r_M1a.as<float4>();
+    R.M2l = ws.r_M2l.as<float4>(); R.M2a = ws.r_M2a.as<float4>();
+    R.lambda = ws.r_lambda.as<float>(); R.Ad = ws.r_Ad.as<float>(); R.findex = ws.r_findex.as<int>();
+    R.contact = ws.r_contact.as<int>(); R.body = ws.r_body.as<int2>();
+    R.n_cap = ws.row_cap;
+    return R;
+}
+
+static int coop_blocks(const void *kernel, int block) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 2) per_sm = 2;
+    return per_sm * num_sms();
+}
+
+static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
+    Bodies B = bodies_view(ws, nb);
+    if (!ensure_rows(ws, ws.contact_cap)) return false;
+    k_bodies<<<grid_for(nb, 128), 128, 0, s>>>(B, P);
+    int grid = 4 * num_sms();
+    const Contact *C = ws.contacts.as<Contact>();
+    const Surface *S = ws.surfaces.as<Surface>();
+    k_contact_m<<<grid, 256, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_mcount.as<int>());
+    scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nrows, ws, s);
+    k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
+    const int dyn = (P.solver == 1) && (P.premature_delta != 0 || P.extra_factor != 0);
+    k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn, nullptr, ws.dc);
+    count_launch(4);
+    return true;
+}
+
+bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStream_t s, cudaEvent_t ev0,
+                      cudaEvent_t ev1) {
+    if (!assemble(ws, nb, P, s)) return false;
+    const Contact *C = ws.contacts.as<Contact>();
+    int grid = 4 * num_sms();
+    // manifolds
+    k_manifold_heads<<<grid, 256, 0, s>>>(C, &ws.dc->ncontacts, ws.m_head.as<int>());
+    scan_exclusive(ws.m_head.as<int>(), ws.m_id.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nmanifolds, ws, s);
+    k_manifold_starts<<<grid, 256, 0, s>>>(&ws.dc->ncontacts, ws.m_head.as<int>(), ws.m_id.as<int>(), ws.m_start.as<int>(),
+                                           ws.dc);
+    // colouring
+    cudaMemsetAsync(ws.m_mask.p, 0, (size_t)(nb > 0 ? nb : 1) * 16, s);
+    cudaMemsetAsync(ws.m_claim.p, 0x7f, (size_t)(nb > 0 ? nb : 1) * GB_MAX_COLOURS * 4, s);
+    cudaMemsetAsync(&ws.dc->ncolours, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
+    {
+        int blocks = coop_blocks((const void *)k_colour, 256);
+        unsigned long long *mask = ws.m_mask.as<unsigned long long>();
+        int *claim = ws.m_claim.as<int>(), *colour = ws.m_colour.as<int>(), *tent = ws.m_tent.as<int>();
+        const int *mstart = ws.m_start.as<int>();
+        DevCounters *dc = ws.dc;
+        void *args[] = {(void *)&C, (void *)&mstart, (void *)&dc, (void *)&mask, (void *)&claim, (void *)&colour,
+                        (void *)&tent, (void *)&nb};
+        if (cudaLaunchCooperativeKernel((const void *)k_colour, blocks, 256, args, 0, s) != cudaSuccess) return false;
+    }
+    cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
+    cudaMemsetAsync(ws.col_fill.p, 0, GB_MAX_COLOURS * 4, s);
+    k_colour_count<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_count.as<int>());
+    scan_exclusive(ws.col_count.as<int>(), ws.col_start.as<int>(), nullptr, GB_MAX_COLOURS, &ws.dc->colour_total, ws, s);
+    k_colour_fill<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_start.as<int>(), ws.col_fill.as<int>(),
+                                       ws.col_list.as<int>());
+    // solve
+    cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
+    cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
+    cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
+    if (ev0) cudaEventRecord(ev0, s);
+    {
+        PgsArgs A;
+        A.Rw = rows_view(ws);
+        A.fc = ws.b_fc.as<float4>();
+        A.C = C;
+        A.rstart = ws.c_rstart.as<int>(); A.mcount = ws.c_mcount.as<int>(); A.mstart = ws.m_start.as<int>();
+        A.clist = ws.col_list.as<int>(); A.cstart = ws.col_start.as<int>(); A.ccount = ws.col_count.as<int>();
+        A.dc = ws.dc;
+        A.iterations = P.iterations;
+        A.max_iterations = P.max_iterations > 0 ? P.max_iterations : P.iterations;
+        A.check_every = P.check_every > 0 ? P.check_every : 10;
+        A.target = P.residual_target;
+        A.w_sor = P.w;
+        int blocks = coop_blocks((const void *)k_pgs, 256);
+        void *args[] = {(void *)&A};
+        if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, 256, args, 0, s) != cudaSuccess) return false;
+    }
+    if (ev1) cudaEventRecord(ev1, s);
+    k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
+    count_launch(9);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, const IslandSchedule &sch, cudaStream_t s,
+                              cudaEvent_t ev0, cudaEvent_t ev1) {
+    if (!assemble(ws, nb, P, s)) return false;
+    int nisl = (int)sch.start.size() - 1;
+    if (nisl > 0) {
+        size_t no = sch.order.size() > 0 ? sch.order.size() : 1;
+        if (!(ws.i_order.ensure(no * 4) && ws.i_start.ensure((nisl + 1) * 4) &&
+              ws.i_bodies.ensure((sch.bodies.size() + 1) * 4) && ws.i_bstart.ensure((nisl + 1) * 4)))
+            return false;
+        if (!sch.order.empty()) cudaMemcpyAsync(ws.i_order.p, sch.order.data(), sch.order.size() * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ws.i_start.p, sch.start.data(), (nisl + 1) * 4, cudaMemcpyHostToDevice, s);
+        if (!sch.bodies.empty()) cudaMemcpyAsync(ws.i_bodies.p, sch.bodies.data(), sch.bodies.size() * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ws.i_bstart.p, sch.bstart.data(), (nisl + 1) * 4, cudaMemcpyHostToDevice, s);
+    }
+    cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
+    if (ev0) cudaEventRecord(ev0, s);
+    if (nisl > 0) {
+        IslandArgs A;
+        A.Rw = rows_view(ws);
+        A.fc = ws.b_fc.as<float4>();
+        A.fa = ws.b_fa.as<float>();
+        A.order = ws.i_order.as<int>(); A.start = ws.i_start.as<int>();
+        A.bodies = ws.i_bodies.as<int>(); A.bstart = ws.i_bstart.as<int>();
+        A.iterations = P.iterations;
+        A.max_extra = (unsigned)((float)P.iterations * P.extra_factor);
+        A.premature = P.premature_delta;
+        A.extra_delta = P.extra_delta;
+        A.dyn = (A.max_extra != 0 || A.premature != 0) ? 1 : 0;
+        A.dc = ws.dc;
+        k_islands<<<nisl, 32, 0, s>>>(A);
+        count_launch();
+    }
+    if (ev1) cudaEventRecord(ev1, s);
+    k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
+    count_launch();
+    // (the reference-order schedule's host vectors are copied before return)
+    cudaStreamSynchronize(s);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s) {
+    ws.res_f.ensure((size_t)(nb > 0 ? nb : 1) * 48);
+    ws.res_v.ensure((size_t)(nb > 0 ? nb : 1) * 48 + 64);
+    cudaMemsetAsync(ws.res_f.p, 0, (size_t)(nb > 0 ? nb : 1) * 48, s);
+    double *out = (double *)((char *)ws.res_v.p + (size_t)(nb > 0 ? nb : 1) * 48);
+    cudaMemsetAsync(out, 0, 24, s);
+    int grid = 4 * num_sms();
+    Rows R = rows_view(ws);
+    Bodies B = bodies_view(ws, nb);
+    k_res_force<<<grid, 256, 0, s>>>(R, &ws.dc->nrows, ws.res_f.as<double>());
+    k_res_vel<<<grid_for(nb, 128), 128, 0, s>>>(B, ws.res_f.as<double>(), ws.res_v.as<double>());
+    k_res_rows<<<grid, 256, 0, s>>>(R, B, &ws.dc->nrows, ws.res_v.as<double>(), out);
+    count_launch(3);
+    double h[3] = {0, 0, 0};
+    cudaMemcpyAsync(h, out, 24, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (compl_err) *compl_err = h[1];
+    if (maxlam) *maxlam = h[2];
+    return h[0];
+}
+
+int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s) {
+    int n = 0;
+    cudaMemcpyAsync(&n, &ws.dc->nrows, 4, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (!rows || cap <= 0 || n <= 0) return n;
+    int k = n < cap ? n : cap;
+    std::vector<float4> J1l(k), J1a(k), J2l(k), J2a(k);
+    std::vector<float> lam(k), Ad(k);
+    std::vector<int> fi(k);
+    std::vector<int2> bd(k);
+    cudaMemcpyAsync(J1l.data(), ws.r_J1l.p, k * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(J1a.data(), ws.r_J1a.p, k * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(J2l.data(), ws.r_J2l.p, k * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(J2a.data(), ws.r_J2a.p, k * 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(lam.data(), ws.r_lambda.p, k * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(Ad.data(), ws.r_Ad.p, k * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(fi.data(), ws.r_findex.p, k * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(bd.data(), ws.r_body.p, k * 8, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int i = 0; i < k; i++) {
+        float *o = rows + 20 * i;
+        float ad = Ad[i];
+        o[0] = J1l[i].x / ad; o[1] = J1l[i].y / ad; o[2] = J1l[i].z / ad;
+        o[3] = J1a[i].x / ad; o[4] = J1a[i].y / ad; o[5] = J1a[i].z / ad;
+        bool two = bd[i].y >= 0;
+        o[6] = two ? J2l[i].x / ad : 0; o[7] = two ? J2l[i].y / ad : 0; o[8] = two ? J2l[i].z / ad : 0;
+        o[9] = two ? J2a[i].x / ad : 0; o[10] = two ? J2a[i].y / ad : 0; o[11] = two ? J2a[i].z / ad : 0;
+        o[12] = J1l[i].w / ad; o[13] = J1a[i].w / ad; o[14] = J2l[i].w; o[15] = J2a[i].w;
+        o[16] = (float)bd[i].x; o[17] = (float)bd[i].y; o[18] = (float)fi[i]; o[19] = lam[i];
+    }
+    return n;
+}
+
+void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s) {
+    out.assign((size_t)ncontacts * 16, 0.f);
+    if (ncontacts <= 0) return;
+    DBuf &tmp = ws.res_f;
+    tmp.ensure((size_t)ncontacts * 64);
+    cudaMemsetAsync(tmp.p, 0, (size_t)ncontacts * 64, s);
+    k_feedback<<<4 * num_sms(), 256, 0, s>>>(rows_view(ws), &ws.dc->nrows, tmp.as<float>());
+    count_launch();
+    cudaMemcpyAsync(out.data(), tmp.p, (size_t)ncontacts * 64, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+}
+
+}  // namespace gb

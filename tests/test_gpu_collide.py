@@ -1,0 +1,161 @@
+"""GPU narrow and broad phase against the reference's golden vectors and the
+oracle, through the C ABI (dCollide, dBoxBox, dSpaceCollide,
+gbodeSpaceCollideContacts)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 1e-5   # contact position / normal / depth (FP32)
+
+
+def make_geom(L, space, cls, pos, R, dims):
+    if cls == 0:
+        g = L.dCreateSphere(space, float(dims[0]))
+    elif cls == 1:
+        g = L.dCreateBox(space, float(dims[0]), float(dims[1]), float(dims[2]))
+    elif cls == 2:
+        g = L.dCreateCapsule(space, float(dims[0]), float(dims[1]))
+    else:
+        return L.dCreatePlane(space, *[float(x) for x in dims])
+    L.dGeomSetPosition(g, *[float(x) for x in pos])
+    Rm = np.ascontiguousarray(R, np.float32)
+    L.dGeomSetRotation(g, Rm.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return g
+
+
+def test_dcollide_matches_reference(gblib, golden):
+    from ode_gb300 import ode
+    L = gblib
+    g = golden("colliders.npz")
+    n = len(g["count"])
+    buf = (ode.dContactGeom * 8)()
+    exact = 0
+    worst = 0.0
+    for k in range(n):
+        c1, c2 = g["cls"][k]
+        a = make_geom(L, None, c1, g["pos"][k, 0], g["R"][k, 0], g["dims"][k, 0])
+        b = make_geom(L, None, c2, g["pos"][k, 1], g["R"][k, 1], g["dims"][k, 1])
+        cnt = L.dCollide(a, b, int(g["flags"][k]), ctypes.addressof(buf), ctypes.sizeof(ode.dContactGeom))
+        assert cnt == g["count"][k], (k, c1, c2, cnt, g["count"][k])
+        same = True
+        for i in range(cnt):
+            p = np.array(buf[i].pos[:3]); nrm = np.array(buf[i].normal[:3]); d = buf[i].depth
+            err = max(np.abs(p - g["cpos"][k, i]).max(), np.abs(nrm - g["cnrm"][k, i]).max(), abs(d - g["cdep"][k, i]))
+            worst = max(worst, err)
+            same &= err == 0
+            assert buf[i].g1 == a and buf[i].g2 == b
+        exact += same
+        L.dGeomDestroy(a)
+        L.dGeomDestroy(b)
+    assert worst <= POS_TOL, worst
+    print(f"dCollide: {n} cases, bit-exact {exact}/{n}, worst abs error {worst:.3g}")
+
+
+def test_boxbox_feature_codes(gblib, golden):
+    from ode_gb300 import ode
+    L = gblib
+    g = golden("colliders.npz")
+    F = ctypes.POINTER(ctypes.c_float)
+    buf = (ode.dContactGeom * 8)()
+    checked = 0
+    for k in np.nonzero((g["cls"][:, 0] == 1) & (g["cls"][:, 1] == 1))[0]:
+        arrs = [np.zeros(4, np.float32) for _ in range(4)] + [np.zeros(12, np.float32) for _ in range(2)]
+        p1, p2, s1, s2, R1, R2 = arrs
+        p1[:3], p2[:3] = g["pos"][k, 0], g["pos"][k, 1]
+        s1[:3], s2[:3] = g["dims"][k, 0][:3], g["dims"][k, 1][:3]
+        R1[:], R2[:] = g["R"][k, 0], g["R"][k, 1]
+        nrm = np.zeros(4, np.float32)
+        depth = ctypes.c_float(0)
+        code = ctypes.c_int(-1)
+        n = L.dBoxBox(p1.ctypes.data_as(F), R1.ctypes.data_as(F), s1.ctypes.data_as(F), p2.ctypes.data_as(F),
+                      R2.ctypes.data_as(F), s2.ctypes.data_as(F), nrm.ctypes.data_as(F), ctypes.byref(depth),
+                      ctypes.byref(code), int(g["flags"][k]), ctypes.addressof(buf), ctypes.sizeof(ode.dContactGeom))
+        assert n == g["count"][k]
+        if n:
+            assert code.value == g["code"][k], (k, code.value, g["code"][k])
+        checked += 1
+    assert checked > 0
+
+
+def test_hash_space_pairs_match_reference(gblib, golden):
+    L = gblib
+    s = golden("space.npz")
+    found = []
+    cb = __import__("ode_gb300.ode", fromlist=["dNearCallback"]).dNearCallback(
+        lambda data, o1, o2: found.append((L.dGeomGetData(o1) or 0, L.dGeomGetData(o2) or 0)))
+    for ci in range(int(s["ncases"][0])):
+        sp = L.dHashSpaceCreate(None)
+        lv = s[f"c{ci}_levels"]
+        L.dHashSpaceSetLevels(sp, int(lv[0]), int(lv[1]))
+        cls = s[f"c{ci}_cls"]
+        for i in range(len(cls)):
+            gg = make_geom(L, sp, cls[i], s[f"c{ci}_pos"][i], s[f"c{ci}_R"][i], s[f"c{ci}_dims"][i])
+            L.dGeomSetData(gg, ctypes.c_void_p(i))
+        found.clear()
+        L.dSpaceCollide(sp, None, cb)
+        mine = {(min(a, b), max(a, b)) for a, b in found}
+        assert len(mine) == len(found), "a pair was reported twice"
+        ref = set(map(tuple, s[f"c{ci}_pairs"].tolist()))
+        # plane-plane pairs have no collider; the reference reports them, this space does not
+        ref_no_pp = {p for p in ref if not (cls[p[0]] == 4 and cls[p[1]] == 4)}
+        assert mine == ref_no_pp, (ci, len(mine ^ ref_no_pp))
+        L.dSpaceDestroy(sp)
+
+
+def test_fused_contacts_match_oracle_on_a_pile(gblib, port):
+    """Full-size broad + narrow phase (gbodeSpaceCollideContacts) on a settled
+    32,768-body pile versus the oracle's hash space + dCollide on the same
+    poses: the same contact set, counts bit-exact, geometry within 1e-5."""
+    from ode_gb300 import scenes, sim
+    sc = scenes.pile(32768, seed=1)
+    w = sim.GBWorld(sc)
+    for _ in range(150):
+        w.step_fused()
+    w.sync()
+    st = w.state()
+    # contacts of the current pose
+    L = gblib
+    assert L.gbodeSpaceCollideContacts(w.space, w.w, w.group, ctypes.byref(w.surface), sc.maxc) == 1
+    gc = w.contacts()
+    L.dJointGroupEmpty(w.group)
+    assert len(gc) > 10000
+    # oracle: same poses, static geoms
+    n = sc.nb
+    cls = sc.geom_cls
+    pos = np.zeros((sc.ng, 3), np.float32)
+    R = np.zeros((sc.ng, 12), np.float32)
+    pos[:n] = st[:, 0:3]
+    R[:n] = st[:, 7:19]
+    R[n:, [0, 5, 10]] = 1
+    body = sc.geom_body
+    pairs = port.hash_pairs(cls, body, pos, R, sc.geom_dims, np.arange(sc.ng)[::-1].copy())
+    touching = set()
+    for a, b in pairs:
+        cnt, _ = port.collide(cls[a], pos[a], R[a], sc.geom_dims[a], cls[b], pos[b], R[b], sc.geom_dims[b], sc.maxc)
+        if cnt:
+            touching.add((min(a, b), max(a, b)))
+    # GPU contacts keyed by geom pair; geom index in the space list is reversed creation order
+    ng = sc.ng
+    mine = {}
+    for c in gc:
+        a, b = ng - 1 - int(c[7]), ng - 1 - int(c[8])
+        mine.setdefault((a, b), []).append(c)
+    assert {(min(a, b), max(a, b)) for a, b in mine} == touching
+    # narrow phase in the GPU's own pair orientation (dCollide(o1,o2) and
+    # dCollide(o2,o1) may differ for box-box: the reference face depends on order)
+    worst, exact = 0.0, 0
+    for (a, b), lst in mine.items():
+        cnt, out = port.collide(cls[a], pos[a], R[a], sc.geom_dims[a], cls[b], pos[b], R[b], sc.geom_dims[b], sc.maxc)
+        assert cnt == len(lst), (a, b)
+        for c, o in zip(lst, out):
+            e = max(np.abs(c[0:3] - o[0:3]).max(), np.abs(c[3:6] - o[3:6]).max(), abs(c[6] - o[6]))
+            worst = max(worst, e)
+            exact += e == 0
+    assert worst <= POS_TOL, worst
+    print(f"pile contacts: {len(gc)}, bit-exact {exact}, worst {worst:.3g}")
+    w.close()
