@@ -1,0 +1,339 @@
+"""Benchmark: body-steps/s of the rigid-body step on the 32,768-body pile at
+LCP residual <= 1e-4 (one GB300).
+
+Workload (`pile32768`): 32,768 bodies (50 % spheres r~U[0.05,0.25] m, 50 %
+boxes sides ~U[0.1,0.5] m, density ~U[500,2000]) dropped on a jittered 32^3
+grid into an open box of 5 static planes; dt 1/120, mu 0.6, dContactApprox1,
+<= 4 contacts per pair, hash-space broad phase.  The pile first settles for
+--settle steps (untimed), then W warm-up and K timed steps run.
+
+A step is the fused path: gbodeSpaceCollideContacts (broad phase, narrow
+phase, contact joints on the device) + dWorldQuickStep with the coloured PGS
+iterating until the natural-map LCP residual (relative to max(1, max|lambda|))
+is <= 1e-4, checked every 10 sweeps, or 3000 sweeps.  `value` counts only
+steps that reached the target.  Timing: CUDA events on the world's stream
+around each step, an L2 flush (256 MB write) before every timed step, outside
+the events.  `e2e` runs the same steps through the C ABI with host buffers:
+the full body state is set from host memory before and read back after every
+step, wall-clock timed.
+
+--impl reference times the reference algorithm on the host CPU (the oracle
+port of ODE's dSpaceCollide + dWorldQuickStep, stock settings: 30 SOR
+iterations, random row reordering, dynamic iteration count) on the same scene
+and reports the residual it reaches.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s at LCP residual <=1e-4 (plain GPU PGS)"
+B_ROW = 132        # algorithmic bytes per PGS row-iteration
+B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbode", choices=["gbode", "reference"])
+    ap.add_argument("--n", type=int, default=32768)
+    ap.add_argument("--settle", type=int, default=240)
+    ap.add_argument("--target", type=float, default=1e-4)
+    ap.add_argument("--check-every", type=int, default=10)
+    ap.add_argument("--max-iters", type=int, default=3000)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0, help="run N steps only (for ncu), no JSON")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index, self.samples, self.proc, self.thread = index, [], None, None
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--id={self.index}",
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = max(mx, float(s[1]))
+                for k, nm in enumerate(names):
+                    if s[4 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gbode" else "gloo"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def dist_max(x: float, ws: int, device) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x: float, ws: int, device) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------- reference arm
+def run_reference(args, ws, rank):
+    """The reference algorithm on the host CPU (oracle port of ODE), stock settings."""
+    if rank != 0:
+        return
+    from oracle.port.port import Port
+    from ode_gb300 import scenes
+    P = Port()
+    sc = scenes.pile(args.n, seed=1)
+    P.lib.port_rand_set_seed(0)
+    w = P.world(sc.bodies, sc.world_params(), sc.iterations, dyn=1, reorder=1)
+    w.attach_space(sc.geom_cls, sc.geom_body, sc.geom_pos, sc.geom_R, sc.geom_dims, sc.hash_levels, sc.maxc,
+                   sc.surface_mode, sc.surface())
+    t0 = time.perf_counter()
+    for _ in range(args.settle + args.warmup):
+        w.sim_step()
+    settle_s = time.perf_counter() - t0
+    steps = max(1, min(args.steps, args.cpu_steps))
+    t0 = time.perf_counter()
+    nc = 0
+    for _ in range(steps):
+        nc += w.sim_step()
+    dt = time.perf_counter() - t0
+    value = sc.nb * steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"pile{sc.nb}", "bodies": sc.nb, "dt": sc.dt, "iterations": sc.iterations,
+                       "settle_steps": args.settle, "solver": "reference quickstep (oracle port), stock settings: "
+                       "30 SOR iterations, random reordering, dynamic iteration count; residual not targeted",
+                       "contacts_per_step": nc / steps},
+            "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{steps} steps of pile{sc.nb} after {args.settle + args.warmup} "
+                                       f"settle steps ({settle_s:.0f} s) on one host core"},
+            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------- gbode arm
+def run_gbode(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from ode_gb300 import build, ode, scenes, sim
+    build.build()
+    L = ode.load()
+    stream = torch.cuda.Stream(device=dev)
+    sc = scenes.pile(args.n, seed=1 + rank)
+    w = sim.GBWorld(sc, stream=ctypes.c_void_p(stream.cuda_stream))
+    # settle with the configured 30 sweeps per step (untimed)
+    for _ in range(args.settle):
+        w.step_fused()
+    w.sync()
+    L.gbodeWorldSetResidualTarget(w.w, args.target, args.check_every, args.max_iters)
+    L.gbodeWorldSetTiming(w.w, 1)
+    if args.profile_steps:
+        for _ in range(args.profile_steps):
+            w.step_fused()
+        w.sync()
+        return
+    for _ in range(args.warmup):
+        w.step_fused()
+    w.sync()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    peak, peak_kind = measured_peak()
+    launches0 = L.gbodeKernelLaunchCount()
+    step_ms, solve_ms, sweeps, resid, rows, contacts, colours = [], [], [], [], [], [], []
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        w.step_fused()
+        e1.record(stream)
+        stream.synchronize()
+        st = w.stats()
+        step_ms.append(e0.elapsed_time(e1))
+        solve_ms.append(st.solve_ms)
+        sweeps.append(st.iterations)
+        resid.append(st.residual)
+        rows.append(st.rows)
+        contacts.append(st.contacts)
+        colours.append(st.colours)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = L.gbodeKernelLaunchCount() - launches0
+    total_ms = sum(step_ms)
+    ok_steps = sum(1 for r in resid if r <= args.target)
+    total_ms_max = dist_max(total_ms, ws, dev)
+    body_steps = dist_sum(sc.nb * ok_steps, ws, dev)
+    value = body_steps / (total_ms_max / 1e3)
+    # FP64 residual of the last step's solution, evaluated on the device
+    r64, ce, ml = w.last_residual()
+    fp64_rel = r64 / max(1.0, ml)
+    # roofline of the dominant kernel (the persistent PGS sweep kernel)
+    checks = [int(np.ceil(s / args.check_every)) for s in sweeps]
+    pgs_bytes = sum(s * m * B_ROW + c * m * B_ROW_CHECK for s, m, c in zip(sweeps, rows, checks))
+    pgs_s = sum(solve_ms) / 1e3
+    achieved = pgs_bytes / pgs_s / 1e9 if pgs_s > 0 else 0.0
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = w.state()
+        h2d = 240 * sc.nb   # pos, q, R, lvel, avel, facc, tacc, I, invI as uploaded by the library
+        d2h = 112 * sc.nb   # pos, q, R, lvel, avel as downloaded
+        n_ok, t0 = 0, time.perf_counter()
+        for _ in range(args.steps):
+            w.set_state(host)
+            w.step_fused()
+            host = w.state()
+            if w.stats().residual <= args.target:
+                n_ok += 1
+        e2e_s = dist_max(time.perf_counter() - t0, ws, dev)
+        e2e = {"value": dist_sum(sc.nb * n_ok, ws, dev) / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+    # CPU baseline: the oracle port from the same settled state, same sweep count
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, w, int(np.median(sweeps)), args.cpu_steps)
+    if rank != 0:
+        return
+    m_mean = float(np.mean(rows))
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"pile{sc.nb}", "bodies": sc.nb, "dt": sc.dt, "mu": sc.mu, "maxc": sc.maxc,
+                   "settle_steps": args.settle, "residual_target": args.target, "check_every": args.check_every,
+                   "max_sweeps": args.max_iters, "l2": "256 MB flush before every timed step (outside the events)",
+                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                   "solver": "coloured PGS, persistent cooperative kernel",
+                   "rows_per_step": m_mean, "contacts_per_step": float(np.mean(contacts)),
+                   "colours": int(np.median(colours)), "sweeps_per_step": float(np.mean(sweeps)),
+                   "steps_at_target": ok_steps, "fp32_residual_max": float(max(resid)),
+                   "fp64_residual_last_step": fp64_rel, "complementarity_last_step": ce,
+                   "contact_rows_per_s": float(np.sum(rows)) / (total_ms / 1e3),
+                   "solve_share": pgs_s * 1e3 / total_ms},
+        "roofline": {"bound": "hbm", "kernel": "gb::k_pgs", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": pgs_bytes / args.steps},
+        "clocks": clk,
+        "gpu_launches": launches,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def cpu_baseline(sc, w, sweeps, steps):
+    from oracle.port.port import Port
+    P = Port()
+    st = w.state()
+    bodies = sc.bodies.copy()
+    bodies[:, 0:3], bodies[:, 3:7], bodies[:, 7:10], bodies[:, 10:13] = st[:, 0:3], st[:, 3:7], st[:, 19:22], st[:, 22:25]
+    pw = P.world(bodies, sc.world_params(), max(1, sweeps), dyn=0, reorder=0)
+    pw.attach_space(sc.geom_cls, sc.geom_body, sc.geom_pos, sc.geom_R, sc.geom_dims, sc.hash_levels, sc.maxc,
+                    sc.surface_mode, sc.surface())
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pw.sim_step()
+    dt = time.perf_counter() - t0
+    return {"value": sc.nb * steps / dt, "unit": "body-steps/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} steps of pile{sc.nb} from the GPU-settled state, {sweeps} SOR sweeps per step "
+                      f"(the GPU's median to reach the target), one host core, {dt:.1f} s"}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gbode(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -213,6 +213,18 @@ __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mas
             }
             n++;
         }
+    } else {
+        // big boxes against each other (collision_space.cpp:597-602), once per pair
+        int nbig = dc->nbig;
+        for (int k = 0; k < nbig; k++) {
+            int b = big_list[k];
+            if (b <= a || !aabb_pair_ok(G, a, b)) continue;
+            if (PASS) {
+                int idx = base + n;
+                if (idx < pair_cap) pairs[idx] = make_int2(a, b);
+            }
+            n++;
+        }
     }
     if (!PASS) {
         pcount[a] = n;

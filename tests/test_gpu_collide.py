@@ -101,9 +101,7 @@ def test_hash_space_pairs_match_reference(gblib, golden):
         mine = {(min(a, b), max(a, b)) for a, b in found}
         assert len(mine) == len(found), "a pair was reported twice"
         ref = set(map(tuple, s[f"c{ci}_pairs"].tolist()))
-        # plane-plane pairs have no collider; the reference reports them, this space does not
-        ref_no_pp = {p for p in ref if not (cls[p[0]] == 4 and cls[p[1]] == 4)}
-        assert mine == ref_no_pp, (ci, len(mine ^ ref_no_pp))
+        assert mine == ref, (ci, len(mine ^ ref))
         L.dSpaceDestroy(sp)
 
 
@@ -118,44 +116,42 @@ def test_fused_contacts_match_oracle_on_a_pile(gblib, port):
         w.step_fused()
     w.sync()
     st = w.state()
-    # contacts of the current pose
     L = gblib
+    ng = sc.ng
+    # broad phase: the GPU's candidate pairs (dSpaceCollide, GPU orientation)
+    # against the oracle's hash space on the same poses, as unordered sets
+    found = []
+    from ode_gb300 import ode
+    cb = ode.dNearCallback(lambda data, o1, o2: found.append((L.dGeomGetData(o1) or 0, L.dGeomGetData(o2) or 0)))
+    L.dSpaceCollide(w.space, None, cb)
+    n = sc.nb
+    cls = sc.geom_cls
+    pos = np.zeros((ng, 3), np.float32)
+    R = np.zeros((ng, 12), np.float32)
+    pos[:n] = st[:, 0:3]
+    R[:n] = st[:, 7:19]
+    R[n:, [0, 5, 10]] = 1
+    pairs = port.hash_pairs(cls, sc.geom_body, pos, R, sc.geom_dims, np.arange(ng)[::-1].copy())
+    assert {(min(a, b), max(a, b)) for a, b in found} == {(min(a, b), max(a, b)) for a, b in pairs.tolist()}
+    # narrow phase: fused contacts against the oracle's dCollide in the GPU's orientation
     assert L.gbodeSpaceCollideContacts(w.space, w.w, w.group, ctypes.byref(w.surface), sc.maxc) == 1
     gc = w.contacts()
     L.dJointGroupEmpty(w.group)
     assert len(gc) > 10000
-    # oracle: same poses, static geoms
-    n = sc.nb
-    cls = sc.geom_cls
-    pos = np.zeros((sc.ng, 3), np.float32)
-    R = np.zeros((sc.ng, 12), np.float32)
-    pos[:n] = st[:, 0:3]
-    R[:n] = st[:, 7:19]
-    R[n:, [0, 5, 10]] = 1
-    body = sc.geom_body
-    pairs = port.hash_pairs(cls, body, pos, R, sc.geom_dims, np.arange(sc.ng)[::-1].copy())
-    touching = set()
-    for a, b in pairs:
-        cnt, _ = port.collide(cls[a], pos[a], R[a], sc.geom_dims[a], cls[b], pos[b], R[b], sc.geom_dims[b], sc.maxc)
-        if cnt:
-            touching.add((min(a, b), max(a, b)))
-    # GPU contacts keyed by geom pair; geom index in the space list is reversed creation order
-    ng = sc.ng
     mine = {}
     for c in gc:
-        a, b = ng - 1 - int(c[7]), ng - 1 - int(c[8])
-        mine.setdefault((a, b), []).append(c)
-    assert {(min(a, b), max(a, b)) for a, b in mine} == touching
-    # narrow phase in the GPU's own pair orientation (dCollide(o1,o2) and
-    # dCollide(o2,o1) may differ for box-box: the reference face depends on order)
-    worst, exact = 0.0, 0
-    for (a, b), lst in mine.items():
+        mine.setdefault((ng - 1 - int(c[7]), ng - 1 - int(c[8])), []).append(c)
+    worst, exact, total = 0.0, 0, 0
+    for a, b in found:
         cnt, out = port.collide(cls[a], pos[a], R[a], sc.geom_dims[a], cls[b], pos[b], R[b], sc.geom_dims[b], sc.maxc)
-        assert cnt == len(lst), (a, b)
+        lst = mine.get((a, b), [])
+        assert cnt == len(lst), (a, b, cnt, len(lst))
         for c, o in zip(lst, out):
             e = max(np.abs(c[0:3] - o[0:3]).max(), np.abs(c[3:6] - o[3:6]).max(), abs(c[6] - o[6]))
             worst = max(worst, e)
             exact += e == 0
+            total += 1
+    assert total == len(gc)
     assert worst <= POS_TOL, worst
-    print(f"pile contacts: {len(gc)}, bit-exact {exact}, worst {worst:.3g}")
+    print(f"pile: {len(found)} candidate pairs, {len(gc)} contacts, bit-exact {exact}, worst {worst:.3g}")
     w.close()
