@@ -5,12 +5,15 @@ Workload (`pile32768`): 32,768 bodies (50 % spheres r~U[0.05,0.25] m, 50 %
 boxes sides ~U[0.1,0.5] m, density ~U[500,2000]) dropped on a jittered 32^3
 grid into an open box of 5 static planes; dt 1/120, mu 0.6, dContactApprox1,
 <= 4 contacts per pair, hash-space broad phase.  The pile first settles for
---settle steps (untimed), then W warm-up and K timed steps run.
+--settle steps (900: the top of the grid falls 19 m, about 2 s) with the
+configured 30 sweeps per step (untimed), then W warm-up and K timed steps run.
 
 A step is the fused path: gbodeSpaceCollideContacts (broad phase, narrow
-phase, contact joints on the device) + dWorldQuickStep with the coloured PGS
-iterating until the natural-map LCP residual (relative to max(1, max|lambda|))
-is <= 1e-4, checked every 10 sweeps, or 3000 sweeps.  `value` counts only
+phase, contact joints on the device) + dWorldQuickStep with the coloured PGS,
+warm-started from the previous step's multipliers (contact cache keyed by geom
+pair and slot), W = 1.0, iterating until the natural-map LCP residual
+(relative to max(1, max|lambda|)) is <= 1e-4, checked every 5 sweeps, or 3000
+sweeps.  `value` counts only
 steps that reached the target.  Timing: CUDA events on the world's stream
 around each step, an L2 flush (256 MB write) before every timed step, outside
 the events.  `e2e` runs the same steps through the C ABI with host buffers:
@@ -51,11 +54,15 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbode", choices=["gbode", "reference"])
     ap.add_argument("--n", type=int, default=32768)
-    ap.add_argument("--settle", type=int, default=240)
+    ap.add_argument("--settle", type=int, default=900)
     ap.add_argument("--target", type=float, default=1e-4)
-    ap.add_argument("--check-every", type=int, default=10)
+    ap.add_argument("--check-every", type=int, default=5)
+    ap.add_argument("--sor-w", type=float, default=1.0,
+                    help="SOR relaxation W (dWorldSetQuickStepW); the reference's default 1.3 stalls when warm-started")
     ap.add_argument("--max-iters", type=int, default=3000)
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--warm-scale", type=float, default=1.0,
+                    help="previous-step lambda warm start from the contact cache (0 = cold start)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="run N steps only (for ncu), no JSON")
@@ -198,6 +205,9 @@ def run_gbode(args, ws, rank, local):
     stream = torch.cuda.Stream(device=dev)
     sc = scenes.pile(args.n, seed=1 + rank)
     w = sim.GBWorld(sc, stream=ctypes.c_void_p(stream.cuda_stream))
+    if args.warm_scale > 0:
+        L.gbodeWorldSetWarmStart(w.w, 1, args.warm_scale)
+    L.dWorldSetQuickStepW(w.w, args.sor_w)
     # settle with the configured 30 sweeps per step (untimed)
     for _ in range(args.settle):
         w.step_fused()
@@ -222,6 +232,7 @@ def run_gbode(args, ws, rank, local):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    torch.cuda.nvtx.range_push("timed")
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -239,6 +250,7 @@ def run_gbode(args, ws, rank, local):
         rows.append(st.rows)
         contacts.append(st.contacts)
         colours.append(st.colours)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = L.gbodeKernelLaunchCount() - launches0
@@ -286,7 +298,8 @@ def run_gbode(args, ws, rank, local):
                    "settle_steps": args.settle, "residual_target": args.target, "check_every": args.check_every,
                    "max_sweeps": args.max_iters, "l2": "256 MB flush before every timed step (outside the events)",
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                   "solver": "coloured PGS, persistent cooperative kernel",
+                   "solver": f"coloured PGS (W {args.sor_w}), persistent cooperative kernel",
+                   "warm_start": f"previous-step lambda x {args.warm_scale}" if args.warm_scale > 0 else "cold",
                    "rows_per_step": m_mean, "contacts_per_step": float(np.mean(contacts)),
                    "colours": int(np.median(colours)), "sweeps_per_step": float(np.mean(sweeps)),
                    "steps_at_target": ok_steps, "fp32_residual_max": float(max(resid)),

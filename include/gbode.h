@@ -241,6 +241,13 @@ void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale);
 int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, const dSurfaceParameters *s,
                               int maxc);
 
+/* Pair rule of a hash space.  0 (default): exactly the pairs the reference's
+ * dHashSpace reports, including its blind spot -- the bucket of a cell is
+ * computed in unsigned arithmetic that wraps for negative z in columns near
+ * the origin (collision_space.cpp:358-361), so some overlapping pairs there
+ * are never reported.  1: every pair whose AABBs overlap. */
+void gbodeHashSpaceSetExactPairs(dSpaceID space, int exact);
+
 /* CUDA stream (cudaStream_t) the world enqueues its work on; NULL = the
  * library's own stream. */
 void gbodeWorldSetStream(dWorldID w, void *stream);
@@ -280,6 +287,11 @@ int gbodeWorldGetLastRows(dWorldID w, float *rows, int cap);
  * body indices creation order among live bodies).  Returns n (writes at most
  * cap).  Synchronises the stream. */
 int gbodeWorldGetContacts(dWorldID w, float *out, int cap);
+
+/* The FP32 relative residual at each residual check of the last solve
+ * (residual-target mode), oldest first.  Returns the number of checks (at
+ * most 256 are kept).  Synchronises the stream. */
+int gbodeWorldGetResidualHistory(dWorldID w, float *out, int cap);
 
 /* Last error message ("" if none) and clear. */
 const char *gbodeGetLastError(void);

@@ -104,12 +104,15 @@ struct dxGeom {
     float pos[4] = {0, 0, 0, 0};
     float R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
     int index = -1;  // position in its space
+    int uid = 0;     // creation serial (warm-start keys of contact joints)
 };
+static int g_geom_uid = 0;
 
 struct dxSpace {
     std::vector<dxGeom *> geoms;
     int minlevel = -3, maxlevel = 10;  // collision_space.cpp:371-376
     int cleanup = 1;
+    int exact_pairs = 0;               // 1: report every overlapping pair (see gbodeHashSpaceSetExactPairs)
     bool dirty = true;                 // geom set or static poses changed since the last upload
 };
 
@@ -674,6 +677,7 @@ void dHashSpaceGetLevels(dSpaceID s, int *minlevel, int *maxlevel) {
     if (maxlevel) *maxlevel = s->maxlevel;
 }
 void dSpaceSetCleanup(dSpaceID s, int mode) { s->cleanup = mode; }
+void gbodeHashSpaceSetExactPairs(dSpaceID s, int exact) { s->exact_pairs = exact != 0; }
 int dSpaceGetNumGeoms(dSpaceID s) { return (int)s->geoms.size(); }
 void dSpaceDestroy(dSpaceID s) {
     for (dxGeom *g : s->geoms) {
@@ -686,6 +690,7 @@ void dSpaceDestroy(dSpaceID s) {
 static dxGeom *geom_new(dSpaceID space, int cls) {
     dxGeom *g = new dxGeom();
     g->cls = cls;
+    g->uid = g_geom_uid++;
     if (space) {
         g->space = space;
         // dSpaceAdd puts new geoms at the head of the space list (collision_space.cpp:160-176)
@@ -858,7 +863,7 @@ void dSpaceCollide(dSpaceID space, void *data, dNearCallback *callback) {
     int ng = (int)space->geoms.size();
     cudaStream_t s = w->stream;
     launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
-    if (!launch_broadphase(w->ws, ng, space->maxlevel, s)) { set_error("broad phase"); return; }
+    if (!launch_broadphase(w->ws, ng, space->exact_pairs, s)) { set_error("broad phase"); return; }
     int np = 0;
     cudaMemcpyAsync(&np, &w->ws.dc->npairs, 4, cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
@@ -895,7 +900,7 @@ int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, c
     staged = surf;
     cudaMemcpyAsync(w->ws.surfaces.p, &staged, sizeof(Surface), cudaMemcpyHostToDevice, s);
     launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
-    if (!launch_broadphase(w->ws, ng, space->maxlevel, s)) { set_error("broad phase"); return 0; }
+    if (!launch_broadphase(w->ws, ng, space->exact_pairs, s)) { set_error("broad phase"); return 0; }
     if (!launch_narrowphase(w->ws, maxc, 0, false, s)) { set_error("narrow phase"); return 0; }
     w->device_contacts = true;
     w->device_surfaces = 1;
@@ -1083,9 +1088,10 @@ static bool upload_host_contacts(dxWorld *w, const std::vector<dxJoint *> &js) {
         o.b1 = js[k]->b1 ? js[k]->b1->index : -1;
         o.b2 = js[k]->b2 ? js[k]->b2->index : -1;
         o.surf = k;
-        o.slot = 0;
-        o.g1 = c.geom.g1 ? c.geom.g1->index : -1;
-        o.g2 = c.geom.g2 ? c.geom.g2->index : -1;
+        o.g1 = c.geom.g1 ? c.geom.g1->uid : -1;
+        o.g2 = c.geom.g2 ? c.geom.g2->uid : -1;
+        // slot: position among consecutive contacts of the same geom pair
+        o.slot = (k > 0 && C[k - 1].g1 == o.g1 && C[k - 1].g2 == o.g2) ? C[k - 1].slot + 1 : 0;
         o.pad0 = o.pad1 = 0;
         Surface &s = S[k];
         memset(&s, 0, sizeof s);
@@ -1178,7 +1184,7 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         cudaMemcpyAsync(w->ws.hc, w->ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream);
         cudaStreamSynchronize(w->stream);
         const DevCounters &h = *w->ws.hc;
-        w->stats.contacts = h.ncontacts;
+        w->stats.contacts = h.step_contacts;
         w->stats.rows = h.nrows;
         w->stats.colours = h.ncolours;
         w->stats.iterations = h.iterations;
@@ -1199,6 +1205,15 @@ double gbodeWorldLastResidual(dWorldID w, double *complementarity, double *max_l
 }
 
 int gbodeWorldGetLastRows(dWorldID w, float *rows, int cap) { return copy_last_rows(w->ws, rows, cap, w->stream); }
+
+int gbodeWorldGetResidualHistory(dWorldID w, float *out, int cap) {
+    if (!w->ws.dc) return 0;
+    cudaMemcpyAsync(w->ws.hc, w->ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    int n = w->ws.hc->nhist;
+    if (out) for (int i = 0; i < n && i < cap; i++) out[i] = w->ws.hc->rhist[i];
+    return n;
+}
 
 int gbodeWorldGetContacts(dWorldID w, float *out, int cap) {
     if (!w->ws.dc) return 0;

@@ -145,6 +145,20 @@ __global__ void k_bp_fill(int ng, const int *entry, const int *start, int *fill,
     members[pos] = e >> 3;
 }
 
+// The reference hashes a cell as (level*1000 + x*100 + y*10 + zbegin) % size
+// with level, x, y as unsigned int and zbegin the int z at which a box starts
+// its column (collision_space.cpp:358-361, :497-499, :545-547), summed in
+// unsigned long.  When zbegin is negative and the column base is smaller than
+// |zbegin| the sum wraps through 2^64, which shifts the bucket by 2^64 mod
+// size: a box that starts its column there and one that does not then look in
+// different buckets for the same cell and never meet.  column_wraps() tells
+// which side of that split a box is on in a given column.
+__device__ __forceinline__ bool column_wraps(int level, int x, int y, int zbegin) {
+    unsigned long long base = (unsigned long long)(unsigned)level * 1000ull + (unsigned long long)(unsigned)x * 100ull +
+                              (unsigned long long)(unsigned)y * 10ull;
+    return zbegin < 0 && base < (unsigned long long)(-(long long)zbegin);
+}
+
 __device__ __forceinline__ int lookup(const unsigned long long *keys, unsigned mask, unsigned long long key) {
     unsigned h = hash64(key) & mask;
     for (unsigned probe = 0; probe <= mask; probe++) {
@@ -169,7 +183,7 @@ __device__ __forceinline__ bool aabb_pair_ok(const Geoms &G, int a, int b) {
 template <int PASS>
 __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mask, const int *start, const int *count,
                            const int *members, const int *big_list, int *pcount, const int *pstart, int2 *pairs,
-                           int pair_cap, DevCounters *dc) {
+                           int pair_cap, DevCounters *dc, int exact) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= G.n) return;
     int la = G.level[a];
@@ -191,9 +205,24 @@ __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mas
                             int b = members[s];
                             if (b == a) continue;
                             if (L == la && b < a) continue;
-                            int4 blo = G.dblo[b];
-                            int cx = max(x0, blo.x), cy = max(y0, blo.y), cz = max(z0, blo.z);
-                            if (cx != x || cy != y || cz != z) continue;
+                            int4 blo = G.dblo[b], bhi = G.dbhi[b];
+                            int cz = max(z0, blo.z);
+                            if (cz != z) continue;
+                            if (exact) {
+                                // every overlapping pair, once: in the low-corner cell of the overlap
+                                if (max(x0, blo.x) != x || max(y0, blo.y) != y) continue;
+                            } else {
+                                // the reference's rule: the pair meets in the first overlap column
+                                // (x, then y ascending) where both boxes hash their column alike
+                                int fx = 0x7fffffff, fy = 0;
+                                for (int cx = max(x0, blo.x); cx <= min(x1, bhi.x) && fx == 0x7fffffff; cx++)
+                                    for (int cy = max(y0, blo.y); cy <= min(y1, bhi.y); cy++)
+                                        if (column_wraps(L, cx, cy, z0) == column_wraps(L, cx, cy, blo.z)) {
+                                            fx = cx; fy = cy;
+                                            break;
+                                        }
+                                if (fx != x || fy != y) continue;
+                            }
                             if (!aabb_pair_ok(G, a, b)) continue;
                             if (PASS) {
                                 int idx = base + n;
@@ -363,7 +392,7 @@ static unsigned table_mask(int ng) {
     return sz - 1;
 }
 
-bool launch_broadphase(Workspace &ws, int ng, int, cudaStream_t s) {
+bool launch_broadphase(Workspace &ws, int ng, int exact, cudaStream_t s) {
     unsigned mask = table_mask(ng);
     size_t tsz = (size_t)mask + 1;
     size_t nge = ng > 0 ? ng : 1;
@@ -387,11 +416,12 @@ bool launch_broadphase(Workspace &ws, int ng, int, cudaStream_t s) {
                                                     ws.h_members.as<int>());
     k_bp_pairs<0><<<grid_for(ng, 128), 128, 0, s>>>(G, ws.h_keys.as<unsigned long long>(), mask, ws.h_start.as<int>(),
                                                     ws.h_count.as<int>(), ws.h_members.as<int>(), ws.g_big.as<int>(),
-                                                    ws.p_count.as<int>(), nullptr, nullptr, 0, ws.dc);
+                                                    ws.p_count.as<int>(), nullptr, nullptr, 0, ws.dc, exact);
     scan_exclusive(ws.p_count.as<int>(), ws.p_start.as<int>(), nullptr, ng, &ws.dc->npairs, ws, s);
     k_bp_pairs<1><<<grid_for(ng, 128), 128, 0, s>>>(G, ws.h_keys.as<unsigned long long>(), mask, ws.h_start.as<int>(),
                                                     ws.h_count.as<int>(), ws.h_members.as<int>(), ws.g_big.as<int>(),
-                                                    nullptr, ws.p_start.as<int>(), ws.pairs.as<int2>(), ws.pair_cap, ws.dc);
+                                                    nullptr, ws.p_start.as<int>(), ws.pairs.as<int2>(), ws.pair_cap, ws.dc,
+                                                    exact);
     k_bp_finish<<<1, 1, 0, s>>>(ws.dc, ws.pair_cap);
     count_launch(5);
     return cudaGetLastError() == cudaSuccess;

@@ -55,6 +55,9 @@ struct DevCounters {
     int cells_total;   // scan scratch (hash cells)
     int colour_total;  // scan scratch (colours)
     float racc[4];     // residual / max|lambda| accumulators, two parities
+    int step_contacts; // contacts of the last dWorldQuickStep (survives dJointGroupEmpty)
+    int nhist;         // residual checks recorded in rhist by the last solve
+    float rhist[256];  // FP32 relative residual at each check of the last solve
     GridSync gsync;    // grid barrier state (zeroed before cooperative launches)
 };
 
@@ -79,6 +82,9 @@ struct Workspace {
     DBuf res_f, res_v;
     // scan scratch
     DBuf scan_tmp;
+    int warm_parity = 0;         // which of the two warm-start tables holds the previous step
+    unsigned warm_mask = 0;      // table size - 1 (power of two)
+    bool warm_valid = false;     // the previous-step table was filled
     DevCounters *dc = nullptr;   // device counters
     DevCounters *hc = nullptr;   // pinned host mirror
     int pair_cap = 0, contact_cap = 0, row_cap = 0;
@@ -101,8 +107,9 @@ struct GeomHost {
 bool upload_geoms(Workspace &ws, const std::vector<GeomHost> &g, cudaStream_t s);
 // pose geoms from bodies, AABBs, levels (one launch)
 void launch_pose_aabb(Workspace &ws, const Bodies &b, int ng, int minlevel, int maxlevel, cudaStream_t s);
-// hash-space broad phase into ws.pairs (device count in dc->npairs)
-bool launch_broadphase(Workspace &ws, int ng, int maxlevel_hint, cudaStream_t s);
+// hash-space broad phase into ws.pairs (device count in dc->npairs); exact = 1
+// reports every AABB-overlapping pair, 0 reproduces the reference's pair set
+bool launch_broadphase(Workspace &ws, int ng, int exact, cudaStream_t s);
 // narrow phase on the pair list; contacts compacted into ws.contacts with
 // surface index `surf`; codes (dBoxBox return_code, -1 n/a) optional per slot
 bool launch_narrowphase(Workspace &ws, int maxc, int surf, bool append, cudaStream_t s);

@@ -152,13 +152,31 @@ __global__ void k_contact_m(const Contact *C, const Surface *S, const int *nc_de
 
 __global__ void k_rows_total(DevCounters *dc, int row_cap) {
     if (dc->nrows > row_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); dc->nrows = row_cap; }
+    dc->step_contacts = dc->ncontacts;
 }
 
 // Contact rows: getInfo2 (contact.cpp:126-347) + Stage2a scaling (quickstep.cpp
 // :1555-1561) + Stage2c J*rhs_tmp (:1022-1055) + compute_invM_JT (:858-897) +
 // Ad scaling (:2251-2316) for each of the contact's rows.
+// Warm-start cache: (geom pair, contact slot) -> the contact's first three
+// multipliers of the previous step, in an open-addressed table.
+__device__ __forceinline__ unsigned long long warm_key(const Contact &k) {
+    return ((unsigned long long)(unsigned)k.g1 << 40) ^ ((unsigned long long)(unsigned)k.g2 << 8) ^
+           (unsigned long long)(unsigned)(k.slot & 0xff);
+}
+__device__ __forceinline__ unsigned warm_hash(unsigned long long k) {
+    k ^= k >> 31; k *= 0x7fb5d329728ea185ull; k ^= k >> 27; k *= 0x81dadef4bc2dd44dull; k ^= k >> 33;
+    return (unsigned)k;
+}
+struct WarmTable {
+    const unsigned long long *keys;  // previous step (read)
+    const float4 *lam;
+    unsigned mask;
+    float scale;
+};
+
 __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, const int *rstart, Bodies B,
-                       Rows Rw, SolverParams P, int dyn_maxabs, const float *warm, DevCounters *dc) {
+                       Rows Rw, SolverParams P, int dyn_maxabs, WarmTable W, DevCounters *dc) {
     const int nc = *nc_dev;
     const float h = P.dt, rh = 1.0f / h;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -283,6 +301,22 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
                 }
             }
         }
+        // warm start: the previous step's multipliers of this (geom pair, slot)
+        float warm3[3] = {0.f, 0.f, 0.f};
+        if (W.keys) {
+            const unsigned long long key = warm_key(k);
+            unsigned h = warm_hash(key) & W.mask;
+            for (unsigned probe = 0; probe <= W.mask; probe++) {
+                const unsigned long long kk = W.keys[h];
+                if (kk == key) {
+                    const float4 l = W.lam[h];
+                    warm3[0] = l.x * W.scale; warm3[1] = l.y * W.scale; warm3[2] = l.z * W.scale;
+                    break;
+                }
+                if (kk == ~0ull) break;
+                h = (h + 1) & W.mask;
+            }
+        }
         // per-row finishing
         float4 rt0l = B.rt[2 * n0], rt0a = B.rt[2 * n0 + 1];
         float4 rt1l = make_float4(0, 0, 0, 0), rt1a = rt1l;
@@ -335,7 +369,26 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
             Rw.findex[gr] = findex[r] >= 0 ? r0 + findex[r] : -1;
             Rw.body[gr] = make_int2(n0, n1);
             Rw.contact[gr] = c;
-            Rw.lambda[gr] = warm ? warm[gr] : 0.f;
+            Rw.lambda[gr] = r < 3 ? warm3[r] : 0.f;
+        }
+    }
+}
+
+__global__ void k_warm_store(const Contact *C, const int *nc_dev, const int *rstart, const int *mcount, Rows Rw,
+                             unsigned long long *keys, float4 *lam, unsigned mask) {
+    const int nc = *nc_dev;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const Contact k = C[c];
+        const unsigned long long key = warm_key(k);
+        unsigned h = warm_hash(key) & mask;
+        for (unsigned probe = 0; probe <= mask; probe++) {
+            unsigned long long prev = atomicCAS(&keys[h], ~0ull, key);
+            if (prev == ~0ull || prev == key) {
+                const int r0 = rstart[c], m = mcount[c];
+                lam[h] = make_float4(Rw.lambda[r0], m > 1 ? Rw.lambda[r0 + 1] : 0.f, m > 2 ? Rw.lambda[r0 + 2] : 0.f, 0.f);
+                break;
+            }
+            h = (h + 1) & mask;
         }
     }
 }
@@ -504,15 +557,27 @@ struct PgsArgs {
     DevCounters *dc;
     int iterations, max_iterations, check_every;
     float target, w_sor;
+    int warm;  // lambda starts non-zero: fc = M^-1 J^T lambda is formed first
+    int nb;    // bodies (fc is re-formed from lambda at every residual check)
 };
 
-__device__ __forceinline__ float atomic_max_pos(float *addr, float v) {
-    return __int_as_float(atomicMax((int *)addr, __float_as_int(v)));
+// Prefetch a manifold's rows into L1: the rows are read-only during the
+// sweeps and contiguous per manifold, so the sequential relaxation below then
+// runs from L1 instead of paying an L2 round trip per row.
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_rows(const Rows &Rw, int r0, int r1) {
+    const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+        const char *b = (const char *)(arr[a] + r0), *e = (const char *)(arr[a] + r1);
+        for (const char *q = (const char *)((uintptr_t)b & ~(uintptr_t)127); q < e; q += 128) prefetch_l1(q);
+    }
+    const char *fb = (const char *)(Rw.findex + r0), *fe = (const char *)(Rw.findex + r1);
+    for (const char *q = (const char *)((uintptr_t)fb & ~(uintptr_t)127); q < fe; q += 128) prefetch_l1(q);
 }
 
-// One manifold: normal (findex < 0) rows of all its contacts first, then the
-// friction rows, mirroring the reference's findex partition.
-__device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
+// fc += M^-1 J^T lambda for one manifold's rows (warm start)
+__device__ __forceinline__ void apply_manifold(const PgsArgs &A, int e) {
     const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
     const int r0 = A.rstart[c0];
     const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
@@ -521,12 +586,191 @@ __device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
     float4 f1l = ldcg4(&A.fc[2 * b.x]), f1a = ldcg4(&A.fc[2 * b.x + 1]);
     float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
     if (two) { f2l = ldcg4(&A.fc[2 * b.y]); f2a = ldcg4(&A.fc[2 * b.y + 1]); }
-    for (int r = r0; r < r1; r++)
-        if (A.Rw.findex[r] < 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
-    for (int r = r0; r < r1; r++)
-        if (A.Rw.findex[r] >= 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+    for (int r = r0; r < r1; r++) {
+        const float l = A.Rw.lambda[r];
+        if (l == 0.f) continue;
+        const float4 m1l = A.Rw.M1l[r], m1a = A.Rw.M1a[r];
+        f1l.x += l * m1l.x; f1l.y += l * m1l.y; f1l.z += l * m1l.z;
+        f1a.x += l * m1a.x; f1a.y += l * m1a.y; f1a.z += l * m1a.z;
+        if (two) {
+            const float4 m2l = A.Rw.M2l[r], m2a = A.Rw.M2a[r];
+            f2l.x += l * m2l.x; f2l.y += l * m2l.y; f2l.z += l * m2l.z;
+            f2a.x += l * m2a.x; f2a.y += l * m2a.y; f2a.z += l * m2a.z;
+        }
+    }
     stcg4(&A.fc[2 * b.x], f1l); stcg4(&A.fc[2 * b.x + 1], f1a);
     if (two) { stcg4(&A.fc[2 * b.y], f2l); stcg4(&A.fc[2 * b.y + 1], f2a); }
+}
+
+__device__ __forceinline__ float atomic_max_pos(float *addr, float v) {
+    return __int_as_float(atomicMax((int *)addr, __float_as_int(v)));
+}
+
+// One manifold: normal (findex < 0) rows of all its contacts first, then the
+// friction rows, mirroring the reference's findex partition.
+// Rows of one manifold whose multipliers stay in thread-local storage while
+// the manifold is relaxed: the rows' own previous values and the normal-row
+// multipliers the friction bounds read are then L1/register hits instead of L2
+// round trips inside the row-to-row dependency chain.
+#define GB_MANIFOLD_ROWS 24
+
+// quickstep.cpp:2917-3033 for one row, multipliers from the local copy
+__device__ __forceinline__ void relax_row_local(const Rows &Rw, int r, float &lam_r, float lam_f, bool has_f,
+                                                float4 &f1l, float4 &f1a, float4 &f2l, float4 &f2a, bool two) {
+    const float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
+    const float old = lam_r;
+    float delta = j1l.w - old * j1a.w;
+    delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
+    if (two) delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
+    float lo, hi;
+    if (has_f) { hi = fabsf(j2a.w * lam_f); lo = -hi; }
+    else { hi = j2a.w; lo = j2l.w; }
+    float nl = old + delta;
+    if (nl < lo) { delta = lo - old; nl = lo; }
+    else if (nl > hi) { delta = hi - old; nl = hi; }
+    lam_r = nl;
+    if (delta != 0) {
+        const float4 m1l = Rw.M1l[r], m1a = Rw.M1a[r];
+        f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
+        f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
+        if (two) {
+            const float4 m2l = Rw.M2l[r], m2a = Rw.M2a[r];
+            f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
+            f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
+        }
+    }
+}
+
+// One manifold: normal (findex < 0) rows of all its contacts first, then the
+// friction rows, mirroring the reference's findex partition.
+__device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
+    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
+    const int r0 = A.rstart[c0];
+    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
+    const int n = r1 - r0;
+    prefetch_rows(A.Rw, r0, r1);
+    const int2 b = A.Rw.body[r0];
+    const bool two = b.y >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * b.x]), f1a = ldcg4(&A.fc[2 * b.x + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (two) { f2l = ldcg4(&A.fc[2 * b.y]); f2a = ldcg4(&A.fc[2 * b.y + 1]); }
+    if (n <= GB_MANIFOLD_ROWS) {
+        float lam[GB_MANIFOLD_ROWS];
+        int fi[GB_MANIFOLD_ROWS];
+        for (int k = 0; k < n; k++) {
+            lam[k] = A.Rw.lambda[r0 + k];
+            const int f = A.Rw.findex[r0 + k];
+            fi[k] = (f >= r0 && f < r1) ? f - r0 : (f >= 0 ? GB_MANIFOLD_ROWS + f : -1);
+        }
+        for (int k = 0; k < n; k++)
+            if (fi[k] < 0) relax_row_local(A.Rw, r0 + k, lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
+        for (int k = 0; k < n; k++) {
+            if (fi[k] < 0) continue;
+            // findex always names a row of the same contact, hence of this manifold;
+            // a row elsewhere is read from memory
+            const float lf = fi[k] < GB_MANIFOLD_ROWS ? lam[fi[k]] : A.Rw.lambda[fi[k] - GB_MANIFOLD_ROWS];
+            relax_row_local(A.Rw, r0 + k, lam[k], lf, true, f1l, f1a, f2l, f2a, two);
+        }
+        for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = lam[k];
+    } else {
+        for (int r = r0; r < r1; r++)
+            if (A.Rw.findex[r] < 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+        for (int r = r0; r < r1; r++)
+            if (A.Rw.findex[r] >= 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+    }
+    stcg4(&A.fc[2 * b.x], f1l); stcg4(&A.fc[2 * b.x + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * b.y], f2l); stcg4(&A.fc[2 * b.y + 1], f2a); }
+}
+
+// Warp-cooperative relaxation of one manifold.  The warp stages the
+// manifold's rows (8 float4 each) in shared memory with coalesced loads, then
+// relaxes the rows in sequence with the 12 Jacobian / M^-1 J^T components
+// spread over lanes 0-11: a row is a 12-lane product, a shuffle reduction,
+// the clamp on lane 0 and a 12-lane fc update.  Lane k keeps the multiplier
+// of row r0 + k, so a friction bound reads its normal row's multiplier with
+// one shuffle.  Up to 32 rows; longer manifolds use the per-thread path.
+#define GB_WARP_ROWS 32
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void relax_manifold_warp(const PgsArgs &A, int e, int lane, float4 *sm) {
+    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
+    const int r0 = A.rstart[c0];
+    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
+    const int n = r1 - r0;
+    const int2 b = A.Rw.body[r0];
+    const bool two = b.y >= 0;
+    if (n > GB_WARP_ROWS) {
+        if (lane == 0) relax_manifold(A, e);
+        __syncwarp();
+        return;
+    }
+    // stage rows: sm[k*8 + a] = array a at row r0 + k
+    const float4 *arr[8] = {A.Rw.J1l, A.Rw.J1a, A.Rw.J2l, A.Rw.J2a, A.Rw.M1l, A.Rw.M1a, A.Rw.M2l, A.Rw.M2a};
+    for (int idx = lane; idx < n * 8; idx += 32) {
+        const int k = idx >> 3, a = idx & 7;
+        sm[idx] = arr[a][r0 + k];
+    }
+    // body accumulators: lanes 0-5 body 1 (l.xyz, a.xyz), lanes 6-11 body 2
+    float fcv = 0.f;
+    {
+        const int which = lane < 6 ? 0 : 1, comp = lane % 6;
+        const int body = which ? b.y : b.x;
+        if (lane < 12 && (which == 0 || two)) {
+            const float *f = (const float *)(A.fc + 2 * body);
+            fcv = __ldcg(f + (comp < 3 ? comp : 4 + comp - 3));
+        }
+    }
+    float lamk = 0.f;
+    int fik = -1;
+    if (lane < n) {
+        lamk = A.Rw.lambda[r0 + lane];
+        const int f = A.Rw.findex[r0 + lane];
+        fik = f < 0 ? -1 : (f >= r0 && f < r1 ? f - r0 : 1000 + f);
+    }
+    __syncwarp();
+    // component layout inside a staged row (floats): J1l 0-3, J1a 4-7, J2l 8-11,
+    // J2a 12-15, M1l 16-19, M1a 20-23, M2l 24-27, M2a 28-31
+    const int jpos = lane < 3 ? lane : lane < 6 ? 4 + lane - 3 : lane < 9 ? 8 + lane - 6 : 12 + lane - 9;
+    const bool active = lane < 6 || (two && lane < 12);
+    for (int pass = 0; pass < 2; pass++) {
+        for (int k = 0; k < n; k++) {
+            const int fk = __shfl_sync(0xffffffffu, fik, k);
+            if ((fk < 0) != (pass == 0)) continue;
+            const float *row = (const float *)(sm + k * 8);
+            const float part = active ? row[jpos] * fcv : 0.f;
+            // one value for every lane: the butterfly sums in a lane-dependent order
+            const float dot = __shfl_sync(0xffffffffu, warp_sum(part), 0);
+            const float old = __shfl_sync(0xffffffffu, lamk, k);
+            float lf = 0.f;
+            if (fk >= 0) {
+                if (fk < 1000) lf = __shfl_sync(0xffffffffu, lamk, fk);
+                else lf = A.Rw.lambda[fk - 1000];
+            }
+            // quickstep.cpp:2917-3033 on every lane (same inputs, same result)
+            const float rhs = row[3], cfm = row[7], lo0 = row[11], hi0 = row[15];
+            float delta = rhs - old * cfm;
+            delta -= dot;
+            float lo, hi;
+            if (fk >= 0) { hi = fabsf(hi0 * lf); lo = -hi; }
+            else { hi = hi0; lo = lo0; }
+            float nl = old + delta;
+            if (nl < lo) { delta = lo - old; nl = lo; }
+            else if (nl > hi) { delta = hi - old; nl = hi; }
+            if (lane == k) lamk = nl;
+            if (active && delta != 0) fcv += delta * row[16 + jpos];
+        }
+    }
+    if (lane < n) A.Rw.lambda[r0 + lane] = lamk;
+    if (lane < 12 && (lane < 6 || two)) {
+        const int which = lane < 6 ? 0 : 1, comp = lane % 6;
+        float *f = (float *)(A.fc + 2 * (which ? b.y : b.x));
+        __stcg(f + (comp < 3 ? comp : 4 + comp - 3), fcv);
+    }
+    __syncwarp();
 }
 
 __global__ void k_pgs(PgsArgs A) {
@@ -535,18 +779,42 @@ __global__ void k_pgs(PgsArgs A) {
     const int ncol = dc->ncolours;
     const int nrows = dc->nrows;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31, wid = tid >> 5, nwarps = nth >> 5;
+    extern __shared__ float4 pgs_smem[];
+    float4 *wsm = pgs_smem + (threadIdx.x >> 5) * (GB_WARP_ROWS * 8);
     const bool residual_mode = A.target > 0;
     const int itmax = residual_mode ? A.max_iterations : A.iterations;
     int it = 0, check = 0;
     float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
+    if (A.warm) {
+        // colour by colour, so no two manifolds of a pass touch one body
+        for (int c = 0; c < ncol; c++) {
+            const int s = A.cstart[c], n = A.ccount[c];
+            for (int k = tid; k < n; k += nth) apply_manifold(A, A.clist[s + k]);
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+        }
+    }
     for (; it < itmax;) {
         for (int c = 0; c < ncol; c++) {
             const int s = A.cstart[c], n = A.ccount[c];
-            for (int k = tid; k < n; k += nth) relax_manifold(A, A.clist[s + k]);
+            for (int k = wid; k < n; k += nwarps) relax_manifold_warp(A, A.clist[s + k], lane, wsm);
             if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
         }
         ++it;
         if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
+            // Re-form fc = M^-1 J^T lambda from lambda: thousands of incremental FP32
+            // updates let fc drift from the multipliers it stands for, and relaxation
+            // against a drifted fc stalls at a residual of ~1e-4..1e-3 on deep piles.
+            for (int b = tid; b < A.nb; b += nth) {
+                stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
+                stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
+            }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            for (int c = 0; c < ncol; c++) {
+                const int s = A.cstart[c], n = A.ccount[c];
+                for (int k = tid; k < n; k += nth) apply_manifold(A, A.clist[s + k]);
+                if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            }
             float *acc = slots + 2 * (check & 1);
             float rmax = 0.f, lmax = 0.f;
             for (int r = tid; r < nrows; r += nth) {
@@ -565,6 +833,7 @@ __global__ void k_pgs(PgsArgs A) {
                 float *other = slots + 2 * ((check + 1) & 1);
                 other[0] = 0.f; other[1] = 0.f;
                 dc->resid = rel; dc->maxlam = ll;
+                if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
             }
             ++check;
             if (rel <= A.target) break;
@@ -869,17 +1138,54 @@ static Rows rows_view(Workspace &ws) {
     return R;
 }
 
-static int coop_blocks(const void *kernel, int block) {
+static int coop_blocks(const void *kernel, int block, int max_per_sm) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
     if (per_sm < 1) per_sm = 1;
-    if (per_sm > 2) per_sm = 2;
+    if (per_sm > max_per_sm) per_sm = max_per_sm;
     return per_sm * num_sms();
+}
+
+static bool ensure_warm(Workspace &ws) {
+    unsigned want = 1024;
+    while (want < 2u * (unsigned)(ws.contact_cap > 0 ? ws.contact_cap : 1) && want < (1u << 23)) want <<= 1;
+    if (ws.warm_mask + 1 != want) {
+        if (!(ws.w_keys.ensure((size_t)2 * want * 8) && ws.w_lambda.ensure((size_t)2 * want * 16))) return false;
+        ws.warm_mask = want - 1;
+        ws.warm_valid = false;
+    }
+    return true;
+}
+
+static WarmTable warm_lookup(Workspace &ws, const SolverParams &P) {
+    WarmTable W{nullptr, nullptr, 0, 0.f};
+    if (P.warm_mode && ws.warm_valid) {
+        size_t T = (size_t)ws.warm_mask + 1;
+        W.keys = ws.w_keys.as<unsigned long long>() + T * ws.warm_parity;
+        W.lam = ws.w_lambda.as<float4>() + T * ws.warm_parity;
+        W.mask = ws.warm_mask;
+        W.scale = P.warm_scale;
+    }
+    return W;
+}
+
+static void warm_store(Workspace &ws, cudaStream_t s) {
+    size_t T = (size_t)ws.warm_mask + 1;
+    int cur = ws.warm_parity ^ 1;
+    unsigned long long *keys = ws.w_keys.as<unsigned long long>() + T * cur;
+    float4 *lam = ws.w_lambda.as<float4>() + T * cur;
+    cudaMemsetAsync(keys, 0xFF, T * 8, s);
+    k_warm_store<<<4 * num_sms(), 256, 0, s>>>(ws.contacts.as<Contact>(), &ws.dc->ncontacts, ws.c_rstart.as<int>(),
+                                               ws.c_mcount.as<int>(), rows_view(ws), keys, lam, ws.warm_mask);
+    count_launch();
+    ws.warm_parity = cur;
+    ws.warm_valid = true;
 }
 
 static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
     Bodies B = bodies_view(ws, nb);
     if (!ensure_rows(ws, ws.contact_cap)) return false;
+    if (P.warm_mode && !ensure_warm(ws)) return false;
     k_bodies<<<grid_for(nb, 128), 128, 0, s>>>(B, P);
     int grid = 4 * num_sms();
     const Contact *C = ws.contacts.as<Contact>();
@@ -888,7 +1194,8 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nrows, ws, s);
     k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
     const int dyn = (P.solver == 1) && (P.premature_delta != 0 || P.extra_factor != 0);
-    k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn, nullptr, ws.dc);
+    k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn,
+                               warm_lookup(ws, P), ws.dc);
     count_launch(4);
     return true;
 }
@@ -909,7 +1216,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     cudaMemsetAsync(&ws.dc->ncolours, 0, 4, s);
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     {
-        int blocks = coop_blocks((const void *)k_colour, 256);
+        int blocks = coop_blocks((const void *)k_colour, 256, 2);
         unsigned long long *mask = ws.m_mask.as<unsigned long long>();
         int *claim = ws.m_claim.as<int>(), *colour = ws.m_colour.as<int>(), *tent = ws.m_tent.as<int>();
         const int *mstart = ws.m_start.as<int>();
@@ -928,6 +1235,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
     cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->nhist, 0, 4, s);
     if (ev0) cudaEventRecord(ev0, s);
     {
         PgsArgs A;
@@ -942,11 +1250,25 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.check_every = P.check_every > 0 ? P.check_every : 10;
         A.target = P.residual_target;
         A.w_sor = P.w;
-        int blocks = coop_blocks((const void *)k_pgs, 256);
+        A.warm = P.warm_mode != 0;
+        A.nb = nb;
+        // one block per SM: the grid barrier's cost grows with the block count
+        const int threads = 1024;
+        const size_t smem = (size_t)(threads / 32) * GB_WARP_ROWS * 8 * sizeof(float4);  // 128 KB
+        static bool smem_set = false;
+        if (!smem_set) {
+            cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            smem_set = true;
+        }
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, (const void *)k_pgs, threads, smem, 0);
+        int blocks = (per_sm >= 1 ? 1 : 0) * num_sms();
+        if (blocks == 0) return false;
         void *args[] = {(void *)&A};
-        if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, 256, args, 0, s) != cudaSuccess) return false;
+        if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, threads, args, smem, s) != cudaSuccess) return false;
     }
     if (ev1) cudaEventRecord(ev1, s);
+    if (P.warm_mode) warm_store(ws, s);
     k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
     count_launch(9);
     return cudaGetLastError() == cudaSuccess;

@@ -122,6 +122,7 @@ _PROTOS = [
     ("gbodeWorldSetResidualTarget", None, [ID, dReal, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetWarmStart", None, [ID, ctypes.c_int, dReal]),
     ("gbodeSpaceCollideContacts", ctypes.c_int, [ID, ID, ID, ctypes.POINTER(dSurfaceParameters), ctypes.c_int]),
+    ("gbodeHashSpaceSetExactPairs", None, [ID, ctypes.c_int]),
     ("gbodeWorldSetStream", None, [ID, ctypes.c_void_p]), ("gbodeWorldGetStream", ctypes.c_void_p, [ID]),
     ("gbodeWorldSynchronize", ctypes.c_int, [ID]),
     ("gbodeWorldGetStepStats", None, [ID, ctypes.POINTER(gbodeStepStats)]),
@@ -130,6 +131,7 @@ _PROTOS = [
                                                  ctypes.POINTER(ctypes.c_double)]),
     ("gbodeWorldGetLastRows", ctypes.c_int, [ID, _F, ctypes.c_int]),
     ("gbodeWorldGetContacts", ctypes.c_int, [ID, _F, ctypes.c_int]),
+    ("gbodeWorldGetResidualHistory", ctypes.c_int, [ID, _F, ctypes.c_int]),
     ("gbodeGetLastError", ctypes.c_char_p, []), ("gbodeKernelLaunchCount", ctypes.c_longlong, []),
     ("gbodeWorldGetBodyCount", ctypes.c_int, [ID]), ("gbodeWorldGetState", None, [ID, _F]),
     ("gbodeWorldSetState", None, [ID, _F]),

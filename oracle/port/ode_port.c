@@ -1034,7 +1034,7 @@ static void hash_collide(int n, const int *order, const int *body, const real *a
         for (int xi = db[0]; xi <= db[1]; xi++) {
             for (int yi = db[2]; yi <= db[3]; yi++) {
                 int zbegin = db[4];
-                unsigned long hi = ((unsigned long)hb[b].level * 1000UL + (unsigned long)(unsigned)xi * 100UL +
+                unsigned long hi = ((unsigned long)(unsigned)hb[b].level * 1000UL + (unsigned long)(unsigned)xi * 100UL +
                                     (unsigned long)(unsigned)yi * 10UL + (unsigned long)(long)zbegin) % sz;
                 for (int zi = zbegin; zi <= db[5]; (hi = hi + 1U != sz ? hi + 1U : 0UL), zi++) {
                     if (nn == ncap) { ncap *= 2; nodes = (hnode *)realloc(nodes, sizeof(hnode) * ncap); }
@@ -1053,7 +1053,7 @@ static void hash_collide(int n, const int *order, const int *body, const real *a
             for (int xi = db[0]; xi <= db[1]; xi++) {
                 for (int yi = db[2]; yi <= db[3]; yi++) {
                     int zbegin = db[4];
-                    unsigned long hi = ((unsigned long)level * 1000UL + (unsigned long)(unsigned)xi * 100UL +
+                    unsigned long hi = ((unsigned long)(unsigned)level * 1000UL + (unsigned long)(unsigned)xi * 100UL +
                                         (unsigned long)(unsigned)yi * 10UL + (unsigned long)(long)zbegin) % sz;
                     for (int zi = zbegin; zi <= db[5]; (hi = hi + 1U != sz ? hi + 1U : 0UL), zi++) {
                         for (int nd = table[hi]; nd >= 0; nd = nodes[nd].next) {

@@ -306,6 +306,53 @@ def gen_steps(exes):
         np.savez_compressed(os.path.join(HERE, f"step_{name}.npz"), **out)
 
 
+def gen_space_pile(exes):
+    """A settled pile (4096 bodies, 200 steps of the oracle, which is bit-exact
+    with the reference's loop) and the reference's hash-space pair set on its
+    poses: bodies resting slightly below z = 0 in the columns at the container
+    corner exercise the reference's unsigned bucket arithmetic."""
+    from oracle.port.port import Port
+    P = Port()
+    sc = scenes.pile(4096, seed=5)
+    w = P.world(sc.bodies, sc.world_params(), sc.iterations, dyn=0, reorder=0)
+    w.attach_space(sc.geom_cls, sc.geom_body, sc.geom_pos, sc.geom_R, sc.geom_dims, sc.hash_levels, sc.maxc,
+                   sc.surface_mode, sc.surface())
+    for _ in range(200):
+        w.sim_step()
+    st = w.state()
+    ng, n = sc.ng, sc.nb
+    pos = np.zeros((ng, 3), np.float32)
+    R = np.zeros((ng, 12), np.float32)
+    pos[:n], R[:n] = st[:, 0:3], st[:, 7:19]
+    # lower the pile 3 cm so resting bodies reach below z = 0 (negative z cells)
+    pos[:n, 2] -= 0.03
+    R[n:, [0, 5, 10]] = 1
+    r = Reader(run(exes["single"], "space", [np.array([ng, -3, 10], np.int32), sc.geom_cls, pos, R, sc.geom_dims]))
+    npairs = int(r.take(np.int32, 1)[0])
+    pairs = r.take(np.int32, 2 * npairs).reshape(-1, 2)
+    assert r.done()
+    np.savez_compressed(os.path.join(HERE, "space_pile.npz"), cls=sc.geom_cls, pos=pos, R=R, dims=sc.geom_dims,
+                        body=sc.geom_body, pairs=pairs)
+    # pairs whose AABBs overlap but the reference does not report (its bucket
+    # arithmetic for negative z near the origin)
+    lo, hi = [], []
+    for i in range(n):
+        d, Rm = sc.geom_dims[i], R[i].reshape(3, 4)[:, :3]
+        if sc.geom_cls[i] == scenes.SPHERE:
+            r3 = np.full(3, d[0], np.float32)
+        else:
+            r3 = (np.float32(0.5) * (np.abs(Rm[:, 0] * d[0]) + np.abs(Rm[:, 1] * d[1]) + np.abs(Rm[:, 2] * d[2])))
+        lo.append(pos[i] - r3)
+        hi.append(pos[i] + r3)
+    lo, hi = np.array(lo, np.float32), np.array(hi, np.float32)
+    ov = np.all((lo[:, None, :] <= hi[None, :, :]) & (lo[None, :, :] <= hi[:, None, :]), axis=2)
+    ii, jj = np.nonzero(np.triu(ov, 1))
+    exact = set(zip(ii.tolist(), jj.tolist()))
+    ref_bodies = {tuple(p) for p in pairs.tolist() if p[1] < n}
+    print(f"space_pile: {ng} geoms, {npairs} reference pairs, {len(exact - ref_bodies)} overlapping pairs the "
+          f"reference misses, {len(ref_bodies - exact)} extra")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -318,6 +365,8 @@ def main():
         gen_space(exes)
     if a.only in ("", "steps"):
         gen_steps(exes)
+    if a.only in ("", "space_pile"):
+        gen_space_pile(exes)
 
 
 if __name__ == "__main__":

@@ -105,6 +105,37 @@ def test_hash_space_pairs_match_reference(gblib, golden):
         L.dSpaceDestroy(sp)
 
 
+def _space_from_arrays(L, cls, pos, R, dims):
+    sp = L.dHashSpaceCreate(None)
+    for i in range(len(cls)):
+        gg = make_geom(L, sp, cls[i], pos[i], R[i], dims[i])
+        L.dGeomSetData(gg, ctypes.c_void_p(i))
+    return sp
+
+
+@pytest.mark.parametrize("exact", [0, 1])
+def test_hash_space_settled_pile(gblib, golden, exact):
+    """Reference mode reproduces the reference's pair set on a settled pile
+    (including the overlapping pairs its unsigned bucket arithmetic drops);
+    exact mode reports every AABB-overlapping pair."""
+    from ode_gb300 import ode
+    L = gblib
+    g = golden("space_pile.npz")
+    sp = _space_from_arrays(L, g["cls"], g["pos"], g["R"], g["dims"])
+    L.gbodeHashSpaceSetExactPairs(sp, exact)
+    found = []
+    cb = ode.dNearCallback(lambda data, o1, o2: found.append((L.dGeomGetData(o1) or 0, L.dGeomGetData(o2) or 0)))
+    L.dSpaceCollide(sp, None, cb)
+    mine = {(min(a, b), max(a, b)) for a, b in found}
+    ref = {tuple(p) for p in g["pairs"].tolist()}
+    if not exact:
+        assert mine == ref
+    else:
+        # make_golden.py counted 3 AABB-overlapping pairs the reference drops
+        assert ref < mine and len(mine - ref) == 3
+    L.dSpaceDestroy(sp)
+
+
 def test_fused_contacts_match_oracle_on_a_pile(gblib, port):
     """Full-size broad + narrow phase (gbodeSpaceCollideContacts) on a settled
     32,768-body pile versus the oracle's hash space + dCollide on the same
