@@ -304,6 +304,61 @@ int gbodeWorldGetBodyCount(dWorldID w);
 void gbodeWorldGetState(dWorldID w, float *out);
 void gbodeWorldSetState(dWorldID w, const float *in);
 
+/* ---- Narrow phase that allocates nothing (no counterpart in the reference).
+ *
+ * For callers that must not allocate device memory once they run: programs
+ * that reserve all their GPU memory up front and hand out pieces of it
+ * themselves (engines, robot controllers, simulators embedded in a larger
+ * GPU application), where a cudaMalloc or cudaFree in the middle of a frame
+ * would synchronise the device, could fail under their memory budget, or is
+ * simply forbidden by the host program's allocator.
+ *
+ * gbodeCollidePairsNoAlloc runs dCollide on every pair of a batch on the
+ * device: for pair p, geoms[pairs[2p]] against geoms[pairs[2p+1]], with the
+ * same colliders, rejections (a geom with itself, two geoms on one body) and
+ * normal orientation as dCollide, and at most flags & 0xffff contacts per
+ * pair (capped at 8).  All pointers are DEVICE pointers the caller owns:
+ *   geoms     [ngeoms] gbodePairGeom records
+ *   pairs     [npairs][2] geom indices
+ *   contacts  [capacity][8] out: pos xyz, depth, normal xyz, 0 -- pair p's
+ *             contacts are rows first[p] .. first[p+1]-1 (rows at or beyond
+ *             capacity are not written)
+ *   first     [npairs+1] out: exclusive prefix sum of the per-pair counts;
+ *             first[npairs] is the total (compare it with capacity)
+ * The work is enqueued on `stream` (a cudaStream_t, NULL = the legacy default
+ * stream); read the outputs after that stream has reached this point.
+ *
+ * Limit: npairs <= GBODE_NOALLOC_MAX_PAIRS.  A larger batch is rejected:
+ * nothing is launched, the call returns 0 and gbodeGetLastError() says why;
+ * split it into several calls.  The temporaries (8 contact slots and a count
+ * per pair) live in one fixed array of 2.03 MiB in device memory that every
+ * GPU which loads this library holds until the process exits.  Each call
+ * writes every part of that array it later reads, so no state carries over
+ * between calls; but all calls share the one array, so two calls whose work
+ * can overlap on the GPU (different streams, or different host threads, with
+ * no ordering between them) race and corrupt each other's results.  Order
+ * them on one stream or wait in between.
+ *
+ * The first call on each device (with that device current) looks up the
+ * array's device address with cudaGetSymbolAddress, which can load the
+ * library's device code on that device; make that first call before any
+ * stream capture begins.
+ *
+ * Returns 1 when the work was enqueued, 0 on a rejected argument or launch
+ * error (gbodeGetLastError() has the message). */
+#define GBODE_NOALLOC_MAX_PAIRS 8192
+typedef struct gbodePairGeom {
+    int cls;          /* dSphereClass, dBoxClass, dCapsuleClass or dPlaneClass */
+    int body;         /* any id of the geom's body, -1 for none */
+    int pad[2];
+    dReal dims[4];    /* sphere: radius; box: side lengths; capsule: radius,
+                         length; plane: unit normal and offset (a, b, c, d) */
+    dReal pos[4];     /* position (xyz) */
+    dReal R[12];      /* rotation, dMatrix3 layout (3 rows of 4) */
+} gbodePairGeom;      /* 96 bytes */
+int gbodeCollidePairsNoAlloc(const gbodePairGeom *geoms, int ngeoms, const int *pairs, int npairs, int flags,
+                             float *contacts, int capacity, int *first, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

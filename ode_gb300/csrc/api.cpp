@@ -76,6 +76,9 @@ static void set_error(const char *where, cudaError_t e = cudaSuccess) {
     else snprintf(buf, sizeof buf, "%s", where);
     g_err = buf;
 }
+namespace gb {
+void report_error(const char *msg) { set_error(msg); }
+}  // namespace gb
 
 // ------------------------------------------------------------------ objects
 struct dxJoint;

@@ -143,5 +143,7 @@ void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cud
 // launch bookkeeping
 void count_launch(int n = 1);
 int num_sms();
+// records the message gbodeGetLastError() returns on this thread
+void report_error(const char *msg);
 
 }  // namespace gb

@@ -135,7 +135,12 @@ _PROTOS = [
     ("gbodeGetLastError", ctypes.c_char_p, []), ("gbodeKernelLaunchCount", ctypes.c_longlong, []),
     ("gbodeWorldGetBodyCount", ctypes.c_int, [ID]), ("gbodeWorldGetState", None, [ID, _F]),
     ("gbodeWorldSetState", None, [ID, _F]),
+    ("gbodeCollidePairsNoAlloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                 ctypes.c_void_p]),
 ]
+
+GBODE_NOALLOC_MAX_PAIRS = 8192  # gbodeCollidePairsNoAlloc's largest batch
 
 GBODE_SOLVER_COLOURED = 0
 GBODE_SOLVER_REFERENCE_ORDER = 1
