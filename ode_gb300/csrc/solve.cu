@@ -394,9 +394,9 @@ __global__ void k_warm_store(const Contact *C, const int *nc_dev, const int *rst
 }
 
 // ------------------------------------------------------------------ manifolds + colouring
-// A manifold is a maximal run of consecutive contacts on the same body pair;
-// its rows are relaxed by one thread in sequence, so manifolds, not rows, are
-// what the colouring separates.
+// A manifold is a maximal run of consecutive contacts on the same geom pair
+// (hence the same body pair); its rows are relaxed by one thread in sequence,
+// so manifolds, not rows, are what the colouring separates.
 __global__ void k_manifold_heads(const Contact *C, const int *nc_dev, int *head) {
     int nc = *nc_dev;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -405,7 +405,9 @@ __global__ void k_manifold_heads(const Contact *C, const int *nc_dev, int *head)
             const Contact a = C[c - 1], b = C[c];
             int a0 = a.b1 >= 0 ? a.b1 : a.b2, a1 = a.b1 >= 0 ? a.b2 : -1;
             int b0 = b.b1 >= 0 ? b.b1 : b.b2, b1 = b.b1 >= 0 ? b.b2 : -1;
-            h = !(a0 == b0 && a1 == b1);
+            // one manifold per geom pair: a body against two static planes
+            // (a box in a corner) gives two manifolds, each at most maxc contacts
+            h = !(a0 == b0 && a1 == b1 && a.g1 == b.g1 && a.g2 == b.g2);
         }
         head[c] = h;
     }
@@ -532,7 +534,7 @@ __device__ __forceinline__ void relax_row(const Rows &Rw, int r, float4 &f1l, fl
 __device__ __forceinline__ float row_residual(const Rows &Rw, const float4 *fc, int r, float w_sor) {
     const float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
     const int2 b = Rw.body[r];
-    const float lam = Rw.lambda[r];
+    const float lam = __ldcg(&Rw.lambda[r]);
     const float4 f1l = ldcg4(&fc[2 * b.x]), f1a = ldcg4(&fc[2 * b.x + 1]);
     float delta = j1l.w - lam * j1a.w;
     delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
@@ -542,7 +544,7 @@ __device__ __forceinline__ float row_residual(const Rows &Rw, const float4 *fc, 
     }
     float lo, hi;
     const int fi = Rw.findex[r];
-    if (fi >= 0) { hi = fabsf(j2a.w * Rw.lambda[fi]); lo = -hi; }
+    if (fi >= 0) { hi = fabsf(j2a.w * __ldcg(&Rw.lambda[fi])); lo = -hi; }
     else { hi = j2a.w; lo = j2l.w; }
     float t = lam + delta / w_sor;
     t = fminf(fmaxf(t, lo), hi);
@@ -552,72 +554,97 @@ __device__ __forceinline__ float row_residual(const Rows &Rw, const float4 *fc, 
 struct PgsArgs {
     Rows Rw;
     float4 *fc;
-    const Contact *C;
-    const int *rstart, *mcount, *mstart, *clist, *cstart, *ccount;
+    const int4 *desc;            // per colour slot: first row, row count, body 1, body 2 (-1: static)
+    const int *cstart, *ccount;  // colour ranges of desc
     DevCounters *dc;
     int iterations, max_iterations, check_every;
     float target, w_sor;
-    int warm;  // lambda starts non-zero: fc = M^-1 J^T lambda is formed first
-    int nb;    // bodies (fc is re-formed from lambda at every residual check)
+    int warm;          // lambda starts non-zero: fc = M^-1 J^T lambda is formed first
+    int nb;            // bodies
+    int reform_every;  // sweeps between re-formations of fc from lambda (residual-target mode)
 };
 
-// Prefetch a manifold's rows into L1: the rows are read-only during the
-// sweeps and contiguous per manifold, so the sequential relaxation below then
-// runs from L1 instead of paying an L2 round trip per row.
+// Manifold descriptors in colour-slot order: the solver reads one int4 per
+// manifold instead of walking colour list -> manifold -> contact -> row ->
+// bodies, four dependent memory round trips on every visit.
+//   x: first row, y: row count | GB_DESC_TRIPLETS, z: body 1, w: body 2 (-1: static)
+// GB_DESC_TRIPLETS marks the common shape of a contact manifold under
+// dContactApprox1 with mu > 0 (contact.cpp:49-122): 1..4 contacts of three
+// consecutive rows, the two friction rows' findex naming the normal row.
+#define GB_DESC_TRIPLETS (1 << 30)
+__device__ __forceinline__ int desc_rows(int4 d) { return d.y & 0xffff; }
+
+__global__ void k_manifold_desc(const int *clist, const int *mstart, const int *rstart, const int *mcount,
+                                const int2 *rbody, const int *findex, DevCounters *dc, int4 *desc) {
+    const int total = dc->colour_total;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        const int e = clist[j];
+        const int c0 = mstart[e], c1 = mstart[e + 1];
+        const int r0 = rstart[c0];
+        const int r1 = rstart[c1 - 1] + mcount[c1 - 1];
+        const int2 b = rbody[r0];
+        bool tri = c1 - c0 <= 4;
+        for (int c = c0; c < c1 && tri; c++) {
+            const int r = r0 + 3 * (c - c0);
+            tri = mcount[c] == 3 && rstart[c] == r && findex[r] < 0 && findex[r + 1] == r && findex[r + 2] == r;
+        }
+        desc[j] = make_int4(r0, (r1 - r0) | (tri ? GB_DESC_TRIPLETS : 0), b.x, b.y);
+    }
+}
+
+// Prefetch a manifold's rows into L1.  The row arrays are read-only while the
+// solver runs and a manifold's rows are contiguous, so the relaxation, issued
+// after the next grid barrier, finds them in L1 instead of paying L2 round
+// trips inside its row-to-row dependency chain.
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_span(const void *b, const void *e) {
+    for (const char *q = (const char *)((uintptr_t)b & ~(uintptr_t)127); q < (const char *)e; q += 128) prefetch_l1(q);
+}
 __device__ __forceinline__ void prefetch_rows(const Rows &Rw, int r0, int r1) {
     const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
 #pragma unroll
-    for (int a = 0; a < 8; a++) {
-        const char *b = (const char *)(arr[a] + r0), *e = (const char *)(arr[a] + r1);
-        for (const char *q = (const char *)((uintptr_t)b & ~(uintptr_t)127); q < e; q += 128) prefetch_l1(q);
-    }
-    const char *fb = (const char *)(Rw.findex + r0), *fe = (const char *)(Rw.findex + r1);
-    for (const char *q = (const char *)((uintptr_t)fb & ~(uintptr_t)127); q < fe; q += 128) prefetch_l1(q);
+    for (int a = 0; a < 8; a++) prefetch_span(arr[a] + r0, arr[a] + r1);
+    prefetch_span(Rw.findex + r0, Rw.findex + r1);
+    prefetch_span(Rw.lambda + r0, Rw.lambda + r1);
 }
 
-// fc += M^-1 J^T lambda for one manifold's rows (warm start)
-__device__ __forceinline__ void apply_manifold(const PgsArgs &A, int e) {
-    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
-    const int r0 = A.rstart[c0];
-    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
-    const int2 b = A.Rw.body[r0];
-    const bool two = b.y >= 0;
-    float4 f1l = ldcg4(&A.fc[2 * b.x]), f1a = ldcg4(&A.fc[2 * b.x + 1]);
+// fc += M^-1 J^T lambda for one manifold's rows (warm start, re-formation)
+__device__ __forceinline__ void apply_desc(const PgsArgs &A, int4 d) {
+    const bool two = d.w >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
     float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
-    if (two) { f2l = ldcg4(&A.fc[2 * b.y]); f2a = ldcg4(&A.fc[2 * b.y + 1]); }
-    for (int r = r0; r < r1; r++) {
-        const float l = A.Rw.lambda[r];
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    for (int r = d.x; r < d.x + desc_rows(d); r++) {
+        const float l = __ldcg(&A.Rw.lambda[r]);
         if (l == 0.f) continue;
-        const float4 m1l = A.Rw.M1l[r], m1a = A.Rw.M1a[r];
+        const float4 m1l = __ldg(&A.Rw.M1l[r]), m1a = __ldg(&A.Rw.M1a[r]);
         f1l.x += l * m1l.x; f1l.y += l * m1l.y; f1l.z += l * m1l.z;
         f1a.x += l * m1a.x; f1a.y += l * m1a.y; f1a.z += l * m1a.z;
         if (two) {
-            const float4 m2l = A.Rw.M2l[r], m2a = A.Rw.M2a[r];
+            const float4 m2l = __ldg(&A.Rw.M2l[r]), m2a = __ldg(&A.Rw.M2a[r]);
             f2l.x += l * m2l.x; f2l.y += l * m2l.y; f2l.z += l * m2l.z;
             f2a.x += l * m2a.x; f2a.y += l * m2a.y; f2a.z += l * m2a.z;
         }
     }
-    stcg4(&A.fc[2 * b.x], f1l); stcg4(&A.fc[2 * b.x + 1], f1a);
-    if (two) { stcg4(&A.fc[2 * b.y], f2l); stcg4(&A.fc[2 * b.y + 1], f2a); }
+    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
 __device__ __forceinline__ float atomic_max_pos(float *addr, float v) {
     return __int_as_float(atomicMax((int *)addr, __float_as_int(v)));
 }
 
-// One manifold: normal (findex < 0) rows of all its contacts first, then the
-// friction rows, mirroring the reference's findex partition.
 // Rows of one manifold whose multipliers stay in thread-local storage while
 // the manifold is relaxed: the rows' own previous values and the normal-row
-// multipliers the friction bounds read are then L1/register hits instead of L2
+// multipliers the friction bounds read are then register / L1 hits instead of
 // round trips inside the row-to-row dependency chain.
 #define GB_MANIFOLD_ROWS 24
 
-// quickstep.cpp:2917-3033 for one row, multipliers from the local copy
+// quickstep.cpp:2917-3033 for one row, multipliers from the local copy, the
+// read-only row arrays through the non-coherent cache
 __device__ __forceinline__ void relax_row_local(const Rows &Rw, int r, float &lam_r, float lam_f, bool has_f,
                                                 float4 &f1l, float4 &f1a, float4 &f2l, float4 &f2a, bool two) {
-    const float4 j1l = Rw.J1l[r], j1a = Rw.J1a[r], j2l = Rw.J2l[r], j2a = Rw.J2a[r];
+    const float4 j1l = __ldg(&Rw.J1l[r]), j1a = __ldg(&Rw.J1a[r]), j2l = __ldg(&Rw.J2l[r]), j2a = __ldg(&Rw.J2a[r]);
     const float old = lam_r;
     float delta = j1l.w - old * j1a.w;
     delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
@@ -630,45 +657,42 @@ __device__ __forceinline__ void relax_row_local(const Rows &Rw, int r, float &la
     else if (nl > hi) { delta = hi - old; nl = hi; }
     lam_r = nl;
     if (delta != 0) {
-        const float4 m1l = Rw.M1l[r], m1a = Rw.M1a[r];
+        const float4 m1l = __ldg(&Rw.M1l[r]), m1a = __ldg(&Rw.M1a[r]);
         f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
         f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
         if (two) {
-            const float4 m2l = Rw.M2l[r], m2a = Rw.M2a[r];
+            const float4 m2l = __ldg(&Rw.M2l[r]), m2a = __ldg(&Rw.M2a[r]);
             f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
             f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
         }
     }
 }
 
-// One manifold: normal (findex < 0) rows of all its contacts first, then the
-// friction rows, mirroring the reference's findex partition.
-__device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
-    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
-    const int r0 = A.rstart[c0];
-    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
-    const int n = r1 - r0;
-    prefetch_rows(A.Rw, r0, r1);
-    const int2 b = A.Rw.body[r0];
-    const bool two = b.y >= 0;
-    float4 f1l = ldcg4(&A.fc[2 * b.x]), f1a = ldcg4(&A.fc[2 * b.x + 1]);
+// One manifold by one thread: the normal (findex < 0) rows of all its
+// contacts first, then the friction rows, mirroring the reference's findex
+// partition (quickstep.cpp:2329-2355).  lambda of a manifold is read and
+// written only by the thread that owns the manifold's slot.
+__device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
+    const int r0 = d.x, n = desc_rows(d), r1 = d.x + n;
+    const bool two = d.w >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
     float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
-    if (two) { f2l = ldcg4(&A.fc[2 * b.y]); f2a = ldcg4(&A.fc[2 * b.y + 1]); }
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
     if (n <= GB_MANIFOLD_ROWS) {
         float lam[GB_MANIFOLD_ROWS];
         int fi[GB_MANIFOLD_ROWS];
         for (int k = 0; k < n; k++) {
             lam[k] = A.Rw.lambda[r0 + k];
-            const int f = A.Rw.findex[r0 + k];
+            const int f = __ldg(&A.Rw.findex[r0 + k]);
             fi[k] = (f >= r0 && f < r1) ? f - r0 : (f >= 0 ? GB_MANIFOLD_ROWS + f : -1);
         }
         for (int k = 0; k < n; k++)
             if (fi[k] < 0) relax_row_local(A.Rw, r0 + k, lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
         for (int k = 0; k < n; k++) {
             if (fi[k] < 0) continue;
-            // findex always names a row of the same contact, hence of this manifold;
-            // a row elsewhere is read from memory
-            const float lf = fi[k] < GB_MANIFOLD_ROWS ? lam[fi[k]] : A.Rw.lambda[fi[k] - GB_MANIFOLD_ROWS];
+            // findex always names a row of the same contact, hence of this
+            // manifold; a row elsewhere is read from memory
+            const float lf = fi[k] < GB_MANIFOLD_ROWS ? lam[fi[k]] : __ldcg(&A.Rw.lambda[fi[k] - GB_MANIFOLD_ROWS]);
             relax_row_local(A.Rw, r0 + k, lam[k], lf, true, f1l, f1a, f2l, f2a, two);
         }
         for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = lam[k];
@@ -678,155 +702,264 @@ __device__ __forceinline__ void relax_manifold(const PgsArgs &A, int e) {
         for (int r = r0; r < r1; r++)
             if (A.Rw.findex[r] >= 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
     }
-    stcg4(&A.fc[2 * b.x], f1l); stcg4(&A.fc[2 * b.x + 1], f1a);
-    if (two) { stcg4(&A.fc[2 * b.y], f2l); stcg4(&A.fc[2 * b.y + 1], f2a); }
+    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
-// Warp-cooperative relaxation of one manifold.  The warp stages the
-// manifold's rows (8 float4 each) in shared memory with coalesced loads, then
-// relaxes the rows in sequence with the 12 Jacobian / M^-1 J^T components
-// spread over lanes 0-11: a row is a 12-lane product, a shuffle reduction,
-// the clamp on lane 0 and a 12-lane fc update.  Lane k keeps the multiplier
-// of row r0 + k, so a friction bound reads its normal row's multiplier with
-// one shuffle.  Up to 32 rows; longer manifolds use the per-thread path.
-#define GB_WARP_ROWS 32
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
+// Per-thread staging area in shared memory for the manifold a thread relaxes
+// next: up to GB_STAGE_ROWS rows (the 8 float4 of J and M^-1 J^T), their
+// multipliers and findex.  The stride is padded by 16 B so that the LDS.128 of
+// eight consecutive threads at the same row offset fall on different banks.
+#define GB_STAGE_ROWS 12
+#define GB_PGS_THREADS 128
+struct StageSlot {
+    float4 row[GB_STAGE_ROWS * 8];
+    float lam[GB_STAGE_ROWS];
+    int fi[GB_STAGE_ROWS];
+    float4 pad;
+};
+static_assert(sizeof(StageSlot) % 16 == 0, "stage slots keep 16-byte alignment");
 
-__device__ __forceinline__ void relax_manifold_warp(const PgsArgs &A, int e, int lane, float4 *sm) {
-    const int c0 = A.mstart[e], c1 = A.mstart[e + 1];
-    const int r0 = A.rstart[c0];
-    const int r1 = A.rstart[c1 - 1] + A.mcount[c1 - 1];
-    const int n = r1 - r0;
-    const int2 b = A.Rw.body[r0];
-    const bool two = b.y >= 0;
-    if (n > GB_WARP_ROWS) {
-        if (lane == 0) relax_manifold(A, e);
-        __syncwarp();
-        return;
-    }
-    // stage rows: sm[k*8 + a] = array a at row r0 + k
+__device__ __forceinline__ void cp_async16(void *smem, const void *g) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *g) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Start copying manifold d's rows into the thread's slot (asynchronously: the
+// copies proceed while the thread waits at the grid barrier).  Rows and
+// findex are read-only during the sweeps; the multipliers of a manifold are
+// written only by the thread that owns it, i.e. this one.
+__device__ __forceinline__ bool stage_desc(const PgsArgs &A, int4 d, StageSlot *st) {
+    const int n = desc_rows(d);
+    if (n > GB_STAGE_ROWS) return false;
     const float4 *arr[8] = {A.Rw.J1l, A.Rw.J1a, A.Rw.J2l, A.Rw.J2a, A.Rw.M1l, A.Rw.M1a, A.Rw.M2l, A.Rw.M2a};
-    for (int idx = lane; idx < n * 8; idx += 32) {
-        const int k = idx >> 3, a = idx & 7;
-        sm[idx] = arr[a][r0 + k];
+    for (int k = 0; k < n; k++) {
+#pragma unroll
+        for (int a = 0; a < 8; a++) cp_async16(&st->row[k * 8 + a], arr[a] + d.x + k);
+        cp_async4(&st->lam[k], A.Rw.lambda + d.x + k);
+        cp_async4(&st->fi[k], A.Rw.findex + d.x + k);
     }
-    // body accumulators: lanes 0-5 body 1 (l.xyz, a.xyz), lanes 6-11 body 2
-    float fcv = 0.f;
-    {
-        const int which = lane < 6 ? 0 : 1, comp = lane % 6;
-        const int body = which ? b.y : b.x;
-        if (lane < 12 && (which == 0 || two)) {
-            const float *f = (const float *)(A.fc + 2 * body);
-            fcv = __ldcg(f + (comp < 3 ? comp : 4 + comp - 3));
-        }
-    }
-    float lamk = 0.f;
-    int fik = -1;
-    if (lane < n) {
-        lamk = A.Rw.lambda[r0 + lane];
-        const int f = A.Rw.findex[r0 + lane];
-        fik = f < 0 ? -1 : (f >= r0 && f < r1 ? f - r0 : 1000 + f);
-    }
-    __syncwarp();
-    // component layout inside a staged row (floats): J1l 0-3, J1a 4-7, J2l 8-11,
-    // J2a 12-15, M1l 16-19, M1a 20-23, M2l 24-27, M2a 28-31
-    const int jpos = lane < 3 ? lane : lane < 6 ? 4 + lane - 3 : lane < 9 ? 8 + lane - 6 : 12 + lane - 9;
-    const bool active = lane < 6 || (two && lane < 12);
-    for (int pass = 0; pass < 2; pass++) {
-        for (int k = 0; k < n; k++) {
-            const int fk = __shfl_sync(0xffffffffu, fik, k);
-            if ((fk < 0) != (pass == 0)) continue;
-            const float *row = (const float *)(sm + k * 8);
-            const float part = active ? row[jpos] * fcv : 0.f;
-            // one value for every lane: the butterfly sums in a lane-dependent order
-            const float dot = __shfl_sync(0xffffffffu, warp_sum(part), 0);
-            const float old = __shfl_sync(0xffffffffu, lamk, k);
-            float lf = 0.f;
-            if (fk >= 0) {
-                if (fk < 1000) lf = __shfl_sync(0xffffffffu, lamk, fk);
-                else lf = A.Rw.lambda[fk - 1000];
-            }
-            // quickstep.cpp:2917-3033 on every lane (same inputs, same result)
-            const float rhs = row[3], cfm = row[7], lo0 = row[11], hi0 = row[15];
-            float delta = rhs - old * cfm;
-            delta -= dot;
-            float lo, hi;
-            if (fk >= 0) { hi = fabsf(hi0 * lf); lo = -hi; }
-            else { hi = hi0; lo = lo0; }
-            float nl = old + delta;
-            if (nl < lo) { delta = lo - old; nl = lo; }
-            else if (nl > hi) { delta = hi - old; nl = hi; }
-            if (lane == k) lamk = nl;
-            if (active && delta != 0) fcv += delta * row[16 + jpos];
-        }
-    }
-    if (lane < n) A.Rw.lambda[r0 + lane] = lamk;
-    if (lane < 12 && (lane < 6 || two)) {
-        const int which = lane < 6 ? 0 : 1, comp = lane % 6;
-        float *f = (float *)(A.fc + 2 * (which ? b.y : b.x));
-        __stcg(f + (comp < 3 ? comp : 4 + comp - 3), fcv);
-    }
-    __syncwarp();
+    cp_async_commit();
+    return true;
 }
 
-__global__ void k_pgs(PgsArgs A) {
+// quickstep.cpp:2917-3033 for one staged row
+__device__ __forceinline__ void relax_staged_row(const float4 *row, float &lam_r, float lam_f, bool has_f, float4 &f1l,
+                                                 float4 &f1a, float4 &f2l, float4 &f2a, bool two) {
+    const float4 j1l = row[0], j1a = row[1], j2l = row[2], j2a = row[3];
+    const float old = lam_r;
+    float delta = j1l.w - old * j1a.w;
+    delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
+    if (two) delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
+    float lo, hi;
+    if (has_f) { hi = fabsf(j2a.w * lam_f); lo = -hi; }
+    else { hi = j2a.w; lo = j2l.w; }
+    float nl = old + delta;
+    if (nl < lo) { delta = lo - old; nl = lo; }
+    else if (nl > hi) { delta = hi - old; nl = hi; }
+    lam_r = nl;
+    if (delta != 0) {
+        const float4 m1l = row[4], m1a = row[5];
+        f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
+        f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
+        if (two) {
+            const float4 m2l = row[6], m2a = row[7];
+            f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
+            f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
+        }
+    }
+}
+
+// relax_desc on a staged manifold: the same operations in the same order
+__device__ __forceinline__ void relax_staged(const PgsArgs &A, int4 d, StageSlot *st) {
+    const int r0 = d.x, n = desc_rows(d), r1 = d.x + n;
+    const bool two = d.w >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    cp_async_wait_all();
+    for (int k = 0; k < n; k++)
+        if (st->fi[k] < 0) relax_staged_row(&st->row[k * 8], st->lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
+    for (int k = 0; k < n; k++) {
+        const int f = st->fi[k];
+        if (f < 0) continue;
+        const float lf = (f >= r0 && f < r1) ? st->lam[f - r0] : __ldcg(&A.Rw.lambda[f]);
+        relax_staged_row(&st->row[k * 8], st->lam[k], lf, true, f1l, f1a, f2l, f2a, two);
+    }
+    for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = st->lam[k];
+    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
+}
+
+// Staged triplet manifold (GB_DESC_TRIPLETS): the rows' operations of
+// quickstep.cpp:2917-3033 with a shorter dependency chain -- the 12-term
+// products J.fc summed as a tree with fused multiply-adds, the clamp as
+// min/max, and fc += delta * M^-1 J^T as independent fused multiply-adds.  The
+// values differ from relax_staged's in rounding only; the order of the rows
+// (all normal rows, then the friction pairs) is the same.
+template <bool TWO>
+__device__ __forceinline__ float dot_fc(const float4 *row, const float4 &f1l, const float4 &f1a, const float4 &f2l,
+                                        const float4 &f2a) {
+    const float4 j1l = row[0], j1a = row[1];
+    float a = fmaf(f1l.x, j1l.x, f1l.y * j1l.y);
+    float b = fmaf(f1l.z, j1l.z, f1a.x * j1a.x);
+    float c = fmaf(f1a.y, j1a.y, f1a.z * j1a.z);
+    if (TWO) {
+        const float4 j2l = row[2], j2a = row[3];
+        a = fmaf(f2l.x, j2l.x, a);
+        b = fmaf(f2l.y, j2l.y, b);
+        c = fmaf(f2l.z, j2l.z, c);
+        a = fmaf(f2a.x, j2a.x, a);
+        b = fmaf(f2a.y, j2a.y, b);
+        c = fmaf(f2a.z, j2a.z, c);
+    }
+    return (a + b) + c;
+}
+
+template <bool TWO>
+__device__ __forceinline__ void relax_fast_row(const float4 *row, float &lam, float lo, float hi, float4 &f1l,
+                                               float4 &f1a, float4 &f2l, float4 &f2a) {
+    const float rhs = row[0].w, cfm = row[1].w;
+    const float old = lam;
+    float delta = fmaf(-old, cfm, rhs) - dot_fc<TWO>(row, f1l, f1a, f2l, f2a);
+    const float nl = old + delta;
+    const float cl = fminf(fmaxf(nl, lo), hi);
+    if (cl != nl) delta = cl - old;
+    lam = cl;
+    const float4 m1l = row[4], m1a = row[5];
+    f1l.x = fmaf(delta, m1l.x, f1l.x); f1l.y = fmaf(delta, m1l.y, f1l.y); f1l.z = fmaf(delta, m1l.z, f1l.z);
+    f1a.x = fmaf(delta, m1a.x, f1a.x); f1a.y = fmaf(delta, m1a.y, f1a.y); f1a.z = fmaf(delta, m1a.z, f1a.z);
+    if (TWO) {
+        const float4 m2l = row[6], m2a = row[7];
+        f2l.x = fmaf(delta, m2l.x, f2l.x); f2l.y = fmaf(delta, m2l.y, f2l.y); f2l.z = fmaf(delta, m2l.z, f2l.z);
+        f2a.x = fmaf(delta, m2a.x, f2a.x); f2a.y = fmaf(delta, m2a.y, f2a.y); f2a.z = fmaf(delta, m2a.z, f2a.z);
+    }
+}
+
+template <bool TWO>
+__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, StageSlot *st) {
+    const int nct = desc_rows(d) / 3;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (TWO) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    cp_async_wait_all();
+    float lam[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) lam[k] = k < 3 * nct ? st->lam[k] : 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+        if (c < nct) {
+            const float4 *row = &st->row[(3 * c) * 8];
+            relax_fast_row<TWO>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+        }
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+        if (c < nct) {
+#pragma unroll
+            for (int q = 1; q < 3; q++) {
+                const float4 *row = &st->row[(3 * c + q) * 8];
+                const float hi = fabsf(row[3].w * lam[3 * c]);
+                relax_fast_row<TWO>(row, lam[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
+            }
+        }
+#pragma unroll
+    for (int k = 0; k < 12; k++)
+        if (k < 3 * nct) A.Rw.lambda[d.x + k] = lam[k];
+    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
+    if (TWO) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
+}
+
+__device__ __forceinline__ void relax_slot(const PgsArgs &A, int4 d, StageSlot *st, bool staged) {
+    if (!staged) relax_desc(A, d);
+    else if (!(d.y & GB_DESC_TRIPLETS)) relax_staged(A, d, st);
+    else if (d.w >= 0) relax_triplets<true>(A, d, st);
+    else relax_triplets<false>(A, d, st);
+}
+
+// The coloured SOR sweeps, one persistent cooperative launch.
+//
+// Slot j of a colour belongs to thread (j mod T) with the blocks interleaved
+// (T threads in all), so a colour's manifolds spread over every SM and the
+// same thread relaxes the same manifold in every sweep.  Before the barrier
+// that ends a colour, each thread fetches the descriptor of its first slot of
+// the next colour and starts copying that manifold's rows into its shared-
+// memory slot; after the barrier only the body accumulators fc (written by the
+// previous colour) are read through L2.
+__global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
     DevCounters *dc = A.dc;
+    __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS];
     const int ncol = dc->ncolours;
     const int nrows = dc->nrows;
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x) { s_cstart[c] = A.cstart[c]; s_ccount[c] = A.ccount[c]; }
+    __syncthreads();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31, wid = tid >> 5, nwarps = nth >> 5;
-    extern __shared__ float4 pgs_smem[];
-    float4 *wsm = pgs_smem + (threadIdx.x >> 5) * (GB_WARP_ROWS * 8);
+    const int g = threadIdx.x * gridDim.x + blockIdx.x;
     const bool residual_mode = A.target > 0;
     const int itmax = residual_mode ? A.max_iterations : A.iterations;
-    int it = 0, check = 0;
+    int it = 0, check = 0, last_reform = 0;
     float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
     if (A.warm) {
         // colour by colour, so no two manifolds of a pass touch one body
         for (int c = 0; c < ncol; c++) {
-            const int s = A.cstart[c], n = A.ccount[c];
-            for (int k = tid; k < n; k += nth) apply_manifold(A, A.clist[s + k]);
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
         }
     }
-    for (; it < itmax;) {
+    extern __shared__ float4 pgs_smem[];
+    StageSlot *st = (StageSlot *)pgs_smem + threadIdx.x;
+    int4 next = make_int4(0, 0, -1, -1);
+    bool has_next = false, staged = false;
+    auto fetch = [&](int c) {
+        has_next = g < s_ccount[c];
+        if (has_next) {
+            next = __ldg(&A.desc[s_cstart[c] + g]);
+            staged = stage_desc(A, next, st);
+        }
+    };
+    if (ncol > 0) fetch(0);
+    for (; it < itmax && ncol > 0;) {
         for (int c = 0; c < ncol; c++) {
-            const int s = A.cstart[c], n = A.ccount[c];
-            for (int k = wid; k < n; k += nwarps) relax_manifold_warp(A, A.clist[s + k], lane, wsm);
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            if (has_next) relax_slot(A, next, st, staged);
+            const int s = s_cstart[c], n = s_ccount[c];
+            for (int k = g + nth; k < n; k += nth) relax_desc(A, __ldg(&A.desc[s + k]));
+            fetch(c + 1 < ncol ? c + 1 : 0);
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
         }
         ++it;
         if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
-            // Re-form fc = M^-1 J^T lambda from lambda: thousands of incremental FP32
-            // updates let fc drift from the multipliers it stands for, and relaxation
-            // against a drifted fc stalls at a residual of ~1e-4..1e-3 on deep piles.
-            for (int b = tid; b < A.nb; b += nth) {
-                stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
-                stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
-            }
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
-            for (int c = 0; c < ncol; c++) {
-                const int s = A.cstart[c], n = A.ccount[c];
-                for (int k = tid; k < n; k += nth) apply_manifold(A, A.clist[s + k]);
-                if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            // Re-form fc = M^-1 J^T lambda from lambda every reform_every sweeps:
+            // thousands of incremental FP32 updates let fc drift from the
+            // multipliers it stands for, and relaxation against a drifted fc
+            // stalls at a residual of ~1e-4..1e-3 on deep piles.
+            if (it - last_reform >= A.reform_every || it == itmax) {
+                last_reform = it;
+                for (int b = tid; b < A.nb; b += nth) {
+                    stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
+                    stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
+                }
+                if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+                for (int c = 0; c < ncol; c++) {
+                    for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
+                    if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+                }
             }
             float *acc = slots + 2 * (check & 1);
             float rmax = 0.f, lmax = 0.f;
             for (int r = tid; r < nrows; r += nth) {
                 rmax = fmaxf(rmax, row_residual(A.Rw, A.fc, r, A.w_sor));
-                lmax = fmaxf(lmax, fabsf(A.Rw.lambda[r]));
+                lmax = fmaxf(lmax, fabsf(__ldcg(&A.Rw.lambda[r])));
             }
             for (int o = 16; o > 0; o >>= 1) {
                 rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
                 lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
             }
             if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
             const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
             const float rel = rr / fmaxf(1.0f, ll);
             if (tid == 0) {
@@ -839,6 +972,7 @@ __global__ void k_pgs(PgsArgs A) {
             if (rel <= A.target) break;
         }
     }
+    cp_async_wait_all();  // the last sweep's staging copies
     if (tid == 0) dc->iterations = it;
 }
 
@@ -1113,7 +1247,7 @@ bool ensure_rows(Workspace &ws, int ncap) {
               ws.m_id.ensure((nc + 1) * 4) && ws.m_start.ensure((nc + 2) * 4) && ws.m_colour.ensure((nc + 1) * 4) &&
               ws.m_tent.ensure((nc + 1) * 4) && ws.col_count.ensure(GB_MAX_COLOURS * 4 + 4) &&
               ws.col_start.ensure(GB_MAX_COLOURS * 4 + 4) && ws.col_fill.ensure(GB_MAX_COLOURS * 4 + 4) &&
-              ws.col_list.ensure((nc + 1) * 4);
+              ws.col_list.ensure((nc + 1) * 4) && ws.m_desc.ensure((nc + 1) * 16);
     if (!ok) return false;
     if (ws.row_cap < (int)rows) {
         ok = ws.r_J1l.ensure(rows * 16) && ws.r_J1a.ensure(rows * 16) && ws.r_J2l.ensure(rows * 16) &&
@@ -1231,6 +1365,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     scan_exclusive(ws.col_count.as<int>(), ws.col_start.as<int>(), nullptr, GB_MAX_COLOURS, &ws.dc->colour_total, ws, s);
     k_colour_fill<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_start.as<int>(), ws.col_fill.as<int>(),
                                        ws.col_list.as<int>());
+    k_manifold_desc<<<grid, 256, 0, s>>>(ws.col_list.as<int>(), ws.m_start.as<int>(), ws.c_rstart.as<int>(),
+                                         ws.c_mcount.as<int>(), ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc,
+                                         ws.m_desc.as<int4>());
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
@@ -1241,9 +1378,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         PgsArgs A;
         A.Rw = rows_view(ws);
         A.fc = ws.b_fc.as<float4>();
-        A.C = C;
-        A.rstart = ws.c_rstart.as<int>(); A.mcount = ws.c_mcount.as<int>(); A.mstart = ws.m_start.as<int>();
-        A.clist = ws.col_list.as<int>(); A.cstart = ws.col_start.as<int>(); A.ccount = ws.col_count.as<int>();
+        A.desc = ws.m_desc.as<int4>();
+        A.cstart = ws.col_start.as<int>(); A.ccount = ws.col_count.as<int>();
         A.dc = ws.dc;
         A.iterations = P.iterations;
         A.max_iterations = P.max_iterations > 0 ? P.max_iterations : P.iterations;
@@ -1252,9 +1388,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.w_sor = P.w;
         A.warm = P.warm_mode != 0;
         A.nb = nb;
+        A.reform_every = 50;
         // one block per SM: the grid barrier's cost grows with the block count
-        const int threads = 1024;
-        const size_t smem = (size_t)(threads / 32) * GB_WARP_ROWS * 8 * sizeof(float4);  // 128 KB
+        const int threads = GB_PGS_THREADS;
+        const size_t smem = (size_t)threads * sizeof(StageSlot);  // 206 KB
         static bool smem_set = false;
         if (!smem_set) {
             cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1270,7 +1407,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     if (ev1) cudaEventRecord(ev1, s);
     if (P.warm_mode) warm_store(ws, s);
     k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
-    count_launch(9);
+    count_launch(10);
     return cudaGetLastError() == cudaSuccess;
 }
 
