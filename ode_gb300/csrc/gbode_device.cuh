@@ -81,6 +81,7 @@ enum : unsigned {
     ERR_HASH_OVERFLOW = 32u,
     ERR_CELL_RANGE = 64u,
     ERR_NONFINITE = 128u,
+    ERR_STAGE_TIMEOUT = 256u,  // a shared-memory staging copy did not complete in time
 };
 
 #if defined(__CUDACC__)
@@ -90,11 +91,18 @@ __device__ __forceinline__ float dot3(const float *a, const float *b) { return a
 __device__ __forceinline__ float dot3v(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 // ------------------------------------------------------------------ grid barrier
-// A sense-free generation barrier for cooperative launches (all blocks
-// co-resident).  Every wait is bounded: after `limit` polls the block records
-// ERR_BARRIER_TIMEOUT in *err and returns false, and every later wait returns
-// false immediately, so a kernel whose barrier can no longer complete still
-// exits.  The counter block must be zeroed before the launch.
+// An arrival-counter barrier for cooperative launches (all blocks
+// co-resident).  Every block adds 1 to one counter with release semantics
+// (after a block-wide __syncthreads, so the whole block's writes are
+// released) and polls it with acquire loads until it reaches the running
+// target, gridDim.x more than at the previous barrier; the counter is never
+// reset within a launch, so the last arrival is itself the release and no
+// block has to write a second word.  Every wait is bounded: after 2^22 polls
+// the block records ERR_BARRIER_TIMEOUT in *err and returns false, pollers
+// give up when they see that bit, and a block that gave up returns false from
+// every later barrier without touching memory, so a kernel whose barrier can
+// no longer complete still exits.  `gen` (per block, kept by the caller)
+// starts at 0; the counter block must be zeroed before the launch.
 struct GridSync {
     unsigned int count;
     unsigned int gen;
@@ -105,36 +113,30 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 __device__ __forceinline__ bool grid_sync(GridSync *gs, unsigned *err, unsigned &gen) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int ok = 1;
-        unsigned target = gen + 1;
-        if (ld_acquire_u32(err) & ERR_BARRIER_TIMEOUT) {
-            ok = 0;
-        } else {
-            __threadfence();
-            unsigned arrived = atomicAdd(&gs->count, 1u);
-            if (arrived == gridDim.x - 1) {
-                gs->count = 0;
-                __threadfence();
-                atomicExch(&gs->gen, target);
-            } else {
-                // bounded poll: 2^22 polls (a few hundred ns each) give up after about two seconds
-                long long polls = 0;
-                while (ld_acquire_u32(&gs->gen) != target) {
-                    if (++polls > (1ll << 22) || (ld_acquire_u32(err) & ERR_BARRIER_TIMEOUT)) {
-                        atomicOr(err, ERR_BARRIER_TIMEOUT);
-                        ok = 0;
-                        break;
-                    }
-                    __nanosleep(32);
+        int ok = 0;
+        if (!(gen & 0x80000000u)) {
+            const unsigned target = gen + gridDim.x;
+            red_release_add_u32(&gs->count, 1u);
+            ok = 1;
+            long long polls = 0;
+            while ((int)(ld_acquire_u32(&gs->count) - target) < 0) {
+                if (++polls > (1ll << 22) || ((polls & 63) == 0 && (ld_acquire_u32(err) & ERR_BARRIER_TIMEOUT))) {
+                    atomicOr(err, ERR_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
                 }
+                __nanosleep(32);
             }
+            gen = ok ? target : (gen | 0x80000000u);
         }
-        gen = target;
         ok_s = ok;
     }
     __syncthreads();
