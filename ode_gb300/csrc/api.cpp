@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);

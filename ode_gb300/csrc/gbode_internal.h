@@ -73,7 +73,7 @@ struct Workspace {
     // rows
     DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
     // colouring / schedule
-    DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc;
+    DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc, p_rows, chunk_rows, chunk_start;
     // reference-order schedule
     DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
     // warm start cache (previous step)

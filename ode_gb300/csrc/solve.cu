@@ -562,6 +562,8 @@ struct PgsArgs {
     int warm;          // lambda starts non-zero: fc = M^-1 J^T lambda is formed first
     int nb;            // bodies
     int reform_every;  // sweeps between re-formations of fc from lambda (residual-target mode)
+    const float4 *packed;                     // staged rows, chunk by chunk
+    const int *chunk_start, *chunk_rows;      // [colour][block]
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -706,100 +708,117 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
-// Per-thread staging area in shared memory for the manifold a thread relaxes
-// next: up to GB_STAGE_ROWS rows (the 8 float4 of J and M^-1 J^T), their
-// multipliers and findex.  The stride is padded by 16 B so that the LDS.128 of
-// eight consecutive threads at the same row offset fall on different banks.
-#define GB_STAGE_ROWS 12
+// Packed staging of triplet manifolds.
+//
+// Colour slot k (k < T, the solver's thread count) belongs to block
+// b = k mod B, thread k / B.  Before the solve, the rows of every block's
+// triplet slots of a colour are packed into one contiguous chunk (colour-major,
+// then block, then thread), 128 B per row, the 8 float4 of a row stored
+// XOR-swizzled by the row's index in its chunk so that the LDS.128 of threads
+// reading different rows spread over the banks.  During the sweeps one thread
+// per block copies the chunk of the colour after the current one into the
+// other of two shared-memory buffers with a single bulk asynchronous copy
+// (TMA) completing on that buffer's mbarrier, so a colour's rows are already
+// on chip when its barrier opens.  A slot's offset in its chunk lives in
+// bits 16-27 of its descriptor's y.
 #define GB_PGS_THREADS 128
-struct StageSlot {
-    float4 row[GB_STAGE_ROWS * 8];
-    float lam[GB_STAGE_ROWS];
-    int fi[GB_STAGE_ROWS];
-    float4 pad;
-};
-static_assert(sizeof(StageSlot) % 16 == 0, "stage slots keep 16-byte alignment");
+#define GB_CHUNK_ROWS 864  // rows per buffer: 2 x 108 KB of shared memory
+__device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
+__device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *g) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g));
-}
-__device__ __forceinline__ void cp_async4(void *smem, const void *g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// Start copying manifold d's rows into the thread's slot (asynchronously: the
-// copies proceed while the thread waits at the grid barrier).  Rows and
-// findex are read-only during the sweeps; the multipliers of a manifold are
-// written only by the thread that owns it, i.e. this one.
-__device__ __forceinline__ bool stage_desc(const PgsArgs &A, int4 d, StageSlot *st) {
-    const int n = desc_rows(d);
-    if (n > GB_STAGE_ROWS) return false;
-    const float4 *arr[8] = {A.Rw.J1l, A.Rw.J1a, A.Rw.J2l, A.Rw.J2a, A.Rw.M1l, A.Rw.M1a, A.Rw.M2l, A.Rw.M2a};
-    for (int k = 0; k < n; k++) {
-#pragma unroll
-        for (int a = 0; a < 8; a++) cp_async16(&st->row[k * 8 + a], arr[a] + d.x + k);
-        cp_async4(&st->lam[k], A.Rw.lambda + d.x + k);
-        cp_async4(&st->fi[k], A.Rw.findex + d.x + k);
+// per (block, colour): row count of the chunk and the slots' offsets in it
+__global__ void k_chunk_offsets(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, int *chunk_rows) {
+    const int b = blockIdx.x, c = blockIdx.y, B = gridDim.x;
+    __shared__ int wsum[GB_PGS_THREADS / 32];
+    if (c >= dc->ncolours) {
+        if (threadIdx.x == 0) chunk_rows[c * B + b] = 0;
+        return;
     }
-    cp_async_commit();
-    return true;
+    const int k = b + threadIdx.x * B;
+    int n = 0;
+    int4 d;
+    if (k < ccount[c]) {
+        d = desc[cstart[c] + k];
+        if (d.y & GB_DESC_TRIPLETS) n = desc_rows(d);
+    }
+    // block exclusive scan of n
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int inc = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < GB_PGS_THREADS / 32; w++) {
+        if (w < wid) before += wsum[w];
+        total += wsum[w];
+    }
+    const int off = before + inc - n;
+    if (n > 0) {
+        d.y = (d.y & ~(0xfff << 16)) | (off << 16);
+        desc[cstart[c] + k] = d;
+    }
+    if (threadIdx.x == 0) chunk_rows[c * B + b] = total;
 }
 
-// quickstep.cpp:2917-3033 for one staged row
-__device__ __forceinline__ void relax_staged_row(const float4 *row, float &lam_r, float lam_f, bool has_f, float4 &f1l,
-                                                 float4 &f1a, float4 &f2l, float4 &f2a, bool two) {
-    const float4 j1l = row[0], j1a = row[1], j2l = row[2], j2a = row[3];
-    const float old = lam_r;
-    float delta = j1l.w - old * j1a.w;
-    delta -= f1l.x * j1l.x + f1l.y * j1l.y + f1l.z * j1l.z + f1a.x * j1a.x + f1a.y * j1a.y + f1a.z * j1a.z;
-    if (two) delta -= f2l.x * j2l.x + f2l.y * j2l.y + f2l.z * j2l.z + f2a.x * j2a.x + f2a.y * j2a.y + f2a.z * j2a.z;
-    float lo, hi;
-    if (has_f) { hi = fabsf(j2a.w * lam_f); lo = -hi; }
-    else { hi = j2a.w; lo = j2l.w; }
-    float nl = old + delta;
-    if (nl < lo) { delta = lo - old; nl = lo; }
-    else if (nl > hi) { delta = hi - old; nl = hi; }
-    lam_r = nl;
-    if (delta != 0) {
-        const float4 m1l = row[4], m1a = row[5];
-        f1l.x += delta * m1l.x; f1l.y += delta * m1l.y; f1l.z += delta * m1l.z;
-        f1a.x += delta * m1a.x; f1a.y += delta * m1a.y; f1a.z += delta * m1a.z;
-        if (two) {
-            const float4 m2l = row[6], m2a = row[7];
-            f2l.x += delta * m2l.x; f2l.y += delta * m2l.y; f2l.z += delta * m2l.z;
-            f2a.x += delta * m2a.x; f2a.y += delta * m2a.y; f2a.z += delta * m2a.z;
+// copy the rows of every staged slot into its chunk (swizzled)
+__global__ void k_pack_rows(Rows Rw, const int *cstart, const int *ccount, DevCounters *dc, const int4 *desc,
+                            const int *chunk_start, float4 *packed) {
+    const int b = blockIdx.x, c = blockIdx.y, B = gridDim.x;
+    if (c >= dc->ncolours) return;
+    const int k = b + threadIdx.x * B;
+    if (k >= ccount[c]) return;
+    const int4 d = desc[cstart[c] + k];
+    if (!(d.y & GB_DESC_TRIPLETS)) return;
+    const int n = desc_rows(d), off = desc_chunk_off(d);
+    float4 *dst = packed + (size_t)chunk_start[c * B + b] * 8;
+    const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
+    for (int i = 0; i < n; i++)
+#pragma unroll
+        for (int a = 0; a < 8; a++) dst[swz(off + i, a)] = arr[a][d.x + i];
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *m) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(m)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *m, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *m, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *m) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(m))
+                 : "memory");
+}
+// bounded wait for a phase of an mbarrier
+__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, unsigned *err) {
+    long long tries = 0;
+    while (!mbar_try_wait(m, parity)) {
+        if (++tries > (1ll << 22)) {
+            atomicOr(err, ERR_STAGE_TIMEOUT);
+            return false;
         }
     }
-}
-
-// relax_desc on a staged manifold: the same operations in the same order
-__device__ __forceinline__ void relax_staged(const PgsArgs &A, int4 d, StageSlot *st) {
-    const int r0 = d.x, n = desc_rows(d), r1 = d.x + n;
-    const bool two = d.w >= 0;
-    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
-    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
-    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
-    cp_async_wait_all();
-    for (int k = 0; k < n; k++)
-        if (st->fi[k] < 0) relax_staged_row(&st->row[k * 8], st->lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
-    for (int k = 0; k < n; k++) {
-        const int f = st->fi[k];
-        if (f < 0) continue;
-        const float lf = (f >= r0 && f < r1) ? st->lam[f - r0] : __ldcg(&A.Rw.lambda[f]);
-        relax_staged_row(&st->row[k * 8], st->lam[k], lf, true, f1l, f1a, f2l, f2a, two);
-    }
-    for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = st->lam[k];
-    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
-    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
+    return true;
 }
 
 // Staged triplet manifold (GB_DESC_TRIPLETS): the rows' operations of
 // quickstep.cpp:2917-3033 with a shorter dependency chain -- the 12-term
 // products J.fc summed as a tree with fused multiply-adds, the clamp as
 // min/max, and fc += delta * M^-1 J^T as independent fused multiply-adds.  The
-// values differ from relax_staged's in rounding only; the order of the rows
+// values differ from relax_desc's in rounding only; the order of the rows
 // (all normal rows, then the friction pairs) is the same.
 template <bool TWO>
 __device__ __forceinline__ float dot_fc(const float4 *row, const float4 &f1l, const float4 &f1a, const float4 &f2l,
@@ -840,62 +859,80 @@ __device__ __forceinline__ void relax_fast_row(const float4 *row, float &lam, fl
     }
 }
 
-template <bool TWO>
-__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, StageSlot *st) {
-    const int nct = desc_rows(d) / 3;
+__device__ __forceinline__ void cp_async4(void *smem, const void *g) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// A staged triplet manifold: rows from the chunk buffer, multipliers from the
+// thread's shared-memory slot.  One code path for one- and two-body
+// manifolds (a static second body contributes fc = 0 and is not written
+// back), loops kept rolled: the solver's inner code stays small enough for
+// the instruction caches.
+__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const float4 *buf, float *lam) {
+    const int nct = desc_rows(d) / 3, off = desc_chunk_off(d);
+    const bool two = d.w >= 0;
     float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
     float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
-    if (TWO) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
     cp_async_wait_all();
-    float lam[12];
+    float4 row[8];
+#pragma unroll 1
+    for (int c = 0; c < nct; c++) {
+        const int r = off + 3 * c;
 #pragma unroll
-    for (int k = 0; k < 12; k++) lam[k] = k < 3 * nct ? st->lam[k] : 0.f;
+        for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
+        relax_fast_row<true>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+    }
+#pragma unroll 1
+    for (int c = 0; c < nct; c++) {
+        const float ln = lam[3 * c];
 #pragma unroll
-    for (int c = 0; c < 4; c++)
-        if (c < nct) {
-            const float4 *row = &st->row[(3 * c) * 8];
-            relax_fast_row<TWO>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+        for (int q = 1; q < 3; q++) {
+            const int r = off + 3 * c + q;
+#pragma unroll
+            for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
+            const float hi = fabsf(row[3].w * ln);
+            relax_fast_row<true>(row, lam[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
         }
-#pragma unroll
-    for (int c = 0; c < 4; c++)
-        if (c < nct) {
-#pragma unroll
-            for (int q = 1; q < 3; q++) {
-                const float4 *row = &st->row[(3 * c + q) * 8];
-                const float hi = fabsf(row[3].w * lam[3 * c]);
-                relax_fast_row<TWO>(row, lam[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
-            }
-        }
-#pragma unroll
-    for (int k = 0; k < 12; k++)
-        if (k < 3 * nct) A.Rw.lambda[d.x + k] = lam[k];
+    }
+#pragma unroll 1
+    for (int k = 0; k < 3 * nct; k++) A.Rw.lambda[d.x + k] = lam[k];
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
-    if (TWO) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
-}
-
-__device__ __forceinline__ void relax_slot(const PgsArgs &A, int4 d, StageSlot *st, bool staged) {
-    if (!staged) relax_desc(A, d);
-    else if (!(d.y & GB_DESC_TRIPLETS)) relax_staged(A, d, st);
-    else if (d.w >= 0) relax_triplets<true>(A, d, st);
-    else relax_triplets<false>(A, d, st);
+    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
 // The coloured SOR sweeps, one persistent cooperative launch.
 //
-// Slot j of a colour belongs to thread (j mod T) with the blocks interleaved
+// Slot k of a colour belongs to thread (k mod T) with the blocks interleaved
 // (T threads in all), so a colour's manifolds spread over every SM and the
-// same thread relaxes the same manifold in every sweep.  Before the barrier
-// that ends a colour, each thread fetches the descriptor of its first slot of
-// the next colour and starts copying that manifold's rows into its shared-
-// memory slot; after the barrier only the body accumulators fc (written by the
-// previous colour) are read through L2.
+// same thread relaxes the same manifold in every sweep.  While a colour is
+// relaxed, the block's chunk of the next colour streams into the other
+// shared-memory buffer, and each thread loads its next manifold's descriptor
+// and multipliers before the barrier; after the barrier only the body
+// accumulators fc (written by the previous colour) are read through L2.
 __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
     DevCounters *dc = A.dc;
     __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS];
+    __shared__ int s_chunk_start[GB_MAX_COLOURS], s_chunk_rows[GB_MAX_COLOURS];
+    __shared__ unsigned long long s_mbar[2];
+    __shared__ float s_lam[GB_PGS_THREADS * 13];  // per thread: the next manifold's multipliers
+    extern __shared__ float4 pgs_smem[];  // two buffers of GB_CHUNK_ROWS rows
     const int ncol = dc->ncolours;
     const int nrows = dc->nrows;
-    for (int c = threadIdx.x; c < ncol; c += blockDim.x) { s_cstart[c] = A.cstart[c]; s_ccount[c] = A.ccount[c]; }
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+        s_cstart[c] = A.cstart[c];
+        s_ccount[c] = A.ccount[c];
+        s_chunk_start[c] = A.chunk_start[c * gridDim.x + blockIdx.x];
+        s_chunk_rows[c] = min(A.chunk_rows[c * gridDim.x + blockIdx.x], GB_CHUNK_ROWS);
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&s_mbar[0]);
+        mbar_init(&s_mbar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int g = threadIdx.x * gridDim.x + blockIdx.x;
@@ -907,28 +944,81 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
         // colour by colour, so no two manifolds of a pass touch one body
         for (int c = 0; c < ncol; c++) {
             for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
         }
     }
-    extern __shared__ float4 pgs_smem[];
-    StageSlot *st = (StageSlot *)pgs_smem + threadIdx.x;
-    int4 next = make_int4(0, 0, -1, -1);
-    bool has_next = false, staged = false;
-    auto fetch = [&](int c) {
-        has_next = g < s_ccount[c];
-        if (has_next) {
-            next = __ldg(&A.desc[s_cstart[c] + g]);
-            staged = stage_desc(A, next, st);
-        }
+    // Buffer q & 1 holds colour number q (counted over all sweeps); its use
+    // number q >> 1 is the mbarrier phase to wait for.
+    unsigned q = 0;
+    unsigned nissued = 0, nwaited = 0;  // thread 0: chunk copies issued / waited for, in colour order
+    auto issue = [&](int c) {           // thread 0: the copy for colour number nissued
+        const unsigned qq = nissued++;
+        unsigned long long *m = &s_mbar[qq & 1];
+        const unsigned bytes = 128u * (unsigned)s_chunk_rows[c];
+        // the block's reads of this buffer (two colours ago) come before the copy's writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(m, bytes);
+        if (bytes) bulk_g2s(pgs_smem + (qq & 1) * (GB_CHUNK_ROWS * 8), A.packed + (size_t)s_chunk_start[c] * 8, bytes, m);
     };
-    if (ncol > 0) fetch(0);
+    auto retire = [&]() {  // thread 0: wait for the oldest copy not yet waited for
+        const unsigned qq = nwaited++;
+        return mbar_wait(&s_mbar[qq & 1], (qq >> 1) & 1, &dc->err);
+    };
+    auto drain = [&]() {  // no copy may still be writing shared memory when the block exits
+        cp_async_wait_all();
+        if (threadIdx.x == 0)
+            while (nwaited < nissued) retire();
+    };
+    float *my_lam = s_lam + threadIdx.x * 13;
+    // Two-deep descriptor pipeline: `ahead` (the slot of the colour after the
+    // next one) is loaded a colour early, so the multiplier copies for `next`
+    // can be issued at once, without waiting for a descriptor load.
+    int4 next = make_int4(0, 0, -1, -1), ahead = next;
+    bool has_next = false, staged = false, has_ahead = false;
+    auto load_ahead = [&](int c) {
+        has_ahead = g < s_ccount[c];
+        if (has_ahead) ahead = __ldg(&A.desc[s_cstart[c] + g]);
+    };
+    auto fetch = [&](int c_after) {
+        has_next = has_ahead;
+        next = ahead;
+        staged = false;
+        if (has_next) {
+            const int n = desc_rows(next);
+            staged = (next.y & GB_DESC_TRIPLETS) && desc_chunk_off(next) + n <= GB_CHUNK_ROWS;
+            if (staged) {
+                for (int k = 0; k < n; k++) cp_async4(&my_lam[k], &A.Rw.lambda[next.x + k]);
+                cp_async_commit();
+            }
+        }
+        load_ahead(c_after);
+    };
+    if (ncol > 0) {
+        if (threadIdx.x == 0) issue(0);
+        load_ahead(0);
+        fetch(ncol > 1 ? 1 : 0);
+    }
     for (; it < itmax && ncol > 0;) {
         for (int c = 0; c < ncol; c++) {
-            if (has_next) relax_slot(A, next, st, staged);
+            const int cn = c + 1 < ncol ? c + 1 : 0;
+            const int cnn = cn + 1 < ncol ? cn + 1 : 0;
+            if (threadIdx.x == 0) issue(cn);
+            if (has_next) {
+                if (!staged) {
+                    relax_desc(A, next);
+                } else {
+                    if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
+                    relax_triplets(A, next, pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8), my_lam);
+                }
+            }
             const int s = s_cstart[c], n = s_ccount[c];
             for (int k = g + nth; k < n; k += nth) relax_desc(A, __ldg(&A.desc[s + k]));
-            fetch(c + 1 < ncol ? c + 1 : 0);
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+            fetch(cnn);
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
+            // the copy for this colour has completed before its buffer's
+            // mbarrier is armed again (threads with no staged slot never waited)
+            if (threadIdx.x == 0) retire();
+            ++q;
         }
         ++it;
         if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
@@ -942,10 +1032,10 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                     stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
                     stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
                 }
-                if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+                if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
                 for (int c = 0; c < ncol; c++) {
                     for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
-                    if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+                    if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
                 }
             }
             float *acc = slots + 2 * (check & 1);
@@ -959,7 +1049,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                 lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
             }
             if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) { cp_async_wait_all(); return; }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
             const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
             const float rel = rr / fmaxf(1.0f, ll);
             if (tid == 0) {
@@ -972,7 +1062,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             if (rel <= A.target) break;
         }
     }
-    cp_async_wait_all();  // the last sweep's staging copies
+    drain();  // the copy issued for the colour after the last one relaxed
     if (tid == 0) dc->iterations = it;
 }
 
@@ -1368,6 +1458,22 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     k_manifold_desc<<<grid, 256, 0, s>>>(ws.col_list.as<int>(), ws.m_start.as<int>(), ws.c_rstart.as<int>(),
                                          ws.c_mcount.as<int>(), ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc,
                                          ws.m_desc.as<int4>());
+    // pack the triplet slots' rows chunk by chunk for the solver's blocks
+    const int pgs_blocks = num_sms();
+    const size_t nchunks = (size_t)GB_MAX_COLOURS * pgs_blocks;
+    if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.chunk_rows.ensure(nchunks * 4) &&
+          ws.chunk_start.ensure(nchunks * 4)))
+        return false;
+    {
+        dim3 cg(pgs_blocks, GB_MAX_COLOURS);
+        k_chunk_offsets<<<cg, GB_PGS_THREADS, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc,
+                                                      ws.m_desc.as<int4>(), ws.chunk_rows.as<int>());
+        scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), nullptr, (int)nchunks, nullptr, ws, s);
+        k_pack_rows<<<cg, GB_PGS_THREADS, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc,
+                                                  ws.m_desc.as<int4>(), ws.chunk_start.as<int>(),
+                                                  ws.p_rows.as<float4>());
+        count_launch(2);
+    }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
@@ -1389,9 +1495,13 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.warm = P.warm_mode != 0;
         A.nb = nb;
         A.reform_every = 50;
-        // one block per SM: the grid barrier's cost grows with the block count
+        A.packed = ws.p_rows.as<float4>();
+        A.chunk_start = ws.chunk_start.as<int>();
+        A.chunk_rows = ws.chunk_rows.as<int>();
+        // one block per SM (the grid barrier's cost grows with the block count;
+        // the chunk packing above assumes exactly pgs_blocks blocks)
         const int threads = GB_PGS_THREADS;
-        const size_t smem = (size_t)threads * sizeof(StageSlot);  // 206 KB
+        const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;  // two chunk buffers, 216 KB
         static bool smem_set = false;
         if (!smem_set) {
             cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1399,8 +1509,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         }
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, (const void *)k_pgs, threads, smem, 0);
-        int blocks = (per_sm >= 1 ? 1 : 0) * num_sms();
-        if (blocks == 0) return false;
+        if (per_sm < 1) return false;
+        const int blocks = pgs_blocks;
         void *args[] = {(void *)&A};
         if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, threads, args, smem, s) != cudaSuccess) return false;
     }
