@@ -304,6 +304,53 @@ int gbodeWorldGetBodyCount(dWorldID w);
 void gbodeWorldGetState(dWorldID w, float *out);
 void gbodeWorldSetState(dWorldID w, const float *in);
 
+/* ---- Learned warm start (extension; the reference has no counterpart).
+ *
+ * A small MLP predicts each contact's three starting multipliers (normal and
+ * two friction rows, dContactApprox1) from twelve local features:
+ *   normal (3), contact-point relative velocity in the contact frame
+ *   (normal, t1, t2), depth, effective mass of the normal row, the
+ *   previous step's three multipliers in units of s, and 1 if a previous
+ *   step's contact was matched
+ * where s = effective mass * |gravity| is the contact's weight scale.  The
+ * network is 12 -> 128 -> 128 -> 128 -> 3 with SiLU; its outputs are
+ * multipliers in units of s.  Parameters: GBODE_MLP_NPARAMS floats, in the
+ * order mean[12] std[12] (input standardisation), W1[128][12] b1[128]
+ * W2[128][128] b2[128] W3[128][128] b3[128] W4[3][128] b4[3].
+ *
+ * With the learned start enabled, dWorldQuickStep predicts the start on the
+ * tensor cores (BF16 operands, FP32 accumulation), projects it onto the
+ * rows' bounds, and compares its LCP residual with the plain start's (the
+ * previous-step multipliers when gbodeWorldSetWarmStart is on, else zero):
+ * the lower residual starts the sweeps, so the network can only help. */
+#define GBODE_MLP_NPARAMS 35099
+int gbodeMlpParamCount(void);
+/* Loss (mean squared error over the three outputs) and its gradient for n
+ * samples X[n][12] (raw features), Y[n][3] (targets in units of s), on the
+ * device.  Host arrays.  Returns 1, or 0 on error. */
+int gbodeMlpLossGrad(const float *params, const float *X, const float *Y, int n, float *grad, float *loss);
+/* Adam training on the device (mini-batches of `batch` shuffled samples);
+ * params is read as the starting point (its standardisation entries are kept
+ * fixed) and overwritten with the result; loss_per_epoch (may be NULL) gets
+ * each epoch's mean batch loss.  Host arrays.  Returns 1, or 0 on error. */
+int gbodeMlpTrain(const float *X, const float *Y, int n, int epochs, int batch, float lr, unsigned seed,
+                  float *params, float *loss_per_epoch);
+/* Inference with the tensor-core kernel: Y[n][3] = MLP(X[n][12]).  Host
+ * arrays.  Returns 1, or 0 on error. */
+int gbodeMlpPredict(const float *params, const float *X, int n, float *Y);
+/* Enable (params != NULL, enabled != 0) or disable the learned start. */
+int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled);
+/* Record the features of every contact of each step (for training data). */
+void gbodeWorldSetLearnCapture(dWorldID w, int enabled);
+/* Samples of the last step (with capture or the learned start on):
+ * [n][17] = 12 features, s, the three rows' multipliers after the solve,
+ * 1 if the contact has the three-row (normal + 2 friction) shape.  Returns n
+ * (writes at most cap).  Synchronises the stream. */
+int gbodeWorldGetLearnSamples(dWorldID w, float *out, int cap);
+/* Last step with the learned start: out[0] = 1 if the network's start was
+ * used, out[1] its relative residual, out[2] the plain start's. */
+void gbodeWorldGetLearnedStats(dWorldID w, float *out3);
+
 /* ---- Narrow phase that allocates nothing (no counterpart in the reference).
  *
  * For callers that must not allocate device memory once they run: programs

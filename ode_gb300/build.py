@@ -1,6 +1,6 @@
 """Builds libgbode.so in-tree with nvcc for sm_103a.
 
-Five translation units compiled in parallel, then linked; the link also
+Six translation units compiled in parallel, then linked; the link also
 pulls in the CUDA runtime statically so the library loads without a
 particular libcudart on the library path.  Flags that matter for results:
 -fmad=false -prec-div=true -prec-sqrt=true keep every float operation
@@ -16,7 +16,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgbode.so")
-SOURCES = ["api.cpp", "collide.cu", "solve.cu", "scan.cu", "noalloc.cu"]
+SOURCES = ["api.cpp", "collide.cu", "solve.cu", "scan.cu", "noalloc.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default"]

@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -531,6 +531,37 @@ void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int 
     w->P.max_iterations = max_iterations;
 }
 void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode = mode; w->P.warm_scale = scale; }
+
+int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
+    if (!enabled) { w->P.learned = 0; return 1; }
+    if (!params) { set_error("gbodeWorldSetLearnedWarmStart: no parameters"); return 0; }
+    Workspace &ws = w->ws;
+    if (!world_upload(w)) return 0;
+    if (!(ws.mlp_P.ensure(GB_MLP_NPARAMS * 4) && ws.mlp_wb.ensure(mlp_wb_bytes()))) {
+        set_error("gbodeWorldSetLearnedWarmStart: device allocation");
+        return 0;
+    }
+    cudaMemcpyAsync(ws.mlp_P.p, params, GB_MLP_NPARAMS * 4, cudaMemcpyHostToDevice, w->stream);
+    if (!mlp_pack(ws.mlp_P.as<float>(), ws.mlp_wb.as<unsigned char>(), w->stream) ||
+        cudaStreamSynchronize(w->stream) != cudaSuccess) {
+        set_error("gbodeWorldSetLearnedWarmStart: packing failed");
+        return 0;
+    }
+    w->P.learned = 1;
+    return 1;
+}
+void gbodeWorldSetLearnCapture(dWorldID w, int enabled) { w->P.learn_capture = enabled != 0; }
+int gbodeWorldGetLearnSamples(dWorldID w, float *out, int cap) {
+    int n = learn_samples(w->ws, out, cap, w->stream);
+    if (n < 0) { set_error("gbodeWorldGetLearnSamples", cudaGetLastError()); return 0; }
+    return n;
+}
+void gbodeWorldGetLearnedStats(dWorldID w, float *out3) {
+    float v[4] = {0, 0, 0, 0};
+    cudaMemcpyAsync(v, w->ws.dc->learn_stats, sizeof v, cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    out3[0] = v[0]; out3[1] = v[1]; out3[2] = v[2];
+}
 void gbodeWorldSetStream(dWorldID w, void *stream) {
     if (w->own_stream && w->stream) { cudaStreamSynchronize(w->stream); cudaStreamDestroy(w->stream); }
     w->stream = (cudaStream_t)stream;

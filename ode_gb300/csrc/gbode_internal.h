@@ -35,7 +35,16 @@ struct SolverParams {
     int warm_mode;
     float warm_scale;
     int solver;  // GBODE_SOLVER_*
+    int learned;        // learned warm start (MLP prediction, residual-judged against the plain start)
+    int learn_capture;  // record the per-contact features of each step
 };
+
+// learned warm start network (parameter layout in mlp.cu)
+#define GB_MLP_IN 12
+#define GB_MLP_HIDDEN 128
+#define GB_MLP_OUT 3
+#define GB_MLP_NPARAMS (2 * GB_MLP_IN + GB_MLP_HIDDEN * GB_MLP_IN + GB_MLP_HIDDEN + \
+                        2 * (GB_MLP_HIDDEN * GB_MLP_HIDDEN + GB_MLP_HIDDEN) + GB_MLP_OUT * GB_MLP_HIDDEN + GB_MLP_OUT)
 
 // Device-side scalars the kernels read and write (one pinned/device block).
 struct DevCounters {
@@ -59,6 +68,7 @@ struct DevCounters {
     int nhist;         // residual checks recorded in rhist by the last solve
     float rhist[256];  // FP32 relative residual at each check of the last solve
     GridSync gsync;    // grid barrier state (zeroed before cooperative launches)
+    float learn_stats[4];  // last learned start: MLP start used (1/0), its residual, the plain start's residual
 };
 
 struct Workspace {
@@ -74,6 +84,8 @@ struct Workspace {
     DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
     // colouring / schedule
     DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc, p_rows, chunk_rows, chunk_start;
+    // learned warm start
+    DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // reference-order schedule
     DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
     // warm start cache (previous step)
@@ -137,6 +149,7 @@ bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, cons
 // FP64 residual of the last step's rows (syncs)
 double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s);
 int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s);
+int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
 // per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
 void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
 
@@ -145,5 +158,10 @@ void count_launch(int n = 1);
 int num_sms();
 // records the message gbodeGetLastError() returns on this thread
 void report_error(const char *msg);
+// learned warm start network (mlp.cu)
+bool mlp_pack(const float *P_dev, unsigned char *wb_dev, cudaStream_t s);
+bool mlp_infer(const unsigned char *wb_dev, const float *X, int n_host, const int *n_dev, float *Y, unsigned *err,
+               cudaStream_t s);
+size_t mlp_wb_bytes();
 
 }  // namespace gb

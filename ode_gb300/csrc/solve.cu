@@ -175,8 +175,14 @@ struct WarmTable {
     float scale;
 };
 
+// Per-contact inputs of the learned warm start (null pointers: not recorded)
+struct LearnOut {
+    float *feat;   // [contact][12]
+    float *scale;  // [contact] weight scale s = m_eff * |g|
+};
+
 __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, const int *rstart, Bodies B,
-                       Rows Rw, SolverParams P, int dyn_maxabs, WarmTable W, DevCounters *dc) {
+                       Rows Rw, SolverParams P, int dyn_maxabs, WarmTable W, DevCounters *dc, LearnOut L) {
     const int nc = *nc_dev;
     const float h = P.dt, rh = 1.0f / h;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -241,6 +247,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
         J[0][6] = cval;
         if (mode & 0x010) J[0][7] = s.soft_cfm;
         J[0][14] = 0; J[0][15] = INFINITY;
+        float tf1[3] = {0, 0, 0}, tf2[3] = {0, 0, 0};  // contact frame, for the learned features
         if (m > 1) {
             float t1[3], t2[3];
             if (mode & 0x002) {
@@ -258,6 +265,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
                 t1[0] = -normal[1] * kq; t1[1] = normal[0] * kq; t1[2] = 0;
                 t2[0] = -normal[2] * t1[1]; t2[1] = normal[2] * t1[0]; t2[2] = a * kq;
             }
+            for (int q = 0; q < 3; q++) { tf1[q] = t1[q]; tf2[q] = t2[q]; }
             int row = 1;
             const float mu = s.mu > 0 ? s.mu : 0.f;
             if (mu > 0) {
@@ -303,6 +311,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
         }
         // warm start: the previous step's multipliers of this (geom pair, slot)
         float warm3[3] = {0.f, 0.f, 0.f};
+        bool warm_found = false;
         if (W.keys) {
             const unsigned long long key = warm_key(k);
             unsigned h = warm_hash(key) & W.mask;
@@ -311,6 +320,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
                 if (kk == key) {
                     const float4 l = W.lam[h];
                     warm3[0] = l.x * W.scale; warm3[1] = l.y * W.scale; warm3[2] = l.z * W.scale;
+                    warm_found = true;
                     break;
                 }
                 if (kk == ~0ull) break;
@@ -322,6 +332,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
         float4 rt1l = make_float4(0, 0, 0, 0), rt1a = rt1l;
         if (n1 >= 0) { rt1l = B.rt[2 * n1]; rt1a = B.rt[2 * n1 + 1]; }
         float I0[12], I1[12];
+        float meff = 0.f;  // effective mass of the normal row, 1 / (J M^-1 J^T)
         load_rows3(B.invIw + 3 * n0, I0);
         const float im0 = B.pos[n0].w;
         float im1 = 0.f;
@@ -350,6 +361,7 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
             float sumA = 0.f;
             for (int q = 0; q < 6; q++) sumA += M1[q] * j[q];
             if (n1 >= 0) for (int q = 0; q < 6; q++) sumA += M2[q] * j[8 + q];
+            if (r == 0) meff = sumA > 0.f ? 1.0f / sumA : 0.f;
             const float cfm_i = j[7];
             const float Ad = P.w / (sumA + cfm_i);
             const int gr = r0 + r;
@@ -371,6 +383,54 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
             Rw.contact[gr] = c;
             Rw.lambda[gr] = r < 3 ? warm3[r] : 0.f;
         }
+        if (L.feat) {
+            // normal, contact-point relative velocity in the contact frame,
+            // depth, effective mass, previous multipliers in units of s, found
+            float v[3];
+            {
+                const float4 lv = B.lvel[n0], av = B.avel[n0];
+                const float w[3] = {av.x, av.y, av.z};
+                float wc[3];
+                cross3(wc, w, c1);
+                v[0] = lv.x + wc[0]; v[1] = lv.y + wc[1]; v[2] = lv.z + wc[2];
+            }
+            if (n1 >= 0) {
+                const float4 lv = B.lvel[n1], av = B.avel[n1];
+                const float w[3] = {av.x, av.y, av.z};
+                float wc[3];
+                cross3(wc, w, c2);
+                v[0] -= lv.x + wc[0]; v[1] -= lv.y + wc[1]; v[2] -= lv.z + wc[2];
+            }
+            const float g = sqrtf(P.gravity[0] * P.gravity[0] + P.gravity[1] * P.gravity[1] + P.gravity[2] * P.gravity[2]);
+            float sc = meff * (g > 0.f ? g : 1.f);
+            if (!(sc > 0.f)) sc = 1.f;
+            float *f = L.feat + (size_t)c * 12;
+            f[0] = normal[0]; f[1] = normal[1]; f[2] = normal[2];
+            f[3] = dot3(v, normal); f[4] = dot3(v, tf1); f[5] = dot3(v, tf2);
+            f[6] = k.pos_depth.w; f[7] = meff;
+            f[8] = warm3[0] / sc; f[9] = warm3[1] / sc; f[10] = warm3[2] / sc;
+            f[11] = warm_found ? 1.f : 0.f;
+            L.scale[c] = sc;
+        }
+    }
+}
+
+// Learned start: the MLP's prediction (units of s) for every triplet contact,
+// projected onto the rows' bounds (normal >= 0, |friction| <= mu * normal);
+// the plain start (previous-step multipliers) is kept in lam_alt.
+__global__ void k_learned_apply(const int *nc_dev, const int *rstart, const int *mcount, const float *scale,
+                                const float *pred, Rows Rw, float *lam_alt) {
+    const int nc = *nc_dev;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int r0 = rstart[c], m = mcount[c];
+        for (int r = r0; r < r0 + m; r++) lam_alt[r] = Rw.lambda[r];
+        if (m != 3 || Rw.findex[r0] >= 0 || Rw.findex[r0 + 1] != r0 || Rw.findex[r0 + 2] != r0) continue;
+        const float s = scale[c];
+        const float ln = fmaxf(pred[3 * c] * s, 0.f);
+        const float h1 = fabsf(Rw.J2a[r0 + 1].w * ln), h2 = fabsf(Rw.J2a[r0 + 2].w * ln);
+        Rw.lambda[r0] = ln;
+        Rw.lambda[r0 + 1] = fminf(fmaxf(pred[3 * c + 1] * s, -h1), h1);
+        Rw.lambda[r0 + 2] = fminf(fmaxf(pred[3 * c + 2] * s, -h2), h2);
     }
 }
 
@@ -564,6 +624,8 @@ struct PgsArgs {
     int reform_every;  // sweeps between re-formations of fc from lambda (residual-target mode)
     const float4 *packed;                     // staged rows, chunk by chunk
     const int *chunk_start, *chunk_rows;      // [colour][block]
+    int learned;      // lambda holds the learned start, lam_alt the plain one: keep the better
+    float *lam_alt;
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -940,12 +1002,69 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     const int itmax = residual_mode ? A.max_iterations : A.iterations;
     int it = 0, check = 0, last_reform = 0;
     float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
-    if (A.warm) {
-        // colour by colour, so no two manifolds of a pass touch one body
+    // fc = M^-1 J^T lambda, colour by colour so no two manifolds of a pass touch one body
+    auto form_fc = [&](bool zero) -> bool {
+        if (zero) {
+            for (int b = tid; b < A.nb; b += nth) {
+                stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
+                stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
+            }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+        }
         for (int c = 0; c < ncol; c++) {
             for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
         }
+        return true;
+    };
+    // FP32 natural-map residual of every row at the current fc, relative to max(1, max|lambda|)
+    auto residual_rel = [&](float &rel) -> bool {
+        float *acc = slots + 2 * (check & 1);
+        float rmax = 0.f, lmax = 0.f;
+        for (int r = tid; r < nrows; r += nth) {
+            rmax = fmaxf(rmax, row_residual(A.Rw, A.fc, r, A.w_sor));
+            lmax = fmaxf(lmax, fabsf(__ldcg(&A.Rw.lambda[r])));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+            lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        }
+        if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+        const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
+        rel = rr / fmaxf(1.0f, ll);
+        if (tid == 0) {
+            float *other = slots + 2 * ((check + 1) & 1);
+            other[0] = 0.f; other[1] = 0.f;
+            dc->resid = rel; dc->maxlam = ll;
+            if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
+        }
+        ++check;
+        return true;
+    };
+    auto swap_alt = [&]() -> bool {
+        for (int r = tid; r < nrows; r += nth) {
+            const float a = __ldcg(&A.Rw.lambda[r]), b = __ldcg(&A.lam_alt[r]);
+            __stcg(&A.Rw.lambda[r], b);
+            __stcg(&A.lam_alt[r], a);
+        }
+        return grid_sync(&dc->gsync, &dc->err, gen);
+    };
+    if (A.learned) {
+        // The learned start has to earn its place: its residual against the
+        // plain (previous-step) start's; the better one starts the sweeps.
+        float r_mlp = 0.f, r_plain = 0.f;
+        if (!form_fc(true) || !residual_rel(r_mlp)) return;
+        if (!swap_alt() || !form_fc(true) || !residual_rel(r_plain)) return;
+        const bool use = r_mlp < r_plain;
+        if (use && (!swap_alt() || !form_fc(true))) return;
+        if (tid == 0) {
+            dc->learn_stats[0] = use ? 1.f : 0.f;
+            dc->learn_stats[1] = r_mlp;
+            dc->learn_stats[2] = r_plain;
+        }
+    } else if (A.warm) {
+        if (!form_fc(false)) return;
     }
     // Buffer q & 1 holds colour number q (counted over all sweeps); its use
     // number q >> 1 is the mbarrier phase to wait for.
@@ -1028,37 +1147,10 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             // stalls at a residual of ~1e-4..1e-3 on deep piles.
             if (it - last_reform >= A.reform_every || it == itmax) {
                 last_reform = it;
-                for (int b = tid; b < A.nb; b += nth) {
-                    stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
-                    stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
-                }
-                if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
-                for (int c = 0; c < ncol; c++) {
-                    for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
-                    if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
-                }
+                if (!form_fc(true)) { drain(); return; }
             }
-            float *acc = slots + 2 * (check & 1);
-            float rmax = 0.f, lmax = 0.f;
-            for (int r = tid; r < nrows; r += nth) {
-                rmax = fmaxf(rmax, row_residual(A.Rw, A.fc, r, A.w_sor));
-                lmax = fmaxf(lmax, fabsf(__ldcg(&A.Rw.lambda[r])));
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-                lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-            }
-            if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
-            const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
-            const float rel = rr / fmaxf(1.0f, ll);
-            if (tid == 0) {
-                float *other = slots + 2 * ((check + 1) & 1);
-                other[0] = 0.f; other[1] = 0.f;
-                dc->resid = rel; dc->maxlam = ll;
-                if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
-            }
-            ++check;
+            float rel;
+            if (!residual_rel(rel)) { drain(); return; }
             if (rel <= A.target) break;
         }
     }
@@ -1418,9 +1510,27 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nrows, ws, s);
     k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
     const int dyn = (P.solver == 1) && (P.premature_delta != 0 || P.extra_factor != 0);
+    LearnOut L = {nullptr, nullptr};
+    if (P.learned || P.learn_capture) {
+        const size_t nc = ws.contact_cap > 0 ? ws.contact_cap : 1;
+        if (!(ws.l_feat.ensure(nc * GB_MLP_IN * 4) && ws.l_scale.ensure(nc * 4) && ws.l_pred.ensure(nc * GB_MLP_OUT * 4)))
+            return false;
+        L.feat = ws.l_feat.as<float>();
+        L.scale = ws.l_scale.as<float>();
+    }
     k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn,
-                               warm_lookup(ws, P), ws.dc);
+                               warm_lookup(ws, P), ws.dc, L);
     count_launch(4);
+    if (P.learned) {
+        if (!ws.mlp_wb.p || !ws.l_alt.ensure((size_t)ws.row_cap * 4)) return false;
+        if (!mlp_infer(ws.mlp_wb.as<unsigned char>(), ws.l_feat.as<float>(), 0, &ws.dc->ncontacts, ws.l_pred.as<float>(),
+                       &ws.dc->err, s))
+            return false;
+        k_learned_apply<<<grid, 128, 0, s>>>(&ws.dc->ncontacts, ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
+                                             ws.l_scale.as<float>(), ws.l_pred.as<float>(), rows_view(ws),
+                                             ws.l_alt.as<float>());
+        count_launch();
+    }
     return true;
 }
 
@@ -1495,6 +1605,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.warm = P.warm_mode != 0;
         A.nb = nb;
         A.reform_every = 50;
+        A.learned = P.learned;
+        A.lam_alt = P.learned ? ws.l_alt.as<float>() : nullptr;
         A.packed = ws.p_rows.as<float4>();
         A.chunk_start = ws.chunk_start.as<int>();
         A.chunk_rows = ws.chunk_rows.as<int>();
@@ -1580,6 +1692,38 @@ double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, c
     if (compl_err) *compl_err = h[1];
     if (maxlam) *maxlam = h[2];
     return h[0];
+}
+
+// Learned-warm-start training samples of the last step (syncs): per contact
+// [12 features][s][lambda of its 3 rows after the solve][1 if a triplet]
+int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s) {
+    int n = 0;
+    cudaMemcpyAsync(&n, &ws.dc->step_contacts, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (!out || cap <= 0 || n <= 0 || !ws.l_feat.p) return ws.l_feat.p ? n : 0;
+    const int k = n < cap ? n : cap;
+    std::vector<float> feat((size_t)k * GB_MLP_IN), sc(k), lam;
+    std::vector<int> rstart(k), mcount(k), fi;
+    cudaMemcpyAsync(feat.data(), ws.l_feat.p, feat.size() * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(sc.data(), ws.l_scale.p, (size_t)k * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(rstart.data(), ws.c_rstart.p, (size_t)k * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(mcount.data(), ws.c_mcount.p, (size_t)k * 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    const int nr = rstart[k - 1] + mcount[k - 1];
+    lam.resize(nr);
+    fi.resize(nr);
+    cudaMemcpyAsync(lam.data(), ws.r_lambda.p, (size_t)nr * 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(fi.data(), ws.r_findex.p, (size_t)nr * 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    for (int c = 0; c < k; c++) {
+        float *o = out + (size_t)c * 17;
+        for (int q = 0; q < GB_MLP_IN; q++) o[q] = feat[(size_t)c * GB_MLP_IN + q];
+        o[12] = sc[c];
+        const int r0 = rstart[c], m = mcount[c];
+        for (int q = 0; q < 3; q++) o[13 + q] = q < m ? lam[r0 + q] : 0.f;
+        o[16] = (m == 3 && fi[r0] < 0 && fi[r0 + 1] == r0 && fi[r0 + 2] == r0) ? 1.f : 0.f;
+    }
+    return k;
 }
 
 int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s) {

@@ -135,12 +135,22 @@ _PROTOS = [
     ("gbodeGetLastError", ctypes.c_char_p, []), ("gbodeKernelLaunchCount", ctypes.c_longlong, []),
     ("gbodeWorldGetBodyCount", ctypes.c_int, [ID]), ("gbodeWorldGetState", None, [ID, _F]),
     ("gbodeWorldSetState", None, [ID, _F]),
+    ("gbodeMlpParamCount", ctypes.c_int, []),
+    ("gbodeMlpLossGrad", ctypes.c_int, [_F, _F, _F, ctypes.c_int, _F, _F]),
+    ("gbodeMlpTrain", ctypes.c_int, [_F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_uint, _F, _F]),
+    ("gbodeMlpPredict", ctypes.c_int, [_F, _F, ctypes.c_int, _F]),
+    ("gbodeWorldSetLearnedWarmStart", ctypes.c_int, [ID, _F, ctypes.c_int]),
+    ("gbodeWorldSetLearnCapture", None, [ID, ctypes.c_int]),
+    ("gbodeWorldGetLearnSamples", ctypes.c_int, [ID, _F, ctypes.c_int]),
+    ("gbodeWorldGetLearnedStats", None, [ID, _F]),
     ("gbodeCollidePairsNoAlloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_void_p]),
 ]
 
 GBODE_NOALLOC_MAX_PAIRS = 8192  # gbodeCollidePairsNoAlloc's largest batch
+GBODE_MLP_NPARAMS = 35099       # learned warm start parameters
 
 GBODE_SOLVER_COLOURED = 0
 GBODE_SOLVER_REFERENCE_ORDER = 1
