@@ -42,7 +42,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "body-steps/s at LCP residual <=1e-4 (plain GPU PGS)"
+METRIC = "body-steps/s at LCP residual \u22641e-4: plain GPU PGS vs learned warm start, 1 GB300"
 B_ROW = 132        # algorithmic bytes per PGS row-iteration
 B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
 
@@ -66,6 +66,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="run N steps only (for ncu), no JSON")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start leg")
+    ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
+    ap.add_argument("--ref-sweeps", type=int, default=1500,
+                    help="reference arm: SOR sweeps per step (cold starts need ~1000-1500 to reach the target)")
+    ap.add_argument("--weights", default=None, help="learned warm start parameters (.npz)")
     return ap.parse_args()
 
 
@@ -157,39 +162,72 @@ def dist_sum(x: float, ws: int, device) -> float:
 
 
 # ---------------------------------------------------------------------- reference arm
+SETTLED = os.path.join(ROOT, "ode_gb300", "data", "pile32768_settled.npz")
+
+
 def run_reference(args, ws, rank):
-    """The reference algorithm on the host CPU (oracle port of ODE), stock settings."""
+    """The reference algorithm on the host CPU (the oracle port of ODE's
+    collide + quickstep, stock random row reordering), from the settled pile:
+    the state the GPU arm times (ode_gb300/data/pile32768_settled.npz, written
+    by `bench.py --save-settled`), stepped with --ref-sweeps SOR sweeps per step
+    -- the GPU's typical count to reach the residual target -- on one core.
+    The FP64 residual of the last step is evaluated by replaying it with rows
+    recorded."""
     if rank != 0:
         return
-    from oracle.port.port import Port
+    from oracle.port.port import Port, world_inv_inertia
     from ode_gb300 import scenes
     P = Port()
     sc = scenes.pile(args.n, seed=1)
+    bodies = sc.bodies.copy()
+    t0 = time.perf_counter()
+    settle_note = "settled state from the fixture"
+    fixture = SETTLED if args.n == 32768 else None
+    if fixture and os.path.exists(fixture):
+        with np.load(fixture) as z:
+            bodies[:, 0:3], bodies[:, 3:7], bodies[:, 7:10], bodies[:, 10:13] = z["pos"], z["q"], z["lvel"], z["avel"]
     P.lib.port_rand_set_seed(0)
-    w = P.world(sc.bodies, sc.world_params(), sc.iterations, dyn=1, reorder=1)
+    w = P.world(bodies, sc.world_params(), args.ref_sweeps, dyn=0, reorder=1)
     w.attach_space(sc.geom_cls, sc.geom_body, sc.geom_pos, sc.geom_R, sc.geom_dims, sc.hash_levels, sc.maxc,
                    sc.surface_mode, sc.surface())
-    t0 = time.perf_counter()
-    for _ in range(args.settle + args.warmup):
+    if not (fixture and os.path.exists(fixture)):
+        settle_note = f"{args.settle} CPU settle steps"
+        for _ in range(args.settle):
+            w.sim_step()
+    for _ in range(min(args.warmup, 2)):
         w.sim_step()
-    settle_s = time.perf_counter() - t0
+    setup_s = time.perf_counter() - t0
     steps = max(1, min(args.steps, args.cpu_steps))
     t0 = time.perf_counter()
     nc = 0
-    for _ in range(steps):
+    for i in range(steps):
+        if i == steps - 1:
+            pre = w.state()
         nc += w.sim_step()
     dt = time.perf_counter() - t0
-    value = sc.nb * steps / dt
+    # replay the last step with its contacts, rows recorded, for the FP64 residual
+    cb, cs = w.last_contacts()
+    rep_bodies = bodies.copy()
+    rep_bodies[:, 0:3], rep_bodies[:, 3:7], rep_bodies[:, 7:10], rep_bodies[:, 10:13] = (
+        pre[:, 0:3], pre[:, 3:7], pre[:, 19:22], pre[:, 22:25])
+    rw = P.world(rep_bodies, sc.world_params(), args.ref_sweeps, dyn=0, reorder=1)
+    lam, rows = rw.quickstep(cb, np.full(len(cb), sc.surface_mode, np.int32), cs, want_rows=True)
+    invI, invm = world_inv_inertia(pre, bodies)
+    r64, ce = P.lcp_residual(rows, invm, invI, rows[:, 19])
+    rel = r64 / max(1.0, float(np.abs(rows[:, 19]).max()))
+    value = sc.nb * steps / dt if rel <= args.target else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "steps": steps, "warmup": min(args.warmup, 2), "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"pile{sc.nb}", "bodies": sc.nb, "dt": sc.dt, "iterations": sc.iterations,
-                       "settle_steps": args.settle, "solver": "reference quickstep (oracle port), stock settings: "
-                       "30 SOR iterations, random reordering, dynamic iteration count; residual not targeted",
-                       "contacts_per_step": nc / steps},
+            "config": {"workload": f"pile{sc.nb}", "bodies": sc.nb, "dt": sc.dt, "sweeps_per_step": args.ref_sweeps,
+                       "solver": "reference quickstep (oracle port of collide + quickstep), stock random "
+                                 "row reordering, no warm start (compiled out in the reference)",
+                       "start": settle_note, "contacts_per_step": nc / steps,
+                       "fp64_residual_last_step": rel, "residual_target": args.target,
+                       "body_steps_per_s_regardless_of_residual": sc.nb * steps / dt},
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": 1, "kind": "port",
-                             "sample": f"{steps} steps of pile{sc.nb} after {args.settle + args.warmup} "
-                                       f"settle steps ({settle_s:.0f} s) on one host core"},
+                             "sample": f"{steps} steps of pile{sc.nb} ({args.ref_sweeps} sweeps each) after "
+                                       f"{setup_s:.0f} s of set-up, one host core"},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -222,38 +260,25 @@ def run_gbode(args, ws, rank, local):
     for _ in range(args.warmup):
         w.step_fused()
     w.sync()
+    settled = w.state()
+    if args.save_settled:
+        np.savez_compressed(args.save_settled, pos=settled[:, 0:3], q=settled[:, 3:7], lvel=settled[:, 19:22],
+                            avel=settled[:, 22:25], seed=1 + rank, settle=args.settle + args.warmup)
+        return
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     peak, peak_kind = measured_peak()
     launches0 = L.gbodeKernelLaunchCount()
-    step_ms, solve_ms, sweeps, resid, rows, contacts, colours = [], [], [], [], [], [], []
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
-    torch.cuda.nvtx.range_push("timed")
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        w.step_fused()
-        e1.record(stream)
-        stream.synchronize()
-        st = w.stats()
-        step_ms.append(e0.elapsed_time(e1))
-        solve_ms.append(st.solve_ms)
-        sweeps.append(st.iterations)
-        resid.append(st.residual)
-        rows.append(st.rows)
-        contacts.append(st.contacts)
-        colours.append(st.colours)
-    torch.cuda.nvtx.range_pop()
-    torch.cuda.synchronize()
+    T = timed_steps(w, stream, flush, args.steps)
     clk = clocks.stop()
     launches = L.gbodeKernelLaunchCount() - launches0
+    step_ms, solve_ms, sweeps, resid, rows, contacts, colours = (T[k] for k in (
+        "step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours"))
     total_ms = sum(step_ms)
     ok_steps = sum(1 for r in resid if r <= args.target)
     total_ms_max = dist_max(total_ms, ws, dev)
@@ -283,6 +308,10 @@ def run_gbode(args, ws, rank, local):
         e2e_s = dist_max(time.perf_counter() - t0, ws, dev)
         e2e = {"value": dist_sum(sc.nb * n_ok, ws, dev) / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
+    # learned warm start: the same settled state, the same timed loop
+    learned = None
+    if not args.no_learned:
+        learned = learned_leg(args, w, L, stream, flush, settled, T, sc.nb, ws, dev)
     # CPU baseline: the oracle port from the same settled state, same sweep count
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -313,8 +342,80 @@ def run_gbode(args, ws, rank, local):
         "gpu_launches": launches,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "learned": learned,
     }
     print(json.dumps(line))
+
+
+def timed_steps(w, stream, flush, steps):
+    """`steps` fused steps, each bracketed by CUDA events on the world's stream
+    (L2 flushed before each, outside the events); per-step statistics."""
+    import torch
+    out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours")}
+    torch.cuda.nvtx.range_push("timed")
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        w.step_fused()
+        e1.record(stream)
+        stream.synchronize()
+        st = w.stats()
+        out["step_ms"].append(e0.elapsed_time(e1))
+        out["solve_ms"].append(st.solve_ms)
+        out["sweeps"].append(st.iterations)
+        out["resid"].append(st.residual)
+        out["rows"].append(st.rows)
+        out["contacts"].append(st.contacts)
+        out["colours"].append(st.colours)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    return out
+
+
+def learned_leg(args, w, L, stream, flush, settled, plain, nb, ws, dev):
+    """Learned warm start from the same settled state as the plain leg: W
+    untimed steps, then the same timed loop; residual target and counting
+    rules unchanged."""
+    import ctypes as C
+    from ode_gb300 import learned
+    path = args.weights or learned.WEIGHTS
+    if not os.path.exists(path):
+        return {"unavailable": f"no trained parameters at {os.path.relpath(path, ROOT)}"}
+    params = learned.load(path)
+    w.set_state(settled)
+    if L.gbodeWorldSetLearnedWarmStart(w.w, params.ctypes.data_as(C.POINTER(C.c_float)), 1) != 1:
+        return {"unavailable": L.gbodeGetLastError().decode()}
+    for _ in range(args.warmup):
+        w.step_fused()
+    w.sync()
+    chosen, r_mlp, r_plain = [], [], []
+    st = np.zeros(3, np.float32)
+    T = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours")}
+    for _ in range(args.steps):
+        t = timed_steps(w, stream, flush, 1)
+        for k in T:
+            T[k] += t[k]
+        L.gbodeWorldGetLearnedStats(w.w, st.ctypes.data_as(C.POINTER(C.c_float)))
+        chosen.append(float(st[0]))
+        r_mlp.append(float(st[1]))
+        r_plain.append(float(st[2]))
+    L.gbodeWorldSetLearnedWarmStart(w.w, None, 0)
+    total_ms_max = dist_max(sum(T["step_ms"]), ws, dev)
+    ok = sum(1 for r in T["resid"] if r <= args.target)
+    value = dist_sum(nb * ok, ws, dev) / (total_ms_max / 1e3)
+    plain_ms = sum(plain["step_ms"])
+    plain_ok = sum(1 for r in plain["resid"] if r <= args.target)
+    plain_value = nb * plain_ok / (plain_ms / 1e3)
+    return {"value": value, "unit": "body-steps/s", "ms_per_step": total_ms_max / args.steps,
+            "vs_plain": value / plain_value if plain_value > 0 else None,
+            "sweeps_per_step": float(np.mean(T["sweeps"])), "plain_sweeps_per_step": float(np.mean(plain["sweeps"])),
+            "steps_at_target": ok, "mlp_start_chosen": float(np.mean(chosen)),
+            "start_residual_mlp": float(np.median(r_mlp)), "start_residual_plain": float(np.median(r_plain)),
+            "weights": os.path.relpath(path, ROOT),
+            "note": "the network's start is used only when its residual beats the previous-step start's"}
 
 
 def cpu_baseline(sc, w, sweeps, steps):
