@@ -192,7 +192,30 @@ void dJointDestroy(dJointID j);
 void dJointSetFeedback(dJointID j, dJointFeedback *fb);
 dJointFeedback *dJointGetFeedback(dJointID j);
 dBodyID dJointGetBody(dJointID j, int index);
-int dAreConnectedExcluding(dBodyID body1, dBodyID body2, int joint_type);
+int dAreConnectedExcluding(dBodyID body1, dBodyID body2, int joint_type);  /* objects.h:3499 */
+int dAreConnected(dBodyID body1, dBodyID body2);                          /* objects.h:3484 */
+
+/* ---- ball and hinge joints: include/ode/common.h:384-403 (types),
+ * :439-455 (parameters), objects.h:1693-2618 */
+enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider, dJointTypeContact };
+enum {
+    dParamLoStop = 0, dParamHiStop, dParamVel, dParamLoVel, dParamHiVel, dParamFMax, dParamFudgeFactor,
+    dParamBounce, dParamCFM, dParamStopERP, dParamStopCFM, dParamSuspensionERP, dParamSuspensionCFM, dParamERP
+};
+dJointID dJointCreateBall(dWorldID w, dJointGroupID group);    /* objects.h:1693 */
+dJointID dJointCreateHinge(dWorldID w, dJointGroupID group);   /* objects.h:1701 */
+int dJointGetType(dJointID j);                                  /* objects.h:1929 */
+void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z);        /* objects.h:1965 */
+void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* objects.h:1977 */
+void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);       /* objects.h:1983 */
+void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);         /* objects.h:1991 */
+void dJointSetHingeParam(dJointID j, int parameter, dReal value);        /* objects.h:2027 */
+void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* objects.h:2555 */
+dReal dJointGetBallParam(dJointID j, int parameter);                      /* objects.h:2573 */
+void dJointGetHingeAnchor(dJointID j, dVector3 result);                  /* objects.h:2582 */
+void dJointGetHingeAxis(dJointID j, dVector3 result);                    /* objects.h:2598 */
+dReal dJointGetHingeParam(dJointID j, int parameter);                     /* objects.h:2604 */
+dReal dJointGetHingeAngle(dJointID j);                                    /* objects.h:2618 */
 
 /* ---- misc: include/ode/misc.h:35-50, rotation.h:40-70 */
 unsigned long dRand(void);

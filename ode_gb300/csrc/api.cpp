@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -124,13 +124,28 @@ struct dxJointGroup {
     dxWorld *device_world = nullptr;   // world holding this group's device-resident contacts
 };
 
+// joints/joint.cpp:495-509 dxJointLimitMotor::init (set from the world's ERP/CFM at creation)
+struct Limot {
+    float vel = 0, fmax = 0, lostop = -INFINITY, histop = INFINITY, fudge_factor = 1, normal_cfm = 0,
+          stop_erp = 0, stop_cfm = 0, bounce = 0;
+};
+
 struct dxJoint {
     dxWorld *world;
     dxJointGroup *group;
+    int type = dJointTypeContact;
     dContact contact;
-    dxBody *b1 = nullptr, *b2 = nullptr;
+    dxBody *b1 = nullptr, *b2 = nullptr;  // as attached; node[0] is b1, or b2 when b1 is null
     bool attached = false;
     dJointFeedback *feedback = nullptr;
+    // ball and hinge (joints/ball.cpp, joints/hinge.cpp): anchors and axes in
+    // the bodies' frames, hinge reference orientation, ball ERP/CFM, hinge limit/motor
+    float anchor1[4] = {0, 0, 0, 0}, anchor2[4] = {0, 0, 0, 0};
+    float axis1[4] = {1, 0, 0, 0}, axis2[4] = {1, 0, 0, 0}, qrel[4] = {0, 0, 0, 0};
+    float erp = 0, cfm = 0;
+    Limot limot;
+    dxBody *node0() const { return b1 ? b1 : b2; }
+    dxBody *node1() const { return b1 ? b2 : nullptr; }
 };
 
 struct dxWorld {
@@ -138,6 +153,7 @@ struct dxWorld {
     SolverParams P;
     std::vector<dxBody *> bodies;
     std::vector<dxJoint *> joints;
+    bool joints_dirty = false;  // ball/hinge joints changed since the last upload
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool dev_dirty = true;    // host body state newer than device
@@ -612,6 +628,7 @@ void dBodyDestroy(dBodyID b) {
         if (j->b1 == b) j->b1 = nullptr;
         if (j->b2 == b) j->b2 = nullptr;
     }
+    w->joints_dirty = true;
     for (dxWorld *ww : g_worlds) (void)ww;
     auto &v = w->bodies;
     for (size_t k = 0; k < v.size(); k++) if (v[k] == b) { v.erase(v.begin() + k); break; }
@@ -947,6 +964,7 @@ dJointGroupID dJointGroupCreate(int) { return new dxJointGroup(); }
 void dJointGroupEmpty(dJointGroupID g) {
     for (dxJoint *j : g->joints) {
         dxWorld *w = j->world;
+        if (j->type != dJointTypeContact) w->joints_dirty = true;
         auto &v = w->joints;
         for (size_t k = v.size(); k-- > 0;) if (v[k] == j) { v.erase(v.begin() + k); break; }
         delete j;
@@ -976,9 +994,11 @@ void dJointAttach(dJointID j, dBodyID body1, dBodyID body2) {
     j->b1 = body1;
     j->b2 = body2;
     j->attached = body1 || body2;
+    if (j->type != dJointTypeContact) j->world->joints_dirty = true;
 }
 void dJointDestroy(dJointID j) {
     dxWorld *w = j->world;
+    if (j->type != dJointTypeContact) w->joints_dirty = true;
     auto &v = w->joints;
     for (size_t k = 0; k < v.size(); k++) if (v[k] == j) { v.erase(v.begin() + k); break; }
     if (j->group) {
@@ -994,13 +1014,232 @@ dBodyID dJointGetBody(dJointID j, int index) {
     dxBody *n0 = j->b1 ? j->b1 : j->b2, *n1 = j->b1 ? j->b2 : nullptr;
     return index == 0 ? n0 : (index == 1 ? n1 : nullptr);
 }
-// ode.cpp dAreConnectedExcluding: contact joints are dJointTypeContact (4),
-// the only joint type of this subset
+// ode.cpp dAreConnectedExcluding: a joint of another type than joint_type
+// connects the two bodies
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type) {
-    if (!b1 || !b2 || joint_type == 4) return 0;
+    if (!b1 || !b2) return 0;
     for (dxJoint *j : b1->world->joints)
-        if (j->attached && ((j->b1 == b1 && j->b2 == b2) || (j->b1 == b2 && j->b2 == b1))) return 1;
+        if (j->attached && j->type != joint_type && ((j->b1 == b1 && j->b2 == b2) || (j->b1 == b2 && j->b2 == b1)))
+            return 1;
     return 0;
+}
+int dAreConnected(dBodyID b1, dBodyID b2) { return dAreConnectedExcluding(b1, b2, -1); }
+
+// ---- ball and hinge joints (joints/ball.cpp, joints/hinge.cpp, joints/joint.cpp)
+static dxJoint *joint_new(dWorldID w, dJointGroupID group, int type) {
+    dxJoint *j = new dxJoint();
+    j->world = w;
+    j->group = group;
+    j->type = type;
+    j->erp = w->P.erp;  // ball.cpp:40-41
+    j->cfm = w->P.cfm;
+    j->limot.normal_cfm = w->P.cfm;  // joint.cpp:495-509
+    j->limot.stop_erp = w->P.erp;
+    j->limot.stop_cfm = w->P.cfm;
+    w->joints.push_back(j);
+    if (group) group->joints.push_back(j);
+    w->joints_dirty = true;
+    return j;
+}
+dJointID dJointCreateBall(dWorldID w, dJointGroupID group) { return joint_new(w, group, dJointTypeBall); }
+dJointID dJointCreateHinge(dWorldID w, dJointGroupID group) { return joint_new(w, group, dJointTypeHinge); }
+int dJointGetType(dJointID j) { return j->type; }
+
+static void mul1_331(float *r, const float *R, const float *q) {  // R^T q (dMultiply1_331)
+    const float r0 = R[0] * q[0] + R[4] * q[1] + R[8] * q[2];
+    const float r1 = R[1] * q[0] + R[5] * q[1] + R[9] * q[2];
+    const float r2 = R[2] * q[0] + R[6] * q[1] + R[10] * q[2];
+    r[0] = r0; r[1] = r1; r[2] = r2;
+}
+static void mul0_331h(float *r, const float *R, const float *v) {  // R v (dMultiply0_331)
+    const float r0 = R[0] * v[0] + R[1] * v[1] + R[2] * v[2];
+    const float r1 = R[4] * v[0] + R[5] * v[1] + R[6] * v[2];
+    const float r2 = R[8] * v[0] + R[9] * v[1] + R[10] * v[2];
+    r[0] = r0; r[1] = r1; r[2] = r2;
+}
+// joint.cpp:289-322 setAnchors
+static void set_anchors(dxJoint *j, float x, float y, float z, float *a1, float *a2) {
+    world_download(j->world);
+    dxBody *b0 = j->node0(), *b1 = j->node1();
+    if (b0) {
+        float q[4] = {x - b0->pos[0], y - b0->pos[1], z - b0->pos[2], 0};
+        mul1_331(a1, b0->R, q);
+        if (b1) {
+            q[0] = x - b1->pos[0]; q[1] = y - b1->pos[1]; q[2] = z - b1->pos[2];
+            mul1_331(a2, b1->R, q);
+        } else {
+            a2[0] = x; a2[1] = y; a2[2] = z;
+        }
+    }
+    a1[3] = 0;
+    a2[3] = 0;
+    j->world->joints_dirty = true;
+}
+// joint.cpp:325-360 setAxes (both axes)
+static void set_axes(dxJoint *j, float x, float y, float z, float *ax1, float *ax2) {
+    world_download(j->world);
+    dxBody *b0 = j->node0(), *b1 = j->node1();
+    if (b0) {
+        float q[4] = {x, y, z, 0};
+        // dNormalize3 (odemath.cpp:95-151): largest component first
+        float l = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        if (l > 0) { l = 1.0f / sqrtf(l); q[0] *= l; q[1] *= l; q[2] *= l; } else { q[0] = 1; q[1] = q[2] = 0; }
+        mul1_331(ax1, b0->R, q);
+        ax1[3] = 0;
+        if (b1) mul1_331(ax2, b1->R, q);
+        else { ax2[0] = x; ax2[1] = y; ax2[2] = z; }
+        ax2[3] = 0;
+    }
+    j->world->joints_dirty = true;
+}
+// hinge.cpp:376-393 computeInitialRelativeRotation
+static void hinge_qrel(dxJoint *j) {
+    dxBody *b0 = j->node0(), *b1 = j->node1();
+    if (!b0) return;
+    if (b1) {
+        const float *qb = b0->q, *qc = b1->q;  // dQMultiply1 (rotation.cpp:201-208)
+        j->qrel[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+        j->qrel[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+        j->qrel[2] = qb[0] * qc[2] - qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+        j->qrel[3] = qb[0] * qc[3] - qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+    } else {
+        j->qrel[0] = b0->q[0]; j->qrel[1] = -b0->q[1]; j->qrel[2] = -b0->q[2]; j->qrel[3] = -b0->q[3];
+    }
+}
+void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z) { set_anchors(j, x, y, z, j->anchor1, j->anchor2); }
+void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z) {
+    set_anchors(j, x, y, z, j->anchor1, j->anchor2);
+    hinge_qrel(j);
+}
+void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z) {
+    set_axes(j, x, y, z, j->axis1, j->axis2);
+    hinge_qrel(j);
+}
+// joint.cpp:363-393 getAnchor: anchor1 in world coordinates (reverse: anchor2 from node 1)
+static void anchor_world(dxJoint *j, dVector3 out, const float *a, bool second) {
+    world_download(j->world);
+    dxBody *b = second ? j->node1() : j->node0();
+    if (!b) { out[0] = a[0]; out[1] = a[1]; out[2] = a[2]; return; }
+    mul0_331h(out, b->R, a);
+    out[0] += b->pos[0]; out[1] += b->pos[1]; out[2] += b->pos[2];
+}
+void dJointGetBallAnchor(dJointID j, dVector3 out) {
+    bool rev = !j->b1 && j->b2;
+    anchor_world(j, out, rev ? j->anchor2 : j->anchor1, rev);
+}
+void dJointGetHingeAnchor(dJointID j, dVector3 out) {
+    bool rev = !j->b1 && j->b2;
+    anchor_world(j, out, rev ? j->anchor2 : j->anchor1, rev);
+}
+void dJointGetHingeAxis(dJointID j, dVector3 out) {
+    world_download(j->world);
+    dxBody *b0 = j->node0();
+    if (b0) mul0_331h(out, b0->R, j->axis1);
+}
+// joint.cpp:511-544 dxJointLimitMotor::set
+static void limot_set(Limot &l, int num, float v) {
+    switch (num) {
+    case dParamLoStop: l.lostop = v; break;
+    case dParamHiStop: l.histop = v; break;
+    case dParamVel: l.vel = v; break;
+    case dParamFMax: if (v >= 0) l.fmax = v; break;
+    case dParamFudgeFactor: if (v >= 0 && v <= 1) l.fudge_factor = v; break;
+    case dParamBounce: l.bounce = v; break;
+    case dParamCFM: l.normal_cfm = v; break;
+    case dParamStopERP: l.stop_erp = v; break;
+    case dParamStopCFM: l.stop_cfm = v; break;
+    }
+}
+static float limot_get(const Limot &l, int num) {
+    switch (num) {
+    case dParamLoStop: return l.lostop;
+    case dParamHiStop: return l.histop;
+    case dParamVel: return l.vel;
+    case dParamFMax: return l.fmax;
+    case dParamFudgeFactor: return l.fudge_factor;
+    case dParamBounce: return l.bounce;
+    case dParamCFM: return l.normal_cfm;
+    case dParamStopERP: return l.stop_erp;
+    case dParamStopCFM: return l.stop_cfm;
+    default: return 0;
+    }
+}
+void dJointSetHingeParam(dJointID j, int parameter, dReal value) {
+    limot_set(j->limot, parameter, value);  // hinge.cpp: all parameters go to the limit/motor
+    j->world->joints_dirty = true;
+}
+dReal dJointGetHingeParam(dJointID j, int parameter) { return limot_get(j->limot, parameter); }
+void dJointSetBallParam(dJointID j, int parameter, dReal value) {  // ball.cpp:150-160
+    if (parameter == dParamCFM) j->cfm = value;
+    else if (parameter == dParamERP) j->erp = value;
+    j->world->joints_dirty = true;
+}
+dReal dJointGetBallParam(dJointID j, int parameter) {
+    return parameter == dParamCFM ? j->cfm : (parameter == dParamERP ? j->erp : 0);
+}
+// joint.cpp:421-492 getHingeAngle
+static float hinge_angle_host(const dxJoint *j) {
+    dxBody *b0 = j->node0(), *b1 = j->node1();
+    if (!b0) return 0;
+    float qrel[4];
+    const float *qb = b0->q, *qi = j->qrel;
+    if (b1) {
+        const float *qc = b1->q;
+        float qq[4];  // dQMultiply1(qq, q0, q1), then dQMultiply2(qrel, qq, q_initial)
+        qq[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+        qq[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+        qq[2] = qb[0] * qc[2] - qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+        qq[3] = qb[0] * qc[3] - qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+        qrel[0] = qq[0] * qi[0] + qq[1] * qi[1] + qq[2] * qi[2] + qq[3] * qi[3];
+        qrel[1] = -qq[0] * qi[1] + qq[1] * qi[0] - qq[2] * qi[3] + qq[3] * qi[2];
+        qrel[2] = -qq[0] * qi[2] + qq[2] * qi[0] - qq[3] * qi[1] + qq[1] * qi[3];
+        qrel[3] = -qq[0] * qi[3] + qq[3] * qi[0] - qq[1] * qi[2] + qq[2] * qi[1];
+    } else {  // dQMultiply3(qrel, q0, q_initial)
+        qrel[0] = qb[0] * qi[0] - qb[1] * qi[1] - qb[2] * qi[2] - qb[3] * qi[3];
+        qrel[1] = -qb[0] * qi[1] - qb[1] * qi[0] + qb[2] * qi[3] - qb[3] * qi[2];
+        qrel[2] = -qb[0] * qi[2] - qb[2] * qi[0] + qb[3] * qi[1] - qb[1] * qi[3];
+        qrel[3] = -qb[0] * qi[3] - qb[3] * qi[0] + qb[1] * qi[2] - qb[2] * qi[1];
+    }
+    const float cost2 = qrel[0];
+    const float sint2 = sqrtf(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+    const float d = qrel[1] * j->axis1[0] + qrel[2] * j->axis1[1] + qrel[3] * j->axis1[2];
+    float theta = d >= 0 ? 2 * atan2f(sint2, cost2) : 2 * atan2f(sint2, -cost2);
+    if (theta > (float)M_PI) theta -= (float)(2 * M_PI);
+    return -theta;
+}
+dReal dJointGetHingeAngle(dJointID j) {
+    world_download(j->world);
+    const float a = hinge_angle_host(j);
+    return (!j->b1 && j->b2) ? -a : a;
+}
+
+// Upload the ball and hinge joints (attached, in world order) when they changed.
+static bool upload_joint_table(dxWorld *w) {
+    if (!w->joints_dirty) return true;
+    std::vector<dxJoint *> jt;
+    for (dxJoint *j : w->joints)
+        if (j->attached && j->type != dJointTypeContact && j->node0()) jt.push_back(j);
+    const int n = (int)jt.size();
+    std::vector<int4> info(n);
+    std::vector<float4> a1(n), a2(n), x1(n), x2(n), qr(n), l0(n), l1(n), l2(n);
+    for (int k = 0; k < n; k++) {
+        const dxJoint *j = jt[k];
+        info[k] = make_int4(j->type, j->node0()->index, j->node1() ? j->node1()->index : -1, (!j->b1 && j->b2) ? 1 : 0);
+        a1[k] = make_float4(j->anchor1[0], j->anchor1[1], j->anchor1[2], 0.f);
+        a2[k] = make_float4(j->anchor2[0], j->anchor2[1], j->anchor2[2], 0.f);
+        x1[k] = make_float4(j->axis1[0], j->axis1[1], j->axis1[2], 0.f);
+        x2[k] = make_float4(j->axis2[0], j->axis2[1], j->axis2[2], 0.f);
+        qr[k] = make_float4(j->qrel[0], j->qrel[1], j->qrel[2], j->qrel[3]);
+        const Limot &L = j->limot;
+        l0[k] = make_float4(L.lostop, L.histop, L.vel, L.fmax);
+        l1[k] = make_float4(L.fudge_factor, L.bounce, L.normal_cfm, L.stop_erp);
+        l2[k] = make_float4(L.stop_cfm, j->erp, j->cfm, 0.f);
+    }
+    std::vector<const void *> src = {info.data(), a1.data(), a2.data(), x1.data(), x2.data(), qr.data(),
+                                     l0.data(), l1.data(), l2.data()};
+    if (!joint_table_upload(w->ws, n, src, w->stream)) return false;
+    w->joints_dirty = false;
+    return true;
 }
 
 // ------------------------------------------------------------------ stepping
@@ -1153,7 +1392,12 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     // host-created contact joints (attached) in creation order
     std::vector<dxJoint *> js;
     js.reserve(w->joints.size());
-    for (dxJoint *j : w->joints) if (j->attached) js.push_back(j);
+    for (dxJoint *j : w->joints) if (j->attached && j->type == dJointTypeContact) js.push_back(j);
+    if (!upload_joint_table(w)) { set_error("dWorldQuickStep: joint table upload"); return 0; }
+    if (w->ws.njoints > 0 && P.solver == GBODE_SOLVER_REFERENCE_ORDER && !w->device_contacts) {
+        set_error("dWorldQuickStep: the reference-order solver handles contact joints only");
+        return 0;
+    }
     int nb = (int)w->bodies.size();
     if (w->timing) cudaEventRecord(w->ev[2], s);
     bool ok;

@@ -289,8 +289,25 @@ __device__ __forceinline__ void load_view(const Geoms &G, int g, GeomView &v) {
 // into fixed per-pair slots.
 // skip_static: drop pairs of two body-less geoms (a contact joint attached to
 // no body never enters the reference's islands); dCollide keeps them.
+// Body pairs connected by a ball or hinge joint (open-addressed set of
+// min << 32 | max keys; empty: ~0): the fused path skips their geom pairs, as
+// an ODE near callback does with dAreConnectedExcluding (demo_boxstack.cpp:140).
+__device__ __forceinline__ bool jointed(const unsigned long long *keys, unsigned mask, int a, int b) {
+    if (!keys || a < 0 || b < 0) return false;
+    const unsigned long long key = ((unsigned long long)(unsigned)min(a, b) << 32) | (unsigned)max(a, b);
+    unsigned h = hash64(key) & mask;
+    for (unsigned probe = 0; probe <= mask; probe++) {
+        const unsigned long long k = keys[h];
+        if (k == key) return true;
+        if (k == ~0ull) return false;
+        h = (h + 1) & mask;
+    }
+    return false;
+}
+
 __global__ void k_narrow(Geoms G, const int2 *pairs, const int *npairs_dev, int np_host, int maxc, int surf,
-                         Contact *slots, int *ccount, int *codes, int skip_static) {
+                         Contact *slots, int *ccount, int *codes, int skip_static, const unsigned long long *jkeys,
+                         unsigned jmask) {
     const int np = npairs_dev ? *npairs_dev : np_host;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         int2 pr = pairs[p];
@@ -298,7 +315,8 @@ __global__ void k_narrow(Geoms G, const int2 *pairs, const int *npairs_dev, int 
         int n = 0, code = -1;
         CPoint c[8];
         const bool both_static = G.body[a] < 0 && G.body[b] < 0;
-        if (a != b && !(G.body[a] == G.body[b] && G.body[a] >= 0) && !(skip_static && both_static)) {
+        if (a != b && !(G.body[a] == G.body[b] && G.body[a] >= 0) && !(skip_static && both_static) &&
+            !jointed(jkeys, jmask, G.body[a], G.body[b])) {
             GeomView va, vb;
             load_view(G, a, va);
             load_view(G, b, vb);
@@ -446,7 +464,8 @@ bool launch_narrowphase(Workspace &ws, int maxc, int surf, bool append, cudaStre
     int grid = 4 * num_sms();
     if (maxc > 8) maxc = 8;
     k_narrow<<<grid, 128, 0, s>>>(G, ws.pairs.as<int2>(), &ws.dc->npairs, 0, maxc, surf, ws.c_slots.as<Contact>(),
-                                  ws.c_count.as<int>(), ws.c_code.as<int>(), 1);
+                                  ws.c_count.as<int>(), ws.c_code.as<int>(), 1,
+                                  ws.njoints > 0 ? ws.j_pairs.as<unsigned long long>() : nullptr, ws.j_pair_mask);
     scan_exclusive(ws.c_count.as<int>(), ws.c_start.as<int>(), &ws.dc->npairs, ws.pair_cap, &ws.dc->narrow_total, ws, s);
     // the base offset when appending is read on the host only in the compat
     // path; the fused path always starts from an empty contact list
@@ -476,7 +495,7 @@ int narrow_pairs_host(Workspace &ws, const int *pairs, int np, int maxc, std::ve
     Geoms G = geoms_view(ws, 0);
     if (maxc > 8) maxc = 8;
     k_narrow<<<grid_for(np, 128), 128, 0, s>>>(G, ws.pairs.as<int2>(), nullptr, np, maxc, 0, ws.c_slots.as<Contact>(),
-                                               ws.c_count.as<int>(), ws.c_code.as<int>(), 0);
+                                               ws.c_count.as<int>(), ws.c_code.as<int>(), 0, nullptr, 0u);
     count_launch();
     counts.resize(np);
     std::vector<Contact> slots((size_t)np * 8);

@@ -69,6 +69,9 @@ struct DevCounters {
     float rhist[256];  // FP32 relative residual at each check of the last solve
     GridSync gsync;    // grid barrier state (zeroed before cooperative launches)
     float learn_stats[4];  // last learned start: MLP start used (1/0), its residual, the plain start's residual
+    int ncmanifolds;       // contact manifolds (the first groups; ball/hinge joints follow)
+    int nrows_contacts;    // rows of the contacts (joint rows follow)
+    int njoint_rows;       // scan scratch (joint rows)
 };
 
 struct Workspace {
@@ -86,6 +89,12 @@ struct Workspace {
     DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc, p_rows, chunk_rows, chunk_start;
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
+    // ball and hinge joints (uploaded when they change) and per-step joint state
+    DBuf j_info, j_a1, j_a2, j_x1, j_x2, j_qrel, j_l0, j_l1, j_l2, j_m, j_rstart, j_limit, j_lerr, j_lam;
+    DBuf grp_body;  // body pair of every constraint group (contact manifolds, then joints)
+    DBuf j_pairs;   // set of jointed body pairs (fused narrow phase skips them)
+    unsigned j_pair_mask = 0;
+    int njoints = 0;
     // reference-order schedule
     DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
     // warm start cache (previous step)
@@ -132,7 +141,7 @@ int narrow_pairs_host(Workspace &ws, const int *pairs, int np, int maxc, std::ve
 // ---- solve.cu
 Bodies bodies_view(Workspace &ws, int nb);
 bool ensure_bodies(Workspace &ws, int nb);
-bool ensure_rows(Workspace &ws, int ncontacts_cap);
+bool ensure_rows(Workspace &ws, int ncontacts_cap, int njoints = 0);
 // full quickstep on the device contact list (count in dc->ncontacts)
 bool launch_quickstep(Workspace &ws, int nb, int nsurf, const SolverParams &P, cudaStream_t s,
                       cudaEvent_t ev_solve0, cudaEvent_t ev_solve1);
@@ -150,6 +159,8 @@ bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, cons
 double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s);
 int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s);
 int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
+// ball/hinge joint table: src = info, anchor1, anchor2, axis1, axis2, qrel, limot 0-2 (n each)
+bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s);
 // per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
 void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
 

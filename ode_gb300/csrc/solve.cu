@@ -18,6 +18,8 @@
 #include <cooperative_groups.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "gbode_internal.h"
 
 namespace gb {
@@ -175,6 +177,73 @@ struct WarmTable {
     float scale;
 };
 
+// Stage2b/2c, compute_invM_JT and the Ad scaling (quickstep.cpp:1644-1747,
+// :858-897, :2251-2316) for the m rows J[0..m) (layout of quickstep.cpp:
+// 1500-1512, rhs and cfm not yet divided by h) of one constraint between
+// bodies n0 and n1 (-1: static), written at rows r0..r0+m-1 with owner tag
+// `owner` (contact index, or -1 - joint index) and starting multipliers lam0.
+// Returns the effective mass 1 / (J M^-1 J^T) of the first row.
+__device__ float finish_rows(float (*J)[16], const int *findex, int m, int r0, int n0, int n1, const Bodies &B,
+                             const Rows &Rw, const SolverParams &P, int dyn_maxabs, int owner, const float *lam0) {
+    const float rh = 1.0f / P.dt;
+    float4 rt0l = B.rt[2 * n0], rt0a = B.rt[2 * n0 + 1];
+    float4 rt1l = make_float4(0, 0, 0, 0), rt1a = rt1l;
+    if (n1 >= 0) { rt1l = B.rt[2 * n1]; rt1a = B.rt[2 * n1 + 1]; }
+    float I0[12], I1[12];
+    float meff = 0.f;
+    load_rows3(B.invIw + 3 * n0, I0);
+    const float im0 = B.pos[n0].w;
+    float im1 = 0.f;
+    if (n1 >= 0) { load_rows3(B.invIw + 3 * n1, I1); im1 = B.pos[n1].w; }
+    for (int r = 0; r < m; r++) {
+        float *j = J[r];
+        j[6] *= rh; j[7] *= rh;
+        float in0[6] = {rt0l.x, rt0l.y, rt0l.z, rt0a.x, rt0a.y, rt0a.z};
+        float sum = 0.f;
+        for (int q = 0; q < 6; q++) sum += j[q] * in0[q];
+        if (n1 >= 0) {
+            float in1[6] = {rt1l.x, rt1l.y, rt1l.z, rt1a.x, rt1a.y, rt1a.z};
+            for (int q = 0; q < 6; q++) sum += j[8 + q] * in1[q];
+        }
+        j[6] += sum;
+        float M1[7], M2[7] = {0, 0, 0, 0, 0, 0, 0};
+        M1[0] = im0 * j[0]; M1[1] = im0 * j[1]; M1[2] = im0 * j[2];
+        mul0_331(M1 + 3, I0, j + 3);
+        M1[6] = 0;
+        if (dyn_maxabs) { float mx = fabsf(M1[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M1[q])); M1[6] = mx; }
+        if (n1 >= 0) {
+            M2[0] = im1 * j[8]; M2[1] = im1 * j[9]; M2[2] = im1 * j[10];
+            mul0_331(M2 + 3, I1, j + 11);
+            if (dyn_maxabs) { float mx = fabsf(M2[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M2[q])); M2[6] = mx; }
+        }
+        float sumA = 0.f;
+        for (int q = 0; q < 6; q++) sumA += M1[q] * j[q];
+        if (n1 >= 0) for (int q = 0; q < 6; q++) sumA += M2[q] * j[8 + q];
+        if (r == 0) meff = sumA > 0.f ? 1.0f / sumA : 0.f;
+        const float cfm_i = j[7];
+        const float Ad = P.w / (sumA + cfm_i);
+        const int gr = r0 + r;
+        Rw.Ad[gr] = Ad;
+        float jc = cfm_i * Ad, jr = j[6] * Ad;
+        float s1[6], s2[6];
+        for (int q = 0; q < 6; q++) s1[q] = j[q] * Ad;
+        for (int q = 0; q < 6; q++) s2[q] = (n1 >= 0) ? j[8 + q] * Ad : j[8 + q];
+        Rw.J1l[gr] = make_float4(s1[0], s1[1], s1[2], jr);
+        Rw.J1a[gr] = make_float4(s1[3], s1[4], s1[5], jc);
+        Rw.J2l[gr] = make_float4(s2[0], s2[1], s2[2], j[14]);
+        Rw.J2a[gr] = make_float4(s2[3], s2[4], s2[5], j[15]);
+        Rw.M1l[gr] = make_float4(M1[0], M1[1], M1[2], M1[6]);
+        Rw.M1a[gr] = make_float4(M1[3], M1[4], M1[5], 0.f);
+        Rw.M2l[gr] = make_float4(M2[0], M2[1], M2[2], M2[6]);
+        Rw.M2a[gr] = make_float4(M2[3], M2[4], M2[5], 0.f);
+        Rw.findex[gr] = findex[r] >= 0 ? r0 + findex[r] : -1;
+        Rw.body[gr] = make_int2(n0, n1);
+        Rw.contact[gr] = owner;
+        Rw.lambda[gr] = lam0 ? lam0[r] : 0.f;
+    }
+    return meff;
+}
+
 // Per-contact inputs of the learned warm start (null pointers: not recorded)
 struct LearnOut {
     float *feat;   // [contact][12]
@@ -327,62 +396,8 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
                 h = (h + 1) & W.mask;
             }
         }
-        // per-row finishing
-        float4 rt0l = B.rt[2 * n0], rt0a = B.rt[2 * n0 + 1];
-        float4 rt1l = make_float4(0, 0, 0, 0), rt1a = rt1l;
-        if (n1 >= 0) { rt1l = B.rt[2 * n1]; rt1a = B.rt[2 * n1 + 1]; }
-        float I0[12], I1[12];
-        float meff = 0.f;  // effective mass of the normal row, 1 / (J M^-1 J^T)
-        load_rows3(B.invIw + 3 * n0, I0);
-        const float im0 = B.pos[n0].w;
-        float im1 = 0.f;
-        if (n1 >= 0) { load_rows3(B.invIw + 3 * n1, I1); im1 = B.pos[n1].w; }
-        for (int r = 0; r < m; r++) {
-            float *j = J[r];
-            j[6] *= rh; j[7] *= rh;
-            float in0[6] = {rt0l.x, rt0l.y, rt0l.z, rt0a.x, rt0a.y, rt0a.z};
-            float sum = 0.f;
-            for (int q = 0; q < 6; q++) sum += j[q] * in0[q];
-            if (n1 >= 0) {
-                float in1[6] = {rt1l.x, rt1l.y, rt1l.z, rt1a.x, rt1a.y, rt1a.z};
-                for (int q = 0; q < 6; q++) sum += j[8 + q] * in1[q];
-            }
-            j[6] += sum;
-            float M1[7], M2[7] = {0, 0, 0, 0, 0, 0, 0};
-            M1[0] = im0 * j[0]; M1[1] = im0 * j[1]; M1[2] = im0 * j[2];
-            mul0_331(M1 + 3, I0, j + 3);
-            M1[6] = 0;
-            if (dyn_maxabs) { float mx = fabsf(M1[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M1[q])); M1[6] = mx; }
-            if (n1 >= 0) {
-                M2[0] = im1 * j[8]; M2[1] = im1 * j[9]; M2[2] = im1 * j[10];
-                mul0_331(M2 + 3, I1, j + 11);
-                if (dyn_maxabs) { float mx = fabsf(M2[0]); for (int q = 1; q < 6; q++) mx = fmaxf(mx, fabsf(M2[q])); M2[6] = mx; }
-            }
-            float sumA = 0.f;
-            for (int q = 0; q < 6; q++) sumA += M1[q] * j[q];
-            if (n1 >= 0) for (int q = 0; q < 6; q++) sumA += M2[q] * j[8 + q];
-            if (r == 0) meff = sumA > 0.f ? 1.0f / sumA : 0.f;
-            const float cfm_i = j[7];
-            const float Ad = P.w / (sumA + cfm_i);
-            const int gr = r0 + r;
-            Rw.Ad[gr] = Ad;
-            float jc = cfm_i * Ad, jr = j[6] * Ad;
-            float s1[6], s2[6];
-            for (int q = 0; q < 6; q++) s1[q] = j[q] * Ad;
-            for (int q = 0; q < 6; q++) s2[q] = (n1 >= 0) ? j[8 + q] * Ad : j[8 + q];
-            Rw.J1l[gr] = make_float4(s1[0], s1[1], s1[2], jr);
-            Rw.J1a[gr] = make_float4(s1[3], s1[4], s1[5], jc);
-            Rw.J2l[gr] = make_float4(s2[0], s2[1], s2[2], j[14]);
-            Rw.J2a[gr] = make_float4(s2[3], s2[4], s2[5], j[15]);
-            Rw.M1l[gr] = make_float4(M1[0], M1[1], M1[2], M1[6]);
-            Rw.M1a[gr] = make_float4(M1[3], M1[4], M1[5], 0.f);
-            Rw.M2l[gr] = make_float4(M2[0], M2[1], M2[2], M2[6]);
-            Rw.M2a[gr] = make_float4(M2[3], M2[4], M2[5], 0.f);
-            Rw.findex[gr] = findex[r] >= 0 ? r0 + findex[r] : -1;
-            Rw.body[gr] = make_int2(n0, n1);
-            Rw.contact[gr] = c;
-            Rw.lambda[gr] = r < 3 ? warm3[r] : 0.f;
-        }
+        float lam0[6] = {warm3[0], warm3[1], warm3[2], 0.f, 0.f, 0.f};
+        const float meff = finish_rows(J, findex, m, r0, n0, n1, B, Rw, P, dyn_maxabs, c, lam0);
         if (L.feat) {
             // normal, contact-point relative velocity in the contact frame,
             // depth, effective mass, previous multipliers in units of s, found
@@ -415,12 +430,252 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
     }
 }
 
+// ------------------------------------------------------------------ ball and hinge joints
+// The joint table (uploaded when the joints change) and the per-step state.
+struct JointTable {
+    const int4 *info;  // type, node-0 body, node-1 body (-1: none), 1 if attached reversed
+    const float4 *a1, *a2, *x1, *x2, *qrel;
+    const float4 *l0;  // lostop histop vel fmax
+    const float4 *l1;  // fudge bounce normal_cfm stop_erp
+    const float4 *l2;  // stop_cfm, ball erp, ball cfm
+    int n;
+    int *m, *rstart, *limit;
+    float *lerr, *lam;  // limit error; [n][6] multipliers of the last step (warm start)
+};
+
+// dxPlaneSpace (odemath.cpp:224-251)
+__device__ __forceinline__ void plane_space(const float *n, float *p, float *q) {
+    if (fabsf(n[2]) > 0.7071067811865476f) {
+        float a = n[1] * n[1] + n[2] * n[2];
+        float k = 1.0f / sqrtf(a);
+        p[0] = 0; p[1] = -n[2] * k; p[2] = n[1] * k;
+        q[0] = a * k; q[1] = -n[0] * p[2]; q[2] = n[0] * p[1];
+    } else {
+        float a = n[0] * n[0] + n[1] * n[1];
+        float k = 1.0f / sqrtf(a);
+        p[0] = -n[1] * k; p[1] = n[0] * k; p[2] = 0;
+        q[0] = -n[2] * p[1]; q[1] = n[2] * p[0]; q[2] = a * k;
+    }
+}
+// device quaternions are stored (w, x, y, z) in float4 (x, y, z, w)
+__device__ __forceinline__ void quat_of(float4 v, float *q) { q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w; }
+// joint.cpp:421-492 getHingeAngle with rotation.cpp:201-228 dQMultiply1/2/3
+__device__ float hinge_angle(const float *qb, const float *qc, const float *axis, const float *qi) {
+    float qrel[4];
+    if (qc) {
+        float qq[4];
+        qq[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+        qq[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+        qq[2] = qb[0] * qc[2] - qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+        qq[3] = qb[0] * qc[3] - qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+        qrel[0] = qq[0] * qi[0] + qq[1] * qi[1] + qq[2] * qi[2] + qq[3] * qi[3];
+        qrel[1] = -qq[0] * qi[1] + qq[1] * qi[0] - qq[2] * qi[3] + qq[3] * qi[2];
+        qrel[2] = -qq[0] * qi[2] + qq[2] * qi[0] - qq[3] * qi[1] + qq[1] * qi[3];
+        qrel[3] = -qq[0] * qi[3] + qq[3] * qi[0] - qq[1] * qi[2] + qq[2] * qi[1];
+    } else {
+        qrel[0] = qb[0] * qi[0] - qb[1] * qi[1] - qb[2] * qi[2] - qb[3] * qi[3];
+        qrel[1] = -qb[0] * qi[1] - qb[1] * qi[0] + qb[2] * qi[3] - qb[3] * qi[2];
+        qrel[2] = -qb[0] * qi[2] - qb[2] * qi[0] + qb[3] * qi[1] - qb[1] * qi[3];
+        qrel[3] = -qb[0] * qi[3] - qb[3] * qi[0] + qb[1] * qi[2] - qb[2] * qi[1];
+    }
+    const float cost2 = qrel[0];
+    const float sint2 = sqrtf(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+    const float d = qrel[1] * axis[0] + qrel[2] * axis[1] + qrel[3] * axis[2];
+    float theta = d >= 0 ? 2 * atan2f(sint2, cost2) : 2 * atan2f(sint2, -cost2);
+    if (theta > 3.14159265358979323846f) theta -= 6.28318530717958647692f;
+    return -theta;
+}
+
+// getInfo1 (ball.cpp:60-65, hinge.cpp:53-75) with the limit test
+// (joint.cpp:574-593), and addLimot's motor torques for a powered joint at a
+// limit (joint.cpp:655-700), which enter the bodies' torque accumulators
+// before the right-hand side is formed.
+__global__ void k_joint_m(JointTable T, Bodies B) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
+        const int4 in = T.info[k];
+        int m = 3, limit = 0;
+        float lerr = 0.f;
+        if (in.x == 2) {  // dJointTypeHinge
+            const float4 l0 = T.l0[k];
+            const float lostop = l0.x, histop = l0.y, vel = l0.z, fmax = l0.w;
+            m = fmax > 0 ? 6 : 5;
+            if ((lostop >= -3.14159265358979323846f || histop <= 3.14159265358979323846f) && lostop <= histop) {
+                float qb[4], qc[4], ax[3], qi[4];
+                quat_of(B.q[in.y], qb);
+                if (in.z >= 0) quat_of(B.q[in.z], qc);
+                const float4 x1 = T.x1[k], qr = T.qrel[k];
+                ax[0] = x1.x; ax[1] = x1.y; ax[2] = x1.z;
+                qi[0] = qr.x; qi[1] = qr.y; qi[2] = qr.z; qi[3] = qr.w;
+                const float angle = hinge_angle(qb, in.z >= 0 ? qc : nullptr, ax, qi);
+                if (angle <= lostop) { limit = 1; lerr = angle - lostop; }
+                else if (angle >= histop) { limit = 2; lerr = angle - histop; }
+                if (limit) m = 6;
+            }
+            if (limit && fmax > 0 && lostop != histop) {
+                float fm = fmax;
+                if (vel > 0 || (vel == 0 && limit == 2)) fm = -fm;
+                if ((limit == 1 && vel > 0) || (limit == 2 && vel < 0)) fm *= T.l1[k].x;
+                float R0[12], a1[3], ax1[3];
+                load_rows3(B.R + 3 * in.y, R0);
+                const float4 x1 = T.x1[k];
+                a1[0] = x1.x; a1[1] = x1.y; a1[2] = x1.z;
+                mul0_331(ax1, R0, a1);
+                const float t0 = fm * ax1[0], t1 = fm * ax1[1], t2 = fm * ax1[2];
+                if (in.z >= 0) {
+                    atomicAdd(&B.tacc[in.z].x, t0); atomicAdd(&B.tacc[in.z].y, t1); atomicAdd(&B.tacc[in.z].z, t2);
+                }
+                atomicAdd(&B.tacc[in.y].x, -t0); atomicAdd(&B.tacc[in.y].y, -t1); atomicAdd(&B.tacc[in.y].z, -t2);
+            }
+        }
+        T.m[k] = m;
+        T.limit[k] = limit;
+        T.lerr[k] = lerr;
+    }
+}
+
+__global__ void k_joint_rows_total(DevCounters *dc, int row_cap) {
+    dc->nrows_contacts = dc->nrows;
+    int total = dc->nrows + dc->njoint_rows;
+    if (total > row_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); total = row_cap; }
+    dc->nrows = total;
+}
+
+// joint.cpp:111-157 setBall into rows 0-2 of J
+__device__ void set_ball(float (*J)[16], const Bodies &B, int n0, int n1, float fps, float erp, const float *anchor1,
+                         const float *anchor2) {
+    float R0[12], a1[3], a2[3];
+    load_rows3(B.R + 3 * n0, R0);
+    J[0][0] = 1; J[1][1] = 1; J[2][2] = 1;
+    mul0_331(a1, R0, anchor1);
+    // dSetCrossMatrixMinus (odemath.h:288-297) into the angular block of body 1
+    J[0][4] = a1[2]; J[0][5] = -a1[1];
+    J[1][3] = -a1[2]; J[1][5] = a1[0];
+    J[2][3] = a1[1]; J[2][4] = -a1[0];
+    const float k = fps * erp;
+    const float4 p0 = B.pos[n0];
+    const float pos0[3] = {p0.x, p0.y, p0.z};
+    if (n1 >= 0) {
+        float R1[12];
+        load_rows3(B.R + 3 * n1, R1);
+        J[0][8] = -1; J[1][9] = -1; J[2][10] = -1;
+        mul0_331(a2, R1, anchor2);
+        // dSetCrossMatrixPlus (odemath.h:277-286) into the angular block of body 2
+        J[0][12] = -a2[2]; J[0][13] = a2[1];
+        J[1][11] = a2[2]; J[1][13] = -a2[0];
+        J[2][11] = -a2[1]; J[2][12] = a2[0];
+        const float4 p1 = B.pos[n1];
+        const float pos1[3] = {p1.x, p1.y, p1.z};
+        for (int j = 0; j < 3; j++) J[j][6] = k * (a2[j] + pos1[j] - a1[j] - pos0[j]);
+    } else {
+        for (int j = 0; j < 3; j++) J[j][6] = k * (anchor2[j] - a1[j] - pos0[j]);
+    }
+}
+
+// getInfo2 of ball (ball.cpp:68-76) and hinge (hinge.cpp:78-150, with
+// joint.cpp:596-790 addLimot for the limit/motor row), then the rows'
+// finishing as for contacts.  Joint rows follow the contact rows.
+__global__ void k_joint_rows(JointTable T, Bodies B, Rows Rw, SolverParams P, int dyn_maxabs, DevCounters *dc,
+                             int warm) {
+    const int base = dc->nrows_contacts;
+    const float fps = 1.0f / P.dt;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
+        const int4 in = T.info[k];
+        const int m = T.m[k], r0 = base + T.rstart[k];
+        if (r0 + m > Rw.n_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); continue; }
+        const int n0 = in.y, n1 = in.z;
+        float J[6][16];
+        int findex[6];
+        for (int r = 0; r < m; r++) {
+            for (int q = 0; q < 16; q++) J[r][q] = 0.f;
+            J[r][7] = P.cfm; J[r][14] = -INFINITY; J[r][15] = INFINITY;
+            findex[r] = -1;
+        }
+        const float4 fa1 = T.a1[k], fa2 = T.a2[k];
+        const float anchor1[3] = {fa1.x, fa1.y, fa1.z}, anchor2[3] = {fa2.x, fa2.y, fa2.z};
+        if (in.x == 1) {  // ball: its own ERP and CFM
+            const float4 l2 = T.l2[k];
+            J[0][7] = l2.z; J[1][7] = l2.z; J[2][7] = l2.z;
+            set_ball(J, B, n0, n1, fps, l2.y, anchor1, anchor2);
+        } else {  // hinge
+            set_ball(J, B, n0, n1, fps, P.erp, anchor1, anchor2);
+            float R0[12], ax1[3], p[3], q[3], b[3];
+            load_rows3(B.R + 3 * n0, R0);
+            const float4 x1 = T.x1[k], x2 = T.x2[k];
+            const float axis1[3] = {x1.x, x1.y, x1.z}, axis2[3] = {x2.x, x2.y, x2.z};
+            mul0_331(ax1, R0, axis1);
+            plane_space(ax1, p, q);
+            for (int i = 0; i < 3; i++) { J[3][3 + i] = p[i]; J[4][3 + i] = q[i]; }
+            if (n1 >= 0) {
+                for (int i = 0; i < 3; i++) { J[3][11 + i] = -p[i]; J[4][11 + i] = -q[i]; }
+                float R1[12], ax2[3];
+                load_rows3(B.R + 3 * n1, R1);
+                mul0_331(ax2, R1, axis2);
+                cross3(b, ax1, ax2);
+            } else {
+                cross3(b, ax1, axis2);
+            }
+            const float kk = fps * P.erp;
+            J[3][6] = kk * dot3(b, p);
+            J[4][6] = kk * dot3(b, q);
+            if (m == 6) {  // addLimot, rotational
+                const float4 l0 = T.l0[k], l1 = T.l1[k], l2 = T.l2[k];
+                const float lostop = l0.x, histop = l0.y, vel = l0.z, fmax = l0.w;
+                const float fudge = l1.x, bounce = l1.y, normal_cfm = l1.z, stop_erp = l1.w, stop_cfm = l2.x;
+                const int limit = T.limit[k];
+                float *r = J[5];
+                r[3] = ax1[0]; r[4] = ax1[1]; r[5] = ax1[2];
+                if (n1 >= 0) { r[11] = -ax1[0]; r[12] = -ax1[1]; r[13] = -ax1[2]; }
+                int powered = fmax > 0;
+                if (limit && lostop == histop) powered = 0;
+                (void)fudge;
+                if (powered) {
+                    r[7] = normal_cfm;
+                    if (!limit) { r[6] = vel; r[14] = -fmax; r[15] = fmax; }
+                }
+                if (limit) {
+                    const float ks = fps * stop_erp;
+                    r[6] = -ks * T.lerr[k];
+                    r[7] = stop_cfm;
+                    if (lostop == histop) {
+                        r[14] = -INFINITY; r[15] = INFINITY;
+                    } else {
+                        if (limit == 1) { r[14] = 0; r[15] = INFINITY; }
+                        else { r[14] = -INFINITY; r[15] = 0; }
+                        if (bounce > 0) {
+                            const float4 w0 = B.avel[n0];
+                            float v = w0.x * ax1[0] + w0.y * ax1[1] + w0.z * ax1[2];
+                            if (n1 >= 0) { const float4 w1 = B.avel[n1]; v -= w1.x * ax1[0] + w1.y * ax1[1] + w1.z * ax1[2]; }
+                            if (limit == 1) { if (v < 0) { const float nc = -bounce * v; if (nc > r[6]) r[6] = nc; } }
+                            else { if (v > 0) { const float nc = -bounce * v; if (nc < r[6]) r[6] = nc; } }
+                        }
+                    }
+                }
+            }
+        }
+        float lam0[6] = {0, 0, 0, 0, 0, 0};
+        if (warm)
+            for (int r = 0; r < m; r++) lam0[r] = T.lam[6 * k + r];
+        finish_rows(J, findex, m, r0, n0, n1, B, Rw, P, dyn_maxabs, -1 - k, lam0);
+    }
+}
+
+// the joints' multipliers after the solve, for the next step's start
+__global__ void k_joint_store(JointTable T, Rows Rw, const DevCounters *dc) {
+    const int base = dc->nrows_contacts;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
+        const int m = T.m[k], r0 = base + T.rstart[k];
+        for (int r = 0; r < 6; r++) T.lam[6 * k + r] = r < m ? Rw.lambda[r0 + r] : 0.f;
+    }
+}
+
 // Learned start: the MLP's prediction (units of s) for every triplet contact,
 // projected onto the rows' bounds (normal >= 0, |friction| <= mu * normal);
 // the plain start (previous-step multipliers) is kept in lam_alt.
 __global__ void k_learned_apply(const int *nc_dev, const int *rstart, const int *mcount, const float *scale,
-                                const float *pred, Rows Rw, float *lam_alt) {
+                                const float *pred, Rows Rw, float *lam_alt, const DevCounters *dc) {
     const int nc = *nc_dev;
+    for (int r = dc->nrows_contacts + blockIdx.x * blockDim.x + threadIdx.x; r < dc->nrows; r += gridDim.x * blockDim.x)
+        lam_alt[r] = Rw.lambda[r];  // joint rows keep their start
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const int r0 = rstart[c], m = mcount[c];
         for (int r = r0; r < r0 + m; r++) lam_alt[r] = Rw.lambda[r];
@@ -480,12 +735,32 @@ __global__ void k_manifold_starts(const int *nc_dev, const int *head, const int 
     if (blockIdx.x == 0 && threadIdx.x == 0) mstart[dc->nmanifolds] = nc;
 }
 
+// Constraint groups: the contact manifolds, then one group per ball/hinge
+// joint; each with the body pair the colouring separates.
+__global__ void k_groups(const Contact *C, const int *mstart, const int4 *jinfo, int nj, DevCounters *dc,
+                         int2 *gbody) {
+    const int ncm = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ncm + nj; e += gridDim.x * blockDim.x) {
+        if (e < ncm) {
+            const Contact k = C[mstart[e]];
+            gbody[e] = make_int2(k.b1 >= 0 ? k.b1 : k.b2, k.b1 >= 0 ? k.b2 : -1);
+        } else {
+            const int4 in = jinfo[e - ncm];
+            gbody[e] = make_int2(in.y, in.z);
+        }
+    }
+}
+__global__ void k_groups_total(DevCounters *dc, int nj) {
+    dc->ncmanifolds = dc->nmanifolds;
+    dc->nmanifolds += nj;
+}
+
 #define GB_MAX_COLOURS 128
 // Speculative first-fit colouring (rounds of: pick the lowest colour free at
 // both bodies; per (body, colour) the lowest manifold index wins; losers
 // retry).  One cooperative launch; every barrier is bounded.
-__global__ void k_colour(const Contact *C, const int *mstart, DevCounters *dc, unsigned long long *mask, int *claim,
-                         int *colour, int *tent, int nb) {
+__global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long *mask, int *claim, int *colour,
+                         int *tent, int nb) {
     unsigned gen = 0;
     const int nm = dc->nmanifolds;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -496,8 +771,8 @@ __global__ void k_colour(const Contact *C, const int *mstart, DevCounters *dc, u
         // phase A: tentative colour + claim
         for (int e = tid; e < nm; e += nth) {
             if (colour[e] >= 0) continue;
-            const Contact k = C[mstart[e]];
-            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            const int2 gb = gbody[e];
+            const int n0 = gb.x, n1 = gb.y;
             unsigned long long m0 = __ldcg(&mask[2 * n0]), m0b = __ldcg(&mask[2 * n0 + 1]);
             unsigned long long m1 = 0, m1b = 0;
             if (n1 >= 0) { m1 = __ldcg(&mask[2 * n1]); m1b = __ldcg(&mask[2 * n1 + 1]); }
@@ -514,8 +789,8 @@ __global__ void k_colour(const Contact *C, const int *mstart, DevCounters *dc, u
         // phase B: winners commit
         for (int e = tid; e < nm; e += nth) {
             if (colour[e] >= 0) continue;
-            const Contact k = C[mstart[e]];
-            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            const int2 gb = gbody[e];
+            const int n0 = gb.x, n1 = gb.y;
             int c = tent[e];
             bool win = __ldcg(&claim[n0 * GB_MAX_COLOURS + c]) == e &&
                        (n1 < 0 || __ldcg(&claim[n1 * GB_MAX_COLOURS + c]) == e);
@@ -531,8 +806,8 @@ __global__ void k_colour(const Contact *C, const int *mstart, DevCounters *dc, u
         // phase C: losers release claims they still hold
         for (int e = tid; e < nm; e += nth) {
             if (colour[e] >= 0) continue;
-            const Contact k = C[mstart[e]];
-            int n0 = k.b1 >= 0 ? k.b1 : k.b2, n1 = k.b1 >= 0 ? k.b2 : -1;
+            const int2 gb = gbody[e];
+            const int n0 = gb.x, n1 = gb.y;
             int c = tent[e];
             atomicCAS(&claim[n0 * GB_MAX_COLOURS + c], e, 0x7fffffff);
             if (n1 >= 0) atomicCAS(&claim[n1 * GB_MAX_COLOURS + c], e, 0x7fffffff);
@@ -639,10 +914,18 @@ struct PgsArgs {
 __device__ __forceinline__ int desc_rows(int4 d) { return d.y & 0xffff; }
 
 __global__ void k_manifold_desc(const int *clist, const int *mstart, const int *rstart, const int *mcount,
-                                const int2 *rbody, const int *findex, DevCounters *dc, int4 *desc) {
+                                const int2 *rbody, const int *findex, DevCounters *dc, int4 *desc,
+                                const int *jrstart, const int *jm, const int2 *gbody) {
     const int total = dc->colour_total;
+    const int ncm = dc->ncmanifolds;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
         const int e = clist[j];
+        if (e >= ncm) {  // a ball or hinge joint: its rows follow the contact rows
+            const int k = e - ncm;
+            const int2 b = gbody[e];
+            desc[j] = make_int4(dc->nrows_contacts + jrstart[k], jm[k], b.x, b.y);
+            continue;
+        }
         const int c0 = mstart[e], c1 = mstart[e + 1];
         const int r0 = rstart[c0];
         const int r1 = rstart[c1 - 1] + mcount[c1 - 1];
@@ -1386,6 +1669,7 @@ __global__ void k_feedback(Rows Rw, const int *nrows_dev, float *fb) {
     int n = *nrows_dev;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const int c = Rw.contact[r];
+        if (c < 0) continue;  // a ball/hinge joint's row
         const int2 b = Rw.body[r];
         const float l = Rw.lambda[r] / Rw.Ad[r];
         float4 a = Rw.J1l[r], d = Rw.J1a[r];
@@ -1422,14 +1706,15 @@ bool ensure_bodies(Workspace &ws, int nb) {
            ws.res_f.ensure(n * 48) && ws.res_v.ensure(n * 48);
 }
 
-bool ensure_rows(Workspace &ws, int ncap) {
+bool ensure_rows(Workspace &ws, int ncap, int nj) {
     size_t nc = ncap > 0 ? ncap : 1;
-    size_t rows = nc * 6;
+    size_t ng = nc + (nj > 0 ? nj : 0);  // constraint groups: contact manifolds (at most one per contact) + joints
+    size_t rows = ng * 6;
     bool ok = ws.c_mcount.ensure((nc + 1) * 4) && ws.c_rstart.ensure((nc + 1) * 4) && ws.m_head.ensure((nc + 1) * 4) &&
-              ws.m_id.ensure((nc + 1) * 4) && ws.m_start.ensure((nc + 2) * 4) && ws.m_colour.ensure((nc + 1) * 4) &&
-              ws.m_tent.ensure((nc + 1) * 4) && ws.col_count.ensure(GB_MAX_COLOURS * 4 + 4) &&
+              ws.m_id.ensure((nc + 1) * 4) && ws.m_start.ensure((nc + 2) * 4) && ws.m_colour.ensure((ng + 1) * 4) &&
+              ws.m_tent.ensure((ng + 1) * 4) && ws.col_count.ensure(GB_MAX_COLOURS * 4 + 4) &&
               ws.col_start.ensure(GB_MAX_COLOURS * 4 + 4) && ws.col_fill.ensure(GB_MAX_COLOURS * 4 + 4) &&
-              ws.col_list.ensure((nc + 1) * 4) && ws.m_desc.ensure((nc + 1) * 16);
+              ws.col_list.ensure((ng + 1) * 4) && ws.m_desc.ensure((ng + 1) * 16) && ws.grp_body.ensure((ng + 1) * 8);
     if (!ok) return false;
     if (ws.row_cap < (int)rows) {
         ok = ws.r_J1l.ensure(rows * 16) && ws.r_J1a.ensure(rows * 16) && ws.r_J2l.ensure(rows * 16) &&
@@ -1441,6 +1726,51 @@ bool ensure_rows(Workspace &ws, int ncap) {
         ws.row_cap = (int)rows;
     }
     return true;
+}
+
+static JointTable joint_view(Workspace &ws) {
+    JointTable T;
+    T.info = ws.j_info.as<int4>();
+    T.a1 = ws.j_a1.as<float4>(); T.a2 = ws.j_a2.as<float4>();
+    T.x1 = ws.j_x1.as<float4>(); T.x2 = ws.j_x2.as<float4>(); T.qrel = ws.j_qrel.as<float4>();
+    T.l0 = ws.j_l0.as<float4>(); T.l1 = ws.j_l1.as<float4>(); T.l2 = ws.j_l2.as<float4>();
+    T.n = ws.njoints;
+    T.m = ws.j_m.as<int>(); T.rstart = ws.j_rstart.as<int>(); T.limit = ws.j_limit.as<int>();
+    T.lerr = ws.j_lerr.as<float>(); T.lam = ws.j_lam.as<float>();
+    return T;
+}
+
+bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s) {
+    const size_t nn = n > 0 ? n : 1;
+    DBuf *f4[8] = {&ws.j_a1, &ws.j_a2, &ws.j_x1, &ws.j_x2, &ws.j_qrel, &ws.j_l0, &ws.j_l1, &ws.j_l2};
+    bool ok = ws.j_info.ensure(nn * 16) && ws.j_m.ensure((nn + 1) * 4) && ws.j_rstart.ensure((nn + 1) * 4) &&
+              ws.j_limit.ensure(nn * 4) && ws.j_lerr.ensure(nn * 4) && ws.j_lam.ensure(nn * 24);
+    for (DBuf *b : f4) ok = ok && b->ensure(nn * 16);
+    if (!ok || src.size() != 9) return false;
+    ws.njoints = n;
+    if (n == 0) return true;
+    cudaMemcpyAsync(ws.j_info.p, src[0], (size_t)n * 16, cudaMemcpyHostToDevice, s);
+    for (int i = 0; i < 8; i++) cudaMemcpyAsync(f4[i]->p, src[1 + i], (size_t)n * 16, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(ws.j_lam.p, 0, (size_t)n * 24, s);  // a new table starts its joints from zero
+    // the set of jointed body pairs, open addressing with the narrow phase's hash
+    unsigned sz = 64;
+    while (sz < 4u * (unsigned)n) sz <<= 1;
+    std::vector<unsigned long long> keys(sz, ~0ull);
+    const int4 *info = (const int4 *)src[0];
+    for (int k = 0; k < n; k++) {
+        const int a = info[k].y, b = info[k].z;
+        if (a < 0 || b < 0) continue;
+        const unsigned long long key = ((unsigned long long)(unsigned)std::min(a, b) << 32) | (unsigned)std::max(a, b);
+        unsigned long long x = key;  // the same mixing as hash64 in collide.cu
+        x ^= x >> 33; x *= 0xff51afd7ed558ccdull; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull; x ^= x >> 33;
+        unsigned h = (unsigned)x & (sz - 1);
+        while (keys[h] != ~0ull && keys[h] != key) h = (h + 1) & (sz - 1);
+        keys[h] = key;
+    }
+    if (!ws.j_pairs.ensure((size_t)sz * 8)) return false;
+    ws.j_pair_mask = sz - 1;
+    cudaMemcpyAsync(ws.j_pairs.p, keys.data(), (size_t)sz * 8, cudaMemcpyHostToDevice, s);
+    return cudaStreamSynchronize(s) == cudaSuccess;  // the host arrays die at return
 }
 
 static Rows rows_view(Workspace &ws) {
@@ -1500,8 +1830,16 @@ static void warm_store(Workspace &ws, cudaStream_t s) {
 
 static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
     Bodies B = bodies_view(ws, nb);
-    if (!ensure_rows(ws, ws.contact_cap)) return false;
+    const int nj = ws.njoints;
+    if (!ensure_rows(ws, ws.contact_cap, nj)) return false;
     if (P.warm_mode && !ensure_warm(ws)) return false;
+    JointTable T = joint_view(ws);
+    // joint getInfo1 first: a powered hinge at its limit adds motor torques to
+    // the bodies before their right-hand side is formed
+    if (nj > 0) {
+        k_joint_m<<<grid_for(nj, 128), 128, 0, s>>>(T, B);
+        count_launch();
+    }
     k_bodies<<<grid_for(nb, 128), 128, 0, s>>>(B, P);
     int grid = 4 * num_sms();
     const Contact *C = ws.contacts.as<Contact>();
@@ -1509,6 +1847,10 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     k_contact_m<<<grid, 256, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_mcount.as<int>());
     scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nrows, ws, s);
     k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
+    if (nj > 0) scan_exclusive(T.m, T.rstart, nullptr, nj, &ws.dc->njoint_rows, ws, s);
+    else cudaMemsetAsync(&ws.dc->njoint_rows, 0, 4, s);
+    k_joint_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
+    count_launch();
     const int dyn = (P.solver == 1) && (P.premature_delta != 0 || P.extra_factor != 0);
     LearnOut L = {nullptr, nullptr};
     if (P.learned || P.learn_capture) {
@@ -1521,6 +1863,10 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn,
                                warm_lookup(ws, P), ws.dc, L);
     count_launch(4);
+    if (nj > 0) {
+        k_joint_rows<<<grid_for(nj, 64), 64, 0, s>>>(T, B, rows_view(ws), P, dyn, ws.dc, P.warm_mode != 0);
+        count_launch();
+    }
     if (P.learned) {
         if (!ws.mlp_wb.p || !ws.l_alt.ensure((size_t)ws.row_cap * 4)) return false;
         if (!mlp_infer(ws.mlp_wb.as<unsigned char>(), ws.l_feat.as<float>(), 0, &ws.dc->ncontacts, ws.l_pred.as<float>(),
@@ -1528,7 +1874,7 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
             return false;
         k_learned_apply<<<grid, 128, 0, s>>>(&ws.dc->ncontacts, ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
                                              ws.l_scale.as<float>(), ws.l_pred.as<float>(), rows_view(ws),
-                                             ws.l_alt.as<float>());
+                                             ws.l_alt.as<float>(), ws.dc);
         count_launch();
     }
     return true;
@@ -1544,6 +1890,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     scan_exclusive(ws.m_head.as<int>(), ws.m_id.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nmanifolds, ws, s);
     k_manifold_starts<<<grid, 256, 0, s>>>(&ws.dc->ncontacts, ws.m_head.as<int>(), ws.m_id.as<int>(), ws.m_start.as<int>(),
                                            ws.dc);
+    k_groups<<<grid, 256, 0, s>>>(C, ws.m_start.as<int>(), ws.j_info.as<int4>(), ws.njoints, ws.dc,
+                                  ws.grp_body.as<int2>());
+    k_groups_total<<<1, 1, 0, s>>>(ws.dc, ws.njoints);
+    count_launch(2);
     // colouring
     cudaMemsetAsync(ws.m_mask.p, 0, (size_t)(nb > 0 ? nb : 1) * 16, s);
     cudaMemsetAsync(ws.m_claim.p, 0x7f, (size_t)(nb > 0 ? nb : 1) * GB_MAX_COLOURS * 4, s);
@@ -1553,10 +1903,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         int blocks = coop_blocks((const void *)k_colour, 256, 2);
         unsigned long long *mask = ws.m_mask.as<unsigned long long>();
         int *claim = ws.m_claim.as<int>(), *colour = ws.m_colour.as<int>(), *tent = ws.m_tent.as<int>();
-        const int *mstart = ws.m_start.as<int>();
+        const int2 *gbody = ws.grp_body.as<int2>();
         DevCounters *dc = ws.dc;
-        void *args[] = {(void *)&C, (void *)&mstart, (void *)&dc, (void *)&mask, (void *)&claim, (void *)&colour,
-                        (void *)&tent, (void *)&nb};
+        void *args[] = {(void *)&gbody, (void *)&dc, (void *)&mask, (void *)&claim, (void *)&colour, (void *)&tent,
+                        (void *)&nb};
         if (cudaLaunchCooperativeKernel((const void *)k_colour, blocks, 256, args, 0, s) != cudaSuccess) return false;
     }
     cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
@@ -1567,7 +1917,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                        ws.col_list.as<int>());
     k_manifold_desc<<<grid, 256, 0, s>>>(ws.col_list.as<int>(), ws.m_start.as<int>(), ws.c_rstart.as<int>(),
                                          ws.c_mcount.as<int>(), ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc,
-                                         ws.m_desc.as<int4>());
+                                         ws.m_desc.as<int4>(), ws.j_rstart.as<int>(), ws.j_m.as<int>(),
+                                         ws.grp_body.as<int2>());
     // pack the triplet slots' rows chunk by chunk for the solver's blocks
     const int pgs_blocks = num_sms();
     const size_t nchunks = (size_t)GB_MAX_COLOURS * pgs_blocks;
@@ -1628,6 +1979,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     }
     if (ev1) cudaEventRecord(ev1, s);
     if (P.warm_mode) warm_store(ws, s);
+    if (P.warm_mode && ws.njoints > 0) {
+        k_joint_store<<<grid_for(ws.njoints, 128), 128, 0, s>>>(joint_view(ws), rows_view(ws), ws.dc);
+        count_launch();
+    }
     k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
     count_launch(10);
     return cudaGetLastError() == cudaSuccess;

@@ -135,6 +135,17 @@ _PROTOS = [
     ("gbodeGetLastError", ctypes.c_char_p, []), ("gbodeKernelLaunchCount", ctypes.c_longlong, []),
     ("gbodeWorldGetBodyCount", ctypes.c_int, [ID]), ("gbodeWorldGetState", None, [ID, _F]),
     ("gbodeWorldSetState", None, [ID, _F]),
+    ("dAreConnected", ctypes.c_int, [ID, ID]),
+    ("dJointCreateBall", ID, [ID, ID]), ("dJointCreateHinge", ID, [ID, ID]),
+    ("dJointGetType", ctypes.c_int, [ID]),
+    ("dJointSetBallAnchor", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetBallParam", None, [ID, ctypes.c_int, dReal]),
+    ("dJointSetHingeAnchor", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHingeAxis", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHingeParam", None, [ID, ctypes.c_int, dReal]),
+    ("dJointGetBallAnchor", None, [ID, _F]), ("dJointGetBallParam", dReal, [ID, ctypes.c_int]),
+    ("dJointGetHingeAnchor", None, [ID, _F]), ("dJointGetHingeAxis", None, [ID, _F]),
+    ("dJointGetHingeParam", dReal, [ID, ctypes.c_int]), ("dJointGetHingeAngle", dReal, [ID]),
     ("gbodeMlpParamCount", ctypes.c_int, []),
     ("gbodeMlpLossGrad", ctypes.c_int, [_F, _F, _F, ctypes.c_int, _F, _F]),
     ("gbodeMlpTrain", ctypes.c_int, [_F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
@@ -151,6 +162,9 @@ _PROTOS = [
 
 GBODE_NOALLOC_MAX_PAIRS = 8192  # gbodeCollidePairsNoAlloc's largest batch
 GBODE_MLP_NPARAMS = 35099       # learned warm start parameters
+
+dJointTypeBall, dJointTypeHinge, dJointTypeContact = 1, 2, 4
+dParamLoStop, dParamHiStop, dParamVel, dParamFMax, dParamCFM, dParamERP = 0, 1, 2, 5, 8, 13
 
 GBODE_SOLVER_COLOURED = 0
 GBODE_SOLVER_REFERENCE_ORDER = 1

@@ -80,6 +80,10 @@ class Scene:
     surface_mode: int = dContactApprox1
     maxc: int = 4
     hash_levels: tuple = (-3, 10)
+    # ball/hinge joints, float32 [nj, 12]: type (1 ball, 2 hinge), body1,
+    # body2 (-1: the static environment), anchor xyz, axis xyz (world frame,
+    # hinge only), lo stop, hi stop (hinge only), 0
+    joints: np.ndarray | None = None
 
     @property
     def nb(self) -> int:
@@ -278,3 +282,93 @@ def capsule_pile(n: int = 96, seed: int = 2, spacing: float = 0.7) -> Scene:
     gR[:, [0, 5, 10]] = 1.0
     return Scene(f"capsule_pile{n}", bodies, gcls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
                  dt=1.0 / 120.0, iterations=20, mu=0.6, maxc=4)
+
+
+def mass_capsule(density, r, length):
+    """dMassSetCapsule (ode/src/mass.cpp:144-170), axis along the body z axis."""
+    r32, l32, d32 = np.float32(r), np.float32(length), np.float32(density)
+    pi = np.float32(math.pi)
+    M1 = pi * r32 * r32 * l32 * d32
+    M2 = np.float32(4.0 / 3.0) * pi * r32 * r32 * r32 * d32
+    mt = M1 + M2
+    Ia = M1 * (np.float32(0.25) * r32 * r32 + np.float32(1.0 / 12.0) * l32 * l32) + \
+        M2 * (np.float32(0.4) * r32 * r32 + np.float32(0.375) * r32 * l32 + np.float32(0.25) * l32 * l32)
+    Ib = (M1 * np.float32(0.5) + M2 * np.float32(0.4)) * r32 * r32
+    return mt, Ia, Ia, Ib
+
+
+def chains(n_chains: int = 8192, seed: int = 3, nmin: int = 2, nmax: int = 32, spacing: float = 17.0,
+           hang: bool = False, density: float = 1000.0) -> Scene:
+    """Articulated chains of capsules (radius 0.05 m, length U[0.2, 0.4] m,
+    N ~ log-uniform in [nmin, nmax]) linked by alternating hinge and ball
+    joints, the hinges limited to +-60 degrees about the chain plane's normal,
+    with seeded random joint angles (+-50 degrees).  Independent chains sit on
+    a square grid `spacing` m apart.  Dropped onto the plane z = 0 (mu 0.6), or
+    with `hang` hanging from a ball joint to the environment at the first
+    link's end, with no geoms (a joints-only scene).  dt 1/240, 20 iterations."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(math.sqrt(n_chains)))
+    r = 0.05
+    pos_l, q_l, mass_l, I_l, dims_l, joints = [], [], [], [], [], []
+    nb = 0
+    for c in range(n_chains):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        n = min(max(n, nmin), nmax)
+        lens = rng.uniform(0.2, 0.4, size=n)
+        yaw = rng.uniform(0, 2 * math.pi)
+        ex = np.array([math.cos(yaw), math.sin(yaw), 0.0])   # chain direction in plane
+        ey = np.array([-math.sin(yaw), math.cos(yaw), 0.0])  # hinge axis (plane normal)
+        phi = rng.uniform(-0.3, 0.3)
+        ang = np.concatenate([[phi], rng.uniform(-np.deg2rad(50), np.deg2rad(50), size=n - 1)])
+        phis = np.cumsum(ang)
+        dirs = np.stack([math.cos(p) * ex + math.sin(p) * np.array([0, 0, 1.0]) for p in phis])
+        ends = np.zeros((n + 1, 3))
+        for k in range(n):
+            ends[k + 1] = ends[k] + dirs[k] * (lens[k] + 2 * r)
+        base = np.array([(c % side + 0.5) * spacing, (c // side + 0.5) * spacing, 0.0])
+        zmin = ends[:, 2].min()
+        base[2] = (2.0 + (lens.sum() + 2 * r * n)) if hang else (0.3 - zmin)
+        for k in range(n):
+            centre = base + 0.5 * (ends[k] + ends[k + 1])
+            # body z axis along the link: rotation taking (0,0,1) to dirs[k]
+            d = dirs[k] / np.linalg.norm(dirs[k])
+            axis = np.cross([0, 0, 1.0], d)
+            sa, ca = np.linalg.norm(axis), d[2]
+            if sa < 1e-9:
+                q = np.array([1.0, 0, 0, 0])
+            else:
+                t = math.atan2(sa, ca)
+                axis = axis / sa
+                q = np.array([math.cos(t / 2), *(math.sin(t / 2) * axis)])
+            m, i1, i2, i3 = mass_capsule(density, r, lens[k])
+            pos_l.append(centre); q_l.append(q); mass_l.append(m); I_l.append((i1, i2, i3))
+            dims_l.append((r, lens[k], 0, 0))
+            if k == 0:
+                if hang:
+                    a = base + ends[0]
+                    joints.append((1, nb, -1, *a, 0, 0, 0, 0, 0, 0))
+            else:
+                a = base + ends[k]
+                if k % 2 == 1:
+                    joints.append((2, nb - 1, nb, *a, *ey, -math.pi / 3, math.pi / 3, 0))
+                else:
+                    joints.append((1, nb - 1, nb, *a, 0, 0, 0, 0, 0, 0))
+            nb += 1
+    pos = np.asarray(pos_l, np.float32)
+    q = np.asarray(q_l, np.float32)
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    bodies = _body_rows(pos, q, np.asarray(mass_l, np.float32), np.asarray(I_l, np.float32))
+    if hang:
+        cls = np.zeros(0, np.int32)
+        gbody = np.zeros(0, np.int32)
+        gdims = np.zeros((0, 4), np.float32)
+    else:
+        cls = np.concatenate([np.full(nb, CAPSULE, np.int32), [PLANE]]).astype(np.int32)
+        gbody = np.concatenate([np.arange(nb, dtype=np.int32), [-1]]).astype(np.int32)
+        gdims = np.concatenate([np.asarray(dims_l, np.float32), [[0, 0, 1, 0]]]).astype(np.float32)
+    ng = len(cls)
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene(f"chains{n_chains}" + ("_hanging" if hang else ""), bodies, cls, gbody,
+                 np.zeros((ng, 3), np.float32), gR, gdims, dt=1.0 / 240.0, iterations=20, mu=0.6, maxc=4,
+                 joints=np.asarray(joints, np.float32).reshape(-1, 12))

@@ -75,6 +75,20 @@ class GBWorld:
                 L.dGeomSetRotation(g, ode.fptr(R))
             L.dGeomSetData(g, ctypes.c_void_p(i))
             self.geoms.append(g)
+        self.joints = []
+        if scene.joints is not None:
+            for row in scene.joints:
+                t, b1, b2 = int(row[0]), int(row[1]), int(row[2])
+                j = L.dJointCreateBall(self.w, None) if t == 1 else L.dJointCreateHinge(self.w, None)
+                L.dJointAttach(j, self.bodies[b1], self.bodies[b2] if b2 >= 0 else None)
+                if t == 1:
+                    L.dJointSetBallAnchor(j, *[float(x) for x in row[3:6]])
+                else:
+                    L.dJointSetHingeAnchor(j, *[float(x) for x in row[3:6]])
+                    L.dJointSetHingeAxis(j, *[float(x) for x in row[6:9]])
+                    L.dJointSetHingeParam(j, ode.dParamLoStop, float(row[9]))
+                    L.dJointSetHingeParam(j, ode.dParamHiStop, float(row[10]))
+                self.joints.append(j)
         self.group = L.dJointGroupCreate(0)
         self.surface = ode.dSurfaceParameters()
         self.surface.mode = scene.surface_mode
@@ -95,8 +109,11 @@ class GBWorld:
         maxc = self.scene.maxc
         for i in range(maxc):
             self._contacts[i].surface = self.surface
-        n = L.dCollide(o1, o2, maxc, ctypes.addressof(self._contacts[0].geom), ctypes.sizeof(ode.dContact))
         b1, b2 = L.dGeomGetBody(o1), L.dGeomGetBody(o2)
+        # demo_boxstack.cpp:140: bodies joined by a (non-contact) joint do not collide
+        if b1 and b2 and L.dAreConnectedExcluding(b1, b2, ode.dJointTypeContact):
+            return
+        n = L.dCollide(o1, o2, maxc, ctypes.addressof(self._contacts[0].geom), ctypes.sizeof(ode.dContact))
         for i in range(n):
             j = L.dJointCreateContact(self.w, self.group, ctypes.byref(self._contacts[i]))
             L.dJointAttach(j, b1, b2)

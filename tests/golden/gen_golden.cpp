@@ -14,6 +14,9 @@
 //   loop IN OUT        the full user loop (dSpaceCollide -> near callback ->
 //                      dCollide -> dJointCreateContact -> dWorldQuickStep ->
 //                      dJointGroupEmpty) with per-step states and snapshots
+//   chain IN OUT       bodies linked by ball and hinge joints (hinge limits),
+//                      no geoms, stepped with dWorldQuickStep: per-step body
+//                      poses and hinge angles (dJointGetHingeAngle)
 #include <ode/ode.h>
 #include <cstdio>
 #include <cstdlib>
@@ -307,6 +310,49 @@ static void mode_loop() {
     dWorldDestroy(w);
 }
 
+// ---------------------------------------------------------------- chain
+static void mode_chain() {
+    int nb = rdi(), nj = rdi(), nsteps = rdi(), iters = rdi(), dyn = rdi();
+    WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
+    std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
+    std::vector<float> jt(12 * nj); rd(jt.data(), jt.size());
+    dWorldID w = dWorldCreate();
+    apply_params(w, P, iters, dyn);
+    std::vector<dBodyID> b(nb);
+    for (int i = 0; i < nb; i++) { b[i] = dBodyCreate(w); set_body(b[i], &bodies[BODY_IN * i]); }
+    std::vector<dJointID> hinges;
+    for (int k = 0; k < nj; k++) {
+        const float *r = &jt[12 * k];
+        const int t = (int)r[0], b1 = (int)r[1], b2 = (int)r[2];
+        dJointID j = t == 1 ? dJointCreateBall(w, 0) : dJointCreateHinge(w, 0);
+        dJointAttach(j, b[b1], b2 >= 0 ? b[b2] : 0);
+        if (t == 1) {
+            dJointSetBallAnchor(j, r[3], r[4], r[5]);
+        } else {
+            dJointSetHingeAnchor(j, r[3], r[4], r[5]);
+            dJointSetHingeAxis(j, r[6], r[7], r[8]);
+            dJointSetHingeParam(j, dParamLoStop, r[9]);
+            dJointSetHingeParam(j, dParamHiStop, r[10]);
+            hinges.push_back(j);
+        }
+    }
+    const int nh = (int)hinges.size();
+    std::vector<float> traj((size_t)nsteps * nb * 7), ang((size_t)nsteps * nh);
+    for (int s = 0; s < nsteps; s++) {
+        dWorldQuickStep(w, P.dt);
+        for (int i = 0; i < nb; i++) {
+            const dReal *p = dBodyGetPosition(b[i]), *q = dBodyGetQuaternion(b[i]);
+            float *o = &traj[((size_t)s * nb + i) * 7];
+            for (int j = 0; j < 3; j++) o[j] = (float)p[j];
+            for (int j = 0; j < 4; j++) o[3 + j] = (float)q[j];
+        }
+        for (int h = 0; h < nh; h++) ang[(size_t)s * nh + h] = (float)dJointGetHingeAngle(hinges[h]);
+    }
+    wr(traj.data(), traj.size());
+    wr(ang.data(), ang.size());
+    dWorldDestroy(w);
+}
+
 int main(int argc, char **argv) {
     if (argc != 4) { fprintf(stderr, "usage: gen_golden MODE IN OUT\n"); return 2; }
     fin = fopen(argv[2], "rb"); fout = fopen(argv[3], "wb");
@@ -316,6 +362,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[1], "space")) mode_space();
     else if (!strcmp(argv[1], "step")) mode_step();
     else if (!strcmp(argv[1], "loop")) mode_loop();
+    else if (!strcmp(argv[1], "chain")) mode_chain();
     else { fprintf(stderr, "bad mode\n"); return 2; }
     dCloseODE();
     fclose(fin); fclose(fout);

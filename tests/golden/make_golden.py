@@ -353,6 +353,25 @@ def gen_space_pile(exes):
           f"reference misses, {len(ref_bodies - exact)} extra")
 
 
+def gen_chain(exes):
+    """Hanging chains of capsules linked by hinge (limited +-60 deg) and ball
+    joints, no geoms: 240 steps of the no-reorder build with 200 iterations
+    (a converged solve), poses and hinge angles per step."""
+    sc = scenes.chains(6, seed=11, nmin=3, nmax=8, hang=True)
+    iters, nsteps = 200, 240
+    jt = np.ascontiguousarray(sc.joints, np.float32)
+    buf = run(exes["single_noreorder"], "chain",
+              [np.array([sc.nb, len(jt), nsteps, iters, 0], np.int32), sc.world_params(),
+               sc.bodies.astype(np.float32), jt])
+    r = Reader(buf)
+    traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
+    nh = int((jt[:, 0] == 2).sum())
+    ang = r.take(np.float32, nsteps * nh).reshape(nsteps, nh)
+    np.savez_compressed(os.path.join(HERE, "chain.npz"), bodies=sc.bodies, joints=jt, params=sc.world_params(),
+                        ints=np.array([iters, nsteps], np.int32), traj=traj, angles=ang)
+    print(f"chain: {sc.nb} bodies, {len(jt)} joints ({nh} hinges), {nsteps} steps")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -367,6 +386,8 @@ def main():
         gen_steps(exes)
     if a.only in ("", "space_pile"):
         gen_space_pile(exes)
+    if a.only in ("", "chain"):
+        gen_chain(exes)
 
 
 if __name__ == "__main__":
