@@ -911,6 +911,10 @@ struct PgsArgs {
 // dContactApprox1 with mu > 0 (contact.cpp:49-122): 1..4 contacts of three
 // consecutive rows, the two friction rows' findex naming the normal row.
 #define GB_DESC_TRIPLETS (1 << 30)
+// GB_DESC_PLAIN marks a group of at most 12 rows none of which has a findex
+// (ball and hinge joints, frictionless contacts): relaxed in row order.
+#define GB_DESC_PLAIN (1 << 29)
+#define GB_DESC_STAGED (GB_DESC_TRIPLETS | GB_DESC_PLAIN)
 __device__ __forceinline__ int desc_rows(int4 d) { return d.y & 0xffff; }
 
 __global__ void k_manifold_desc(const int *clist, const int *mstart, const int *rstart, const int *mcount,
@@ -923,7 +927,7 @@ __global__ void k_manifold_desc(const int *clist, const int *mstart, const int *
         if (e >= ncm) {  // a ball or hinge joint: its rows follow the contact rows
             const int k = e - ncm;
             const int2 b = gbody[e];
-            desc[j] = make_int4(dc->nrows_contacts + jrstart[k], jm[k], b.x, b.y);
+            desc[j] = make_int4(dc->nrows_contacts + jrstart[k], jm[k] | GB_DESC_PLAIN, b.x, b.y);
             continue;
         }
         const int c0 = mstart[e], c1 = mstart[e + 1];
@@ -935,7 +939,9 @@ __global__ void k_manifold_desc(const int *clist, const int *mstart, const int *
             const int r = r0 + 3 * (c - c0);
             tri = mcount[c] == 3 && rstart[c] == r && findex[r] < 0 && findex[r + 1] == r && findex[r + 2] == r;
         }
-        desc[j] = make_int4(r0, (r1 - r0) | (tri ? GB_DESC_TRIPLETS : 0), b.x, b.y);
+        bool plain = !tri && r1 - r0 <= 12;
+        for (int r = r0; r < r1 && plain; r++) plain = findex[r] < 0;
+        desc[j] = make_int4(r0, (r1 - r0) | (tri ? GB_DESC_TRIPLETS : 0) | (plain ? GB_DESC_PLAIN : 0), b.x, b.y);
     }
 }
 
@@ -1066,8 +1072,8 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
 // (TMA) completing on that buffer's mbarrier, so a colour's rows are already
 // on chip when its barrier opens.  A slot's offset in its chunk lives in
 // bits 16-27 of its descriptor's y.
-#define GB_PGS_THREADS 128
-#define GB_CHUNK_ROWS 864  // rows per buffer: 2 x 108 KB of shared memory
+#define GB_PGS_THREADS 256
+#define GB_CHUNK_ROWS 800  // rows per buffer: 2 x 100 KB of shared memory
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
 
@@ -1084,7 +1090,7 @@ __global__ void k_chunk_offsets(const int *cstart, const int *ccount, DevCounter
     int4 d;
     if (k < ccount[c]) {
         d = desc[cstart[c] + k];
-        if (d.y & GB_DESC_TRIPLETS) n = desc_rows(d);
+        if (d.y & GB_DESC_STAGED) n = desc_rows(d);
     }
     // block exclusive scan of n
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1116,7 +1122,7 @@ __global__ void k_pack_rows(Rows Rw, const int *cstart, const int *ccount, DevCo
     const int k = b + threadIdx.x * B;
     if (k >= ccount[c]) return;
     const int4 d = desc[cstart[c] + k];
-    if (!(d.y & GB_DESC_TRIPLETS)) return;
+    if (!(d.y & GB_DESC_STAGED)) return;
     const int n = desc_rows(d), off = desc_chunk_off(d);
     float4 *dst = packed + (size_t)chunk_start[c * B + b] * 8;
     const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
@@ -1244,6 +1250,27 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
     }
 #pragma unroll 1
     for (int k = 0; k < 3 * nct; k++) A.Rw.lambda[d.x + k] = lam[k];
+    stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
+    if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
+}
+
+// A staged plain group (GB_DESC_PLAIN): every row in order with its own bounds.
+__device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const float4 *buf, float *lam) {
+    const int n = desc_rows(d), off = desc_chunk_off(d);
+    const bool two = d.w >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    cp_async_wait_all();
+    float4 row[8];
+#pragma unroll 1
+    for (int k = 0; k < n; k++) {
+#pragma unroll
+        for (int a = 0; a < 8; a++) row[a] = buf[swz(off + k, a)];
+        relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+    }
+#pragma unroll 1
+    for (int k = 0; k < n; k++) A.Rw.lambda[d.x + k] = lam[k];
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
@@ -1387,7 +1414,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
         staged = false;
         if (has_next) {
             const int n = desc_rows(next);
-            staged = (next.y & GB_DESC_TRIPLETS) && desc_chunk_off(next) + n <= GB_CHUNK_ROWS;
+            staged = (next.y & GB_DESC_STAGED) && desc_chunk_off(next) + n <= GB_CHUNK_ROWS;
             if (staged) {
                 for (int k = 0; k < n; k++) cp_async4(&my_lam[k], &A.Rw.lambda[next.x + k]);
                 cp_async_commit();
@@ -1410,7 +1437,9 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                     relax_desc(A, next);
                 } else {
                     if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
-                    relax_triplets(A, next, pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8), my_lam);
+                    const float4 *buf = pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8);
+                    if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam);
+                    else relax_plain(A, next, buf, my_lam);
                 }
             }
             const int s = s_cstart[c], n = s_ccount[c];
@@ -1964,7 +1993,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         // one block per SM (the grid barrier's cost grows with the block count;
         // the chunk packing above assumes exactly pgs_blocks blocks)
         const int threads = GB_PGS_THREADS;
-        const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;  // two chunk buffers, 216 KB
+        const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;  // two chunk buffers, 200 KB
         static bool smem_set = false;
         if (!smem_set) {
             cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
