@@ -373,13 +373,18 @@ def batched_leg(args, L, stream, dev):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     out = {"workload": f"chains{args.chains}", "bodies": sc.nb, "joints": int(len(sc.joints)), "dt": sc.dt,
            "setup_s": round(setup_s, 1)}
-    for label, target in (("iterations20", 0.0), ("residual", args.target)):
+    L.gbodeWorldSetTiming(w.w, 0)
+    for label, target, graph in (("iterations20", 0.0, False), ("iterations20_graph", 0.0, True),
+                                 ("residual", args.target, False), ("residual_graph", args.target, True)):
         if target > 0:
             L.gbodeWorldSetResidualTarget(w.w, target, args.check_every, args.max_iters)
         for _ in range(args.warmup):
-            w.step_fused()
+            if graph:
+                w.step_graph()
+            else:
+                w.step_fused()
         w.sync()
-        T = timed_steps(w, stream, flush, args.steps)
+        T = timed_steps(w, stream, flush, args.steps, graph=graph)
         ms = sum(T["step_ms"])
         ok = sum(1 for r in T["resid"] if target == 0 or r <= target)
         out[label] = {"body_steps_per_s": sc.nb * ok / (ms / 1e3), "ms_per_step": ms / args.steps,
@@ -390,12 +395,12 @@ def batched_leg(args, L, stream, dev):
     out["fp64_residual_last_step"] = r64 / max(1.0, ml)
     out["note"] = ("value counts steps at the residual target (residual) or every step at the configured 20 "
                    "sweeps (iterations20); the chains are islands of one world, solved by the same coloured "
-                   "persistent kernel")
+                   "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused)")
     w.close()
     return out
 
 
-def timed_steps(w, stream, flush, steps):
+def timed_steps(w, stream, flush, steps, graph=False):
     """`steps` fused steps, each bracketed by CUDA events on the world's stream
     (L2 flushed before each, outside the events); per-step statistics."""
     import torch
@@ -407,7 +412,10 @@ def timed_steps(w, stream, flush, steps):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        w.step_fused()
+        if graph:
+            w.step_graph()
+        else:
+            w.step_fused()
         e1.record(stream)
         stream.synchronize()
         st = w.stats()

@@ -264,6 +264,16 @@ void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale);
 int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, const dSurfaceParameters *s,
                               int maxc);
 
+/* One fused step (no counterpart in the reference): gbodeSpaceCollideContacts
+ * + dWorldQuickStep(w, dt) + dJointGroupEmpty(group).  With use_graph != 0
+ * the step is recorded once into a CUDA graph -- on the second call after
+ * anything that changes the recorded work (body, geom or joint edits on the
+ * host, parameters, sizes) -- and later calls replay it with a single
+ * cudaGraphLaunch on the world's stream.  The world needs its own stream (the
+ * default) and step timing off.  Returns 1, or 0 on error. */
+int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *s, int maxc,
+                        dReal dt, int use_graph);
+
 /* Pair rule of a hash space.  0 (default): exactly the pairs the reference's
  * dHashSpace reports, including its blind spot -- the bucket of a cell is
  * computed in unsigned arithmetic that wraps for negative z in columns near

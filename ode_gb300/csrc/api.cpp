@@ -154,6 +154,11 @@ struct dxWorld {
     std::vector<dxBody *> bodies;
     std::vector<dxJoint *> joints;
     bool joints_dirty = false;  // ball/hinge joints changed since the last upload
+    // gbodeWorldStepFused's CUDA graph of one fused step
+    int graph_state = 0;  // 0 none, 1 capture on the next call, 2 replaying
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> graph_key;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool dev_dirty = true;    // host body state newer than device
@@ -368,6 +373,7 @@ static bool space_upload(dxSpace *sp, dxWorld *w) {
 
 // ------------------------------------------------------------------ init / misc
 extern "C" {
+static void drop_graph(dxWorld *w);
 
 int dInitODE2(unsigned int) { return 1; }
 void dInitODE(void) {}
@@ -507,6 +513,7 @@ void dWorldDestroy(dWorldID w) {
         delete j;
     }
     if (w->stream) cudaStreamSynchronize(w->stream);
+    drop_graph(w);
     for (int i = 0; i < 4; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     w->ws.release();
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
@@ -947,9 +954,7 @@ int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, c
     surf.bounce = sp->bounce; surf.bounce_vel = sp->bounce_vel; surf.soft_erp = sp->soft_erp; surf.soft_cfm = sp->soft_cfm;
     surf.motion1 = sp->motion1; surf.motion2 = sp->motion2; surf.motionN = sp->motionN; surf.slip1 = sp->slip1; surf.slip2 = sp->slip2;
     if (!w->ws.surfaces.ensure(sizeof(Surface))) { set_error("device allocation (surfaces)"); return 0; }
-    static thread_local Surface staged;  // pageable source kept alive past the async copy
-    staged = surf;
-    cudaMemcpyAsync(w->ws.surfaces.p, &staged, sizeof(Surface), cudaMemcpyHostToDevice, s);
+    launch_set_surface(w->ws, surf, s);  // by value: no host buffer outlives the call
     launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
     if (!launch_broadphase(w->ws, ng, space->exact_pairs, s)) { set_error("broad phase"); return 0; }
     if (!launch_narrowphase(w->ws, maxc, 0, false, s)) { set_error("narrow phase"); return 0; }
@@ -1449,6 +1454,84 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
 
 // dWorldStep (the Dantzig LCP stepper, ode.cpp:1828-1845) is outside this
 // library's path; it runs the quickstep solver with a large iteration count.
+static void drop_graph(dxWorld *w) {
+    if (w->gexec) cudaGraphExecDestroy(w->gexec);
+    if (w->graph) cudaGraphDestroy(w->graph);
+    w->gexec = nullptr;
+    w->graph = nullptr;
+    w->graph_state = 0;
+}
+
+// One fused step: gbodeSpaceCollideContacts + dWorldQuickStep +
+// dJointGroupEmpty.  With use_graph, the step's kernels, copies and memsets
+// are recorded once into a CUDA graph (on the second call after anything that
+// changes them: sizes, parameters, host-side edits of bodies, joints or
+// geoms) and replayed by one cudaGraphLaunch afterwards.
+int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *sp, int maxc,
+                        dReal dt, int use_graph) {
+    if (!w || !space || !group || !sp || maxc < 1 || !(dt > 0)) {
+        set_error("gbodeWorldStepFused: bad argument");
+        return 0;
+    }
+    auto plain = [&]() -> int {
+        if (!gbodeSpaceCollideContacts(space, w, group, sp, maxc)) return 0;
+        const int ok = dWorldQuickStep(w, dt);
+        dJointGroupEmpty(group);
+        return ok;
+    };
+    if (!use_graph) return plain();
+    std::vector<unsigned char> key;
+    auto put = [&](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        key.insert(key.end(), c, c + n);
+    };
+    const int nb = (int)w->bodies.size(), ng = (int)space->geoms.size();
+    put(&space, sizeof space); put(&group, sizeof group); put(&maxc, sizeof maxc); put(&dt, sizeof dt);
+    put(sp, sizeof *sp); put(&w->P, sizeof w->P); put(&nb, sizeof nb); put(&ng, sizeof ng);
+    const bool clean = !w->dev_dirty && !w->joints_dirty && !space->dirty && w->uploaded_space == space &&
+                       !w->timing && w->stream != nullptr && group->joints.empty();
+    if (clean && key == w->graph_key && w->graph_state == 2) {
+        cudaError_t e = cudaGraphLaunch(w->gexec, w->stream);
+        if (e != cudaSuccess) { set_error("gbodeWorldStepFused: graph launch", e); drop_graph(w); return 0; }
+        // the host-side effects of a fused step
+        w->host_valid = false;
+        w->stats_pending = true;
+        w->last_host_contacts = 0;
+        w->device_contacts = false;
+        w->device_surfaces = 1;
+        return 1;
+    }
+    if (clean && key == w->graph_key && w->graph_state == 1) {
+        drop_graph(w);
+        cudaError_t e = cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { set_error("gbodeWorldStepFused: begin capture", e); return 0; }
+        const int ok = plain();  // recorded, not run
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(w->stream, &g);
+        if (!ok || e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            set_error("gbodeWorldStepFused: capture failed", e);
+            return 0;
+        }
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); set_error("gbodeWorldStepFused: instantiate", e); return 0; }
+        w->graph = g;
+        w->gexec = ex;
+        w->graph_state = 2;
+        e = cudaGraphLaunch(ex, w->stream);  // run the step just recorded
+        if (e != cudaSuccess) { set_error("gbodeWorldStepFused: graph launch", e); drop_graph(w); return 0; }
+        return 1;
+    }
+    // a plain step settles buffer sizes and uploads; the next call captures
+    drop_graph(w);
+    const int ok = plain();
+    w->graph_key = key;
+    w->graph_state = ok ? 1 : 0;
+    return ok;
+}
+
 int dWorldStep(dWorldID w, dReal stepsize) {
     int it = w->P.iterations;
     w->P.iterations = 200;

@@ -396,12 +396,22 @@ bool upload_geoms(Workspace &ws, const std::vector<GeomHost> &g, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess;
 }
 
+__global__ void k_set_surface(Surface v, Surface *dst) { *dst = v; }
+void launch_set_surface(Workspace &ws, const Surface &v, cudaStream_t s) {
+    k_set_surface<<<1, 1, 0, s>>>(v, ws.surfaces.as<Surface>());
+    count_launch();
+}
+
+__global__ void k_pose_init(DevCounters *dc) {
+    dc->nbig = 0;
+    dc->maxlevel = -1000;
+}
+
 void launch_pose_aabb(Workspace &ws, const Bodies &b, int ng, int minlevel, int maxlevel, cudaStream_t s) {
     // big-list count and coarsest level in use are rebuilt by the kernel
-    static const int init[2] = {0, -1000};
-    cudaMemcpyAsync(&ws.dc->nbig, init, sizeof init, cudaMemcpyHostToDevice, s);
+    k_pose_init<<<1, 1, 0, s>>>(ws.dc);
     k_pose_aabb<<<grid_for(ng, 128), 128, 0, s>>>(geoms_view(ws, ng), b, minlevel, maxlevel, ws.g_big.as<int>(), ws.dc);
-    count_launch();
+    count_launch(2);
 }
 
 static unsigned table_mask(int ng) {

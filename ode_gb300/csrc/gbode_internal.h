@@ -72,6 +72,7 @@ struct DevCounters {
     int ncmanifolds;       // contact manifolds (the first groups; ball/hinge joints follow)
     int nrows_contacts;    // rows of the contacts (joint rows follow)
     int njoint_rows;       // scan scratch (joint rows)
+    int warm_parity;       // which warm-start table holds the previous step
 };
 
 struct Workspace {
@@ -103,7 +104,6 @@ struct Workspace {
     DBuf res_f, res_v;
     // scan scratch
     DBuf scan_tmp;
-    int warm_parity = 0;         // which of the two warm-start tables holds the previous step
     unsigned warm_mask = 0;      // table size - 1 (power of two)
     bool warm_valid = false;     // the previous-step table was filled
     DevCounters *dc = nullptr;   // device counters
@@ -167,6 +167,7 @@ void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cud
 // launch bookkeeping
 void count_launch(int n = 1);
 int num_sms();
+void launch_set_surface(Workspace &ws, const Surface &v, cudaStream_t s);
 // records the message gbodeGetLastError() returns on this thread
 void report_error(const char *msg);
 // learned warm start network (mlp.cu)

@@ -170,8 +170,11 @@ __device__ __forceinline__ unsigned warm_hash(unsigned long long k) {
     k ^= k >> 31; k *= 0x7fb5d329728ea185ull; k ^= k >> 27; k *= 0x81dadef4bc2dd44dull; k ^= k >> 33;
     return (unsigned)k;
 }
+// Two tables of mask+1 entries each; DevCounters.warm_parity (device-side,
+// flipped by a kernel, so a recorded CUDA graph alternates them too) says
+// which one holds the previous step.
 struct WarmTable {
-    const unsigned long long *keys;  // previous step (read)
+    const unsigned long long *keys;  // both tables (null: no warm start)
     const float4 *lam;
     unsigned mask;
     float scale;
@@ -383,11 +386,12 @@ __global__ void k_rows(const Contact *C, const Surface *S, const int *nc_dev, co
         bool warm_found = false;
         if (W.keys) {
             const unsigned long long key = warm_key(k);
+            const size_t tb = (size_t)(W.mask + 1) * dc->warm_parity;
             unsigned h = warm_hash(key) & W.mask;
             for (unsigned probe = 0; probe <= W.mask; probe++) {
-                const unsigned long long kk = W.keys[h];
+                const unsigned long long kk = W.keys[tb + h];
                 if (kk == key) {
-                    const float4 l = W.lam[h];
+                    const float4 l = W.lam[tb + h];
                     warm3[0] = l.x * W.scale; warm3[1] = l.y * W.scale; warm3[2] = l.z * W.scale;
                     warm_found = true;
                     break;
@@ -689,9 +693,19 @@ __global__ void k_learned_apply(const int *nc_dev, const int *rstart, const int 
     }
 }
 
+// clear the table the step writes (the one not holding the previous step)
+__global__ void k_warm_clear(unsigned long long *keys, unsigned mask, const DevCounters *dc) {
+    unsigned long long *t = keys + (size_t)(mask + 1) * (dc->warm_parity ^ 1);
+    for (size_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= mask; i += (size_t)gridDim.x * blockDim.x) t[i] = ~0ull;
+}
+__global__ void k_warm_flip(DevCounters *dc) { dc->warm_parity ^= 1; }
+
 __global__ void k_warm_store(const Contact *C, const int *nc_dev, const int *rstart, const int *mcount, Rows Rw,
-                             unsigned long long *keys, float4 *lam, unsigned mask) {
+                             unsigned long long *keys_all, float4 *lam_all, unsigned mask, const DevCounters *dc) {
     const int nc = *nc_dev;
+    const size_t tb = (size_t)(mask + 1) * (dc->warm_parity ^ 1);
+    unsigned long long *keys = keys_all + tb;
+    float4 *lam = lam_all + tb;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const Contact k = C[c];
         const unsigned long long key = warm_key(k);
@@ -1814,8 +1828,16 @@ static Rows rows_view(Workspace &ws) {
 }
 
 static int coop_blocks(const void *kernel, int block, int max_per_sm) {
+    // queried once per kernel (the answer does not change; no query runs while a step is captured)
+    static const void *k_cached = nullptr;
+    static int per_sm_cached = 0;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (k_cached == kernel) per_sm = per_sm_cached;
+    else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+        k_cached = kernel;
+        per_sm_cached = per_sm;
+    }
     if (per_sm < 1) per_sm = 1;
     if (per_sm > max_per_sm) per_sm = max_per_sm;
     return per_sm * num_sms();
@@ -1835,9 +1857,8 @@ static bool ensure_warm(Workspace &ws) {
 static WarmTable warm_lookup(Workspace &ws, const SolverParams &P) {
     WarmTable W{nullptr, nullptr, 0, 0.f};
     if (P.warm_mode && ws.warm_valid) {
-        size_t T = (size_t)ws.warm_mask + 1;
-        W.keys = ws.w_keys.as<unsigned long long>() + T * ws.warm_parity;
-        W.lam = ws.w_lambda.as<float4>() + T * ws.warm_parity;
+        W.keys = ws.w_keys.as<unsigned long long>();
+        W.lam = ws.w_lambda.as<float4>();
         W.mask = ws.warm_mask;
         W.scale = P.warm_scale;
     }
@@ -1845,15 +1866,13 @@ static WarmTable warm_lookup(Workspace &ws, const SolverParams &P) {
 }
 
 static void warm_store(Workspace &ws, cudaStream_t s) {
-    size_t T = (size_t)ws.warm_mask + 1;
-    int cur = ws.warm_parity ^ 1;
-    unsigned long long *keys = ws.w_keys.as<unsigned long long>() + T * cur;
-    float4 *lam = ws.w_lambda.as<float4>() + T * cur;
-    cudaMemsetAsync(keys, 0xFF, T * 8, s);
+    unsigned long long *keys = ws.w_keys.as<unsigned long long>();
+    float4 *lam = ws.w_lambda.as<float4>();
+    k_warm_clear<<<4 * num_sms(), 256, 0, s>>>(keys, ws.warm_mask, ws.dc);
     k_warm_store<<<4 * num_sms(), 256, 0, s>>>(ws.contacts.as<Contact>(), &ws.dc->ncontacts, ws.c_rstart.as<int>(),
-                                               ws.c_mcount.as<int>(), rows_view(ws), keys, lam, ws.warm_mask);
-    count_launch();
-    ws.warm_parity = cur;
+                                               ws.c_mcount.as<int>(), rows_view(ws), keys, lam, ws.warm_mask, ws.dc);
+    k_warm_flip<<<1, 1, 0, s>>>(ws.dc);
+    count_launch(3);
     ws.warm_valid = true;
 }
 
@@ -1999,8 +2018,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             smem_set = true;
         }
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, (const void *)k_pgs, threads, smem, 0);
+        static int per_sm = -1;  // queried once
+        if (per_sm < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, (const void *)k_pgs, threads, smem, 0);
         if (per_sm < 1) return false;
         const int blocks = pgs_blocks;
         void *args[] = {(void *)&A};

@@ -146,6 +146,7 @@ _PROTOS = [
     ("dJointGetBallAnchor", None, [ID, _F]), ("dJointGetBallParam", dReal, [ID, ctypes.c_int]),
     ("dJointGetHingeAnchor", None, [ID, _F]), ("dJointGetHingeAxis", None, [ID, _F]),
     ("dJointGetHingeParam", dReal, [ID, ctypes.c_int]), ("dJointGetHingeAngle", dReal, [ID]),
+    ("gbodeWorldStepFused", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int]),
     ("gbodeMlpParamCount", ctypes.c_int, []),
     ("gbodeMlpLossGrad", ctypes.c_int, [_F, _F, _F, ctypes.c_int, _F, _F]),
     ("gbodeMlpTrain", ctypes.c_int, [_F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,

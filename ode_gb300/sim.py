@@ -128,6 +128,14 @@ class GBWorld:
         self.L.dJointGroupEmpty(self.group)
         return ok
 
+    def step_graph(self):
+        """A fused step replayed from a CUDA graph (gbodeWorldStepFused)."""
+        L = self.L
+        if not L.gbodeWorldStepFused(self.w, self.space, self.group, ctypes.byref(self.surface), self.scene.maxc,
+                                     self.scene.dt, 1):
+            raise RuntimeError(L.gbodeGetLastError().decode())
+        return 1
+
     def step_fused(self):
         L = self.L
         if not L.gbodeSpaceCollideContacts(self.space, self.w, self.group, ctypes.byref(self.surface),

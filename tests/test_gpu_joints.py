@@ -111,3 +111,26 @@ def test_dropped_chains_rest_on_the_ground(gblib):
     assert np.abs(ang).max() < np.pi / 3 + 0.15
     print(f"dropped chains: {sc.nb} bodies, {w.stats().contacts} contacts, max |hinge angle| {np.abs(ang).max():.3f}")
     w.close()
+
+
+def test_graph_replay_matches_plain_steps(gblib):
+    """gbodeWorldStepFused with a CUDA graph gives the same states, to the
+    bit, as the same steps issued one call at a time (chains with joints and
+    ground contacts, residual-target sweeps)."""
+    from ode_gb300 import scenes, sim
+    L = gblib
+    sc = scenes.chains(32, seed=9)
+    worlds = [sim.GBWorld(sc), sim.GBWorld(sc)]
+    for w in worlds:
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+        L.gbodeWorldSetResidualTarget(w.w, 1e-4, 5, 3000)
+    for _ in range(40):
+        worlds[0].step_fused()
+        worlds[1].step_graph()
+    a, b = worlds[0].state(), worlds[1].state()
+    assert np.isfinite(a).all()
+    assert np.array_equal(a, b), float(np.abs(a - b).max())
+    assert worlds[1].stats().iterations > 0
+    for w in worlds:
+        w.close()
