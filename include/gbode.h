@@ -197,10 +197,15 @@ int dAreConnected(dBodyID body1, dBodyID body2);                          /* obj
 
 /* ---- ball and hinge joints: include/ode/common.h:384-403 (types),
  * :439-455 (parameters), objects.h:1693-2618 */
-enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider, dJointTypeContact };
+enum {
+    dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider, dJointTypeContact, dJointTypeUniversal,
+    dJointTypeHinge2
+};
 enum {
     dParamLoStop = 0, dParamHiStop, dParamVel, dParamLoVel, dParamHiVel, dParamFMax, dParamFudgeFactor,
-    dParamBounce, dParamCFM, dParamStopERP, dParamStopCFM, dParamSuspensionERP, dParamSuspensionCFM, dParamERP
+    dParamBounce, dParamCFM, dParamStopERP, dParamStopCFM, dParamSuspensionERP, dParamSuspensionCFM, dParamERP,
+    dParamGroup2 = 0x100, dParamLoStop2 = 0x100, dParamHiStop2, dParamVel2, dParamLoVel2, dParamHiVel2, dParamFMax2,
+    dParamFudgeFactor2, dParamBounce2, dParamCFM2, dParamStopERP2, dParamStopCFM2
 };
 dJointID dJointCreateBall(dWorldID w, dJointGroupID group);    /* objects.h:1693 */
 dJointID dJointCreateHinge(dWorldID w, dJointGroupID group);   /* objects.h:1701 */
@@ -216,6 +221,15 @@ void dJointGetHingeAnchor(dJointID j, dVector3 result);                  /* obje
 void dJointGetHingeAxis(dJointID j, dVector3 result);                    /* objects.h:2598 */
 dReal dJointGetHingeParam(dJointID j, int parameter);                     /* objects.h:2604 */
 dReal dJointGetHingeAngle(dJointID j);                                    /* objects.h:2618 */
+dJointID dJointCreateHinge2(dWorldID w, dJointGroupID group);                  /* objects.h:1725 */
+void dJointSetHinge2Anchor(dJointID j, dReal x, dReal y, dReal z);            /* objects.h:2070 */
+void dJointSetHinge2Axes(dJointID j, const dReal *axis1, const dReal *axis2); /* objects.h:2084 */
+void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z);             /* objects.h:2094 */
+void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z);             /* objects.h:2104 */
+void dJointSetHinge2Param(dJointID j, int parameter, dReal value);             /* objects.h:2110 */
+void dJointGetHinge2Anchor(dJointID j, dVector3 result);                       /* objects.h:2663 */
+dReal dJointGetHinge2Param(dJointID j, int parameter);                          /* objects.h:2691 */
+dReal dJointGetHinge2Angle1(dJointID j);                                        /* objects.h:2697 */
 
 /* ---- misc: include/ode/misc.h:35-50, rotation.h:40-70 */
 unsigned long dRand(void);

@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -144,6 +144,10 @@ struct dxJoint {
     float axis1[4] = {1, 0, 0, 0}, axis2[4] = {1, 0, 0, 0}, qrel[4] = {0, 0, 0, 0};
     float erp = 0, cfm = 0;
     Limot limot;
+    // hinge2 (joints/hinge2.cpp): angle-measuring vectors in body 1's frame,
+    // sin/cos of the rest angle between the axes, suspension, axis-2 motor
+    float v1[4] = {1, 0, 0, 0}, v2[4] = {0, 1, 0, 0}, s0 = 0, c0 = 0, susp_erp = 0, susp_cfm = 0;
+    Limot limot2;
     dxBody *node0() const { return b1 ? b1 : b2; }
     dxBody *node1() const { return b1 ? b2 : nullptr; }
 };
@@ -1041,6 +1045,12 @@ static dxJoint *joint_new(dWorldID w, dJointGroupID group, int type) {
     j->limot.normal_cfm = w->P.cfm;  // joint.cpp:495-509
     j->limot.stop_erp = w->P.erp;
     j->limot.stop_cfm = w->P.cfm;
+    j->limot2 = j->limot;
+    if (type == dJointTypeHinge2) {  // hinge2.cpp:74-98
+        j->axis2[0] = 0; j->axis2[1] = 1;
+        j->susp_erp = w->P.erp;
+        j->susp_cfm = w->P.cfm;
+    }
     w->joints.push_back(j);
     if (group) group->joints.push_back(j);
     w->joints_dirty = true;
@@ -1048,6 +1058,7 @@ static dxJoint *joint_new(dWorldID w, dJointGroupID group, int type) {
 }
 dJointID dJointCreateBall(dWorldID w, dJointGroupID group) { return joint_new(w, group, dJointTypeBall); }
 dJointID dJointCreateHinge(dWorldID w, dJointGroupID group) { return joint_new(w, group, dJointTypeHinge); }
+dJointID dJointCreateHinge2(dWorldID w, dJointGroupID group) { return joint_new(w, group, dJointTypeHinge2); }
 int dJointGetType(dJointID j) { return j->type; }
 
 static void mul1_331(float *r, const float *R, const float *q) {  // R^T q (dMultiply1_331)
@@ -1080,22 +1091,70 @@ static void set_anchors(dxJoint *j, float x, float y, float z, float *a1, float 
     a2[3] = 0;
     j->world->joints_dirty = true;
 }
-// joint.cpp:325-360 setAxes (both axes)
+// odemath.cpp:95-151 dxSafeNormalize3: scale by the largest component first
+static bool safe_normalize3(float *a) {
+    const float a0 = fabsf(a[0]), a1 = fabsf(a[1]), a2 = fabsf(a[2]);
+    int idx;
+    if (a1 > a0) idx = a2 > a1 ? 2 : 1;
+    else if (a2 > a0) idx = 2;
+    else {
+        if (!(a0 > 0.0f)) return false;
+        idx = 0;
+    }
+    const int i1 = idx == 0 ? 1 : 0, i2 = idx == 2 ? 1 : 2;
+    const float r = 1.0f / fabsf(a[idx]);
+    const float b1 = a[i1] * r, b2 = a[i2] * r;
+    const float l = 1.0f / sqrtf(1.0f + b1 * b1 + b2 * b2);
+    a[i1] = b1 * l;
+    a[i2] = b2 * l;
+    a[idx] = copysignf(l, a[idx]);
+    return true;
+}
+// joint.cpp:325-360 setAxes: either target may be null
 static void set_axes(dxJoint *j, float x, float y, float z, float *ax1, float *ax2) {
     world_download(j->world);
     dxBody *b0 = j->node0(), *b1 = j->node1();
     if (b0) {
         float q[4] = {x, y, z, 0};
-        // dNormalize3 (odemath.cpp:95-151): largest component first
-        float l = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        if (l > 0) { l = 1.0f / sqrtf(l); q[0] *= l; q[1] *= l; q[2] *= l; } else { q[0] = 1; q[1] = q[2] = 0; }
-        mul1_331(ax1, b0->R, q);
-        ax1[3] = 0;
-        if (b1) mul1_331(ax2, b1->R, q);
-        else { ax2[0] = x; ax2[1] = y; ax2[2] = z; }
-        ax2[3] = 0;
+        safe_normalize3(q);  // dNormalize3
+        if (ax1) {
+            mul1_331(ax1, b0->R, q);
+            ax1[3] = 0;
+        }
+        if (ax2) {
+            if (b1) mul1_331(ax2, b1->R, q);
+            else { ax2[0] = x; ax2[1] = y; ax2[2] = z; }
+            ax2[3] = 0;
+        }
     }
     j->world->joints_dirty = true;
+}
+static void cross3h(float *r, const float *a, const float *b) {
+    const float r0 = a[1] * b[2] - a[2] * b[1], r1 = a[2] * b[0] - a[0] * b[2], r2 = a[0] * b[1] - a[1] * b[0];
+    r[0] = r0; r[1] = r1; r[2] = r2;
+}
+static float dot3h(const float *a, const float *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+// hinge2.cpp:135-144 getAxisInfo (sin and cos of the angle between the axes)
+static void hinge2_axis_info(const dxJoint *j, float *ax1, float *ax2, float *q, float &sa, float &ca) {
+    mul0_331h(ax1, j->node0()->R, j->axis1);
+    mul0_331h(ax2, j->node1()->R, j->axis2);
+    cross3h(q, ax1, ax2);
+    sa = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    ca = dot3h(ax1, ax2);
+}
+// hinge2.cpp:215-240 makeV1andV2
+static void hinge2_make_v(dxJoint *j) {
+    if (!j->node0() || !j->node1()) return;
+    float ax1[3], ax2[3], v[3];
+    mul0_331h(ax1, j->node0()->R, j->axis1);
+    mul0_331h(ax2, j->node1()->R, j->axis2);
+    const float k = dot3h(ax1, ax2);
+    ax2[0] = ax2[0] + ax1[0] * -k; ax2[1] = ax2[1] + ax1[1] * -k; ax2[2] = ax2[2] + ax1[2] * -k;
+    if (safe_normalize3(ax2)) {
+        cross3h(v, ax1, ax2);
+        mul1_331(j->v1, j->node0()->R, ax2);
+        mul1_331(j->v2, j->node0()->R, v);
+    }
 }
 // hinge.cpp:376-393 computeInitialRelativeRotation
 static void hinge_qrel(dxJoint *j) {
@@ -1218,6 +1277,56 @@ dReal dJointGetHingeAngle(dJointID j) {
     return (!j->b1 && j->b2) ? -a : a;
 }
 
+// hinge2.cpp:272-330
+void dJointSetHinge2Anchor(dJointID j, dReal x, dReal y, dReal z) {
+    set_anchors(j, x, y, z, j->anchor1, j->anchor2);
+    hinge2_make_v(j);
+}
+void dJointSetHinge2Axes(dJointID j, const dReal *axis1, const dReal *axis2) {
+    if (axis1) set_axes(j, axis1[0], axis1[1], axis1[2], j->axis1, nullptr);
+    if (axis2) set_axes(j, axis2[0], axis2[1], axis2[2], nullptr, j->axis2);
+    if (j->node0() && j->node1()) {
+        float ax1[3], ax2[3], q[3];
+        hinge2_axis_info(j, ax1, ax2, q, j->s0, j->c0);
+    }
+    hinge2_make_v(j);
+}
+void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z) {
+    const dReal a[3] = {x, y, z};
+    dJointSetHinge2Axes(j, a, nullptr);
+}
+void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z) {
+    const dReal a[3] = {x, y, z};
+    dJointSetHinge2Axes(j, nullptr, a);
+}
+void dJointSetHinge2Param(dJointID j, int parameter, dReal value) {  // hinge2.cpp:333-347
+    if ((parameter & 0xff00) == 0x100) limot_set(j->limot2, parameter & 0xff, value);
+    else if (parameter == dParamSuspensionERP) j->susp_erp = value;
+    else if (parameter == dParamSuspensionCFM) j->susp_cfm = value;
+    else limot_set(j->limot, parameter, value);
+    j->world->joints_dirty = true;
+}
+dReal dJointGetHinge2Param(dJointID j, int parameter) {
+    if ((parameter & 0xff00) == 0x100) return limot_get(j->limot2, parameter & 0xff);
+    if (parameter == dParamSuspensionERP) return j->susp_erp;
+    if (parameter == dParamSuspensionCFM) return j->susp_cfm;
+    return limot_get(j->limot, parameter);
+}
+void dJointGetHinge2Anchor(dJointID j, dVector3 out) {
+    bool rev = !j->b1 && j->b2;
+    anchor_world(j, out, rev ? j->anchor2 : j->anchor1, rev);
+}
+// hinge2.cpp:33-51 measureAngle1
+dReal dJointGetHinge2Angle1(dJointID j) {
+    world_download(j->world);
+    float p[3], q[3];
+    if (j->node1()) mul0_331h(p, j->node1()->R, j->axis2);
+    else { p[0] = j->axis2[0]; p[1] = j->axis2[1]; p[2] = j->axis2[2]; }
+    if (j->node0()) mul1_331(q, j->node0()->R, p);
+    else { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; }
+    return -atan2f(dot3h(j->v2, q), dot3h(j->v1, q));
+}
+
 // Upload the ball and hinge joints (attached, in world order) when they changed.
 static bool upload_joint_table(dxWorld *w) {
     if (!w->joints_dirty) return true;
@@ -1226,7 +1335,7 @@ static bool upload_joint_table(dxWorld *w) {
         if (j->attached && j->type != dJointTypeContact && j->node0()) jt.push_back(j);
     const int n = (int)jt.size();
     std::vector<int4> info(n);
-    std::vector<float4> a1(n), a2(n), x1(n), x2(n), qr(n), l0(n), l1(n), l2(n);
+    std::vector<float4> a1(n), a2(n), x1(n), x2(n), qr(n), l0(n), l1(n), l2(n), hv1(n), hv2(n), m0(n), m1(n), m2(n);
     for (int k = 0; k < n; k++) {
         const dxJoint *j = jt[k];
         info[k] = make_int4(j->type, j->node0()->index, j->node1() ? j->node1()->index : -1, (!j->b1 && j->b2) ? 1 : 0);
@@ -1239,9 +1348,16 @@ static bool upload_joint_table(dxWorld *w) {
         l0[k] = make_float4(L.lostop, L.histop, L.vel, L.fmax);
         l1[k] = make_float4(L.fudge_factor, L.bounce, L.normal_cfm, L.stop_erp);
         l2[k] = make_float4(L.stop_cfm, j->erp, j->cfm, 0.f);
+        hv1[k] = make_float4(j->v1[0], j->v1[1], j->v1[2], j->s0);
+        hv2[k] = make_float4(j->v2[0], j->v2[1], j->v2[2], j->c0);
+        const Limot &M = j->limot2;
+        m0[k] = make_float4(M.lostop, M.histop, M.vel, M.fmax);
+        m1[k] = make_float4(M.fudge_factor, M.bounce, M.normal_cfm, M.stop_erp);
+        m2[k] = make_float4(M.stop_cfm, j->susp_erp, j->susp_cfm, 0.f);
     }
     std::vector<const void *> src = {info.data(), a1.data(), a2.data(), x1.data(), x2.data(), qr.data(),
-                                     l0.data(), l1.data(), l2.data()};
+                                     l0.data(), l1.data(), l2.data(), hv1.data(), hv2.data(), m0.data(),
+                                     m1.data(), m2.data()};
     if (!joint_table_upload(w->ws, n, src, w->stream)) return false;
     w->joints_dirty = false;
     return true;

@@ -92,6 +92,7 @@ struct Workspace {
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state
     DBuf j_info, j_a1, j_a2, j_x1, j_x2, j_qrel, j_l0, j_l1, j_l2, j_m, j_rstart, j_limit, j_lerr, j_lam;
+    DBuf j_v1, j_v2, j_m0, j_m1, j_m2;  // hinge2: angle vectors (+ s0, c0), axis-2 motor, suspension
     DBuf grp_body;  // body pair of every constraint group (contact manifolds, then joints)
     DBuf j_pairs;   // set of jointed body pairs (fused narrow phase skips them)
     unsigned j_pair_mask = 0;
@@ -159,7 +160,8 @@ bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, cons
 double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s);
 int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s);
 int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
-// ball/hinge joint table: src = info, anchor1, anchor2, axis1, axis2, qrel, limot 0-2 (n each)
+// ball/hinge/hinge2 joint table: src = info, anchor1, anchor2, axis1, axis2, qrel, limot 0-2,
+// hinge2 v1(+s0), v2(+c0), second limot 0-2 (n each)
 bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s);
 // per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
 void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);

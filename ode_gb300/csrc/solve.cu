@@ -442,6 +442,8 @@ struct JointTable {
     const float4 *l0;  // lostop histop vel fmax
     const float4 *l1;  // fudge bounce normal_cfm stop_erp
     const float4 *l2;  // stop_cfm, ball erp, ball cfm
+    const float4 *v1, *v2;          // hinge2: angle vectors in body 1's frame; w = s0 / c0
+    const float4 *m0, *m1, *m2;     // hinge2: axis-2 limot (as l0..l2), m2.y/z = suspension ERP/CFM
     int n;
     int *m, *rstart, *limit;
     float *lerr, *lam;  // limit error; [n][6] multipliers of the last step (warm start)
@@ -531,10 +533,134 @@ __global__ void k_joint_m(JointTable T, Bodies B) {
                 atomicAdd(&B.tacc[in.y].x, -t0); atomicAdd(&B.tacc[in.y].y, -t1); atomicAdd(&B.tacc[in.y].z, -t2);
             }
         }
+        if (in.x == 6 && in.z >= 0) {  // dJointTypeHinge2 (hinge2.cpp:104-125)
+            const float4 l0 = T.l0[k];
+            const float lostop = l0.x, histop = l0.y, vel = l0.z, fmax = l0.w;
+            m = 4;
+            if ((lostop >= -3.14159265358979323846f || histop <= 3.14159265358979323846f) && lostop <= histop) {
+                // measureAngle1 (hinge2.cpp:33-51)
+                float R0[12], R1[12], p[3], q[3];
+                load_rows3(B.R + 3 * in.y, R0);
+                load_rows3(B.R + 3 * in.z, R1);
+                const float4 x2 = T.x2[k], v1 = T.v1[k], v2 = T.v2[k];
+                const float a2[3] = {x2.x, x2.y, x2.z};
+                mul0_331(p, R1, a2);
+                q[0] = R0[0] * p[0] + R0[4] * p[1] + R0[8] * p[2];  // dMultiply1_331
+                q[1] = R0[1] * p[0] + R0[5] * p[1] + R0[9] * p[2];
+                q[2] = R0[2] * p[0] + R0[6] * p[1] + R0[10] * p[2];
+                const float x = v1.x * q[0] + v1.y * q[1] + v1.z * q[2];
+                const float y = v2.x * q[0] + v2.y * q[1] + v2.z * q[2];
+                const float angle = -atan2f(y, x);
+                if (angle <= lostop) { limit = 1; lerr = angle - lostop; }
+                else if (angle >= histop) { limit = 2; lerr = angle - histop; }
+            }
+            if (limit || fmax > 0) m++;
+            if (T.m0[k].w > 0) m++;  // axis 2 is powered (never limited)
+            if (limit && fmax > 0 && lostop != histop) {
+                float fm = fmax;
+                if (vel > 0 || (vel == 0 && limit == 2)) fm = -fm;
+                if ((limit == 1 && vel > 0) || (limit == 2 && vel < 0)) fm *= T.l1[k].x;
+                float R0[12], a1[3], ax1[3];
+                load_rows3(B.R + 3 * in.y, R0);
+                const float4 x1 = T.x1[k];
+                a1[0] = x1.x; a1[1] = x1.y; a1[2] = x1.z;
+                mul0_331(ax1, R0, a1);
+                const float t0 = fm * ax1[0], t1 = fm * ax1[1], t2 = fm * ax1[2];
+                atomicAdd(&B.tacc[in.z].x, t0); atomicAdd(&B.tacc[in.z].y, t1); atomicAdd(&B.tacc[in.z].z, t2);
+                atomicAdd(&B.tacc[in.y].x, -t0); atomicAdd(&B.tacc[in.y].y, -t1); atomicAdd(&B.tacc[in.y].z, -t2);
+            }
+        }
         T.m[k] = m;
         T.limit[k] = limit;
         T.lerr[k] = lerr;
     }
+}
+
+// joint.cpp:596-790 addLimot, rotational, into one row r (J layout as k_rows)
+__device__ void limot_row(float *r, const float *ax1, int n0, int n1, const Bodies &B, float fps, int limit,
+                          float lerr, float4 l0, float4 l1, float stop_cfm) {
+    const float lostop = l0.x, histop = l0.y, vel = l0.z, fmax = l0.w;
+    const float bounce = l1.y, normal_cfm = l1.z, stop_erp = l1.w;
+    r[3] = ax1[0]; r[4] = ax1[1]; r[5] = ax1[2];
+    if (n1 >= 0) { r[11] = -ax1[0]; r[12] = -ax1[1]; r[13] = -ax1[2]; }
+    int powered = fmax > 0;
+    if (limit && lostop == histop) powered = 0;
+    if (powered) {
+        r[7] = normal_cfm;
+        if (!limit) { r[6] = vel; r[14] = -fmax; r[15] = fmax; }
+    }
+    if (limit) {
+        const float ks = fps * stop_erp;
+        r[6] = -ks * lerr;
+        r[7] = stop_cfm;
+        if (lostop == histop) {
+            r[14] = -INFINITY; r[15] = INFINITY;
+        } else {
+            if (limit == 1) { r[14] = 0; r[15] = INFINITY; }
+            else { r[14] = -INFINITY; r[15] = 0; }
+            if (bounce > 0) {
+                const float4 w0 = B.avel[n0];
+                float v = w0.x * ax1[0] + w0.y * ax1[1] + w0.z * ax1[2];
+                if (n1 >= 0) { const float4 w1 = B.avel[n1]; v -= w1.x * ax1[0] + w1.y * ax1[1] + w1.z * ax1[2]; }
+                if (limit == 1) { if (v < 0) { const float nc = -bounce * v; if (nc > r[6]) r[6] = nc; } }
+                else { if (v > 0) { const float nc = -bounce * v; if (nc < r[6]) r[6] = nc; } }
+            }
+        }
+    }
+}
+
+// odemath.cpp:95-151 dxSafeNormalize3
+__device__ bool safe_normalize3(float *a) {
+    const float a0 = fabsf(a[0]), a1 = fabsf(a[1]), a2 = fabsf(a[2]);
+    int idx;
+    if (a1 > a0) idx = a2 > a1 ? 2 : 1;
+    else if (a2 > a0) idx = 2;
+    else {
+        if (!(a0 > 0.0f)) return false;
+        idx = 0;
+    }
+    const int i1 = idx == 0 ? 1 : 0, i2 = idx == 2 ? 1 : 2;
+    const float r = 1.0f / fabsf(a[idx]);
+    const float b1 = a[i1] * r, b2 = a[i2] * r;
+    const float l = 1.0f / sqrtf(1.0f + b1 * b1 + b2 * b2);
+    a[i1] = b1 * l;
+    a[i2] = b2 * l;
+    a[idx] = copysignf(l, a[idx]);
+    return true;
+}
+
+// joint.cpp:165-226 setBall2 into rows 0-2 of J: the first row along `axis`
+__device__ void set_ball2(float (*J)[16], const Bodies &B, int n0, int n1, float fps, float erp, const float *anchor1,
+                          const float *anchor2, const float *axis, float erp1) {
+    float R0[12], a1[3], a2[3], q1[3], q2[3];
+    plane_space(axis, q1, q2);
+    const float *dirs[3] = {axis, q1, q2};
+    load_rows3(B.R + 3 * n0, R0);
+    mul0_331(a1, R0, anchor1);
+    for (int r = 0; r < 3; r++) {
+        for (int i = 0; i < 3; i++) J[r][i] = dirs[r][i];
+        cross3(&J[r][3], a1, dirs[r]);
+    }
+    const float4 p0 = B.pos[n0];
+    a1[0] += p0.x; a1[1] += p0.y; a1[2] += p0.z;
+    const float k1 = fps * erp1, k = fps * erp;
+    float d[3];
+    if (n1 >= 0) {
+        float R1[12];
+        load_rows3(B.R + 3 * n1, R1);
+        for (int r = 0; r < 3; r++)
+            for (int i = 0; i < 3; i++) J[r][8 + i] = -dirs[r][i];
+        mul0_331(a2, R1, anchor2);
+        for (int r = 0; r < 3; r++) cross3(&J[r][11], dirs[r], a2);
+        const float4 p1 = B.pos[n1];
+        a2[0] += p1.x; a2[1] += p1.y; a2[2] += p1.z;
+        d[0] = a2[0] - a1[0]; d[1] = a2[1] - a1[1]; d[2] = a2[2] - a1[2];
+    } else {
+        d[0] = anchor2[0] - a1[0]; d[1] = anchor2[1] - a1[1]; d[2] = anchor2[2] - a1[2];
+    }
+    J[0][6] = k1 * dot3(axis, d);
+    J[1][6] = k * dot3(q1, d);
+    J[2][6] = k * dot3(q2, d);
 }
 
 __global__ void k_joint_rows_total(DevCounters *dc, int row_cap) {
@@ -600,6 +726,30 @@ __global__ void k_joint_rows(JointTable T, Bodies B, Rows Rw, SolverParams P, in
             const float4 l2 = T.l2[k];
             J[0][7] = l2.z; J[1][7] = l2.z; J[2][7] = l2.z;
             set_ball(J, B, n0, n1, fps, l2.y, anchor1, anchor2);
+        } else if (in.x == 6) {  // hinge2 (hinge2.cpp:147-207)
+            float R0[12], R1[12], ax1[3], ax2[3], q[3];
+            load_rows3(B.R + 3 * n0, R0);
+            load_rows3(B.R + 3 * n1, R1);
+            const float4 x1 = T.x1[k], x2 = T.x2[k], v1 = T.v1[k], v2 = T.v2[k], m2 = T.m2[k];
+            const float axis1[3] = {x1.x, x1.y, x1.z}, axis2[3] = {x2.x, x2.y, x2.z};
+            mul0_331(ax1, R0, axis1);
+            mul0_331(ax2, R1, axis2);
+            cross3(q, ax1, ax2);
+            const float sa = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+            const float ca = dot3(ax1, ax2);
+            safe_normalize3(q);
+            set_ball2(J, B, n0, n1, fps, P.erp, anchor1, anchor2, ax1, m2.y);
+            J[0][7] = m2.z;  // suspension CFM
+            for (int i = 0; i < 3; i++) { J[3][3 + i] = q[i]; J[3][11 + i] = -q[i]; }
+            J[3][6] = fps * P.erp * (v2.w * sa - v1.w * ca);  // k * (c0 * s - s0 * c)
+            int row = 4;
+            const float4 l0 = T.l0[k];
+            const int limit = T.limit[k];
+            if (limit || l0.w > 0) {
+                limot_row(J[row], ax1, n0, n1, B, fps, limit, T.lerr[k], l0, T.l1[k], T.l2[k].x);
+                ++row;
+            }
+            if (T.m0[k].w > 0) limot_row(J[row], ax2, n0, n1, B, fps, 0, 0.f, T.m0[k], T.m1[k], m2.x);
         } else {  // hinge
             set_ball(J, B, n0, n1, fps, P.erp, anchor1, anchor2);
             float R0[12], ax1[3], p[3], q[3], b[3];
@@ -621,40 +771,8 @@ __global__ void k_joint_rows(JointTable T, Bodies B, Rows Rw, SolverParams P, in
             const float kk = fps * P.erp;
             J[3][6] = kk * dot3(b, p);
             J[4][6] = kk * dot3(b, q);
-            if (m == 6) {  // addLimot, rotational
-                const float4 l0 = T.l0[k], l1 = T.l1[k], l2 = T.l2[k];
-                const float lostop = l0.x, histop = l0.y, vel = l0.z, fmax = l0.w;
-                const float fudge = l1.x, bounce = l1.y, normal_cfm = l1.z, stop_erp = l1.w, stop_cfm = l2.x;
-                const int limit = T.limit[k];
-                float *r = J[5];
-                r[3] = ax1[0]; r[4] = ax1[1]; r[5] = ax1[2];
-                if (n1 >= 0) { r[11] = -ax1[0]; r[12] = -ax1[1]; r[13] = -ax1[2]; }
-                int powered = fmax > 0;
-                if (limit && lostop == histop) powered = 0;
-                (void)fudge;
-                if (powered) {
-                    r[7] = normal_cfm;
-                    if (!limit) { r[6] = vel; r[14] = -fmax; r[15] = fmax; }
-                }
-                if (limit) {
-                    const float ks = fps * stop_erp;
-                    r[6] = -ks * T.lerr[k];
-                    r[7] = stop_cfm;
-                    if (lostop == histop) {
-                        r[14] = -INFINITY; r[15] = INFINITY;
-                    } else {
-                        if (limit == 1) { r[14] = 0; r[15] = INFINITY; }
-                        else { r[14] = -INFINITY; r[15] = 0; }
-                        if (bounce > 0) {
-                            const float4 w0 = B.avel[n0];
-                            float v = w0.x * ax1[0] + w0.y * ax1[1] + w0.z * ax1[2];
-                            if (n1 >= 0) { const float4 w1 = B.avel[n1]; v -= w1.x * ax1[0] + w1.y * ax1[1] + w1.z * ax1[2]; }
-                            if (limit == 1) { if (v < 0) { const float nc = -bounce * v; if (nc > r[6]) r[6] = nc; } }
-                            else { if (v > 0) { const float nc = -bounce * v; if (nc < r[6]) r[6] = nc; } }
-                        }
-                    }
-                }
-            }
+            if (m == 6)  // addLimot, rotational
+                limot_row(J[5], ax1, n0, n1, B, fps, T.limit[k], T.lerr[k], T.l0[k], T.l1[k], T.l2[k].x);
         }
         float lam0[6] = {0, 0, 0, 0, 0, 0};
         if (warm)
@@ -1777,6 +1895,8 @@ static JointTable joint_view(Workspace &ws) {
     T.a1 = ws.j_a1.as<float4>(); T.a2 = ws.j_a2.as<float4>();
     T.x1 = ws.j_x1.as<float4>(); T.x2 = ws.j_x2.as<float4>(); T.qrel = ws.j_qrel.as<float4>();
     T.l0 = ws.j_l0.as<float4>(); T.l1 = ws.j_l1.as<float4>(); T.l2 = ws.j_l2.as<float4>();
+    T.v1 = ws.j_v1.as<float4>(); T.v2 = ws.j_v2.as<float4>();
+    T.m0 = ws.j_m0.as<float4>(); T.m1 = ws.j_m1.as<float4>(); T.m2 = ws.j_m2.as<float4>();
     T.n = ws.njoints;
     T.m = ws.j_m.as<int>(); T.rstart = ws.j_rstart.as<int>(); T.limit = ws.j_limit.as<int>();
     T.lerr = ws.j_lerr.as<float>(); T.lam = ws.j_lam.as<float>();
@@ -1785,15 +1905,16 @@ static JointTable joint_view(Workspace &ws) {
 
 bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s) {
     const size_t nn = n > 0 ? n : 1;
-    DBuf *f4[8] = {&ws.j_a1, &ws.j_a2, &ws.j_x1, &ws.j_x2, &ws.j_qrel, &ws.j_l0, &ws.j_l1, &ws.j_l2};
+    DBuf *f4[13] = {&ws.j_a1, &ws.j_a2, &ws.j_x1, &ws.j_x2, &ws.j_qrel, &ws.j_l0, &ws.j_l1, &ws.j_l2,
+                    &ws.j_v1, &ws.j_v2, &ws.j_m0, &ws.j_m1, &ws.j_m2};
     bool ok = ws.j_info.ensure(nn * 16) && ws.j_m.ensure((nn + 1) * 4) && ws.j_rstart.ensure((nn + 1) * 4) &&
               ws.j_limit.ensure(nn * 4) && ws.j_lerr.ensure(nn * 4) && ws.j_lam.ensure(nn * 24);
     for (DBuf *b : f4) ok = ok && b->ensure(nn * 16);
-    if (!ok || src.size() != 9) return false;
+    if (!ok || src.size() != 14) return false;
     ws.njoints = n;
     if (n == 0) return true;
     cudaMemcpyAsync(ws.j_info.p, src[0], (size_t)n * 16, cudaMemcpyHostToDevice, s);
-    for (int i = 0; i < 8; i++) cudaMemcpyAsync(f4[i]->p, src[1 + i], (size_t)n * 16, cudaMemcpyHostToDevice, s);
+    for (int i = 0; i < 13; i++) cudaMemcpyAsync(f4[i]->p, src[1 + i], (size_t)n * 16, cudaMemcpyHostToDevice, s);
     cudaMemsetAsync(ws.j_lam.p, 0, (size_t)n * 24, s);  // a new table starts its joints from zero
     // the set of jointed body pairs, open addressing with the narrow phase's hash
     unsigned sz = 64;

@@ -146,6 +146,14 @@ _PROTOS = [
     ("dJointGetBallAnchor", None, [ID, _F]), ("dJointGetBallParam", dReal, [ID, ctypes.c_int]),
     ("dJointGetHingeAnchor", None, [ID, _F]), ("dJointGetHingeAxis", None, [ID, _F]),
     ("dJointGetHingeParam", dReal, [ID, ctypes.c_int]), ("dJointGetHingeAngle", dReal, [ID]),
+    ("dJointCreateHinge2", ID, [ID, ID]),
+    ("dJointSetHinge2Anchor", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHinge2Axes", None, [ID, _F, _F]),
+    ("dJointSetHinge2Axis1", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHinge2Axis2", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHinge2Param", None, [ID, ctypes.c_int, dReal]),
+    ("dJointGetHinge2Anchor", None, [ID, _F]), ("dJointGetHinge2Param", dReal, [ID, ctypes.c_int]),
+    ("dJointGetHinge2Angle1", dReal, [ID]),
     ("gbodeWorldStepFused", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int]),
     ("gbodeMlpParamCount", ctypes.c_int, []),
     ("gbodeMlpLossGrad", ctypes.c_int, [_F, _F, _F, ctypes.c_int, _F, _F]),
@@ -164,8 +172,10 @@ _PROTOS = [
 GBODE_NOALLOC_MAX_PAIRS = 8192  # gbodeCollidePairsNoAlloc's largest batch
 GBODE_MLP_NPARAMS = 35099       # learned warm start parameters
 
-dJointTypeBall, dJointTypeHinge, dJointTypeContact = 1, 2, 4
+dJointTypeBall, dJointTypeHinge, dJointTypeContact, dJointTypeHinge2 = 1, 2, 4, 6
 dParamLoStop, dParamHiStop, dParamVel, dParamFMax, dParamCFM, dParamERP = 0, 1, 2, 5, 8, 13
+dParamSuspensionERP, dParamSuspensionCFM = 11, 12
+dParamVel2, dParamFMax2 = 0x102, 0x105
 
 GBODE_SOLVER_COLOURED = 0
 GBODE_SOLVER_REFERENCE_ORDER = 1

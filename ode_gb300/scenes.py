@@ -34,6 +34,7 @@ import math
 import numpy as np
 
 SPHERE, BOX, CAPSULE, PLANE = 0, 1, 2, 4
+JOINT_COLS = 20
 
 # dSurfaceParameters.mode bits (include/ode/contact.h:28-52)
 dContactMu2 = 0x001
@@ -80,9 +81,11 @@ class Scene:
     surface_mode: int = dContactApprox1
     maxc: int = 4
     hash_levels: tuple = (-3, 10)
-    # ball/hinge joints, float32 [nj, 12]: type (1 ball, 2 hinge), body1,
-    # body2 (-1: the static environment), anchor xyz, axis xyz (world frame,
-    # hinge only), lo stop, hi stop (hinge only), 0
+    # joints, float32 [nj, JOINT_COLS]: type (1 ball, 2 hinge, 6 hinge2),
+    # body1, body2 (-1: the static environment), anchor xyz, axis (hinge) or
+    # axis 1 (hinge2) xyz, lo stop, hi stop (axis 1), axis 2 xyz (hinge2),
+    # axis-2 motor velocity and max force, suspension ERP and CFM (hinge2),
+    # axis-1 motor velocity and max force -- all in the world frame
     joints: np.ndarray | None = None
 
     @property
@@ -346,13 +349,13 @@ def chains(n_chains: int = 8192, seed: int = 3, nmin: int = 2, nmax: int = 32, s
             if k == 0:
                 if hang:
                     a = base + ends[0]
-                    joints.append((1, nb, -1, *a, 0, 0, 0, 0, 0, 0))
+                    joints.append((1, nb, -1, *a) + (0,) * 14)
             else:
                 a = base + ends[k]
                 if k % 2 == 1:
-                    joints.append((2, nb - 1, nb, *a, *ey, -math.pi / 3, math.pi / 3, 0))
+                    joints.append((2, nb - 1, nb, *a, *ey, -math.pi / 3, math.pi / 3) + (0,) * 9)
                 else:
-                    joints.append((1, nb - 1, nb, *a, 0, 0, 0, 0, 0, 0))
+                    joints.append((1, nb - 1, nb, *a) + (0,) * 14)
             nb += 1
     pos = np.asarray(pos_l, np.float32)
     q = np.asarray(q_l, np.float32)
@@ -371,4 +374,75 @@ def chains(n_chains: int = 8192, seed: int = 3, nmin: int = 2, nmax: int = 32, s
     gR[:, [0, 5, 10]] = 1.0
     return Scene(f"chains{n_chains}" + ("_hanging" if hang else ""), bodies, cls, gbody,
                  np.zeros((ng, 3), np.float32), gR, gdims, dt=1.0 / 240.0, iterations=20, mu=0.6, maxc=4,
-                 joints=np.asarray(joints, np.float32).reshape(-1, 12))
+                 joints=np.asarray(joints, np.float32).reshape(-1, JOINT_COLS))
+
+
+def vehicles(n_worlds: int = 65536, seed: int = 4, spacing: float = 12.0, hang: bool = False,
+             obstacles: bool = True) -> Scene:
+    """Four-wheeled vehicles, one per independent world: a box chassis
+    2 x 1 x 0.5 m of 800 kg and four sphere wheels (r 0.3 m, 20 kg) on hinge2
+    joints (axis 1 vertical, steering locked with lo = hi stop = 0; axis 2 the
+    axle, motored at a seeded velocity U[-20, 20] rad/s with 200 N m), with
+    suspension ERP 0.4 / CFM 1e-3, K ~ U{0..16} static box obstacles (sides
+    U[0.2, 1] m) around each vehicle, on the plane z = 0; dt 1/120.  The
+    worlds sit on a square grid `spacing` m apart.  With `hang` the chassis
+    hangs from the environment by a ball joint at its centre top, no geoms
+    (a joints-only scene)."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(math.sqrt(n_worlds)))
+    pos_l, q_l, mass_l, I_l, cls_l, dims_l, body_l, gpos_l = [], [], [], [], [], [], [], []
+    joints = []
+    nb = 0
+    cm, ci1, ci2, ci3 = mass_box(1.0, 2.0, 1.0, 0.5)
+    cm_scale = np.float32(800.0) / cm
+    wm, wi, _, _ = mass_sphere(1.0, 0.3)
+    wm_scale = np.float32(20.0) / wm
+    for c in range(n_worlds):
+        base = np.array([(c % side + 0.5) * spacing, (c // side + 0.5) * spacing, 0.0])
+        yaw = rng.uniform(0, 2 * math.pi)
+        fwd = np.array([math.cos(yaw), math.sin(yaw), 0.0])
+        left = np.array([-math.sin(yaw), math.cos(yaw), 0.0])
+        zc = (3.0 if hang else 0.6)
+        chassis = base + np.array([0, 0, zc])
+        q = np.array([math.cos(yaw / 2), 0, 0, math.sin(yaw / 2)])
+        pos_l.append(chassis); q_l.append(q); mass_l.append(cm * cm_scale)
+        I_l.append((ci1 * cm_scale, ci2 * cm_scale, ci3 * cm_scale))
+        cls_l.append(BOX); dims_l.append((2.0, 1.0, 0.5, 0)); body_l.append(nb); gpos_l.append((0, 0, 0))
+        cb = nb
+        nb += 1
+        if hang:
+            joints.append((1, cb, -1, *(chassis + np.array([0, 0, 0.25]))) + (0,) * 14)
+        vel = rng.uniform(-20, 20)
+        for sx in (-0.8, 0.8):
+            for sy in (-0.7, 0.7):
+                wp = chassis + sx * fwd + sy * left + np.array([0, 0, -0.3])
+                pos_l.append(wp); q_l.append((1, 0, 0, 0)); mass_l.append(wm * wm_scale)
+                I_l.append((wi * wm_scale,) * 3)
+                cls_l.append(SPHERE); dims_l.append((0.3, 0, 0, 0)); body_l.append(nb); gpos_l.append((0, 0, 0))
+                joints.append((6, cb, nb, *wp, 0, 0, 1, 0, 0, *left, vel, 200.0, 0.4, 1e-3, 0, 0))
+                nb += 1
+        if obstacles and not hang:
+            for _ in range(int(rng.integers(0, 17))):
+                sdim = rng.uniform(0.2, 1.0, size=3)
+                r = rng.uniform(3.0, spacing / 2 - 0.8)
+                a = rng.uniform(0, 2 * math.pi)
+                p = base + np.array([r * math.cos(a), r * math.sin(a), sdim[2] / 2])
+                cls_l.append(BOX); dims_l.append((*sdim, 0)); body_l.append(-1); gpos_l.append(p)
+    pos = np.asarray(pos_l, np.float32)
+    q = np.asarray(q_l, np.float32)
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    bodies = _body_rows(pos, q, np.asarray(mass_l, np.float32), np.asarray(I_l, np.float32))
+    if hang:
+        cls = np.zeros(0, np.int32); gbody = np.zeros(0, np.int32)
+        gdims = np.zeros((0, 4), np.float32); gpos = np.zeros((0, 3), np.float32)
+    else:
+        cls = np.asarray(cls_l + [PLANE], np.int32)
+        gbody = np.asarray(body_l + [-1], np.int32)
+        gdims = np.asarray(dims_l + [(0, 0, 1, 0)], np.float32)
+        gpos = np.asarray(gpos_l + [(0, 0, 0)], np.float32)
+    ng = len(cls)
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene(f"vehicles{n_worlds}" + ("_hanging" if hang else ""), bodies, cls, gbody, gpos, gR, gdims,
+                 dt=1.0 / 120.0, iterations=20, mu=0.8, maxc=4,
+                 joints=np.asarray(joints, np.float32).reshape(-1, JOINT_COLS))

@@ -18,6 +18,42 @@ from . import ode
 from .scenes import BOX, CAPSULE, PLANE, SPHERE, Scene
 
 
+def make_joint(L, w, bodies, row):
+    """Create and attach one joint from a scene joint row (scenes.Scene.joints)
+    with the same call sequence an ODE program would use."""
+    row = [float(x) for x in row] + [0.0] * (20 - len(row))
+    t, b1, b2 = int(row[0]), int(row[1]), int(row[2])
+    if t == 1:
+        j = L.dJointCreateBall(w, None)
+    elif t == 2:
+        j = L.dJointCreateHinge(w, None)
+    else:
+        j = L.dJointCreateHinge2(w, None)
+    L.dJointAttach(j, bodies[b1], bodies[b2] if b2 >= 0 else None)
+    if t == 1:
+        L.dJointSetBallAnchor(j, *row[3:6])
+    elif t == 2:
+        L.dJointSetHingeAnchor(j, *row[3:6])
+        L.dJointSetHingeAxis(j, *row[6:9])
+        L.dJointSetHingeParam(j, ode.dParamLoStop, row[9])
+        L.dJointSetHingeParam(j, ode.dParamHiStop, row[10])
+        if row[19] > 0:
+            L.dJointSetHingeParam(j, ode.dParamVel, row[18])
+            L.dJointSetHingeParam(j, ode.dParamFMax, row[19])
+    else:
+        L.dJointSetHinge2Anchor(j, *row[3:6])
+        a1 = np.array(row[6:9] + [0.0], np.float32)
+        a2 = np.array(row[11:14] + [0.0], np.float32)
+        L.dJointSetHinge2Axes(j, ode.fptr(a1), ode.fptr(a2))
+        L.dJointSetHinge2Param(j, ode.dParamLoStop, row[9])
+        L.dJointSetHinge2Param(j, ode.dParamHiStop, row[10])
+        L.dJointSetHinge2Param(j, ode.dParamVel2, row[14])
+        L.dJointSetHinge2Param(j, ode.dParamFMax2, row[15])
+        L.dJointSetHinge2Param(j, ode.dParamSuspensionERP, row[16])
+        L.dJointSetHinge2Param(j, ode.dParamSuspensionCFM, row[17])
+    return j
+
+
 class GBWorld:
     def __init__(self, scene: Scene, solver: int = ode.GBODE_SOLVER_COLOURED, dyn: bool = False,
                  iterations: int | None = None, stream=None):
@@ -78,17 +114,7 @@ class GBWorld:
         self.joints = []
         if scene.joints is not None:
             for row in scene.joints:
-                t, b1, b2 = int(row[0]), int(row[1]), int(row[2])
-                j = L.dJointCreateBall(self.w, None) if t == 1 else L.dJointCreateHinge(self.w, None)
-                L.dJointAttach(j, self.bodies[b1], self.bodies[b2] if b2 >= 0 else None)
-                if t == 1:
-                    L.dJointSetBallAnchor(j, *[float(x) for x in row[3:6]])
-                else:
-                    L.dJointSetHingeAnchor(j, *[float(x) for x in row[3:6]])
-                    L.dJointSetHingeAxis(j, *[float(x) for x in row[6:9]])
-                    L.dJointSetHingeParam(j, ode.dParamLoStop, float(row[9]))
-                    L.dJointSetHingeParam(j, ode.dParamHiStop, float(row[10]))
-                self.joints.append(j)
+                self.joints.append(make_joint(L, self.w, self.bodies, row))
         self.group = L.dJointGroupCreate(0)
         self.surface = ode.dSurfaceParameters()
         self.surface.mode = scene.surface_mode

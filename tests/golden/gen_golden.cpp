@@ -315,28 +315,44 @@ static void mode_chain() {
     int nb = rdi(), nj = rdi(), nsteps = rdi(), iters = rdi(), dyn = rdi();
     WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
     std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
-    std::vector<float> jt(12 * nj); rd(jt.data(), jt.size());
+    const int JC = 20;
+    std::vector<float> jt(JC * nj); rd(jt.data(), jt.size());
     dWorldID w = dWorldCreate();
     apply_params(w, P, iters, dyn);
     std::vector<dBodyID> b(nb);
     for (int i = 0; i < nb; i++) { b[i] = dBodyCreate(w); set_body(b[i], &bodies[BODY_IN * i]); }
     std::vector<dJointID> hinges;
+    std::vector<dJointID> hinge2s;
     for (int k = 0; k < nj; k++) {
-        const float *r = &jt[12 * k];
+        const float *r = &jt[JC * k];
         const int t = (int)r[0], b1 = (int)r[1], b2 = (int)r[2];
-        dJointID j = t == 1 ? dJointCreateBall(w, 0) : dJointCreateHinge(w, 0);
+        dJointID j = t == 1 ? dJointCreateBall(w, 0) : (t == 2 ? dJointCreateHinge(w, 0) : dJointCreateHinge2(w, 0));
         dJointAttach(j, b[b1], b2 >= 0 ? b[b2] : 0);
         if (t == 1) {
             dJointSetBallAnchor(j, r[3], r[4], r[5]);
-        } else {
+        } else if (t == 2) {
             dJointSetHingeAnchor(j, r[3], r[4], r[5]);
             dJointSetHingeAxis(j, r[6], r[7], r[8]);
             dJointSetHingeParam(j, dParamLoStop, r[9]);
             dJointSetHingeParam(j, dParamHiStop, r[10]);
+            if (r[19] > 0) { dJointSetHingeParam(j, dParamVel, r[18]); dJointSetHingeParam(j, dParamFMax, r[19]); }
             hinges.push_back(j);
+        } else {
+            dJointSetHinge2Anchor(j, r[3], r[4], r[5]);
+            const dReal a1[4] = {r[6], r[7], r[8], 0}, a2[4] = {r[11], r[12], r[13], 0};
+            dJointSetHinge2Axes(j, a1, a2);
+            dJointSetHinge2Param(j, dParamLoStop, r[9]);
+            dJointSetHinge2Param(j, dParamHiStop, r[10]);
+            dJointSetHinge2Param(j, dParamVel2, r[14]);
+            dJointSetHinge2Param(j, dParamFMax2, r[15]);
+            dJointSetHinge2Param(j, dParamSuspensionERP, r[16]);
+            dJointSetHinge2Param(j, dParamSuspensionCFM, r[17]);
+            hinge2s.push_back(j);
         }
     }
-    const int nh = (int)hinges.size();
+    // angles: the hinges' dJointGetHingeAngle, then the hinge2s' dJointGetHinge2Angle1
+    for (dJointID j : hinge2s) hinges.push_back(j);
+    const int nh = (int)hinges.size(), nh1 = nh - (int)hinge2s.size();
     std::vector<float> traj((size_t)nsteps * nb * 7), ang((size_t)nsteps * nh);
     for (int s = 0; s < nsteps; s++) {
         dWorldQuickStep(w, P.dt);
@@ -346,7 +362,9 @@ static void mode_chain() {
             for (int j = 0; j < 3; j++) o[j] = (float)p[j];
             for (int j = 0; j < 4; j++) o[3 + j] = (float)q[j];
         }
-        for (int h = 0; h < nh; h++) ang[(size_t)s * nh + h] = (float)dJointGetHingeAngle(hinges[h]);
+        for (int h = 0; h < nh; h++)
+            ang[(size_t)s * nh + h] =
+                (float)(h < nh1 ? dJointGetHingeAngle(hinges[h]) : dJointGetHinge2Angle1(hinges[h]));
     }
     wr(traj.data(), traj.size());
     wr(ang.data(), ang.size());

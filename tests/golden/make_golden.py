@@ -353,6 +353,27 @@ def gen_space_pile(exes):
           f"reference misses, {len(ref_bodies - exact)} extra")
 
 
+def gen_joint_scene(exes, sc, name, iters=200, nsteps=240):
+    jt = np.ascontiguousarray(sc.joints, np.float32)
+    buf = run(exes["single_noreorder"], "chain",
+              [np.array([sc.nb, len(jt), nsteps, iters, 0], np.int32), sc.world_params(),
+               sc.bodies.astype(np.float32), jt])
+    r = Reader(buf)
+    traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
+    nh = int(((jt[:, 0] == 2) | (jt[:, 0] == 6)).sum())
+    ang = r.take(np.float32, nsteps * nh).reshape(nsteps, nh)
+    np.savez_compressed(os.path.join(HERE, name), bodies=sc.bodies, joints=jt, params=sc.world_params(),
+                        ints=np.array([iters, nsteps], np.int32), traj=traj, angles=ang)
+    print(f"{name}: {sc.nb} bodies, {len(jt)} joints ({nh} with angles), {nsteps} steps")
+
+
+def gen_hinge2(exes):
+    """Vehicles hanging from the environment by a ball joint at the chassis,
+    wheels on hinge2 joints (suspension, locked steering, motored axles), no
+    geoms: 240 steps of the no-reorder build with 200 iterations."""
+    gen_joint_scene(exes, scenes.vehicles(4, seed=21, hang=True), "hinge2.npz")
+
+
 def gen_chain(exes):
     """Hanging chains of capsules linked by hinge (limited +-60 deg) and ball
     joints, no geoms: 240 steps of the no-reorder build with 200 iterations
@@ -388,6 +409,8 @@ def main():
         gen_space_pile(exes)
     if a.only in ("", "chain"):
         gen_chain(exes)
+    if a.only in ("", "hinge2"):
+        gen_hinge2(exes)
 
 
 if __name__ == "__main__":

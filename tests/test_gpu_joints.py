@@ -134,3 +134,56 @@ def test_graph_replay_matches_plain_steps(gblib):
     assert worlds[1].stats().iterations > 0
     for w in worlds:
         w.close()
+
+
+def test_hanging_vehicles_hinge2_follow_reference(gblib, golden):
+    """Hinge2 joints (suspension ERP/CFM, steering locked by lo = hi stop,
+    motored axles) on vehicles hung from the environment: the GPU follows
+    the reference's converged trajectory (tests/golden/hinge2.npz), and
+    dJointGetHinge2Angle1 matches."""
+    from ode_gb300 import ode, sim
+    L = gblib
+    g = golden("hinge2.npz")
+    sc = _chain_scene(g)
+    w = sim.GBWorld(sc)
+    L.dWorldSetQuickStepW(w.w, 1.0)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    L.gbodeWorldSetResidualTarget(w.w, 1e-7, 5, 3000)
+    h2 = [j for j, row in zip(w.joints, sc.joints) if int(row[0]) == 6]
+    assert all(L.dJointGetType(j) == ode.dJointTypeHinge2 for j in h2)
+    worst_p, worst_a = 0.0, 0.0
+    for s in range(HORIZON):
+        assert w.step_fused() == 1
+        st = w.state()
+        worst_p = max(worst_p, float(np.abs(st[:, 0:3] - g["traj"][s, :, 0:3]).max()))
+        ang = np.array([L.dJointGetHinge2Angle1(j) for j in h2])
+        worst_a = max(worst_a, float(np.abs(ang - g["angles"][s]).max()))
+    print(f"hinge2 vehicles: {sc.nb} bodies; over {HORIZON} steps max position difference {worst_p:.2e} m, "
+          f"max steering angle difference {worst_a:.2e} rad")
+    assert worst_p <= POS_TOL
+    assert worst_a <= ANGLE_TOL
+    w.close()
+
+
+def test_vehicles_drive_among_obstacles(gblib):
+    """Vehicles with hinge2 wheels on the plane among static box obstacles
+    (fused path): finite, wheels on the ground, every step at the residual
+    target, the motored wheels spinning."""
+    from ode_gb300 import scenes, sim
+    L = gblib
+    sc = scenes.vehicles(64, seed=6)
+    w = sim.GBWorld(sc)
+    L.dWorldSetQuickStepW(w.w, 1.0)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    L.gbodeWorldSetResidualTarget(w.w, 1e-4, 5, 3000)
+    for _ in range(120):
+        w.step_fused()
+        assert w.stats().residual <= 1e-4
+    st = w.state()
+    assert np.isfinite(st).all()
+    wheels = np.arange(sc.nb) % 5 != 0
+    assert st[wheels, 2].min() > 0.2 and st[wheels, 2].max() < 0.45
+    assert np.abs(st[wheels, 22:25]).max() > 1.0  # angular velocity of the motored wheels
+    print(f"vehicles: {sc.nb} bodies, {w.stats().contacts} contacts, wheel z in "
+          f"[{st[wheels, 2].min():.3f}, {st[wheels, 2].max():.3f}]")
+    w.close()
