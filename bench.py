@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched capsule-chain leg")
     ap.add_argument("--chains", type=int, default=8192, help="batched leg: independent capsule chains")
+    ap.add_argument("--vehicles", type=int, default=65536, help="batched leg: independent vehicle worlds (0: skip)")
     ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
     ap.add_argument("--ref-sweeps", type=int, default=1500,
                     help="reference arm: SOR sweeps per step (cold starts need ~1000-1500 to reach the target)")
@@ -317,7 +318,12 @@ def run_gbode(args, ws, rank, local):
     # batched independent worlds: capsule chains with hinge/ball joints
     batched = None
     if not args.no_batched and ws == 1:
-        batched = batched_leg(args, L, stream, dev)
+        batched = {"chains": batched_leg(args, L, stream, dev, "chains")}
+        if args.vehicles > 0:
+            try:
+                batched["vehicles"] = batched_leg(args, L, stream, dev, "vehicles")
+            except RuntimeError as e:
+                batched["vehicles"] = {"unavailable": str(e)}
     # CPU baseline: the oracle port from the same settled state, same sweep count
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -354,25 +360,31 @@ def run_gbode(args, ws, rank, local):
     print(json.dumps(line))
 
 
-def batched_leg(args, L, stream, dev):
-    """Thousands of independent worlds as islands of one step: articulated
-    capsule chains (N log-uniform in [2, 32], hinge +-60 deg limits alternating
-    with ball joints) dropped onto a plane, dt 1/240.  All chains are stepped
-    by one fused step (one persistent PGS launch); timed like the pile."""
+def batched_leg(args, L, stream, dev, kind):
+    """Thousands of independent worlds as islands of one step, stepped by one
+    fused step (one persistent PGS launch) and timed like the pile:
+    chains -- articulated capsule chains (N log-uniform in [2, 32], hinge +-60
+    deg limits alternating with ball joints) dropped onto a plane, dt 1/240;
+    vehicles -- a box chassis on four hinge2-suspended, motored sphere wheels
+    among 0-16 static box obstacles per world, dt 1/120."""
     import torch
     from ode_gb300 import scenes, sim
     t0 = time.perf_counter()
-    sc = scenes.chains(args.chains, seed=3)
+    if kind == "chains":
+        sc, settle = scenes.chains(args.chains, seed=3), 240
+    else:
+        sc, settle = scenes.vehicles(args.vehicles, seed=4), 120
     w = sim.GBWorld(sc, stream=ctypes.c_void_p(stream.cuda_stream))
     L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
     L.dWorldSetQuickStepW(w.w, 1.0)
-    for _ in range(240):  # fall and land with the configured 20 iterations
-        w.step_fused()
+    for _ in range(settle):  # fall and land with the configured 20 iterations
+        if not w.step_fused():
+            raise RuntimeError(L.gbodeGetLastError().decode())
     w.sync()
     setup_s = time.perf_counter() - t0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    out = {"workload": f"chains{args.chains}", "bodies": sc.nb, "joints": int(len(sc.joints)), "dt": sc.dt,
-           "setup_s": round(setup_s, 1)}
+    out = {"workload": f"{kind}{args.chains if kind == 'chains' else args.vehicles}", "bodies": sc.nb,
+           "geoms": sc.ng, "joints": int(len(sc.joints)), "dt": sc.dt, "setup_s": round(setup_s, 1)}
     L.gbodeWorldSetTiming(w.w, 0)
     for label, target, graph in (("iterations20", 0.0, False), ("iterations20_graph", 0.0, True),
                                  ("residual", args.target, False), ("residual_graph", args.target, True)):

@@ -278,6 +278,25 @@ void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale);
 int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, const dSurfaceParameters *s,
                               int maxc);
 
+/* Bulk builders for large batched scenes (no counterpart in the reference):
+ * the same creation calls an ODE program makes per object, looped inside the
+ * library.  Returns 1, or 0 on a bad argument.
+ *   gbodeCreateBodies: rows [n][20] = pos(3) q(4, w first) lvel(3) avel(3)
+ *     mass I11 I22 I33 I12 I13 I23 (dMassSetParameters with the COM at 0)
+ *   gbodeCreateGeoms: cls [n] (dSphereClass, dBoxClass, dCapsuleClass,
+ *     dPlaneClass), dims [n][4], body [n] (NULL entry or array: static geom,
+ *     placed by pos [n][3] and R [n][12])
+ *   gbodeCreateJoints: rows [n][GBODE_JOINT_COLS] = type (dJointTypeBall,
+ *     Hinge, Hinge2), body1, body2 (indices into `bodies`, -1: none),
+ *     anchor(3), axis or axis 1 (3), lo stop, hi stop, axis 2 (3), axis-2
+ *     motor velocity, max force, suspension ERP, CFM, axis-1 motor velocity,
+ *     max force -- world frame */
+#define GBODE_JOINT_COLS 20
+int gbodeCreateBodies(dWorldID w, int n, const float *rows, dBodyID *out);
+int gbodeCreateGeoms(dSpaceID space, int n, const int *cls, const float *dims, const float *pos, const float *R,
+                     const dBodyID *body, dGeomID *out);
+int gbodeCreateJoints(dWorldID w, int n, const float *rows, const dBodyID *bodies, dJointID *out);
+
 /* One fused step (no counterpart in the reference): gbodeSpaceCollideContacts
  * + dWorldQuickStep(w, dt) + dJointGroupEmpty(group).  With use_graph != 0
  * the step is recorded once into a CUDA graph -- on the second call after

@@ -959,6 +959,7 @@ int gbodeSpaceCollideContacts(dSpaceID space, dWorldID w, dJointGroupID group, c
     surf.motion1 = sp->motion1; surf.motion2 = sp->motion2; surf.motionN = sp->motionN; surf.slip1 = sp->slip1; surf.slip2 = sp->slip2;
     if (!w->ws.surfaces.ensure(sizeof(Surface))) { set_error("device allocation (surfaces)"); return 0; }
     launch_set_surface(w->ws, surf, s);  // by value: no host buffer outlives the call
+    w->ws.rows_per_contact = (sp->mode & dContactRolling) ? 6 : 3;
     launch_pose_aabb(w->ws, bodies_view(w->ws, (int)w->bodies.size()), ng, space->minlevel, space->maxlevel, s);
     if (!launch_broadphase(w->ws, ng, space->exact_pairs, s)) { set_error("broad phase"); return 0; }
     if (!launch_narrowphase(w->ws, maxc, 0, false, s)) { set_error("narrow phase"); return 0; }
@@ -1327,6 +1328,82 @@ dReal dJointGetHinge2Angle1(dJointID j) {
     return -atan2f(dot3h(j->v2, q), dot3h(j->v1, q));
 }
 
+// ---- bulk builders for large batched scenes (extensions): the same calls an
+// ODE program makes per object, looped on the host side of the library
+int gbodeCreateBodies(dWorldID w, int n, const float *rows, dBodyID *out) {
+    if (!w || n < 0 || (n > 0 && (!rows || !out))) { set_error("gbodeCreateBodies: bad argument"); return 0; }
+    dMass m;
+    for (int i = 0; i < n; i++) {
+        const float *r = rows + 20 * (size_t)i;
+        dBodyID b = dBodyCreate(w);
+        dBodySetPosition(b, r[0], r[1], r[2]);
+        const dReal q[4] = {r[3], r[4], r[5], r[6]};
+        dBodySetQuaternion(b, q);
+        dBodySetLinearVel(b, r[7], r[8], r[9]);
+        dBodySetAngularVel(b, r[10], r[11], r[12]);
+        dMassSetParameters(&m, r[13], 0, 0, 0, r[14], r[15], r[16], r[17], r[18], r[19]);
+        dBodySetMass(b, &m);
+        out[i] = b;
+    }
+    return 1;
+}
+int gbodeCreateGeoms(dSpaceID space, int n, const int *cls, const float *dims, const float *pos, const float *R,
+                     const dBodyID *body, dGeomID *out) {
+    if (!space || n < 0 || (n > 0 && (!cls || !dims || !out))) { set_error("gbodeCreateGeoms: bad argument"); return 0; }
+    for (int i = 0; i < n; i++) {
+        const float *d = dims + 4 * (size_t)i;
+        dGeomID g;
+        switch (cls[i]) {
+        case dSphereClass: g = dCreateSphere(space, d[0]); break;
+        case dBoxClass: g = dCreateBox(space, d[0], d[1], d[2]); break;
+        case dCapsuleClass: g = dCreateCapsule(space, d[0], d[1]); break;
+        case dPlaneClass: g = dCreatePlane(space, d[0], d[1], d[2], d[3]); break;
+        default: set_error("gbodeCreateGeoms: unsupported class"); return 0;
+        }
+        if (body && body[i]) dGeomSetBody(g, body[i]);
+        else if (cls[i] != dPlaneClass) {
+            if (pos) dGeomSetPosition(g, pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2]);
+            if (R) dGeomSetRotation(g, R + 12 * (size_t)i);
+        }
+        out[i] = g;
+    }
+    return 1;
+}
+int gbodeCreateJoints(dWorldID w, int n, const float *rows, const dBodyID *bodies, dJointID *out) {
+    if (!w || n < 0 || (n > 0 && (!rows || !bodies || !out))) { set_error("gbodeCreateJoints: bad argument"); return 0; }
+    for (int i = 0; i < n; i++) {
+        const float *r = rows + GBODE_JOINT_COLS * (size_t)i;
+        const int t = (int)r[0], b1 = (int)r[1], b2 = (int)r[2];
+        dJointID j;
+        if (t == dJointTypeBall) j = dJointCreateBall(w, nullptr);
+        else if (t == dJointTypeHinge) j = dJointCreateHinge(w, nullptr);
+        else if (t == dJointTypeHinge2) j = dJointCreateHinge2(w, nullptr);
+        else { set_error("gbodeCreateJoints: unsupported joint type"); return 0; }
+        dJointAttach(j, b1 >= 0 ? bodies[b1] : nullptr, b2 >= 0 ? bodies[b2] : nullptr);
+        if (t == dJointTypeBall) {
+            dJointSetBallAnchor(j, r[3], r[4], r[5]);
+        } else if (t == dJointTypeHinge) {
+            dJointSetHingeAnchor(j, r[3], r[4], r[5]);
+            dJointSetHingeAxis(j, r[6], r[7], r[8]);
+            dJointSetHingeParam(j, dParamLoStop, r[9]);
+            dJointSetHingeParam(j, dParamHiStop, r[10]);
+            if (r[19] > 0) { dJointSetHingeParam(j, dParamVel, r[18]); dJointSetHingeParam(j, dParamFMax, r[19]); }
+        } else {
+            dJointSetHinge2Anchor(j, r[3], r[4], r[5]);
+            const dReal a1[3] = {r[6], r[7], r[8]}, a2[3] = {r[11], r[12], r[13]};
+            dJointSetHinge2Axes(j, a1, a2);
+            dJointSetHinge2Param(j, dParamLoStop, r[9]);
+            dJointSetHinge2Param(j, dParamHiStop, r[10]);
+            dJointSetHinge2Param(j, dParamVel2, r[14]);
+            dJointSetHinge2Param(j, dParamFMax2, r[15]);
+            dJointSetHinge2Param(j, dParamSuspensionERP, r[16]);
+            dJointSetHinge2Param(j, dParamSuspensionCFM, r[17]);
+        }
+        out[i] = j;
+    }
+    return 1;
+}
+
 // Upload the ball and hinge joints (attached, in world order) when they changed.
 static bool upload_joint_table(dxWorld *w) {
     if (!w->joints_dirty) return true;
@@ -1474,6 +1551,9 @@ static bool upload_host_contacts(dxWorld *w, const std::vector<dxJoint *> &js) {
     if (!ws.surfaces.ensure((size_t)(nc > 0 ? nc : 1) * sizeof(Surface))) return false;
     std::vector<Contact> C(nc);
     std::vector<Surface> S(nc);
+    ws.rows_per_contact = 3;
+    for (const dxJoint *j : js)
+        if (j->contact.surface.mode & dContactRolling) ws.rows_per_contact = 6;
     for (int k = 0; k < nc; k++) {
         const dContact &c = js[k]->contact;
         Contact &o = C[k];

@@ -97,6 +97,7 @@ struct Workspace {
     DBuf j_pairs;   // set of jointed body pairs (fused narrow phase skips them)
     unsigned j_pair_mask = 0;
     int njoints = 0;
+    int rows_per_contact = 6;  // row capacity per contact: 3, or 6 when a surface uses rolling friction
     // reference-order schedule
     DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
     // warm start cache (previous step)

@@ -1870,7 +1870,8 @@ bool ensure_bodies(Workspace &ws, int nb) {
 bool ensure_rows(Workspace &ws, int ncap, int nj) {
     size_t nc = ncap > 0 ? ncap : 1;
     size_t ng = nc + (nj > 0 ? nj : 0);  // constraint groups: contact manifolds (at most one per contact) + joints
-    size_t rows = ng * 6;
+    // rows: up to 3 per contact (6 when a surface uses rolling friction), 6 per joint
+    size_t rows = nc * (size_t)(ws.rows_per_contact > 0 ? ws.rows_per_contact : 6) + (size_t)(nj > 0 ? nj : 0) * 6;
     bool ok = ws.c_mcount.ensure((nc + 1) * 4) && ws.c_rstart.ensure((nc + 1) * 4) && ws.m_head.ensure((nc + 1) * 4) &&
               ws.m_id.ensure((nc + 1) * 4) && ws.m_start.ensure((nc + 2) * 4) && ws.m_colour.ensure((ng + 1) * 4) &&
               ws.m_tent.ensure((ng + 1) * 4) && ws.col_count.ensure(GB_MAX_COLOURS * 4 + 4) &&

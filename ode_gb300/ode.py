@@ -154,6 +154,10 @@ _PROTOS = [
     ("dJointSetHinge2Param", None, [ID, ctypes.c_int, dReal]),
     ("dJointGetHinge2Anchor", None, [ID, _F]), ("dJointGetHinge2Param", dReal, [ID, ctypes.c_int]),
     ("dJointGetHinge2Angle1", dReal, [ID]),
+    ("gbodeCreateBodies", ctypes.c_int, [ID, ctypes.c_int, _F, ctypes.c_void_p]),
+    ("gbodeCreateGeoms", ctypes.c_int, [ID, ctypes.c_int, ctypes.c_void_p, _F, _F, _F, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    ("gbodeCreateJoints", ctypes.c_int, [ID, ctypes.c_int, _F, ctypes.c_void_p, ctypes.c_void_p]),
     ("gbodeWorldStepFused", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int]),
     ("gbodeMlpParamCount", ctypes.c_int, []),
     ("gbodeMlpLossGrad", ctypes.c_int, [_F, _F, _F, ctypes.c_int, _F, _F]),

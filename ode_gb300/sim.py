@@ -54,6 +54,9 @@ def make_joint(L, w, bodies, row):
     return j
 
 
+BULK_BODIES = 20000  # larger scenes are built through the bulk builders
+
+
 class GBWorld:
     def __init__(self, scene: Scene, solver: int = ode.GBODE_SOLVER_COLOURED, dyn: bool = False,
                  iterations: int | None = None, stream=None):
@@ -74,6 +77,28 @@ class GBWorld:
             zero = (ctypes.c_float * 1)(0.0)
             L.dWorldSetQuickStepDynamicIterationParameters(self.w, zero, zero, None)
         L.gbodeWorldSetSolver(self.w, solver)
+        self.space = None
+        if scene.nb > BULK_BODIES:
+            self._build_bulk(scene)
+        else:
+            self._build_calls(scene)
+        self.group = L.dJointGroupCreate(0)
+        self.surface = ode.dSurfaceParameters()
+        self.surface.mode = scene.surface_mode
+        self.surface.mu = scene.mu
+        self.surface.mu2 = scene.mu2
+        self.surface.bounce = scene.bounce
+        self.surface.bounce_vel = scene.bounce_vel
+        self.surface.soft_erp = scene.soft_erp
+        self.surface.soft_cfm = scene.soft_cfm
+        self.body_index = {int(b): k for k, b in enumerate(self.bodies)}
+        self._contacts = (ode.dContact * 16)()
+        self.made = []   # contacts made by the last compat step: (b1, b2, dContact copy)
+        self._cb = ode.dNearCallback(self._near)
+
+    def _build_calls(self, scene):
+        """One ODE call per object, as an ODE program builds a world."""
+        L = self.L
         self.bodies = []
         m = ode.dMass()
         for row in scene.bodies:
@@ -115,19 +140,42 @@ class GBWorld:
         if scene.joints is not None:
             for row in scene.joints:
                 self.joints.append(make_joint(L, self.w, self.bodies, row))
-        self.group = L.dJointGroupCreate(0)
-        self.surface = ode.dSurfaceParameters()
-        self.surface.mode = scene.surface_mode
-        self.surface.mu = scene.mu
-        self.surface.mu2 = scene.mu2
-        self.surface.bounce = scene.bounce
-        self.surface.bounce_vel = scene.bounce_vel
-        self.surface.soft_erp = scene.soft_erp
-        self.surface.soft_cfm = scene.soft_cfm
-        self.body_index = {int(b): k for k, b in enumerate(self.bodies)}
-        self._contacts = (ode.dContact * 16)()
-        self.made = []   # contacts made by the last compat step: (b1, b2, dContact copy)
-        self._cb = ode.dNearCallback(self._near)
+
+    def _build_bulk(self, scene):
+        """The same objects through the bulk builders (gbodeCreateBodies,
+        gbodeCreateGeoms, gbodeCreateJoints): one call per kind."""
+        L = self.L
+        nb, ng = scene.nb, scene.ng
+        ids = (ctypes.c_void_p * max(nb, 1))()
+        rows = np.ascontiguousarray(scene.bodies, np.float32)
+        if L.gbodeCreateBodies(self.w, nb, ode.fptr(rows), ids) != 1:
+            raise RuntimeError(L.gbodeGetLastError().decode())
+        self.bodies = list(ids[:nb])
+        self.space = L.dHashSpaceCreate(None)
+        L.dHashSpaceSetLevels(self.space, scene.hash_levels[0], scene.hash_levels[1])
+        gb = (ctypes.c_void_p * max(ng, 1))()
+        for i in range(ng):
+            bi = int(scene.geom_body[i])
+            gb[i] = ids[bi] if bi >= 0 else None
+        gids = (ctypes.c_void_p * max(ng, 1))()
+        cls = np.ascontiguousarray(scene.geom_cls, np.int32)
+        dims = np.ascontiguousarray(scene.geom_dims, np.float32)
+        pos = np.ascontiguousarray(scene.geom_pos, np.float32)
+        R = np.ascontiguousarray(scene.geom_R, np.float32)
+        if L.gbodeCreateGeoms(self.space, ng, cls.ctypes.data, ode.fptr(dims), ode.fptr(pos), ode.fptr(R), gb,
+                              gids) != 1:
+            raise RuntimeError(L.gbodeGetLastError().decode())
+        self.geoms = list(gids[:ng])
+        for i, g in enumerate(self.geoms):
+            L.dGeomSetData(g, ctypes.c_void_p(i))
+        self.joints = []
+        if scene.joints is not None and len(scene.joints):
+            jr = np.zeros((len(scene.joints), 20), np.float32)
+            jr[:, :scene.joints.shape[1]] = scene.joints
+            jids = (ctypes.c_void_p * len(jr))()
+            if L.gbodeCreateJoints(self.w, len(jr), ode.fptr(jr), ids, jids) != 1:
+                raise RuntimeError(L.gbodeGetLastError().decode())
+            self.joints = list(jids)
 
     # ---------------------------------------------------------------- loops
     def _near(self, data, o1, o2):
