@@ -113,6 +113,24 @@ void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal vel);
 dReal dWorldGetContactMaxCorrectingVel(dWorldID w);
 void dWorldSetContactSurfaceLayer(dWorldID w, dReal depth);
 dReal dWorldGetContactSurfaceLayer(dWorldID w);
+/* damping and the angular speed cap, world defaults copied into bodies by
+ * dBodyCreate: include/ode/objects.h:430-520, ode/src/ode.cpp:1950-2048.
+ * Applied in the integration step (ode/src/util.cpp:583-593, :675-691):
+ * angular speed above the cap is scaled down to it before the move; after
+ * the move a velocity whose squared norm exceeds the squared threshold is
+ * multiplied by (1 - scale).  Thresholds are stored squared; scale 0 and an
+ * infinite cap switch the terms off. */
+void dWorldSetLinearDamping(dWorldID w, dReal scale);
+void dWorldSetAngularDamping(dWorldID w, dReal scale);
+void dWorldSetDamping(dWorldID w, dReal linear_scale, dReal angular_scale);
+void dWorldSetLinearDampingThreshold(dWorldID w, dReal threshold);
+void dWorldSetAngularDampingThreshold(dWorldID w, dReal threshold);
+dReal dWorldGetLinearDamping(dWorldID w);
+dReal dWorldGetAngularDamping(dWorldID w);
+dReal dWorldGetLinearDampingThreshold(dWorldID w);
+dReal dWorldGetAngularDampingThreshold(dWorldID w);
+void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed);
+dReal dWorldGetMaxAngularSpeed(dWorldID w);
 
 /* ---- bodies: include/ode/objects.h:700-1400 */
 dBodyID dBodyCreate(dWorldID w);
@@ -137,6 +155,19 @@ const dReal *dBodyGetForce(dBodyID b);
 const dReal *dBodyGetTorque(dBodyID b);
 void dBodySetGyroscopicMode(dBodyID b, int enabled);
 int dBodyGetGyroscopicMode(dBodyID b);
+/* per-body damping and angular speed cap: ode/src/ode.cpp:1025-1113 */
+void dBodySetLinearDamping(dBodyID b, dReal scale);
+void dBodySetAngularDamping(dBodyID b, dReal scale);
+void dBodySetDamping(dBodyID b, dReal linear_scale, dReal angular_scale);
+void dBodySetLinearDampingThreshold(dBodyID b, dReal threshold);
+void dBodySetAngularDampingThreshold(dBodyID b, dReal threshold);
+void dBodySetDampingDefaults(dBodyID b);
+dReal dBodyGetLinearDamping(dBodyID b);
+dReal dBodyGetAngularDamping(dBodyID b);
+dReal dBodyGetLinearDampingThreshold(dBodyID b);
+dReal dBodyGetAngularDampingThreshold(dBodyID b);
+void dBodySetMaxAngularSpeed(dBodyID b, dReal max_speed);
+dReal dBodyGetMaxAngularSpeed(dBodyID b);
 int dBodyGetNumJoints(dBodyID b);
 
 /* ---- mass helpers: include/ode/mass.h:40-96 */

@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -94,6 +94,9 @@ struct dxBody {
     float invI[12];
     float invMass = 1;
     int gyro = 1;  // ode.cpp:283 -- dBodyCreate enables the implicit gyroscopic term
+    // damping (objects.h:100-108: scales, squared thresholds; scale 0 = off) and angular speed cap
+    float damp[4] = {0, 0, 0.01f * 0.01f, 0.01f * 0.01f};
+    float max_w = INFINITY;
     int njoints = 0;
 };
 
@@ -158,6 +161,9 @@ struct dxWorld {
     std::vector<dxBody *> bodies;
     std::vector<dxJoint *> joints;
     bool joints_dirty = false;  // ball/hinge joints changed since the last upload
+    // defaults copied into bodies at creation (objects.cpp:63-69, ode.cpp:265-285)
+    float damp[4] = {0, 0, 0.01f * 0.01f, 0.01f * 0.01f};
+    float max_w = INFINITY;
     // gbodeWorldStepFused's CUDA graph of one fused step
     int graph_state = 0;  // 0 none, 1 capture on the next call, 2 replaying
     cudaGraph_t graph = nullptr;
@@ -311,7 +317,8 @@ static bool world_upload(dxWorld *w) {
     int nb = (int)w->bodies.size();
     if (!ensure_bodies(w->ws, nb)) { set_error("device allocation (bodies)"); return false; }
     if (!w->dev_dirty) return true;
-    std::vector<float4> pos(nb), q(nb), R(3 * nb), lv(nb), av(nb), fa(nb), ta(nb), Ib(3 * nb), iIb(3 * nb);
+    std::vector<float4> pos(nb), q(nb), R(3 * nb), lv(nb), av(nb), fa(nb), ta(nb), Ib(3 * nb), iIb(3 * nb), dm(nb);
+    std::vector<float> mw(nb);
     for (int i = 0; i < nb; i++) {
         dxBody *b = w->bodies[i];
         b->index = i;
@@ -329,6 +336,8 @@ static bool world_upload(dxWorld *w) {
         av[i] = make_float4(b->avel[0], b->avel[1], b->avel[2], ff);
         fa[i] = make_float4(b->facc[0], b->facc[1], b->facc[2], 0.f);
         ta[i] = make_float4(b->tacc[0], b->tacc[1], b->tacc[2], 0.f);
+        dm[i] = make_float4(b->damp[0], b->damp[1], b->damp[2], b->damp[3]);
+        mw[i] = b->max_w;
     }
     if (nb > 0) {
         cudaStream_t s = w->stream;
@@ -341,6 +350,8 @@ static bool world_upload(dxWorld *w) {
         cudaMemcpyAsync(w->ws.b_tacc.p, ta.data(), 16 * nb, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(w->ws.b_Ib.p, Ib.data(), 48 * nb, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(w->ws.b_invIb.p, iIb.data(), 48 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_damp.p, dm.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(w->ws.b_maxw.p, mw.data(), 4 * nb, cudaMemcpyHostToDevice, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) { set_error("upload bodies", e); return false; }
     }
@@ -628,10 +639,43 @@ dBodyID dBodyCreate(dWorldID w) {
     dMassSetParameters(&b->mass, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0);  // ode.cpp:249-254
     memset(b->invI, 0, sizeof b->invI);
     b->invI[0] = b->invI[5] = b->invI[10] = 1;
+    memcpy(b->damp, w->damp, sizeof b->damp);  // dBodySetDampingDefaults
+    b->max_w = w->max_w;
     w->bodies.push_back(b);
     w->dev_dirty = true;
     return b;
 }
+// ---- damping and angular speed cap: ode.cpp:1025-1113 (bodies), :1970-2048 (world)
+void dWorldSetLinearDamping(dWorldID w, dReal scale) { w->damp[0] = scale; }
+void dWorldSetAngularDamping(dWorldID w, dReal scale) { w->damp[1] = scale; }
+void dWorldSetDamping(dWorldID w, dReal linear_scale, dReal angular_scale) {
+    w->damp[0] = linear_scale;
+    w->damp[1] = angular_scale;
+}
+void dWorldSetLinearDampingThreshold(dWorldID w, dReal threshold) { w->damp[2] = threshold * threshold; }
+void dWorldSetAngularDampingThreshold(dWorldID w, dReal threshold) { w->damp[3] = threshold * threshold; }
+dReal dWorldGetLinearDamping(dWorldID w) { return w->damp[0]; }
+dReal dWorldGetAngularDamping(dWorldID w) { return w->damp[1]; }
+dReal dWorldGetLinearDampingThreshold(dWorldID w) { return sqrtf(w->damp[2]); }
+dReal dWorldGetAngularDampingThreshold(dWorldID w) { return sqrtf(w->damp[3]); }
+void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed) { w->max_w = max_speed; }
+dReal dWorldGetMaxAngularSpeed(dWorldID w) { return w->max_w; }
+void dBodySetLinearDamping(dBodyID b, dReal scale) { mark_host_changed(b); b->damp[0] = scale; }
+void dBodySetAngularDamping(dBodyID b, dReal scale) { mark_host_changed(b); b->damp[1] = scale; }
+void dBodySetDamping(dBodyID b, dReal linear_scale, dReal angular_scale) {
+    mark_host_changed(b);
+    b->damp[0] = linear_scale;
+    b->damp[1] = angular_scale;
+}
+void dBodySetLinearDampingThreshold(dBodyID b, dReal threshold) { mark_host_changed(b); b->damp[2] = threshold * threshold; }
+void dBodySetAngularDampingThreshold(dBodyID b, dReal threshold) { mark_host_changed(b); b->damp[3] = threshold * threshold; }
+void dBodySetDampingDefaults(dBodyID b) { mark_host_changed(b); memcpy(b->damp, b->world->damp, sizeof b->damp); }
+dReal dBodyGetLinearDamping(dBodyID b) { return b->damp[0]; }
+dReal dBodyGetAngularDamping(dBodyID b) { return b->damp[1]; }
+dReal dBodyGetLinearDampingThreshold(dBodyID b) { return sqrtf(b->damp[2]); }
+dReal dBodyGetAngularDampingThreshold(dBodyID b) { return sqrtf(b->damp[3]); }
+void dBodySetMaxAngularSpeed(dBodyID b, dReal max_speed) { mark_host_changed(b); b->max_w = max_speed; }
+dReal dBodyGetMaxAngularSpeed(dBodyID b) { return b->max_w; }
 void dBodyDestroy(dBodyID b) {
     dxWorld *w = b->world;
     world_download(w);

@@ -23,6 +23,8 @@ namespace gb {
 //   rt          2 float4 per body: -(M^-1 f_ext + v/h) (quickstep.cpp:1644-1690)
 struct Bodies {
     float4 *pos, *q, *R, *lvel, *avel, *facc, *tacc, *Ib, *invIb, *invIw, *fc, *rt;
+    float4 *damp;  // linear scale, angular scale, squared thresholds (scale 0: no damping)
+    float *maxw;   // angular speed cap (infinity: none)
     int n;
 };
 

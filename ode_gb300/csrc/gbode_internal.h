@@ -84,6 +84,7 @@ struct Workspace {
     DBuf c_slots, c_count, c_start, contacts, surfaces, c_mcount, c_rstart, c_code;
     // bodies
     DBuf b_pos, b_q, b_R, b_lvel, b_avel, b_facc, b_tacc, b_Ib, b_invIb, b_invIw, b_fc, b_rt, b_fa;
+    DBuf b_damp, b_maxw;  // damping (scales, squared thresholds), angular speed cap
     // rows
     DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
     // colouring / schedule

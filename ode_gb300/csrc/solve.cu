@@ -1715,7 +1715,15 @@ __global__ void k_integrate(Bodies B, SolverParams P) {
     load_rows3(B.invIw + 3 * i, invIw);
     mul0_331(tmp, invIw, tacc);
     avel[0] = avel[0] + tmp[0]; avel[1] = avel[1] + tmp[1]; avel[2] = avel[2] + tmp[2];
-    // dxStepBody (infinitesimal rotation; no finite-rotation, damping or speed cap)
+    // dxStepBody (util.cpp:583-692; infinitesimal rotation, no finite-rotation mode)
+    const float maxw = B.maxw[i];
+    if (maxw < INFINITY) {  // the angular speed cap
+        const float aspeed = avel[0] * avel[0] + avel[1] * avel[1] + avel[2] * avel[2];
+        if (aspeed > maxw * maxw) {
+            const float coef = maxw / sqrtf(aspeed);
+            avel[0] *= coef; avel[1] *= coef; avel[2] *= coef;
+        }
+    }
     float pos[3] = {ps.x + h * lvel[0], ps.y + h * lvel[1], ps.z + h * lvel[2]};
     float q[4] = {q4.x, q4.y, q4.z, q4.w};
     const float *w = avel;
@@ -1734,6 +1742,15 @@ __global__ void k_integrate(Bodies B, SolverParams P) {
     R[4] = 2 * (q[1] * q[2] + q[0] * q[3]); R[5] = 1 - qq1 - qq3; R[6] = 2 * (q[2] * q[3] - q[0] * q[1]);
     R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2;
     R[3] = R[7] = R[11] = 0;
+    const float4 dm = B.damp[i];  // damping after the move (util.cpp:675-691)
+    if (dm.x != 0.f) {
+        const float s2 = lvel[0] * lvel[0] + lvel[1] * lvel[1] + lvel[2] * lvel[2];
+        if (s2 > dm.z) { const float k = 1 - dm.x; lvel[0] *= k; lvel[1] *= k; lvel[2] *= k; }
+    }
+    if (dm.y != 0.f) {
+        const float s2 = avel[0] * avel[0] + avel[1] * avel[1] + avel[2] * avel[2];
+        if (s2 > dm.w) { const float k = 1 - dm.y; avel[0] *= k; avel[1] *= k; avel[2] *= k; }
+    }
     B.pos[i] = make_float4(pos[0], pos[1], pos[2], ps.w);
     B.q[i] = make_float4(q[0], q[1], q[2], q[3]);
     store_rows3(B.R + 3 * i, R);
@@ -1854,6 +1871,7 @@ Bodies bodies_view(Workspace &ws, int nb) {
     B.lvel = ws.b_lvel.as<float4>(); B.avel = ws.b_avel.as<float4>(); B.facc = ws.b_facc.as<float4>();
     B.tacc = ws.b_tacc.as<float4>(); B.Ib = ws.b_Ib.as<float4>(); B.invIb = ws.b_invIb.as<float4>();
     B.invIw = ws.b_invIw.as<float4>(); B.fc = ws.b_fc.as<float4>(); B.rt = ws.b_rt.as<float4>();
+    B.damp = ws.b_damp.as<float4>(); B.maxw = ws.b_maxw.as<float>();
     B.n = nb;
     return B;
 }
@@ -1864,7 +1882,7 @@ bool ensure_bodies(Workspace &ws, int nb) {
            ws.b_avel.ensure(n * 16) && ws.b_facc.ensure(n * 16) && ws.b_tacc.ensure(n * 16) && ws.b_Ib.ensure(n * 48) &&
            ws.b_invIb.ensure(n * 48) && ws.b_invIw.ensure(n * 48) && ws.b_fc.ensure(n * 32) && ws.b_rt.ensure(n * 32) &&
            ws.b_fa.ensure(n * 8) && ws.m_mask.ensure(n * 16) && ws.m_claim.ensure(n * GB_MAX_COLOURS * 4) &&
-           ws.res_f.ensure(n * 48) && ws.res_v.ensure(n * 48);
+           ws.res_f.ensure(n * 48) && ws.res_v.ensure(n * 48) && ws.b_damp.ensure(n * 16) && ws.b_maxw.ensure(n * 4);
 }
 
 bool ensure_rows(Workspace &ws, int ncap, int nj) {

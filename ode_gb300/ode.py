@@ -74,6 +74,12 @@ _PROTOS = [
     ("dWorldGetQuickStepDynamicIterationParameters", None, [ID, _F, _F, _F]),
     ("dWorldSetContactMaxCorrectingVel", None, [ID, dReal]), ("dWorldGetContactMaxCorrectingVel", dReal, [ID]),
     ("dWorldSetContactSurfaceLayer", None, [ID, dReal]), ("dWorldGetContactSurfaceLayer", dReal, [ID]),
+    ("dWorldSetLinearDamping", None, [ID, dReal]), ("dWorldSetAngularDamping", None, [ID, dReal]),
+    ("dWorldSetDamping", None, [ID, dReal, dReal]),
+    ("dWorldSetLinearDampingThreshold", None, [ID, dReal]), ("dWorldSetAngularDampingThreshold", None, [ID, dReal]),
+    ("dWorldGetLinearDamping", dReal, [ID]), ("dWorldGetAngularDamping", dReal, [ID]),
+    ("dWorldGetLinearDampingThreshold", dReal, [ID]), ("dWorldGetAngularDampingThreshold", dReal, [ID]),
+    ("dWorldSetMaxAngularSpeed", None, [ID, dReal]), ("dWorldGetMaxAngularSpeed", dReal, [ID]),
     ("dBodyCreate", ID, [ID]), ("dBodyDestroy", None, [ID]),
     ("dBodySetData", None, [ID, ctypes.c_void_p]), ("dBodyGetData", ctypes.c_void_p, [ID]),
     ("dBodySetPosition", None, [ID, dReal, dReal, dReal]), ("dBodySetRotation", None, [ID, _F]),
@@ -86,6 +92,13 @@ _PROTOS = [
     ("dBodyGetForce", _F, [ID]), ("dBodyGetTorque", _F, [ID]),
     ("dBodySetGyroscopicMode", None, [ID, ctypes.c_int]), ("dBodyGetGyroscopicMode", ctypes.c_int, [ID]),
     ("dBodyGetNumJoints", ctypes.c_int, [ID]),
+    ("dBodySetLinearDamping", None, [ID, dReal]), ("dBodySetAngularDamping", None, [ID, dReal]),
+    ("dBodySetDamping", None, [ID, dReal, dReal]),
+    ("dBodySetLinearDampingThreshold", None, [ID, dReal]), ("dBodySetAngularDampingThreshold", None, [ID, dReal]),
+    ("dBodySetDampingDefaults", None, [ID]),
+    ("dBodyGetLinearDamping", dReal, [ID]), ("dBodyGetAngularDamping", dReal, [ID]),
+    ("dBodyGetLinearDampingThreshold", dReal, [ID]), ("dBodyGetAngularDampingThreshold", dReal, [ID]),
+    ("dBodySetMaxAngularSpeed", None, [ID, dReal]), ("dBodyGetMaxAngularSpeed", dReal, [ID]),
     ("dMassSetZero", None, [ctypes.POINTER(dMass)]),
     ("dMassSetParameters", None, [ctypes.POINTER(dMass), dReal, dReal, dReal, dReal, dReal, dReal, dReal, dReal,
                                   dReal, dReal]),

@@ -87,6 +87,9 @@ class Scene:
     # axis-2 motor velocity and max force, suspension ERP and CFM (hinge2),
     # axis-1 motor velocity and max force -- all in the world frame
     joints: np.ndarray | None = None
+    # world damping defaults copied into every body: linear scale, angular
+    # scale, linear threshold, angular threshold, max angular speed
+    damping: tuple = (0.0, 0.0, 0.01, 0.01, float("inf"))
 
     @property
     def nb(self) -> int:

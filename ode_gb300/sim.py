@@ -77,6 +77,11 @@ class GBWorld:
             zero = (ctypes.c_float * 1)(0.0)
             L.dWorldSetQuickStepDynamicIterationParameters(self.w, zero, zero, None)
         L.gbodeWorldSetSolver(self.w, solver)
+        ls, as_, lt, at, mw = scene.damping
+        L.dWorldSetDamping(self.w, ls, as_)
+        L.dWorldSetLinearDampingThreshold(self.w, lt)
+        L.dWorldSetAngularDampingThreshold(self.w, at)
+        L.dWorldSetMaxAngularSpeed(self.w, mw)
         self.space = None
         if scene.nb > BULK_BODIES:
             self._build_bulk(scene)

@@ -317,8 +317,13 @@ static void mode_chain() {
     std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
     const int JC = 20;
     std::vector<float> jt(JC * nj); rd(jt.data(), jt.size());
+    float damp[5]; rd(damp, 5);  // linear/angular scale, linear/angular threshold, max angular speed
     dWorldID w = dWorldCreate();
     apply_params(w, P, iters, dyn);
+    dWorldSetDamping(w, damp[0], damp[1]);
+    dWorldSetLinearDampingThreshold(w, damp[2]);
+    dWorldSetAngularDampingThreshold(w, damp[3]);
+    dWorldSetMaxAngularSpeed(w, damp[4]);
     std::vector<dBodyID> b(nb);
     for (int i = 0; i < nb; i++) { b[i] = dBodyCreate(w); set_body(b[i], &bodies[BODY_IN * i]); }
     std::vector<dJointID> hinges;

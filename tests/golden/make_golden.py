@@ -354,16 +354,19 @@ def gen_space_pile(exes):
 
 
 def gen_joint_scene(exes, sc, name, iters=200, nsteps=240):
+    """The reference (no-reorder build) steps a jointed scene without geoms:
+    poses per step, then the hinge angles and hinge2 steering angles."""
     jt = np.ascontiguousarray(sc.joints, np.float32)
+    damp = np.asarray(sc.damping, np.float32)
     buf = run(exes["single_noreorder"], "chain",
               [np.array([sc.nb, len(jt), nsteps, iters, 0], np.int32), sc.world_params(),
-               sc.bodies.astype(np.float32), jt])
+               sc.bodies.astype(np.float32), jt, damp])
     r = Reader(buf)
     traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
     nh = int(((jt[:, 0] == 2) | (jt[:, 0] == 6)).sum())
     ang = r.take(np.float32, nsteps * nh).reshape(nsteps, nh)
     np.savez_compressed(os.path.join(HERE, name), bodies=sc.bodies, joints=jt, params=sc.world_params(),
-                        ints=np.array([iters, nsteps], np.int32), traj=traj, angles=ang)
+                        ints=np.array([iters, nsteps], np.int32), traj=traj, angles=ang, damping=damp)
     print(f"{name}: {sc.nb} bodies, {len(jt)} joints ({nh} with angles), {nsteps} steps")
 
 
@@ -378,19 +381,16 @@ def gen_chain(exes):
     """Hanging chains of capsules linked by hinge (limited +-60 deg) and ball
     joints, no geoms: 240 steps of the no-reorder build with 200 iterations
     (a converged solve), poses and hinge angles per step."""
+    gen_joint_scene(exes, scenes.chains(6, seed=11, nmin=3, nmax=8, hang=True), "chain.npz")
+
+
+def gen_damped(exes):
+    """The hanging chains of chain.npz with world damping (linear 0.02 above
+    0.05 m/s, angular 0.05 above 0.1 rad/s) and an angular speed cap of
+    1.5 rad/s that the swinging links reach."""
     sc = scenes.chains(6, seed=11, nmin=3, nmax=8, hang=True)
-    iters, nsteps = 200, 240
-    jt = np.ascontiguousarray(sc.joints, np.float32)
-    buf = run(exes["single_noreorder"], "chain",
-              [np.array([sc.nb, len(jt), nsteps, iters, 0], np.int32), sc.world_params(),
-               sc.bodies.astype(np.float32), jt])
-    r = Reader(buf)
-    traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
-    nh = int((jt[:, 0] == 2).sum())
-    ang = r.take(np.float32, nsteps * nh).reshape(nsteps, nh)
-    np.savez_compressed(os.path.join(HERE, "chain.npz"), bodies=sc.bodies, joints=jt, params=sc.world_params(),
-                        ints=np.array([iters, nsteps], np.int32), traj=traj, angles=ang)
-    print(f"chain: {sc.nb} bodies, {len(jt)} joints ({nh} hinges), {nsteps} steps")
+    sc.damping = (0.02, 0.05, 0.05, 0.1, 1.5)
+    gen_joint_scene(exes, sc, "damped.npz")
 
 
 def main():
@@ -411,6 +411,8 @@ def main():
         gen_chain(exes)
     if a.only in ("", "hinge2"):
         gen_hinge2(exes)
+    if a.only in ("", "damped"):
+        gen_damped(exes)
 
 
 if __name__ == "__main__":

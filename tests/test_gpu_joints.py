@@ -33,7 +33,9 @@ def _chain_scene(g):
     return scenes.Scene("chain", g["bodies"], z, z, np.zeros((0, 3), np.float32), np.zeros((0, 12), np.float32),
                         np.zeros((0, 4), np.float32), dt=float(p[0]), gravity=tuple(float(x) for x in p[1:4]),
                         erp=float(p[4]), cfm=float(p[5]), w=float(p[6]), iterations=int(g["ints"][0]),
-                        joints=g["joints"])
+                        joints=g["joints"],
+                        damping=tuple(float(x) for x in g["damping"]) if "damping" in g.files
+                        else (0.0, 0.0, 0.01, 0.01, float("inf")))
 
 
 def test_hanging_chains_follow_reference(gblib, golden):
@@ -187,3 +189,66 @@ def test_vehicles_drive_among_obstacles(gblib):
     print(f"vehicles: {sc.nb} bodies, {w.stats().contacts} contacts, wheel z in "
           f"[{st[wheels, 2].min():.3f}, {st[wheels, 2].max():.3f}]")
     w.close()
+
+
+def test_damped_chains_follow_reference(gblib, golden):
+    """World damping (linear and angular scales above their thresholds) and
+    the angular speed cap, copied into the bodies at dBodyCreate, applied by
+    the integration kernel: the GPU follows the reference's damped chains
+    (tests/golden/damped.npz) as closely as the undamped ones."""
+    from ode_gb300 import sim
+    L = gblib
+    g = golden("damped.npz")
+    sc = _chain_scene(g)
+    assert sc.damping[4] < float("inf")
+    w = sim.GBWorld(sc)
+    L.dWorldSetQuickStepW(w.w, 1.0)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    L.gbodeWorldSetResidualTarget(w.w, 1e-7, 5, 3000)
+    b0 = w.bodies[0]
+    assert abs(L.dBodyGetLinearDamping(b0) - sc.damping[0]) < 1e-7
+    assert abs(L.dBodyGetAngularDampingThreshold(b0) - sc.damping[3]) < 1e-6
+    assert L.dBodyGetMaxAngularSpeed(b0) == np.float32(sc.damping[4])
+    hinges = [j for j, row in zip(w.joints, sc.joints) if int(row[0]) == 2]
+    worst_p, worst_a, wmax = 0.0, 0.0, 0.0
+    for s in range(HORIZON):
+        assert w.step_fused() == 1
+        st = w.state()
+        worst_p = max(worst_p, float(np.abs(st[:, 0:3] - g["traj"][s, :, 0:3]).max()))
+        ang = np.array([L.dJointGetHingeAngle(h) for h in hinges])
+        worst_a = max(worst_a, float(np.abs(ang - g["angles"][s]).max()))
+        wmax = max(wmax, float(np.linalg.norm(st[:, 22:25], axis=1).max()))
+    print(f"damped chains: over {HORIZON} steps max position difference {worst_p:.2e} m, max hinge angle "
+          f"difference {worst_a:.2e} rad, max angular speed {wmax:.3f} (cap {sc.damping[4]})")
+    assert worst_p <= POS_TOL
+    assert worst_a <= ANGLE_TOL
+    # the cap holds after the step, up to the angular damping applied after it
+    assert wmax <= sc.damping[4] * (1 + 1e-5)
+    w.close()
+
+
+def test_damping_api_round_trip(gblib):
+    """World and body damping setters and getters (thresholds are stored
+    squared and returned as their square roots), dBodySetDampingDefaults,
+    and the max angular speed default (infinity)."""
+    L = gblib
+    L.dInitODE2(0)
+    w = L.dWorldCreate()
+    assert L.dWorldGetMaxAngularSpeed(w) == float("inf")
+    assert abs(L.dWorldGetLinearDampingThreshold(w) - 0.01) < 1e-7
+    L.dWorldSetDamping(w, 0.1, 0.2)
+    L.dWorldSetLinearDampingThreshold(w, 0.3)
+    L.dWorldSetAngularDampingThreshold(w, 0.4)
+    L.dWorldSetMaxAngularSpeed(w, 5.0)
+    b = L.dBodyCreate(w)
+    assert abs(L.dBodyGetLinearDamping(b) - 0.1) < 1e-7 and abs(L.dBodyGetAngularDamping(b) - 0.2) < 1e-7
+    assert abs(L.dBodyGetLinearDampingThreshold(b) - 0.3) < 1e-6
+    assert abs(L.dBodyGetAngularDampingThreshold(b) - 0.4) < 1e-6
+    assert L.dBodyGetMaxAngularSpeed(b) == 5.0
+    L.dBodySetLinearDamping(b, 0.0)
+    L.dBodySetAngularDampingThreshold(b, 2.0)
+    assert L.dBodyGetLinearDamping(b) == 0.0 and abs(L.dBodyGetAngularDampingThreshold(b) - 2.0) < 1e-6
+    L.dBodySetDampingDefaults(b)
+    assert abs(L.dBodyGetLinearDamping(b) - 0.1) < 1e-7
+    assert abs(L.dBodyGetAngularDampingThreshold(b) - 0.4) < 1e-6
+    L.dWorldDestroy(w)
