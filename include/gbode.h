@@ -131,6 +131,22 @@ dReal dWorldGetLinearDampingThreshold(dWorldID w);
 dReal dWorldGetAngularDampingThreshold(dWorldID w);
 void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed);
 dReal dWorldGetMaxAngularSpeed(dWorldID w);
+/* auto-disable defaults copied into bodies by dBodyCreate: include/ode/
+ * objects.h:185-320, ode/src/ode.cpp:1880-1965.  Thresholds are stored
+ * squared.  dWorldGetAutoDisableFlag returns the reference's flag bit (16)
+ * when on. */
+void dWorldSetAutoDisableFlag(dWorldID w, int do_auto_disable);
+int dWorldGetAutoDisableFlag(dWorldID w);
+void dWorldSetAutoDisableLinearThreshold(dWorldID w, dReal linear_average_threshold);
+dReal dWorldGetAutoDisableLinearThreshold(dWorldID w);
+void dWorldSetAutoDisableAngularThreshold(dWorldID w, dReal angular_average_threshold);
+dReal dWorldGetAutoDisableAngularThreshold(dWorldID w);
+void dWorldSetAutoDisableAverageSamplesCount(dWorldID w, unsigned int average_samples_count);
+int dWorldGetAutoDisableAverageSamplesCount(dWorldID w);
+void dWorldSetAutoDisableSteps(dWorldID w, int steps);
+int dWorldGetAutoDisableSteps(dWorldID w);
+void dWorldSetAutoDisableTime(dWorldID w, dReal time);
+dReal dWorldGetAutoDisableTime(dWorldID w);
 
 /* ---- bodies: include/ode/objects.h:700-1400 */
 dBodyID dBodyCreate(dWorldID w);
@@ -168,6 +184,30 @@ dReal dBodyGetLinearDampingThreshold(dBodyID b);
 dReal dBodyGetAngularDampingThreshold(dBodyID b);
 void dBodySetMaxAngularSpeed(dBodyID b, dReal max_speed);
 dReal dBodyGetMaxAngularSpeed(dBodyID b);
+/* enable state and auto-disable per body: ode/src/ode.cpp:850-1020.  Each
+ * step, before the solve (util.cpp:427-561), a body with auto-disable on, no
+ * disabled flag and at least one joint (contacts of the step count) samples
+ * its velocities; when the average of the last `average samples` samples is
+ * within both thresholds for `steps` steps and `time` seconds the body is
+ * disabled and its velocities zeroed.  A step processes every body connected
+ * through contacts and joints to an enabled body and enables it again
+ * (util.cpp:724-860); components of disabled bodies only are not stepped. */
+void dBodyEnable(dBodyID b);
+void dBodyDisable(dBodyID b);
+int dBodyIsEnabled(dBodyID b);
+void dBodySetAutoDisableFlag(dBodyID b, int do_auto_disable);
+int dBodyGetAutoDisableFlag(dBodyID b);
+void dBodySetAutoDisableLinearThreshold(dBodyID b, dReal linear_average_threshold);
+dReal dBodyGetAutoDisableLinearThreshold(dBodyID b);
+void dBodySetAutoDisableAngularThreshold(dBodyID b, dReal angular_average_threshold);
+dReal dBodyGetAutoDisableAngularThreshold(dBodyID b);
+void dBodySetAutoDisableAverageSamplesCount(dBodyID b, unsigned int average_samples_count);
+int dBodyGetAutoDisableAverageSamplesCount(dBodyID b);
+void dBodySetAutoDisableSteps(dBodyID b, int steps);
+int dBodyGetAutoDisableSteps(dBodyID b);
+void dBodySetAutoDisableTime(dBodyID b, dReal time);
+dReal dBodyGetAutoDisableTime(dBodyID b);
+void dBodySetAutoDisableDefaults(dBodyID b);
 int dBodyGetNumJoints(dBodyID b);
 
 /* ---- mass helpers: include/ode/mass.h:40-96 */
@@ -362,6 +402,7 @@ typedef struct gbodeStepStats {
     int pairs;             /* candidate pairs of the last broad phase */
     float solve_ms;        /* device time of the PGS sweeps, if timing is on */
     float step_ms;         /* device time of the whole dWorldQuickStep, if timing is on */
+    int sleeping;          /* bodies not stepped: their component is disabled (auto-disable) */
 } gbodeStepStats;
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */

@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -98,6 +98,12 @@ struct dxBody {
     float damp[4] = {0, 0, 0.01f * 0.01f, 0.01f * 0.01f};
     float max_w = INFINITY;
     int njoints = 0;
+    // auto-disable (objects.h:73-84 dxAutoDisable, ode.cpp:240-285, :887-1020):
+    // GB_ADIS_* flags, countdowns, squared thresholds, velocity ring buffer
+    int adis_flags = 0, adis_counter = 0;
+    int adis_idle_steps = 10, adis_steps_left = 10, adis_samples = 1;
+    float adis_lin = 0.01f * 0.01f, adis_ang = 0.01f * 0.01f, adis_idle_time = 0, adis_time_left = 0;
+    std::vector<float> adis_buf;  // adis_samples x (lvel xyz_, avel xyz_)
 };
 
 struct dxSpace;
@@ -164,6 +170,9 @@ struct dxWorld {
     // defaults copied into bodies at creation (objects.cpp:63-69, ode.cpp:265-285)
     float damp[4] = {0, 0, 0.01f * 0.01f, 0.01f * 0.01f};
     float max_w = INFINITY;
+    // auto-disable defaults (objects.cpp:55-60) and the world's flag
+    int adis_on = 0, adis_idle_steps = 10, adis_samples = 1;
+    float adis_lin = 0.01f * 0.01f, adis_ang = 0.01f * 0.01f, adis_idle_time = 0;
     // gbodeWorldStepFused's CUDA graph of one fused step
     int graph_state = 0;  // 0 none, 1 capture on the next call, 2 replaying
     cudaGraph_t graph = nullptr;
@@ -287,6 +296,18 @@ static void world_download(dxWorld *w) {
         cudaMemcpyAsync(R.data(), w->ws.b_R.p, 48 * nb, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(lv.data(), w->ws.b_lvel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(av.data(), w->ws.b_avel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        // sleeping bodies keep their force accumulators and auto-disable state
+        const bool sl = w->ws.sleep_on;
+        const int S = w->ws.adis_S;
+        std::vector<float4> fa(sl ? nb : 0), ta(sl ? nb : 0), af(sl ? nb : 0), buf(sl ? (size_t)nb * S * 2 : 0);
+        std::vector<int4> ai(sl ? nb : 0);
+        if (sl) {
+            cudaMemcpyAsync(fa.data(), w->ws.b_facc.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(ta.data(), w->ws.b_tacc.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(ai.data(), w->ws.b_adis_i.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(af.data(), w->ws.b_adis_f.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(buf.data(), w->ws.b_adis_buf.p, buf.size() * 16, cudaMemcpyDeviceToHost, s);
+        }
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) { set_error("download bodies", e); return; }
         for (int i = 0; i < nb; i++) {
@@ -298,9 +319,23 @@ static void world_download(dxWorld *w) {
             }
             b->lvel[0] = lv[i].x; b->lvel[1] = lv[i].y; b->lvel[2] = lv[i].z;
             b->avel[0] = av[i].x; b->avel[1] = av[i].y; b->avel[2] = av[i].z;
-            // the device consumed the force accumulators
-            b->facc[0] = b->facc[1] = b->facc[2] = 0;
-            b->tacc[0] = b->tacc[1] = b->tacc[2] = 0;
+            if (sl) {
+                b->facc[0] = fa[i].x; b->facc[1] = fa[i].y; b->facc[2] = fa[i].z;
+                b->tacc[0] = ta[i].x; b->tacc[1] = ta[i].y; b->tacc[2] = ta[i].z;
+                b->adis_flags = ai[i].x & (GB_ADIS_ON | GB_ADIS_DISABLED | GB_ADIS_READY);
+                b->adis_counter = (ai[i].x >> 8) & 0xffff;
+                b->adis_steps_left = ai[i].z;
+                b->adis_time_left = af[i].w;
+                for (int k = 0; k < b->adis_samples && k < S; k++) {
+                    const float4 l = buf[((size_t)i * S + k) * 2], a = buf[((size_t)i * S + k) * 2 + 1];
+                    float *o = &b->adis_buf[8 * k];
+                    o[0] = l.x; o[1] = l.y; o[2] = l.z; o[4] = a.x; o[5] = a.y; o[6] = a.z;
+                }
+            } else {
+                // the device consumed the force accumulators
+                b->facc[0] = b->facc[1] = b->facc[2] = 0;
+                b->tacc[0] = b->tacc[1] = b->tacc[2] = 0;
+            }
         }
     }
     w->host_valid = true;
@@ -339,6 +374,35 @@ static bool world_upload(dxWorld *w) {
         dm[i] = make_float4(b->damp[0], b->damp[1], b->damp[2], b->damp[3]);
         mw[i] = b->max_w;
     }
+    // auto-disable state: uploaded while some body has it on or is disabled
+    bool sleep_on = false;
+    int S = 1;
+    for (int i = 0; i < nb; i++) {
+        const dxBody *b = w->bodies[i];
+        if (b->adis_flags & (GB_ADIS_ON | GB_ADIS_DISABLED)) sleep_on = true;
+        if (b->adis_samples > S) S = b->adis_samples;
+    }
+    w->ws.sleep_on = sleep_on;
+    std::vector<int4> ai;
+    std::vector<float4> af, abuf;
+    if (sleep_on) {
+        if (!ensure_sleep(w->ws, nb, S)) { set_error("device allocation (auto-disable)"); return false; }
+        w->ws.adis_S = S;
+        ai.resize(nb);
+        af.resize(nb);
+        abuf.assign((size_t)nb * S * 2, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int i = 0; i < nb; i++) {
+            const dxBody *b = w->bodies[i];
+            ai[i] = make_int4((b->adis_flags & 0xff) | (b->adis_counter << 8), b->adis_idle_steps, b->adis_steps_left,
+                              b->adis_samples);
+            af[i] = make_float4(b->adis_lin, b->adis_ang, b->adis_idle_time, b->adis_time_left);
+            for (int k = 0; k < b->adis_samples; k++) {
+                const float *o = &b->adis_buf[8 * k];
+                abuf[((size_t)i * S + k) * 2] = make_float4(o[0], o[1], o[2], 0.f);
+                abuf[((size_t)i * S + k) * 2 + 1] = make_float4(o[4], o[5], o[6], 0.f);
+            }
+        }
+    }
     if (nb > 0) {
         cudaStream_t s = w->stream;
         cudaMemcpyAsync(w->ws.b_pos.p, pos.data(), 16 * nb, cudaMemcpyHostToDevice, s);
@@ -352,6 +416,11 @@ static bool world_upload(dxWorld *w) {
         cudaMemcpyAsync(w->ws.b_invIb.p, iIb.data(), 48 * nb, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(w->ws.b_damp.p, dm.data(), 16 * nb, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(w->ws.b_maxw.p, mw.data(), 4 * nb, cudaMemcpyHostToDevice, s);
+        if (sleep_on) {
+            cudaMemcpyAsync(w->ws.b_adis_i.p, ai.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_adis_f.p, af.data(), 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_adis_buf.p, abuf.data(), abuf.size() * 16, cudaMemcpyHostToDevice, s);
+        }
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) { set_error("upload bodies", e); return false; }
     }
@@ -642,9 +711,77 @@ dBodyID dBodyCreate(dWorldID w) {
     memcpy(b->damp, w->damp, sizeof b->damp);  // dBodySetDampingDefaults
     b->max_w = w->max_w;
     w->bodies.push_back(b);
+    dBodySetAutoDisableDefaults(b);  // ode.cpp:268-274
+    b->adis_steps_left = b->adis_idle_steps;
+    b->adis_time_left = b->adis_idle_time;
+    b->adis_counter = 0;
+    b->adis_flags &= ~GB_ADIS_READY;
+    dBodySetAutoDisableAverageSamplesCount(b, b->adis_samples);
     w->dev_dirty = true;
     return b;
 }
+// ---- auto-disable: ode.cpp:850-870 (enable), :887-1020 (bodies), :1880-1965 (world)
+void dBodyEnable(dBodyID b) {
+    mark_host_changed(b);
+    b->adis_flags &= ~GB_ADIS_DISABLED;
+    b->adis_steps_left = b->adis_idle_steps;
+    b->adis_time_left = b->adis_idle_time;
+}
+void dBodyDisable(dBodyID b) { mark_host_changed(b); b->adis_flags |= GB_ADIS_DISABLED; }
+int dBodyIsEnabled(dBodyID b) { world_download(b->world); return (b->adis_flags & GB_ADIS_DISABLED) == 0; }
+dReal dBodyGetAutoDisableLinearThreshold(dBodyID b) { return sqrtf(b->adis_lin); }
+void dBodySetAutoDisableLinearThreshold(dBodyID b, dReal t) { mark_host_changed(b); b->adis_lin = t * t; }
+dReal dBodyGetAutoDisableAngularThreshold(dBodyID b) { return sqrtf(b->adis_ang); }
+void dBodySetAutoDisableAngularThreshold(dBodyID b, dReal t) { mark_host_changed(b); b->adis_ang = t * t; }
+int dBodyGetAutoDisableAverageSamplesCount(dBodyID b) { return b->adis_samples; }
+void dBodySetAutoDisableAverageSamplesCount(dBodyID b, unsigned int n) {
+    mark_host_changed(b);
+    if (n > 0xffff) n = 0xffff;  // the device keeps the ring position in 16 bits
+    b->adis_samples = (int)n;
+    b->adis_buf.assign((size_t)n * 8, 0.f);  // the new buffer is empty
+    b->adis_counter = 0;
+    b->adis_flags &= ~GB_ADIS_READY;
+}
+int dBodyGetAutoDisableSteps(dBodyID b) { return b->adis_idle_steps; }
+void dBodySetAutoDisableSteps(dBodyID b, int steps) { mark_host_changed(b); b->adis_idle_steps = steps; }
+dReal dBodyGetAutoDisableTime(dBodyID b) { return b->adis_idle_time; }
+void dBodySetAutoDisableTime(dBodyID b, dReal t) { mark_host_changed(b); b->adis_idle_time = t; }
+int dBodyGetAutoDisableFlag(dBodyID b) { return (b->adis_flags & GB_ADIS_ON) != 0; }
+void dBodySetAutoDisableFlag(dBodyID b, int do_auto_disable) {
+    mark_host_changed(b);
+    if (!do_auto_disable) {
+        dxWorld *w = b->world;
+        b->adis_flags &= ~(GB_ADIS_ON | GB_ADIS_DISABLED);
+        b->adis_idle_steps = w->adis_idle_steps;
+        b->adis_idle_time = w->adis_idle_time;
+        dBodySetAutoDisableAverageSamplesCount(b, (unsigned)w->adis_samples);
+    } else {
+        b->adis_flags |= GB_ADIS_ON;
+    }
+}
+void dBodySetAutoDisableDefaults(dBodyID b) {
+    dxWorld *w = b->world;
+    mark_host_changed(b);
+    b->adis_idle_steps = w->adis_idle_steps;
+    b->adis_idle_time = w->adis_idle_time;
+    b->adis_samples = w->adis_samples;
+    b->adis_lin = w->adis_lin;
+    b->adis_ang = w->adis_ang;
+    dBodySetAutoDisableFlag(b, w->adis_on);
+}
+dReal dWorldGetAutoDisableLinearThreshold(dWorldID w) { return sqrtf(w->adis_lin); }
+void dWorldSetAutoDisableLinearThreshold(dWorldID w, dReal t) { w->adis_lin = t * t; }
+dReal dWorldGetAutoDisableAngularThreshold(dWorldID w) { return sqrtf(w->adis_ang); }
+void dWorldSetAutoDisableAngularThreshold(dWorldID w, dReal t) { w->adis_ang = t * t; }
+int dWorldGetAutoDisableAverageSamplesCount(dWorldID w) { return w->adis_samples; }
+void dWorldSetAutoDisableAverageSamplesCount(dWorldID w, unsigned int n) { w->adis_samples = n > 0xffff ? 0xffff : (int)n; }
+int dWorldGetAutoDisableSteps(dWorldID w) { return w->adis_idle_steps; }
+void dWorldSetAutoDisableSteps(dWorldID w, int steps) { w->adis_idle_steps = steps; }
+dReal dWorldGetAutoDisableTime(dWorldID w) { return w->adis_idle_time; }
+void dWorldSetAutoDisableTime(dWorldID w, dReal t) { w->adis_idle_time = t; }
+// the reference returns its flag bit (dxBodyAutoDisable, 16), not 1
+int dWorldGetAutoDisableFlag(dWorldID w) { return w->adis_on ? 16 : 0; }
+void dWorldSetAutoDisableFlag(dWorldID w, int do_auto_disable) { w->adis_on = do_auto_disable != 0; }
 // ---- damping and angular speed cap: ode.cpp:1025-1113 (bodies), :1970-2048 (world)
 void dWorldSetLinearDamping(dWorldID w, dReal scale) { w->damp[0] = scale; }
 void dWorldSetAngularDamping(dWorldID w, dReal scale) { w->damp[1] = scale; }
@@ -1657,15 +1794,34 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
         ws.contact_cap = 1;
     }
     if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
+    // the contact joints whose index the rows carry (feedback below)
+    std::vector<dxJoint *> awake_js;
+    const std::vector<dxJoint *> *solved = &js;
     if (P.solver == GBODE_SOLVER_REFERENCE_ORDER && !w->device_contacts) {
-        int nc = (int)js.size();
+        if (ws.sleep_on) {
+            // the sleep stage sees every contact joint; the host-built islands
+            // then hold the contacts of awake components only
+            if (!launch_sleep(ws, nb, stepsize, s)) { set_error("dWorldQuickStep: sleep stage", cudaGetLastError()); return 0; }
+            std::vector<int> asleep(nb > 0 ? nb : 1);
+            if (nb > 0) cudaMemcpyAsync(asleep.data(), ws.b_asleep.p, 4 * (size_t)nb, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("dWorldQuickStep: sleep stage"); return 0; }
+            for (dxJoint *j : js) {
+                const dxBody *b = j->b1 ? j->b1 : j->b2;
+                if (b && !asleep[b->index]) awake_js.push_back(j);
+            }
+            if (!upload_host_contacts(w, awake_js)) { set_error("upload contacts"); return 0; }
+            ws.sleep_precomputed = true;
+            solved = &awake_js;
+        }
+        const std::vector<dxJoint *> &sj = *solved;
+        int nc = (int)sj.size();
         std::vector<int> mrows(nc), rstart(nc + 1, 0);
         for (int k = 0; k < nc; k++) {
-            mrows[k] = host_contact_m(js[k]->contact.surface);
+            mrows[k] = host_contact_m(sj[k]->contact.surface);
             rstart[k + 1] = rstart[k] + mrows[k];
         }
         IslandSchedule sch;
-        build_islands(w, js, rstart, mrows, sch);
+        build_islands(w, sj, rstart, mrows, sch);
         ok = launch_quickstep_islands(ws, nb, P, sch, s, w->timing ? w->ev[0] : nullptr, w->timing ? w->ev[1] : nullptr);
     } else {
         ok = launch_quickstep(ws, nb, 1, P, s, w->timing ? w->ev[0] : nullptr, w->timing ? w->ev[1] : nullptr);
@@ -1676,15 +1832,17 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     w->stats_pending = true;
     w->last_host_contacts = (int)js.size();
     // joint feedback (quickstep.cpp:3108-3181): F = J^T lambda per contact
+    // (a contact of a sleeping component is not solved; its feedback is left as it was)
     bool any_fb = false;
-    for (dxJoint *j : js) if (j->feedback) { any_fb = true; break; }
+    for (dxJoint *j : *solved) if (j->feedback) { any_fb = true; break; }
     if (any_fb) {
         std::vector<float> fb;
-        contact_feedback(ws, (int)js.size(), fb, s);
-        for (size_t k = 0; k < js.size(); k++) {
-            dJointFeedback *f = js[k]->feedback;
+        contact_feedback(ws, (int)solved->size(), fb, s);
+        for (size_t k = 0; k < solved->size(); k++) {
+            dJointFeedback *f = (*solved)[k]->feedback;
             if (!f) continue;
             const float *o = &fb[16 * k];
+            if (o[3] == 0.f) continue;
             for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
             f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
         }
@@ -1728,6 +1886,7 @@ int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const d
     const int nb = (int)w->bodies.size(), ng = (int)space->geoms.size();
     put(&space, sizeof space); put(&group, sizeof group); put(&maxc, sizeof maxc); put(&dt, sizeof dt);
     put(sp, sizeof *sp); put(&w->P, sizeof w->P); put(&nb, sizeof nb); put(&ng, sizeof ng);
+    put(&w->ws.sleep_on, sizeof w->ws.sleep_on); put(&w->ws.adis_S, sizeof w->ws.adis_S);
     const bool clean = !w->dev_dirty && !w->joints_dirty && !space->dirty && w->uploaded_space == space &&
                        !w->timing && w->stream != nullptr && group->joints.empty();
     if (clean && key == w->graph_key && w->graph_state == 2) {
@@ -1790,6 +1949,7 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         w->stats.colours = h.ncolours;
         w->stats.iterations = h.iterations;
         w->stats.residual = h.resid;
+        w->stats.sleeping = w->ws.sleep_on ? h.nasleep : 0;
         w->stats.solve_ms = 0;
         w->stats.step_ms = 0;
         if (w->timing) {

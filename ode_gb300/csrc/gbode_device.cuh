@@ -25,6 +25,7 @@ struct Bodies {
     float4 *pos, *q, *R, *lvel, *avel, *facc, *tacc, *Ib, *invIb, *invIw, *fc, *rt;
     float4 *damp;  // linear scale, angular scale, squared thresholds (scale 0: no damping)
     float *maxw;   // angular speed cap (infinity: none)
+    const int *asleep;  // 1: the body's component sleeps this step (null: sleeping off)
     int n;
 };
 
@@ -84,6 +85,7 @@ enum : unsigned {
     ERR_CELL_RANGE = 64u,
     ERR_NONFINITE = 128u,
     ERR_STAGE_TIMEOUT = 256u,  // a shared-memory staging copy did not complete in time
+    ERR_ISLAND_LIMIT = 512u,   // a union-find merge did not settle within the body count
 };
 
 #if defined(__CUDACC__)

@@ -73,7 +73,17 @@ struct DevCounters {
     int nrows_contacts;    // rows of the contacts (joint rows follow)
     int njoint_rows;       // scan scratch (joint rows)
     int warm_parity;       // which warm-start table holds the previous step
+    int nawake;            // contacts of awake components (the solver's contacts when sleeping is on)
+    int nasleep;           // bodies not stepped (their component sleeps)
 };
+
+// auto-disable state per body, int4: x flags, y idle steps, z steps left,
+// w average samples; float4: squared linear / angular thresholds, idle time,
+// time left.  Flags: bit 0 auto-disable on, bit 1 disabled, bit 2 the
+// velocity ring buffer is full, bits 8-23 the ring buffer's next slot.
+#define GB_ADIS_ON 1
+#define GB_ADIS_DISABLED 2
+#define GB_ADIS_READY 4
 
 struct Workspace {
     // geoms
@@ -85,6 +95,13 @@ struct Workspace {
     // bodies
     DBuf b_pos, b_q, b_R, b_lvel, b_avel, b_facc, b_tacc, b_Ib, b_invIb, b_invIw, b_fc, b_rt, b_fa;
     DBuf b_damp, b_maxw;  // damping (scales, squared thresholds), angular speed cap
+    // sleeping: auto-disable state and velocity ring buffers (adis_S samples a
+    // body), per-step components, and the contacts of awake components
+    DBuf b_adis_i, b_adis_f, b_adis_buf, b_touch, b_parent, b_awake, b_asleep, c_keep, c_kpos, c_awake, c_orig;
+    int adis_S = 1;
+    bool sleep_on = false;  // some body has auto-disable on or is disabled
+    bool sleep_precomputed = false;  // the caller ran the sleep stage of this step already
+    bool use_awake = false;          // the solver of this step reads c_awake / dc->nawake
     // rows
     DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
     // colouring / schedule
@@ -167,6 +184,10 @@ int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
 bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s);
 // per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
 void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
+
+// ---- sleep.cu: auto-disable state buffers; the sleep stage of a step
+bool ensure_sleep(Workspace &ws, int nb, int samples);
+bool launch_sleep(Workspace &ws, int nb, float h, cudaStream_t s);
 
 // launch bookkeeping
 void count_launch(int n = 1);

@@ -64,6 +64,7 @@ __device__ __forceinline__ void cross3(float *r, const float *a, const float *b)
 __global__ void k_bodies(Bodies B, SolverParams P) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.n) return;
+    if (B.asleep && B.asleep[i]) return;  // not in any island this step
     const float h = P.dt;
     float4 lv = B.lvel[i], av = B.avel[i], fa = B.facc[i], ta = B.tacc[i], ps = B.pos[i];
     const float mass = lv.w, invMass = ps.w;
@@ -499,6 +500,11 @@ __device__ float hinge_angle(const float *qb, const float *qc, const float *axis
 __global__ void k_joint_m(JointTable T, Bodies B) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
         const int4 in = T.info[k];
+        if (B.asleep && B.asleep[in.y]) {  // the joint's component sleeps: no rows
+            T.m[k] = 0;
+            T.limit[k] = 0;
+            continue;
+        }
         int m = 3, limit = 0;
         float lerr = 0.f;
         if (in.x == 2) {  // dJointTypeHinge
@@ -711,6 +717,7 @@ __global__ void k_joint_rows(JointTable T, Bodies B, Rows Rw, SolverParams P, in
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
         const int4 in = T.info[k];
         const int m = T.m[k], r0 = base + T.rstart[k];
+        if (m == 0) continue;
         if (r0 + m > Rw.n_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); continue; }
         const int n0 = in.y, n1 = in.z;
         float J[6][16];
@@ -786,6 +793,7 @@ __global__ void k_joint_store(JointTable T, Rows Rw, const DevCounters *dc) {
     const int base = dc->nrows_contacts;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.n; k += gridDim.x * blockDim.x) {
         const int m = T.m[k], r0 = base + T.rstart[k];
+        if (m == 0) continue;  // not solved this step: the multipliers are kept
         for (int r = 0; r < 6; r++) T.lam[6 * k + r] = r < m ? Rw.lambda[r0 + r] : 0.f;
     }
 }
@@ -1700,6 +1708,7 @@ __global__ void k_islands(IslandArgs A) {
 __global__ void k_integrate(Bodies B, SolverParams P) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B.n) return;
+    if (B.asleep && B.asleep[i]) return;  // a sleeping component: not moved, accumulators kept
     const float h = P.dt;
     float4 lv = B.lvel[i], av = B.avel[i], ps = B.pos[i], q4 = B.q[i];
     const float4 fl = B.fc[2 * i], fa = B.fc[2 * i + 1], facc = B.facc[i], tacc4 = B.tacc[i];
@@ -1843,15 +1852,19 @@ __global__ void k_res_rows(Rows Rw, Bodies B, const int *nrows_dev, const double
 }
 
 // joint feedback per contact: f = J^T lambda with the unscaled rows
-__global__ void k_feedback(Rows Rw, const int *nrows_dev, float *fb) {
+// (orig: solver contact -> caller's contact index when sleeping compacted the
+// list, else null); word 3 of a contact's record is set to 1 when it was solved
+__global__ void k_feedback(Rows Rw, const int *nrows_dev, const int *orig, float *fb) {
     int n = *nrows_dev;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-        const int c = Rw.contact[r];
+        int c = Rw.contact[r];
         if (c < 0) continue;  // a ball/hinge joint's row
+        if (orig) c = orig[c];
         const int2 b = Rw.body[r];
         const float l = Rw.lambda[r] / Rw.Ad[r];
         float4 a = Rw.J1l[r], d = Rw.J1a[r];
         float *o = fb + 16 * c;
+        o[3] = 1.f;
         atomicAdd(&o[0], a.x * l); atomicAdd(&o[1], a.y * l); atomicAdd(&o[2], a.z * l);
         atomicAdd(&o[4], d.x * l); atomicAdd(&o[5], d.y * l); atomicAdd(&o[6], d.z * l);
         if (b.y >= 0) {
@@ -1872,6 +1885,7 @@ Bodies bodies_view(Workspace &ws, int nb) {
     B.tacc = ws.b_tacc.as<float4>(); B.Ib = ws.b_Ib.as<float4>(); B.invIb = ws.b_invIb.as<float4>();
     B.invIw = ws.b_invIw.as<float4>(); B.fc = ws.b_fc.as<float4>(); B.rt = ws.b_rt.as<float4>();
     B.damp = ws.b_damp.as<float4>(); B.maxw = ws.b_maxw.as<float>();
+    B.asleep = ws.sleep_on ? ws.b_asleep.as<int>() : nullptr;
     B.n = nb;
     return B;
 }
@@ -2005,11 +2019,18 @@ static WarmTable warm_lookup(Workspace &ws, const SolverParams &P) {
     return W;
 }
 
+// The contacts the solver reads: all of them, or, when the sleep stage ran in
+// this step, the compacted contacts of awake components.
+static const Contact *solve_contacts(Workspace &ws) {
+    return ws.use_awake ? ws.c_awake.as<Contact>() : ws.contacts.as<Contact>();
+}
+static const int *solve_count(Workspace &ws) { return ws.use_awake ? &ws.dc->nawake : &ws.dc->ncontacts; }
+
 static void warm_store(Workspace &ws, cudaStream_t s) {
     unsigned long long *keys = ws.w_keys.as<unsigned long long>();
     float4 *lam = ws.w_lambda.as<float4>();
     k_warm_clear<<<4 * num_sms(), 256, 0, s>>>(keys, ws.warm_mask, ws.dc);
-    k_warm_store<<<4 * num_sms(), 256, 0, s>>>(ws.contacts.as<Contact>(), &ws.dc->ncontacts, ws.c_rstart.as<int>(),
+    k_warm_store<<<4 * num_sms(), 256, 0, s>>>(solve_contacts(ws), solve_count(ws), ws.c_rstart.as<int>(),
                                                ws.c_mcount.as<int>(), rows_view(ws), keys, lam, ws.warm_mask, ws.dc);
     k_warm_flip<<<1, 1, 0, s>>>(ws.dc);
     count_launch(3);
@@ -2022,6 +2043,15 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     if (!ensure_rows(ws, ws.contact_cap, nj)) return false;
     if (P.warm_mode && !ensure_warm(ws)) return false;
     JointTable T = joint_view(ws);
+    // sleeping: the idle test and the island rule decide which bodies, joints
+    // and contacts this step processes (skipped when the caller ran it already
+    // and handed over the contacts of awake components only)
+    ws.use_awake = false;
+    if (ws.sleep_on && !ws.sleep_precomputed) {
+        if (!launch_sleep(ws, nb, P.dt, s)) return false;
+        ws.use_awake = true;
+    }
+    ws.sleep_precomputed = false;
     // joint getInfo1 first: a powered hinge at its limit adds motor torques to
     // the bodies before their right-hand side is formed
     if (nj > 0) {
@@ -2030,10 +2060,11 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     }
     k_bodies<<<grid_for(nb, 128), 128, 0, s>>>(B, P);
     int grid = 4 * num_sms();
-    const Contact *C = ws.contacts.as<Contact>();
+    const Contact *C = solve_contacts(ws);
+    const int *ncp = solve_count(ws);
     const Surface *S = ws.surfaces.as<Surface>();
-    k_contact_m<<<grid, 256, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_mcount.as<int>());
-    scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nrows, ws, s);
+    k_contact_m<<<grid, 256, 0, s>>>(C, S, ncp, ws.c_mcount.as<int>());
+    scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), ncp, ws.contact_cap, &ws.dc->nrows, ws, s);
     k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
     if (nj > 0) scan_exclusive(T.m, T.rstart, nullptr, nj, &ws.dc->njoint_rows, ws, s);
     else cudaMemsetAsync(&ws.dc->njoint_rows, 0, 4, s);
@@ -2048,7 +2079,7 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
         L.feat = ws.l_feat.as<float>();
         L.scale = ws.l_scale.as<float>();
     }
-    k_rows<<<grid, 64, 0, s>>>(C, S, &ws.dc->ncontacts, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn,
+    k_rows<<<grid, 64, 0, s>>>(C, S, ncp, ws.c_rstart.as<int>(), B, rows_view(ws), P, dyn,
                                warm_lookup(ws, P), ws.dc, L);
     count_launch(4);
     if (nj > 0) {
@@ -2057,10 +2088,10 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     }
     if (P.learned) {
         if (!ws.mlp_wb.p || !ws.l_alt.ensure((size_t)ws.row_cap * 4)) return false;
-        if (!mlp_infer(ws.mlp_wb.as<unsigned char>(), ws.l_feat.as<float>(), 0, &ws.dc->ncontacts, ws.l_pred.as<float>(),
+        if (!mlp_infer(ws.mlp_wb.as<unsigned char>(), ws.l_feat.as<float>(), 0, ncp, ws.l_pred.as<float>(),
                        &ws.dc->err, s))
             return false;
-        k_learned_apply<<<grid, 128, 0, s>>>(&ws.dc->ncontacts, ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
+        k_learned_apply<<<grid, 128, 0, s>>>(ncp, ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
                                              ws.l_scale.as<float>(), ws.l_pred.as<float>(), rows_view(ws),
                                              ws.l_alt.as<float>(), ws.dc);
         count_launch();
@@ -2071,12 +2102,13 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
 bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStream_t s, cudaEvent_t ev0,
                       cudaEvent_t ev1) {
     if (!assemble(ws, nb, P, s)) return false;
-    const Contact *C = ws.contacts.as<Contact>();
+    const Contact *C = solve_contacts(ws);
+    const int *ncp = solve_count(ws);
     int grid = 4 * num_sms();
     // manifolds
-    k_manifold_heads<<<grid, 256, 0, s>>>(C, &ws.dc->ncontacts, ws.m_head.as<int>());
-    scan_exclusive(ws.m_head.as<int>(), ws.m_id.as<int>(), &ws.dc->ncontacts, ws.contact_cap, &ws.dc->nmanifolds, ws, s);
-    k_manifold_starts<<<grid, 256, 0, s>>>(&ws.dc->ncontacts, ws.m_head.as<int>(), ws.m_id.as<int>(), ws.m_start.as<int>(),
+    k_manifold_heads<<<grid, 256, 0, s>>>(C, ncp, ws.m_head.as<int>());
+    scan_exclusive(ws.m_head.as<int>(), ws.m_id.as<int>(), ncp, ws.contact_cap, &ws.dc->nmanifolds, ws, s);
+    k_manifold_starts<<<grid, 256, 0, s>>>(ncp, ws.m_head.as<int>(), ws.m_id.as<int>(), ws.m_start.as<int>(),
                                            ws.dc);
     k_groups<<<grid, 256, 0, s>>>(C, ws.m_start.as<int>(), ws.j_info.as<int4>(), ws.njoints, ws.dc,
                                   ws.grp_body.as<int2>());
@@ -2241,7 +2273,7 @@ double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, c
 // [12 features][s][lambda of its 3 rows after the solve][1 if a triplet]
 int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s) {
     int n = 0;
-    cudaMemcpyAsync(&n, &ws.dc->step_contacts, 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&n, ws.use_awake ? &ws.dc->nawake : &ws.dc->step_contacts, 4, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
     if (!out || cap <= 0 || n <= 0 || !ws.l_feat.p) return ws.l_feat.p ? n : 0;
     const int k = n < cap ? n : cap;
@@ -2308,7 +2340,8 @@ void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cud
     DBuf &tmp = ws.res_f;
     tmp.ensure((size_t)ncontacts * 64);
     cudaMemsetAsync(tmp.p, 0, (size_t)ncontacts * 64, s);
-    k_feedback<<<4 * num_sms(), 256, 0, s>>>(rows_view(ws), &ws.dc->nrows, tmp.as<float>());
+    k_feedback<<<4 * num_sms(), 256, 0, s>>>(rows_view(ws), &ws.dc->nrows, ws.use_awake ? ws.c_orig.as<int>() : nullptr,
+                                             tmp.as<float>());
     count_launch();
     cudaMemcpyAsync(out.data(), tmp.p, (size_t)ncontacts * 64, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);

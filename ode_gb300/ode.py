@@ -52,7 +52,7 @@ class dJointFeedback(ctypes.Structure):
 class gbodeStepStats(ctypes.Structure):
     _fields_ = [("contacts", ctypes.c_int), ("rows", ctypes.c_int), ("colours", ctypes.c_int),
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
-                ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float)]
+                ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int)]
 
 
 dNearCallback = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ID, ID)
@@ -80,6 +80,13 @@ _PROTOS = [
     ("dWorldGetLinearDamping", dReal, [ID]), ("dWorldGetAngularDamping", dReal, [ID]),
     ("dWorldGetLinearDampingThreshold", dReal, [ID]), ("dWorldGetAngularDampingThreshold", dReal, [ID]),
     ("dWorldSetMaxAngularSpeed", None, [ID, dReal]), ("dWorldGetMaxAngularSpeed", dReal, [ID]),
+    ("dWorldSetAutoDisableFlag", None, [ID, ctypes.c_int]), ("dWorldGetAutoDisableFlag", ctypes.c_int, [ID]),
+    ("dWorldSetAutoDisableLinearThreshold", None, [ID, dReal]), ("dWorldGetAutoDisableLinearThreshold", dReal, [ID]),
+    ("dWorldSetAutoDisableAngularThreshold", None, [ID, dReal]), ("dWorldGetAutoDisableAngularThreshold", dReal, [ID]),
+    ("dWorldSetAutoDisableAverageSamplesCount", None, [ID, ctypes.c_uint]),
+    ("dWorldGetAutoDisableAverageSamplesCount", ctypes.c_int, [ID]),
+    ("dWorldSetAutoDisableSteps", None, [ID, ctypes.c_int]), ("dWorldGetAutoDisableSteps", ctypes.c_int, [ID]),
+    ("dWorldSetAutoDisableTime", None, [ID, dReal]), ("dWorldGetAutoDisableTime", dReal, [ID]),
     ("dBodyCreate", ID, [ID]), ("dBodyDestroy", None, [ID]),
     ("dBodySetData", None, [ID, ctypes.c_void_p]), ("dBodyGetData", ctypes.c_void_p, [ID]),
     ("dBodySetPosition", None, [ID, dReal, dReal, dReal]), ("dBodySetRotation", None, [ID, _F]),
@@ -99,6 +106,15 @@ _PROTOS = [
     ("dBodyGetLinearDamping", dReal, [ID]), ("dBodyGetAngularDamping", dReal, [ID]),
     ("dBodyGetLinearDampingThreshold", dReal, [ID]), ("dBodyGetAngularDampingThreshold", dReal, [ID]),
     ("dBodySetMaxAngularSpeed", None, [ID, dReal]), ("dBodyGetMaxAngularSpeed", dReal, [ID]),
+    ("dBodyEnable", None, [ID]), ("dBodyDisable", None, [ID]), ("dBodyIsEnabled", ctypes.c_int, [ID]),
+    ("dBodySetAutoDisableFlag", None, [ID, ctypes.c_int]), ("dBodyGetAutoDisableFlag", ctypes.c_int, [ID]),
+    ("dBodySetAutoDisableLinearThreshold", None, [ID, dReal]), ("dBodyGetAutoDisableLinearThreshold", dReal, [ID]),
+    ("dBodySetAutoDisableAngularThreshold", None, [ID, dReal]), ("dBodyGetAutoDisableAngularThreshold", dReal, [ID]),
+    ("dBodySetAutoDisableAverageSamplesCount", None, [ID, ctypes.c_uint]),
+    ("dBodyGetAutoDisableAverageSamplesCount", ctypes.c_int, [ID]),
+    ("dBodySetAutoDisableSteps", None, [ID, ctypes.c_int]), ("dBodyGetAutoDisableSteps", ctypes.c_int, [ID]),
+    ("dBodySetAutoDisableTime", None, [ID, dReal]), ("dBodyGetAutoDisableTime", dReal, [ID]),
+    ("dBodySetAutoDisableDefaults", None, [ID]),
     ("dMassSetZero", None, [ctypes.POINTER(dMass)]),
     ("dMassSetParameters", None, [ctypes.POINTER(dMass), dReal, dReal, dReal, dReal, dReal, dReal, dReal, dReal,
                                   dReal, dReal]),

@@ -90,6 +90,10 @@ class Scene:
     # world damping defaults copied into every body: linear scale, angular
     # scale, linear threshold, angular threshold, max angular speed
     damping: tuple = (0.0, 0.0, 0.01, 0.01, float("inf"))
+    # world auto-disable defaults copied into every body (None: the reference's
+    # defaults, auto-disable off): flag, linear threshold, angular threshold,
+    # idle steps, idle time, average samples
+    adis: tuple | None = None
 
     @property
     def nb(self) -> int:
@@ -190,6 +194,41 @@ def box_stack(seed: int = 0, n: int = 10) -> Scene:
     gR[:, [0, 5, 10]] = 1.0
     return Scene("box_stack", bodies, cls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
                  dt=0.01, iterations=20, mu=0.5, maxc=4)
+
+
+def sleep_stacks(seed: int = 0, adis=(1, 0.15, 0.15, 10, 0.0, 1), drop_height: float = 4.0) -> Scene:
+    """Two stacks of three unit boxes 3 m apart on the plane z = 0 and a
+    fourth unit box dropped from `drop_height` onto the first stack, slightly
+    off-centre: with auto-disable on, both stacks fall asleep before the drop
+    lands, the struck stack wakes (the dropped box is never idle while it has
+    no contact) and settles again, the other one sleeps throughout."""
+    rng = np.random.default_rng(seed)
+    n = 7
+    pos = np.zeros((n, 3), dtype=np.float32)
+    pos[0:3, 0] = 0.0
+    pos[3:6, 0] = 3.0
+    pos[0:6, 0:2] += rng.uniform(-0.01, 0.01, size=(6, 2)).astype(np.float32)
+    pos[0:6, 2] = 0.5 + np.tile(np.arange(3, dtype=np.float32), 2)
+    pos[6] = (0.05, 0.02, drop_height)
+    yaw = np.deg2rad(rng.uniform(-5.0, 5.0, size=n))
+    yaw[6] = np.deg2rad(10.0)
+    q = np.zeros((n, 4), dtype=np.float32)
+    q[:, 0] = np.cos(yaw / 2)
+    q[:, 3] = np.sin(yaw / 2)
+    m, i1, i2, i3 = mass_box(1.0, 1.0, 1.0, 1.0)
+    bodies = _body_rows(pos, q, m, np.array([i1, i2, i3], dtype=np.float32))
+    ng = n + 1
+    cls = np.full(ng, BOX, dtype=np.int32)
+    cls[-1] = PLANE
+    gbody = np.arange(ng, dtype=np.int32)
+    gbody[-1] = -1
+    gdims = np.zeros((ng, 4), dtype=np.float32)
+    gdims[:n, 0:3] = 1.0
+    gdims[-1] = (0, 0, 1, 0)
+    gR = np.zeros((ng, 12), dtype=np.float32)
+    gR[:, [0, 5, 10]] = 1.0
+    return Scene("sleep_stacks", bodies, cls, gbody, np.zeros((ng, 3), np.float32), gR, gdims,
+                 dt=0.01, iterations=20, mu=0.5, maxc=4, adis=tuple(adis))
 
 
 def pile(n: int = 32768, seed: int = 1, spacing: float = 0.6, jitter: float = 0.05) -> Scene:

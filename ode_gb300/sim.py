@@ -82,6 +82,14 @@ class GBWorld:
         L.dWorldSetLinearDampingThreshold(self.w, lt)
         L.dWorldSetAngularDampingThreshold(self.w, at)
         L.dWorldSetMaxAngularSpeed(self.w, mw)
+        if scene.adis is not None:
+            flag, lin, ang, steps, t, samples = scene.adis
+            L.dWorldSetAutoDisableFlag(self.w, int(flag))
+            L.dWorldSetAutoDisableLinearThreshold(self.w, lin)
+            L.dWorldSetAutoDisableAngularThreshold(self.w, ang)
+            L.dWorldSetAutoDisableSteps(self.w, int(steps))
+            L.dWorldSetAutoDisableTime(self.w, t)
+            L.dWorldSetAutoDisableAverageSamplesCount(self.w, int(samples))
         self.space = None
         if scene.nb > BULK_BODIES:
             self._build_bulk(scene)

@@ -310,6 +310,60 @@ static void mode_loop() {
     dWorldDestroy(w);
 }
 
+// ---------------------------------------------------------------- sleep
+// The loop of mode_loop with auto-disable on in the world (flag, linear and
+// angular thresholds, steps, time, average samples, read after the geoms):
+// per step the poses and every body's dBodyIsEnabled.
+static void mode_sleep() {
+    int nb = rdi(), ng = rdi(), nsteps = rdi(), iters = rdi(), dyn = rdi(), maxc = rdi(), mode = rdi();
+    int minlevel = rdi(), maxlevel = rdi();
+    WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
+    float surf[8]; rd(surf, 8);
+    std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
+    std::vector<int> gcls(ng), gbody(ng);
+    std::vector<float> gpos(3 * ng), gR(12 * ng), gdims(4 * ng);
+    rd(gcls.data(), ng); rd(gbody.data(), ng); rd(gpos.data(), gpos.size()); rd(gR.data(), gR.size()); rd(gdims.data(), gdims.size());
+    float adis[6]; rd(adis, 6);
+    dWorldID w = dWorldCreate();
+    apply_params(w, P, iters, dyn);
+    dWorldSetAutoDisableFlag(w, adis[0] != 0);
+    dWorldSetAutoDisableLinearThreshold(w, adis[1]);
+    dWorldSetAutoDisableAngularThreshold(w, adis[2]);
+    dWorldSetAutoDisableSteps(w, (int)adis[3]);
+    dWorldSetAutoDisableTime(w, adis[4]);
+    dWorldSetAutoDisableAverageSamplesCount(w, (unsigned)adis[5]);
+    std::vector<dBodyID> b(nb);
+    for (int i = 0; i < nb; i++) { b[i] = dBodyCreate(w); set_body(b[i], &bodies[BODY_IN * i]); }
+    dSpaceID sp = dHashSpaceCreate(0);
+    dHashSpaceSetLevels(sp, minlevel, maxlevel);
+    for (int i = 0; i < ng; i++) {
+        dGeomID g = make_geom(sp, gcls[i], &gpos[3 * i], &gR[12 * i], &gdims[4 * i]);
+        if (gbody[i] >= 0) dGeomSetBody(g, b[gbody[i]]);
+    }
+    LoopCtx L; L.world = w; L.group = dJointGroupCreate(0); L.maxc = maxc; L.mode = mode;
+    memcpy(L.surf, surf, sizeof surf); L.bodies = &b;
+    std::vector<float> traj((size_t)nsteps * nb * 7);
+    std::vector<int> en((size_t)nsteps * nb);
+    for (int s = 0; s < nsteps; s++) {
+        L.made.clear(); L.made_b.clear();
+        dSpaceCollide(sp, &L, &loop_cb);
+        dWorldQuickStep(w, P.dt);
+        dJointGroupEmpty(L.group);
+        for (int i = 0; i < nb; i++) {
+            const dReal *p = dBodyGetPosition(b[i]), *q = dBodyGetQuaternion(b[i]);
+            float *o = &traj[((size_t)s * nb + i) * 7];
+            for (int j = 0; j < 3; j++) o[j] = (float)p[j];
+            for (int j = 0; j < 4; j++) o[3 + j] = (float)q[j];
+            en[(size_t)s * nb + i] = dBodyIsEnabled(b[i]);
+        }
+    }
+    wr(traj.data(), traj.size());
+    wr(en.data(), en.size());
+    dJointGroupDestroy(L.group);
+    dSpaceDestroy(sp);
+    dWorldDestroy(w);
+}
+
 // ---------------------------------------------------------------- chain
 static void mode_chain() {
     int nb = rdi(), nj = rdi(), nsteps = rdi(), iters = rdi(), dyn = rdi();
@@ -386,6 +440,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[1], "step")) mode_step();
     else if (!strcmp(argv[1], "loop")) mode_loop();
     else if (!strcmp(argv[1], "chain")) mode_chain();
+    else if (!strcmp(argv[1], "sleep")) mode_sleep();
     else { fprintf(stderr, "bad mode\n"); return 2; }
     dCloseODE();
     fclose(fin); fclose(fout);

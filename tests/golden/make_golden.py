@@ -393,6 +393,33 @@ def gen_damped(exes):
     gen_joint_scene(exes, sc, "damped.npz")
 
 
+def gen_sleep(exes):
+    """Auto-disable in the reference's loop (no-reorder build): two box
+    stacks that fall asleep, one struck by a dropped box and woken, for two
+    sets of auto-disable parameters (instantaneous velocity over 10 idle
+    steps; a 4-sample average over 5 idle steps and 0.05 s): poses and
+    dBodyIsEnabled per step."""
+    out = {}
+    for tag, adis in (("a", (1, 0.15, 0.15, 10, 0.0, 1)), ("b", (1, 0.02, 0.05, 5, 0.05, 4))):
+        sc = scenes.sleep_stacks(seed=0, adis=adis)
+        nsteps = 300
+        hdr = np.array([sc.nb, sc.ng, nsteps, sc.iterations, 0, sc.maxc, sc.surface_mode,
+                        sc.hash_levels[0], sc.hash_levels[1]], np.int32)
+        r = Reader(run(exes["single_noreorder"], "sleep",
+                       [hdr, sc.world_params(), sc.surface(), sc.bodies, sc.geom_cls, sc.geom_body, sc.geom_pos,
+                        sc.geom_R, sc.geom_dims, np.asarray(adis, np.float32)]))
+        traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
+        en = r.take(np.int32, nsteps * sc.nb).reshape(nsteps, sc.nb)
+        assert r.done()
+        out[f"{tag}_adis"] = np.asarray(adis, np.float32)
+        out[f"{tag}_traj"] = traj
+        out[f"{tag}_enabled"] = en
+        asleep = (en == 0).sum(axis=1)
+        print(f"sleep {tag}: asleep bodies at steps 0,10,20,50,80,100,150,200,299: "
+              f"{asleep[[0, 10, 20, 50, 80, 100, 150, 200, 299]].tolist()}")
+    np.savez_compressed(os.path.join(HERE, "sleep.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -413,6 +440,8 @@ def main():
         gen_hinge2(exes)
     if a.only in ("", "damped"):
         gen_damped(exes)
+    if a.only in ("", "sleep"):
+        gen_sleep(exes)
 
 
 if __name__ == "__main__":
