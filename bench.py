@@ -45,6 +45,9 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s at LCP residual \u22641e-4: plain GPU PGS vs learned warm start, 1 GB300"
 B_ROW = 132        # algorithmic bytes per PGS row-iteration
 B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
+# DRAM bytes per k_pgs launch on the settled 32,768-body pile, measured with ncu (mean of two
+# launches: 238.0 + 2.4 MB and 203.9 + 0.3 MB): the rows stay in L2 across sweeps
+PGS_TRAFFIC = 2.223e8
 
 
 def parse():
@@ -71,6 +74,8 @@ def parse():
     ap.add_argument("--chains", type=int, default=8192, help="batched leg: independent capsule chains")
     ap.add_argument("--vehicles", type=int, default=65536, help="batched leg: independent vehicle worlds (0: skip)")
     ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
+    ap.add_argument("--from-settled", action="store_true",
+                    help="start the pile from ode_gb300/data/pile32768_settled.npz instead of settling (profiling)")
     ap.add_argument("--ref-sweeps", type=int, default=1500,
                     help="reference arm: SOR sweeps per step (cold starts need ~1000-1500 to reach the target)")
     ap.add_argument("--weights", default=None, help="learned warm start parameters (.npz)")
@@ -249,9 +254,16 @@ def run_gbode(args, ws, rank, local):
     if args.warm_scale > 0:
         L.gbodeWorldSetWarmStart(w.w, 1, args.warm_scale)
     L.dWorldSetQuickStepW(w.w, args.sor_w)
-    # settle with the configured 30 sweeps per step (untimed)
-    for _ in range(args.settle):
-        w.step_fused()
+    if args.from_settled:
+        with np.load(SETTLED) as z:
+            st = w.state()
+            st[:, 0:3], st[:, 3:7], st[:, 19:22], st[:, 22:25] = z["pos"], z["q"], z["lvel"], z["avel"]
+            st[:, 7:19] = scenes.quat_to_R(z["q"])
+        w.set_state(st)
+    else:
+        # settle with the configured 30 sweeps per step (untimed)
+        for _ in range(args.settle):
+            w.step_fused()
     w.sync()
     L.gbodeWorldSetResidualTarget(w.w, args.target, args.check_every, args.max_iters)
     L.gbodeWorldSetTiming(w.w, 1)
@@ -348,7 +360,9 @@ def run_gbode(args, ws, rank, local):
                    "contact_rows_per_s": float(np.sum(rows)) / (total_ms / 1e3),
                    "solve_share": pgs_s * 1e3 / total_ms},
         "roofline": {"bound": "hbm", "kernel": "gb::k_pgs", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": PGS_TRAFFIC,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean of two k_pgs "
+                                       "launches from the settled pile (profiles/k_pgs_pile32768_dram.md)",
                      "algorithmic_bytes_per_launch": pgs_bytes / args.steps},
         "clocks": clk,
         "gpu_launches": launches,
