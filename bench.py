@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--chains", type=int, default=8192, help="batched leg: independent capsule chains")
     ap.add_argument("--vehicles", type=int, default=65536, help="batched leg: independent vehicle worlds (0: skip)")
     ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
+    ap.add_argument("--pgs-blocks", type=int, default=0, help="thread blocks of the PGS kernel (0: one per SM)")
+    ap.add_argument("--passes", type=int, default=1, help="passes over a manifold's rows per visit")
     ap.add_argument("--from-settled", action="store_true",
                     help="start the pile from ode_gb300/data/pile32768_settled.npz instead of settling (profiling)")
     ap.add_argument("--ref-sweeps", type=int, default=1500,
@@ -254,6 +256,9 @@ def run_gbode(args, ws, rank, local):
     if args.warm_scale > 0:
         L.gbodeWorldSetWarmStart(w.w, 1, args.warm_scale)
     L.dWorldSetQuickStepW(w.w, args.sor_w)
+    if args.pgs_blocks:
+        L.gbodeWorldSetSolverBlocks(w.w, args.pgs_blocks)
+    L.gbodeWorldSetManifoldPasses(w.w, args.passes)
     if args.from_settled:
         with np.load(SETTLED) as z:
             st = w.state()

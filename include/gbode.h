@@ -98,6 +98,14 @@ dReal dWorldGetERP(dWorldID w);
 void dWorldSetCFM(dWorldID w, dReal cfm);
 dReal dWorldGetCFM(dWorldID w);
 int dWorldQuickStep(dWorldID w, dReal stepsize);
+/* dWorldStep (ode.cpp:1828-1845, step.cpp): the rows as dWorldQuickStep forms
+ * them, then for every island (bodies connected by this step's contact joints
+ * and ball/hinge/hinge2 joints) the dense mixed LCP A lambda = b + w,
+ * A = J M^-1 J^T + diag(cfm), solved exactly on the device as the reference's
+ * Dantzig solver defines it (friction rows bounded by the normal multipliers
+ * of the problem without them), FP64 with FP32 factorisations; one thread
+ * block per island, at most 2048 rows an island.  Contact joints from
+ * dJointCreateContact only.  Returns 0 on failure (gbodeGetLastError). */
 int dWorldStep(dWorldID w, dReal stepsize);
 void dWorldSetQuickStepNumIterations(dWorldID w, int num);
 int dWorldGetQuickStepNumIterations(dWorldID w);
@@ -339,6 +347,21 @@ void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int 
 /* Warm start: 0 = cold (lambda = 0, the reference default), 1 = previous-step
  * lambda of the same (geom pair, contact slot) scaled by `scale`. */
 void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale);
+
+/* Thread blocks of the coloured solver's persistent kernel (256 threads
+ * each; 0 or more than the SM count: one per SM).  Fewer blocks make each
+ * colour's grid barrier cheaper; a colour with more manifolds than the
+ * blocks' threads relaxes the rest from global memory. */
+void gbodeWorldSetSolverBlocks(dWorldID w, int blocks);
+int gbodeWorldGetSolverBlocks(dWorldID w);
+
+/* Passes over a constraint group's rows (a contact manifold's normal rows,
+ * then its friction rows; a joint's rows in order) each time the coloured
+ * solver visits it in a sweep (1 to 16; default 1).  Repeating the strongly
+ * coupled rows of one manifold while they are in registers is a Gauss-Seidel
+ * order with repetition; it can lower the sweeps a residual target needs. */
+void gbodeWorldSetManifoldPasses(dWorldID w, int passes);
+int gbodeWorldGetManifoldPasses(dWorldID w);
 
 /* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
  * creation without leaving the device.  Equivalent to dSpaceCollide with a near

@@ -16,7 +16,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libgbode.so")
-SOURCES = ["api.cpp", "collide.cu", "solve.cu", "scan.cu", "noalloc.cu", "mlp.cu", "sleep.cu"]
+SOURCES = ["api.cpp", "collide.cu", "solve.cu", "scan.cu", "noalloc.cu", "mlp.cu", "sleep.cu", "dantzig.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default"]

@@ -59,7 +59,7 @@ void Workspace::release() {
                    &b_R, &b_lvel, &b_avel, &b_facc, &b_tacc, &b_Ib, &b_invIb, &b_invIw, &b_fc, &b_rt, &b_fa, &r_J1l,
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
-                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &w_keys, &w_lambda,
+                   &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &d_off, &d_scr, &d_iscr, &d_rloc, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
@@ -638,6 +638,10 @@ void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int 
     w->P.max_iterations = max_iterations;
 }
 void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode = mode; w->P.warm_scale = scale; }
+void gbodeWorldSetSolverBlocks(dWorldID w, int blocks) { w->P.pgs_blocks = blocks > 0 ? blocks : 0; }
+void gbodeWorldSetManifoldPasses(dWorldID w, int passes) { w->P.pgs_passes = passes > 1 ? (passes > 16 ? 16 : passes) : 1; }
+int gbodeWorldGetManifoldPasses(dWorldID w) { return w->P.pgs_passes > 1 ? w->P.pgs_passes : 1; }
+int gbodeWorldGetSolverBlocks(dWorldID w) { return w->P.pgs_blocks > 0 && w->P.pgs_blocks < num_sms() ? w->P.pgs_blocks : num_sms(); }
 
 int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
     if (!enabled) { w->P.learned = 0; return 1; }
@@ -1850,8 +1854,6 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     return 1;
 }
 
-// dWorldStep (the Dantzig LCP stepper, ode.cpp:1828-1845) is outside this
-// library's path; it runs the quickstep solver with a large iteration count.
 static void drop_graph(dxWorld *w) {
     if (w->gexec) cudaGraphExecDestroy(w->gexec);
     if (w->graph) cudaGraphDestroy(w->graph);
@@ -1931,12 +1933,120 @@ int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const d
     return ok;
 }
 
+// dWorldStep (ode.cpp:1828-1845, step.cpp): the rows of the step as for
+// dWorldQuickStep, then one dense LCP per island solved exactly on the device
+// (dantzig.cu), then the same integration.  Islands (util.cpp:724-860) are the
+// connected components of the bodies through this step's contact joints and
+// the ball/hinge/hinge2 joints; the static environment joins nothing.
 int dWorldStep(dWorldID w, dReal stepsize) {
-    int it = w->P.iterations;
-    w->P.iterations = 200;
-    int r = dWorldQuickStep(w, stepsize);
-    w->P.iterations = it;
-    return r;
+    if (!world_upload(w)) return 0;
+    Workspace &ws = w->ws;
+    SolverParams P = w->P;
+    P.dt = stepsize;
+    P.warm_mode = 0;
+    P.learned = 0;
+    P.learn_capture = 0;
+    cudaStream_t s = w->stream;
+    if (w->device_contacts) {
+        set_error("dWorldStep: steps contact joints made by dJointCreateContact, not device contacts");
+        return 0;
+    }
+    std::vector<dxJoint *> js;
+    for (dxJoint *j : w->joints) if (j->attached && j->type == dJointTypeContact) js.push_back(j);
+    if (!upload_joint_table(w)) { set_error("dWorldStep: joint table upload"); return 0; }
+    if (!upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
+    if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
+    const int nb = (int)w->bodies.size();
+    std::vector<dxJoint *> awake_js;
+    const std::vector<dxJoint *> *solved = &js;
+    if (ws.sleep_on) {
+        if (!launch_sleep(ws, nb, stepsize, s)) { set_error("dWorldStep: sleep stage", cudaGetLastError()); return 0; }
+        std::vector<int> asleep(nb > 0 ? nb : 1);
+        if (nb > 0) cudaMemcpyAsync(asleep.data(), ws.b_asleep.p, 4 * (size_t)nb, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("dWorldStep: sleep stage"); return 0; }
+        for (dxJoint *j : js) {
+            const dxBody *b = j->b1 ? j->b1 : j->b2;
+            if (b && !asleep[b->index]) awake_js.push_back(j);
+        }
+        if (!upload_host_contacts(w, awake_js)) { set_error("upload contacts"); return 0; }
+        ws.sleep_precomputed = true;
+        solved = &awake_js;
+    }
+    if (w->timing) cudaEventRecord(w->ev[2], s);
+    if (!assemble_step(ws, nb, P, s)) { set_error("dWorldStep: assembly", cudaGetLastError()); return 0; }
+    // row ranges: contacts in order (rows per contact from getInfo1), then the
+    // joints' rows after all contact rows (row counts from the device)
+    const std::vector<dxJoint *> &sj = *solved;
+    const int nc = (int)sj.size(), nj = ws.njoints;
+    std::vector<int> crs(nc + 1, 0);
+    for (int k = 0; k < nc; k++) crs[k + 1] = crs[k] + host_contact_m(sj[k]->contact.surface);
+    std::vector<int> jm(nj > 0 ? nj : 1), jr(nj > 0 ? nj : 1);
+    std::vector<int4> jinfo(nj > 0 ? nj : 1);
+    if (nj > 0) {
+        cudaMemcpyAsync(jm.data(), ws.j_m.p, 4 * (size_t)nj, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(jr.data(), ws.j_rstart.p, 4 * (size_t)nj, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(jinfo.data(), ws.j_info.p, 16 * (size_t)nj, cudaMemcpyDeviceToHost, s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("dWorldStep: row counts"); return 0; }
+    // components (union-find over bodies)
+    std::vector<int> parent(nb > 0 ? nb : 1);
+    for (int i = 0; i < nb; i++) parent[i] = i;
+    auto find = [&](int x) {
+        while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
+        return x;
+    };
+    auto unite = [&](int a, int b) {
+        if (a < 0 || b < 0) return;
+        a = find(a); b = find(b);
+        if (a != b) parent[a > b ? a : b] = a > b ? b : a;
+    };
+    for (const dxJoint *j : sj) unite(j->b1 ? j->b1->index : -1, j->b2 ? j->b2->index : -1);
+    for (int k = 0; k < nj; k++)
+        if (jm[k] > 0) unite(jinfo[k].y, jinfo[k].z);
+    std::vector<std::vector<int>> rows_of(nb > 0 ? nb : 1);
+    for (int k = 0; k < nc; k++) {
+        const dxJoint *j = sj[k];
+        const int b = j->b1 ? j->b1->index : (j->b2 ? j->b2->index : -1);
+        if (b < 0) continue;
+        auto &v = rows_of[find(b)];
+        for (int r = crs[k]; r < crs[k + 1]; r++) v.push_back(r);
+    }
+    for (int k = 0; k < nj; k++) {
+        if (jm[k] <= 0) continue;
+        const int b = jinfo[k].y >= 0 ? jinfo[k].y : jinfo[k].z;
+        if (b < 0) continue;
+        auto &v = rows_of[find(b)];
+        for (int r = 0; r < jm[k]; r++) v.push_back(crs[nc] + jr[k] + r);
+    }
+    std::vector<int> order, start(1, 0);
+    for (int i = 0; i < nb; i++) {
+        if (rows_of[i].empty()) continue;
+        order.insert(order.end(), rows_of[i].begin(), rows_of[i].end());
+        start.push_back((int)order.size());
+    }
+    if (w->timing) cudaEventRecord(w->ev[0], s);
+    if (!launch_dantzig(ws, order, start, s)) { set_error("dWorldStep: island solve", cudaGetLastError()); return 0; }
+    if (w->timing) cudaEventRecord(w->ev[1], s);
+    if (!launch_integrate(ws, nb, P, s)) { set_error("dWorldStep: integration", cudaGetLastError()); return 0; }
+    if (w->timing) cudaEventRecord(w->ev[3], s);
+    w->host_valid = false;
+    w->stats_pending = true;
+    w->last_host_contacts = (int)js.size();
+    bool any_fb = false;
+    for (dxJoint *j : sj) if (j->feedback) { any_fb = true; break; }
+    if (any_fb) {
+        std::vector<float> fb;
+        contact_feedback(ws, (int)sj.size(), fb, s);
+        for (size_t k = 0; k < sj.size(); k++) {
+            dJointFeedback *f = sj[k]->feedback;
+            if (!f) continue;
+            const float *o = &fb[16 * k];
+            if (o[3] == 0.f) continue;
+            for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
+            f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
+        }
+    }
+    return 1;
 }
 
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {

@@ -86,6 +86,7 @@ enum : unsigned {
     ERR_NONFINITE = 128u,
     ERR_STAGE_TIMEOUT = 256u,  // a shared-memory staging copy did not complete in time
     ERR_ISLAND_LIMIT = 512u,   // a union-find merge did not settle within the body count
+    ERR_LCP_FAILED = 1024u,    // the dense LCP solve of an island did not finish (its multipliers are zero)
 };
 
 #if defined(__CUDACC__)

@@ -37,6 +37,8 @@ struct SolverParams {
     int solver;  // GBODE_SOLVER_*
     int learned;        // learned warm start (MLP prediction, residual-judged against the plain start)
     int learn_capture;  // record the per-contact features of each step
+    int pgs_blocks;     // thread blocks of the coloured solver (0: one per SM)
+    int pgs_passes;     // passes over a manifold's rows per visit (0 or 1: one)
 };
 
 // learned warm start network (parameter layout in mlp.cu)
@@ -118,6 +120,8 @@ struct Workspace {
     int rows_per_contact = 6;  // row capacity per contact: 3, or 6 when a surface uses rolling friction
     // reference-order schedule
     DBuf i_order, i_start, i_bodies, i_bstart, i_normals;
+    // dense island solves (dWorldStep): scratch offsets, FP64 and int scratch, row -> island index
+    DBuf d_off, d_scr, d_iscr, d_rloc;
     // warm start cache (previous step)
     DBuf w_keys, w_lambda, w_keys_prev, w_lambda_prev;
     // residual
@@ -184,6 +188,17 @@ int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
 bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s);
 // per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
 void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
+
+// ---- dantzig.cu: dWorldStep's dense LCP per island (rows: island by island
+// in `order`, island k = order[start[k] .. start[k+1])), fc accumulated for the
+// islands' bodies; syncs
+#define GB_DANTZIG_MAX_ROWS 2048
+bool launch_dantzig(Workspace &ws, const std::vector<int> &order, const std::vector<int> &start, cudaStream_t s);
+// solve.cu entry points the step drivers share: the rows of a step (body pass,
+// contact and joint rows), the integration, and the rows' view
+bool assemble_step(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s);
+bool launch_integrate(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s);
+Rows rows_view_public(Workspace &ws);
 
 // ---- sleep.cu: auto-disable state buffers; the sleep stage of a step
 bool ensure_sleep(Workspace &ws, int nb, int samples);

@@ -1041,6 +1041,7 @@ struct PgsArgs {
     const int *chunk_start, *chunk_rows;      // [colour][block]
     int learned;      // lambda holds the learned start, lam_alt the plain one: keep the better
     float *lam_alt;
+    int passes;       // passes over a manifold's rows each time it is relaxed (>= 1)
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -1179,14 +1180,16 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
             const int f = __ldg(&A.Rw.findex[r0 + k]);
             fi[k] = (f >= r0 && f < r1) ? f - r0 : (f >= 0 ? GB_MANIFOLD_ROWS + f : -1);
         }
-        for (int k = 0; k < n; k++)
-            if (fi[k] < 0) relax_row_local(A.Rw, r0 + k, lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
-        for (int k = 0; k < n; k++) {
-            if (fi[k] < 0) continue;
-            // findex always names a row of the same contact, hence of this
-            // manifold; a row elsewhere is read from memory
-            const float lf = fi[k] < GB_MANIFOLD_ROWS ? lam[fi[k]] : __ldcg(&A.Rw.lambda[fi[k] - GB_MANIFOLD_ROWS]);
-            relax_row_local(A.Rw, r0 + k, lam[k], lf, true, f1l, f1a, f2l, f2a, two);
+        for (int pass = 0; pass < A.passes; pass++) {
+            for (int k = 0; k < n; k++)
+                if (fi[k] < 0) relax_row_local(A.Rw, r0 + k, lam[k], 0.f, false, f1l, f1a, f2l, f2a, two);
+            for (int k = 0; k < n; k++) {
+                if (fi[k] < 0) continue;
+                // findex always names a row of the same contact, hence of this
+                // manifold; a row elsewhere is read from memory
+                const float lf = fi[k] < GB_MANIFOLD_ROWS ? lam[fi[k]] : __ldcg(&A.Rw.lambda[fi[k] - GB_MANIFOLD_ROWS]);
+                relax_row_local(A.Rw, r0 + k, lam[k], lf, true, f1l, f1a, f2l, f2a, two);
+            }
         }
         for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = lam[k];
     } else {
@@ -1370,22 +1373,25 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
     cp_async_wait_all();
     float4 row[8];
 #pragma unroll 1
-    for (int c = 0; c < nct; c++) {
-        const int r = off + 3 * c;
-#pragma unroll
-        for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
-        relax_fast_row<true>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
-    }
+    for (int pass = 0; pass < A.passes; pass++) {
 #pragma unroll 1
-    for (int c = 0; c < nct; c++) {
-        const float ln = lam[3 * c];
-#pragma unroll
-        for (int q = 1; q < 3; q++) {
-            const int r = off + 3 * c + q;
+        for (int c = 0; c < nct; c++) {
+            const int r = off + 3 * c;
 #pragma unroll
             for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
-            const float hi = fabsf(row[3].w * ln);
-            relax_fast_row<true>(row, lam[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
+            relax_fast_row<true>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+        }
+#pragma unroll 1
+        for (int c = 0; c < nct; c++) {
+            const float ln = lam[3 * c];
+#pragma unroll
+            for (int q = 1; q < 3; q++) {
+                const int r = off + 3 * c + q;
+#pragma unroll
+                for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
+                const float hi = fabsf(row[3].w * ln);
+                relax_fast_row<true>(row, lam[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
+            }
         }
     }
 #pragma unroll 1
@@ -1404,10 +1410,13 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
     cp_async_wait_all();
     float4 row[8];
 #pragma unroll 1
-    for (int k = 0; k < n; k++) {
+    for (int pass = 0; pass < A.passes; pass++) {
+#pragma unroll 1
+        for (int k = 0; k < n; k++) {
 #pragma unroll
-        for (int a = 0; a < 8; a++) row[a] = buf[swz(off + k, a)];
-        relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+            for (int a = 0; a < 8; a++) row[a] = buf[swz(off + k, a)];
+            relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+        }
     }
 #pragma unroll 1
     for (int k = 0; k < n; k++) A.Rw.lambda[d.x + k] = lam[k];
@@ -2099,6 +2108,17 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     return true;
 }
 
+bool assemble_step(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
+    cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
+    return assemble(ws, nb, P, s);
+}
+bool launch_integrate(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
+    k_integrate<<<grid_for(nb, 128), 128, 0, s>>>(bodies_view(ws, nb), P);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess;
+}
+Rows rows_view_public(Workspace &ws) { return rows_view(ws); }
+
 bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStream_t s, cudaEvent_t ev0,
                       cudaEvent_t ev1) {
     if (!assemble(ws, nb, P, s)) return false;
@@ -2140,7 +2160,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.m_desc.as<int4>(), ws.j_rstart.as<int>(), ws.j_m.as<int>(),
                                          ws.grp_body.as<int2>());
     // pack the triplet slots' rows chunk by chunk for the solver's blocks
-    const int pgs_blocks = num_sms();
+    const int pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
     const size_t nchunks = (size_t)GB_MAX_COLOURS * pgs_blocks;
     if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.chunk_rows.ensure(nchunks * 4) &&
           ws.chunk_start.ensure(nchunks * 4)))
@@ -2178,6 +2198,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.reform_every = 50;
         A.learned = P.learned;
         A.lam_alt = P.learned ? ws.l_alt.as<float>() : nullptr;
+        A.passes = P.pgs_passes > 1 ? P.pgs_passes : 1;
         A.packed = ws.p_rows.as<float4>();
         A.chunk_start = ws.chunk_start.as<int>();
         A.chunk_rows = ws.chunk_rows.as<int>();

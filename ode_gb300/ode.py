@@ -150,6 +150,8 @@ _PROTOS = [
     ("gbodeWorldSetSolver", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolver", ctypes.c_int, [ID]),
     ("gbodeWorldSetResidualTarget", None, [ID, dReal, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetWarmStart", None, [ID, ctypes.c_int, dReal]),
+    ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
+    ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
     ("gbodeSpaceCollideContacts", ctypes.c_int, [ID, ID, ID, ctypes.POINTER(dSurfaceParameters), ctypes.c_int]),
     ("gbodeHashSpaceSetExactPairs", None, [ID, ctypes.c_int]),
     ("gbodeWorldSetStream", None, [ID, ctypes.c_void_p]), ("gbodeWorldGetStream", ctypes.c_void_p, [ID]),

@@ -223,6 +223,11 @@ class GBWorld:
             raise RuntimeError(L.gbodeGetLastError().decode())
         return 1
 
+    def step_dantzig(self):
+        """One dWorldStep (a dense LCP per island) on the joints alone: no
+        collision (for jointed scenes without geoms)."""
+        return self.L.dWorldStep(self.w, self.scene.dt)
+
     def step_fused(self):
         L = self.L
         if not L.gbodeSpaceCollideContacts(self.space, self.w, self.group, ctypes.byref(self.surface),
@@ -275,9 +280,10 @@ class GBWorld:
         L.dWorldDestroy(self.w)
 
 
-def step_contacts(world: GBWorld, cb: np.ndarray, cs: np.ndarray, mode: int):
-    """One dWorldQuickStep on an explicit contact list (the golden snapshots'
-    contact joints, created and attached in their recorded order)."""
+def step_contacts(world: GBWorld, cb: np.ndarray, cs: np.ndarray, mode: int, stepper: bool = False):
+    """One dWorldQuickStep (dWorldStep with `stepper`) on an explicit contact
+    list (the golden snapshots' contact joints, created and attached in their
+    recorded order)."""
     L = world.L
     c = ode.dContact()
     for k in range(cb.shape[0]):
@@ -294,5 +300,5 @@ def step_contacts(world: GBWorld, cb: np.ndarray, cs: np.ndarray, mode: int):
         b1 = world.bodies[cb[k, 0]] if cb[k, 0] >= 0 else None
         b2 = world.bodies[cb[k, 1]] if cb[k, 1] >= 0 else None
         L.dJointAttach(j, b1, b2)
-    ok = L.dWorldQuickStep(world.w, world.scene.dt)
+    ok = (L.dWorldStep if stepper else L.dWorldQuickStep)(world.w, world.scene.dt)
     return ok

@@ -366,7 +366,10 @@ static void mode_sleep() {
 
 // ---------------------------------------------------------------- chain
 static void mode_chain() {
+    // dyn bit 0: the reference's dynamic iteration rule; bit 1: dWorldStep instead of dWorldQuickStep
     int nb = rdi(), nj = rdi(), nsteps = rdi(), iters = rdi(), dyn = rdi();
+    const bool stepper = (dyn & 2) != 0;
+    dyn &= 1;
     WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
     std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
     const int JC = 20;
@@ -414,7 +417,8 @@ static void mode_chain() {
     const int nh = (int)hinges.size(), nh1 = nh - (int)hinge2s.size();
     std::vector<float> traj((size_t)nsteps * nb * 7), ang((size_t)nsteps * nh);
     for (int s = 0; s < nsteps; s++) {
-        dWorldQuickStep(w, P.dt);
+        if (stepper) dWorldStep(w, P.dt);
+        else dWorldQuickStep(w, P.dt);
         for (int i = 0; i < nb; i++) {
             const dReal *p = dBodyGetPosition(b[i]), *q = dBodyGetQuaternion(b[i]);
             float *o = &traj[((size_t)s * nb + i) * 7];

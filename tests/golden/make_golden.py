@@ -43,13 +43,17 @@ def build(ref: str) -> dict:
     return exes
 
 
-def run(exe: str, mode: str, arrays: list) -> bytes:
+def run(exe: str, mode: str, arrays: list, messages: list | None = None) -> bytes:
+    """Runs gen_golden MODE on the arrays; the reference's messages (stderr)
+    are appended to `messages` when given."""
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
             for a in arrays:
                 f.write(np.ascontiguousarray(a).tobytes())
-        subprocess.check_call([exe, mode, fin, fout])
+        p = subprocess.run([exe, mode, fin, fout], stderr=subprocess.PIPE, text=True, check=True)
+        if messages is not None:
+            messages.append(p.stderr)
         with open(fout, "rb") as f:
             return f.read()
 
@@ -258,11 +262,11 @@ def bodies_from_state(state, sc: scenes.Scene):
     return b
 
 
-def run_step(exe, sc, bodies, cb, cs, iters, dyn, stepper):
+def run_step(exe, sc, bodies, cb, cs, iters, dyn, stepper, messages=None):
     nb, nc = bodies.shape[0], cb.shape[0]
     hdr = np.array([nb, nc, iters, dyn, stepper], np.int32)
     mode = np.full(nc, sc.surface_mode, np.int32)
-    r = Reader(run(exe, "step", [hdr, sc.world_params(), bodies, cb.astype(np.int32), mode, cs]))
+    r = Reader(run(exe, "step", [hdr, sc.world_params(), bodies, cb.astype(np.int32), mode, cs], messages))
     ok = int(r.take(np.int32, 1)[0])
     lam = r.take(np.float32, 3 * nc).reshape(nc, 3)
     raw = r.take(np.float32, 12 * nc).reshape(nc, 12)
@@ -353,13 +357,14 @@ def gen_space_pile(exes):
           f"reference misses, {len(ref_bodies - exact)} extra")
 
 
-def gen_joint_scene(exes, sc, name, iters=200, nsteps=240):
-    """The reference (no-reorder build) steps a jointed scene without geoms:
-    poses per step, then the hinge angles and hinge2 steering angles."""
+def gen_joint_scene(exes, sc, name, iters=200, nsteps=240, stepper=False):
+    """The reference (no-reorder build) steps a jointed scene without geoms
+    (dWorldQuickStep, or dWorldStep with `stepper`): poses per step, then the
+    hinge angles and hinge2 steering angles."""
     jt = np.ascontiguousarray(sc.joints, np.float32)
     damp = np.asarray(sc.damping, np.float32)
     buf = run(exes["single_noreorder"], "chain",
-              [np.array([sc.nb, len(jt), nsteps, iters, 0], np.int32), sc.world_params(),
+              [np.array([sc.nb, len(jt), nsteps, iters, 2 if stepper else 0], np.int32), sc.world_params(),
                sc.bodies.astype(np.float32), jt, damp])
     r = Reader(buf)
     traj = r.take(np.float32, nsteps * sc.nb * 7).reshape(nsteps, sc.nb, 7)
@@ -391,6 +396,40 @@ def gen_damped(exes):
     sc = scenes.chains(6, seed=11, nmin=3, nmax=8, hang=True)
     sc.damping = (0.02, 0.05, 0.05, 0.1, 1.5)
     gen_joint_scene(exes, sc, "damped.npz")
+
+
+def gen_chain_step(exes):
+    """The hanging chains of chain.npz stepped by the reference's dWorldStep
+    (Dantzig LCP per island)."""
+    gen_joint_scene(exes, scenes.chains(6, seed=11, nmin=3, nmax=8, hang=True), "chain_step.npz", stepper=True)
+
+
+def gen_step_dantzig32(exes):
+    """Adds to every step golden the single-precision reference's dWorldStep
+    (Dantzig) multipliers and post-step state of each snapshot, and for both
+    precisions whether the reference's LCP solver reported its internal error
+    (s <= 0: it then zeroes the multipliers it has not reached, lcp.cpp:1087-
+    1096) -- it does on the box stack, whose four coplanar contacts per face
+    make the island's matrix nearly singular."""
+    cases = [("box_stack", scenes.box_stack(seed=0)), ("pile256", scenes.pile(256, seed=3)),
+             ("capsule_pile96", scenes.capsule_pile(96, seed=2))]
+    for name, sc in cases:
+        path = os.path.join(HERE, f"step_{name}.npz")
+        with np.load(path) as z:
+            out = {k: z[k] for k in z.files}
+        for k in range(len(out["snaps"])):
+            bodies = bodies_from_state(out[f"s{k}_pre"], sc)
+            m32, m64 = [], []
+            lam, _, post = run_step(exes["single_noreorder"], sc, bodies, out[f"s{k}_cb"], out[f"s{k}_cs"],
+                                    sc.iterations, 0, 1, m32)
+            run_step(exes["double"], sc, bodies, out[f"s{k}_cb"], out[f"s{k}_cs"], sc.iterations, 0, 1, m64)
+            out[f"s{k}_lambda_dantzig32"], out[f"s{k}_post_dantzig32"] = lam, post
+            err32, err64 = "LCP internal error" in m32[0], "LCP internal error" in m64[0]
+            out[f"s{k}_dantzig_lcp_error"] = np.array([err32, err64], np.int32)
+            d = np.abs(lam - out[f"s{k}_lambda_dantzig"]).max() / max(1.0, float(np.abs(lam).max()))
+            print(f"{name} snapshot {k}: {len(lam)} contacts, single vs double Dantzig lambda {d:.2e}, "
+                  f"LCP error single {err32} double {err64}")
+        np.savez_compressed(path, **out)
 
 
 def gen_sleep(exes):
@@ -442,6 +481,10 @@ def main():
         gen_damped(exes)
     if a.only in ("", "sleep"):
         gen_sleep(exes)
+    if a.only in ("", "chain_step"):
+        gen_chain_step(exes)
+    if a.only in ("", "dantzig32"):
+        gen_step_dantzig32(exes)
 
 
 if __name__ == "__main__":
