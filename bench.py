@@ -422,11 +422,24 @@ def batched_leg(args, L, stream, dev, kind):
                       "sweeps_per_step": float(np.mean(T["sweeps"])), "rows_per_step": float(np.mean(T["rows"])),
                       "contacts_per_step": float(np.mean(T["contacts"])), "colours": int(np.median(T["colours"])),
                       "steps_at_target": ok}
+    # solver settings tuned on the running world (gbodeWorldAutotune), then the residual leg again
+    tu = w.autotune(steps=3, graph=True)
+    for _ in range(args.warmup):
+        w.step_graph()
+    w.sync()
+    T = timed_steps(w, stream, flush, args.steps, graph=True)
+    ms = sum(T["step_ms"])
+    ok = sum(1 for r in T["resid"] if r <= args.target)
+    out["residual_tuned_graph"] = {"body_steps_per_s": sc.nb * ok / (ms / 1e3), "ms_per_step": ms / args.steps,
+                                   "sweeps_per_step": float(np.mean(T["sweeps"])), "steps_at_target": ok,
+                                   "tuning": {"blocks": tu.blocks, "passes": tu.passes,
+                                              "check_every": tu.check_every, "candidates": tu.candidates}}
     r64, _, ml = w.last_residual()
     out["fp64_residual_last_step"] = r64 / max(1.0, ml)
     out["note"] = ("value counts steps at the residual target (residual) or every step at the configured 20 "
                    "sweeps (iterations20); the chains are islands of one world, solved by the same coloured "
-                   "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused)")
+                   "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused); "
+                   "*_tuned: after gbodeWorldAutotune chose the solver blocks, passes per group and check interval")
     w.close()
     return out
 

@@ -431,6 +431,26 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */
 void gbodeWorldSetTiming(dWorldID w, int enabled);
 
+/* Solver settings tuned on the running world.  gbodeWorldAutotune makes one
+ * plain fused step, copies the device-side state aside, and for each
+ * candidate -- solver blocks: one per SM or half as many; passes over a
+ * constraint group's rows per visit: 1, 2, 3; residual checks every 5 or 10
+ * sweeps when a residual target is set -- restores that state and times
+ * `steps` gbodeWorldStepFused steps (after two untimed ones) with CUDA
+ * events.  It keeps the candidate with the lowest median step time, leaves
+ * it set, and restores the state once more: the world continues from the
+ * one plain step.  Returns 1 and the choice in *best, or 0
+ * (gbodeGetLastError). */
+typedef struct gbodeTuning {
+    int blocks;       /* gbodeWorldSetSolverBlocks */
+    int passes;       /* gbodeWorldSetManifoldPasses */
+    int check_every;  /* residual checks every this many sweeps (0: no residual target) */
+    float ms_per_step;
+    int candidates;   /* candidates timed */
+} gbodeTuning;
+int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *s, int maxc,
+                       dReal dt, int steps, int use_graph, gbodeTuning *best);
+
 /* FP64 LCP residual and complementarity error of the last step's solution,
  * evaluated on the device from the step's FP32 rows (unscaled) and lambda:
  * max_i |lambda_i - proj_[lo,hi](lambda_i - (A lambda - b)_i / A_ii)|, not

@@ -16,6 +16,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/gbode.h"
@@ -2046,6 +2047,113 @@ int dWorldStep(dWorldID w, dReal stepsize) {
             f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
         }
     }
+    return 1;
+}
+
+int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *sp, int maxc,
+                       dReal dt, int steps, int use_graph, gbodeTuning *best) {
+    if (!w || !space || !group || !sp || maxc < 1 || !(dt > 0) || steps < 1 || !best) {
+        set_error("gbodeWorldAutotune: bad argument");
+        return 0;
+    }
+    if (!world_init_device(w)) return 0;
+    struct Cand { int blocks, passes, check; };
+    std::vector<Cand> cands;
+    const int sms = num_sms();
+    const bool resid = w->P.residual_target > 0;
+    for (int blocks : {sms, sms / 2})
+        for (int passes : {1, 2, 3})
+            for (int check : {5, 10}) {
+                if (!resid && check != 5) continue;
+                cands.push_back({blocks, passes, resid ? check : 0});
+            }
+    // every candidate starts from the same state: the device-side simulation
+    // state (bodies, warm-start tables, joint multipliers, auto-disable state,
+    // counters) is copied aside once and put back before each candidate and
+    // at the end, so the world leaves the tuner as it entered it
+    if (!world_upload(w)) return 0;
+    if (!w->host_valid) world_download(w);
+    Workspace &ws = w->ws;
+    DBuf *keep[] = {&ws.b_pos, &ws.b_q, &ws.b_R, &ws.b_lvel, &ws.b_avel, &ws.b_facc, &ws.b_tacc, &ws.w_keys,
+                    &ws.w_lambda, &ws.j_lam, &ws.b_adis_i, &ws.b_adis_f, &ws.b_adis_buf};
+    const int nkeep = (int)(sizeof keep / sizeof keep[0]);
+    std::vector<DBuf> copies(nkeep + 1);
+    const bool warm_valid = ws.warm_valid;
+    const unsigned warm_mask = ws.warm_mask;
+    auto save = [&]() -> bool {
+        for (int k = 0; k < nkeep; k++) {
+            if (!keep[k]->p) continue;
+            if (!copies[k].ensure(keep[k]->bytes)) return false;
+            cudaMemcpyAsync(copies[k].p, keep[k]->p, keep[k]->bytes, cudaMemcpyDeviceToDevice, w->stream);
+        }
+        if (!copies[nkeep].ensure(sizeof(DevCounters))) return false;
+        cudaMemcpyAsync(copies[nkeep].p, ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
+        return cudaStreamSynchronize(w->stream) == cudaSuccess;
+    };
+    auto restore = [&]() {
+        for (int k = 0; k < nkeep; k++)
+            if (keep[k]->p && copies[k].p && keep[k]->bytes == copies[k].bytes)
+                cudaMemcpyAsync(keep[k]->p, copies[k].p, keep[k]->bytes, cudaMemcpyDeviceToDevice, w->stream);
+        cudaMemcpyAsync(ws.dc, copies[nkeep].p, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
+        cudaStreamSynchronize(w->stream);
+        ws.warm_valid = warm_valid && ws.warm_mask == warm_mask;
+        w->host_valid = false;
+    };
+    auto release = [&]() { for (DBuf &c : copies) c.release(); };
+    // one plain step settles buffer sizes (a later reallocation would not be restored)
+    const SolverParams saved = w->P;
+    if (!gbodeWorldStepFused(w, space, group, sp, maxc, dt, 0)) return 0;
+    if (cudaStreamSynchronize(w->stream) != cudaSuccess) return 0;
+    if (!save()) { set_error("gbodeWorldAutotune: device allocation"); release(); return 0; }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int timing = w->timing;
+    w->timing = false;
+    float best_ms = INFINITY;
+    int best_i = -1;
+    for (size_t i = 0; i < cands.size(); i++) {
+        restore();
+        w->P.pgs_blocks = cands[i].blocks;
+        w->P.pgs_passes = cands[i].passes;
+        if (resid) w->P.check_every = cands[i].check;
+        std::vector<float> t;
+        for (int k = 0; k < steps + 2; k++) {
+            cudaEventRecord(e0, w->stream);
+            if (!gbodeWorldStepFused(w, space, group, sp, maxc, dt, use_graph)) {
+                w->P = saved;
+                w->timing = timing;
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                restore();
+                release();
+                return 0;
+            }
+            cudaEventRecord(e1, w->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (k >= 2) t.push_back(ms);
+        }
+        std::nth_element(t.begin(), t.begin() + t.size() / 2, t.end());
+        const float med = t[t.size() / 2];
+        if (med < best_ms) { best_ms = med; best_i = (int)i; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    restore();
+    release();
+    w->P = saved;
+    w->timing = timing;
+    const Cand &c = cands[best_i];
+    w->P.pgs_blocks = c.blocks >= sms ? 0 : c.blocks;
+    w->P.pgs_passes = c.passes;
+    if (resid) w->P.check_every = c.check;
+    best->blocks = c.blocks;
+    best->passes = c.passes;
+    best->check_every = c.check;
+    best->ms_per_step = best_ms;
+    best->candidates = (int)cands.size();
     return 1;
 }
 

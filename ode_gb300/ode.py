@@ -49,6 +49,11 @@ class dJointFeedback(ctypes.Structure):
     _fields_ = [("f1", dVector3), ("t1", dVector3), ("f2", dVector3), ("t2", dVector3)]
 
 
+class gbodeTuning(ctypes.Structure):
+    _fields_ = [("blocks", ctypes.c_int), ("passes", ctypes.c_int), ("check_every", ctypes.c_int),
+                ("ms_per_step", ctypes.c_float), ("candidates", ctypes.c_int)]
+
+
 class gbodeStepStats(ctypes.Structure):
     _fields_ = [("contacts", ctypes.c_int), ("rows", ctypes.c_int), ("colours", ctypes.c_int),
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
@@ -152,6 +157,8 @@ _PROTOS = [
     ("gbodeWorldSetWarmStart", None, [ID, ctypes.c_int, dReal]),
     ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
+    ("gbodeWorldAutotune", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p]),
     ("gbodeSpaceCollideContacts", ctypes.c_int, [ID, ID, ID, ctypes.POINTER(dSurfaceParameters), ctypes.c_int]),
     ("gbodeHashSpaceSetExactPairs", None, [ID, ctypes.c_int]),
     ("gbodeWorldSetStream", None, [ID, ctypes.c_void_p]), ("gbodeWorldGetStream", ctypes.c_void_p, [ID]),

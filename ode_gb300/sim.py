@@ -228,6 +228,14 @@ class GBWorld:
         collision (for jointed scenes without geoms)."""
         return self.L.dWorldStep(self.w, self.scene.dt)
 
+    def autotune(self, steps: int = 3, graph: bool = True) -> ode.gbodeTuning:
+        """gbodeWorldAutotune on the fused step (the tuning steps advance the world)."""
+        t = ode.gbodeTuning()
+        if not self.L.gbodeWorldAutotune(self.w, self.space, self.group, ctypes.byref(self.surface), self.scene.maxc,
+                                         self.scene.dt, steps, 1 if graph else 0, ctypes.byref(t)):
+            raise RuntimeError(self.L.gbodeGetLastError().decode())
+        return t
+
     def step_fused(self):
         L = self.L
         if not L.gbodeSpaceCollideContacts(self.space, self.w, self.group, ctypes.byref(self.surface),

@@ -252,3 +252,34 @@ def test_damping_api_round_trip(gblib):
     assert abs(L.dBodyGetLinearDamping(b) - 0.1) < 1e-7
     assert abs(L.dBodyGetAngularDampingThreshold(b) - 0.4) < 1e-6
     L.dWorldDestroy(w)
+
+
+def test_autotune_keeps_a_candidate(gblib):
+    """gbodeWorldAutotune times every candidate on the running chains from
+    the same saved state and leaves the fastest one set; the world comes out
+    exactly as one plain fused step leaves it (a twin world checks this to the
+    bit) and keeps stepping at the residual target."""
+    from ode_gb300 import scenes, sim
+    L = gblib
+    sc = scenes.chains(64, seed=2)
+    w, twin = sim.GBWorld(sc), sim.GBWorld(sc)
+    for x in (w, twin):
+        L.dWorldSetQuickStepW(x.w, 1.0)
+        L.gbodeWorldSetWarmStart(x.w, 1, 1.0)
+        for _ in range(60):
+            x.step_fused()
+        L.gbodeWorldSetResidualTarget(x.w, 1e-4, 5, 3000)
+    t = w.autotune(steps=2, graph=True)
+    twin.step_fused()
+    assert np.array_equal(w.state(), twin.state())
+    twin.close()
+    assert t.candidates == 12 and t.ms_per_step > 0
+    assert t.passes in (1, 2, 3) and t.check_every in (5, 10)
+    assert L.gbodeWorldGetManifoldPasses(w.w) == t.passes
+    assert L.gbodeWorldGetSolverBlocks(w.w) == t.blocks
+    for _ in range(20):
+        w.step_graph()
+    w.sync()
+    assert w.stats().residual <= 1e-4
+    print(f"autotune: blocks {t.blocks}, passes {t.passes}, check every {t.check_every}, {t.ms_per_step:.3f} ms/step")
+    w.close()
