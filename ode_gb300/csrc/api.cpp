@@ -191,7 +191,7 @@ struct dxWorld {
     gbodeStepStats stats{};
     bool stats_pending = false;
     int last_host_contacts = 0;
-    std::vector<dxJoint *> last_fb_joints;
+    std::vector<dxJoint *> table_joints;  // the ball/hinge/hinge2 joints in device-table order
 };
 
 static dxWorld *g_default_world = nullptr;
@@ -1622,8 +1622,35 @@ static bool upload_joint_table(dxWorld *w) {
                                      l0.data(), l1.data(), l2.data(), hv1.data(), hv2.data(), m0.data(),
                                      m1.data(), m2.data()};
     if (!joint_table_upload(w->ws, n, src, w->stream)) return false;
+    w->table_joints = jt;
     w->joints_dirty = false;
     return true;
+}
+
+// Joint feedback of the last step (quickstep.cpp:3108-3181, the same for
+// dWorldStep): F = J^T lambda for every contact joint in `cj` (the step's
+// solved contact joints, in row order) and every ball/hinge/hinge2 joint
+// with a dJointFeedback; a joint that was not solved (its component sleeps)
+// keeps what it had.
+static void write_feedback(dxWorld *w, const std::vector<dxJoint *> &cj) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(w->stream, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+        return;  // a step being recorded into a graph: the launch that runs it reads the feedback
+    bool any = false;
+    for (dxJoint *j : cj) if (j->feedback) { any = true; break; }
+    for (dxJoint *j : w->table_joints) if (j->feedback) { any = true; break; }
+    if (!any) return;
+    std::vector<float> fb;
+    const int nc = (int)cj.size(), nj = (int)w->table_joints.size();
+    joint_feedback(w->ws, nc, nj, fb, w->stream);
+    for (int k = 0; k < nc + nj; k++) {
+        dJointFeedback *f = k < nc ? cj[k]->feedback : w->table_joints[k - nc]->feedback;
+        if (!f) continue;
+        const float *o = &fb[16 * (size_t)k];
+        if (o[3] == 0.f) continue;
+        for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
+        f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
+    }
 }
 
 // ------------------------------------------------------------------ stepping
@@ -1836,22 +1863,7 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     w->host_valid = false;
     w->stats_pending = true;
     w->last_host_contacts = (int)js.size();
-    // joint feedback (quickstep.cpp:3108-3181): F = J^T lambda per contact
-    // (a contact of a sleeping component is not solved; its feedback is left as it was)
-    bool any_fb = false;
-    for (dxJoint *j : *solved) if (j->feedback) { any_fb = true; break; }
-    if (any_fb) {
-        std::vector<float> fb;
-        contact_feedback(ws, (int)solved->size(), fb, s);
-        for (size_t k = 0; k < solved->size(); k++) {
-            dJointFeedback *f = (*solved)[k]->feedback;
-            if (!f) continue;
-            const float *o = &fb[16 * k];
-            if (o[3] == 0.f) continue;
-            for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
-            f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
-        }
-    }
+    write_feedback(w, *solved);
     return 1;
 }
 
@@ -1901,6 +1913,7 @@ int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const d
         w->last_host_contacts = 0;
         w->device_contacts = false;
         w->device_surfaces = 1;
+        write_feedback(w, {});
         return 1;
     }
     if (clean && key == w->graph_key && w->graph_state == 1) {
@@ -1924,6 +1937,7 @@ int gbodeWorldStepFused(dWorldID w, dSpaceID space, dJointGroupID group, const d
         w->graph_state = 2;
         e = cudaGraphLaunch(ex, w->stream);  // run the step just recorded
         if (e != cudaSuccess) { set_error("gbodeWorldStepFused: graph launch", e); drop_graph(w); return 0; }
+        write_feedback(w, {});
         return 1;
     }
     // a plain step settles buffer sizes and uploads; the next call captures
@@ -2033,20 +2047,7 @@ int dWorldStep(dWorldID w, dReal stepsize) {
     w->host_valid = false;
     w->stats_pending = true;
     w->last_host_contacts = (int)js.size();
-    bool any_fb = false;
-    for (dxJoint *j : sj) if (j->feedback) { any_fb = true; break; }
-    if (any_fb) {
-        std::vector<float> fb;
-        contact_feedback(ws, (int)sj.size(), fb, s);
-        for (size_t k = 0; k < sj.size(); k++) {
-            dJointFeedback *f = sj[k]->feedback;
-            if (!f) continue;
-            const float *o = &fb[16 * k];
-            if (o[3] == 0.f) continue;
-            for (int q = 0; q < 3; q++) { f->f1[q] = o[q]; f->t1[q] = o[4 + q]; f->f2[q] = o[8 + q]; f->t2[q] = o[12 + q]; }
-            f->f1[3] = f->t1[3] = f->f2[3] = f->t2[3] = 0;
-        }
-    }
+    write_feedback(w, sj);
     return 1;
 }
 

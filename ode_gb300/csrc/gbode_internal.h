@@ -186,8 +186,10 @@ int learn_samples(Workspace &ws, float *out, int cap, cudaStream_t s);
 // ball/hinge/hinge2 joint table: src = info, anchor1, anchor2, axis1, axis2, qrel, limot 0-2,
 // hinge2 v1(+s0), v2(+c0), second limot 0-2 (n each)
 bool joint_table_upload(Workspace &ws, int n, const std::vector<const void *> &src, cudaStream_t s);
-// per-contact joint feedback (f1 t1 f2 t2) of the last step into host array (syncs)
-void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s);
+// joint feedback (f1 t1 f2 t2, 16 floats a record; word 3 = 1 when solved) of the
+// last step into a host array: the ncontacts contacts, then the njoints
+// ball/hinge/hinge2 joints of the joint table (syncs)
+void joint_feedback(Workspace &ws, int ncontacts, int njoints, std::vector<float> &out, cudaStream_t s);
 
 // ---- dantzig.cu: dWorldStep's dense LCP per island (rows: island by island
 // in `order`, island k = order[start[k] .. start[k+1])), fc accumulated for the

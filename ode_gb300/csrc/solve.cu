@@ -1861,14 +1861,15 @@ __global__ void k_res_rows(Rows Rw, Bodies B, const int *nrows_dev, const double
 }
 
 // joint feedback per contact: f = J^T lambda with the unscaled rows
-// (orig: solver contact -> caller's contact index when sleeping compacted the
-// list, else null); word 3 of a contact's record is set to 1 when it was solved
-__global__ void k_feedback(Rows Rw, const int *nrows_dev, const int *orig, float *fb) {
+// Records: the contacts' first (orig: solver contact -> caller's contact index
+// when sleeping compacted the list, else null), then the ball/hinge/hinge2
+// joints' from record nc on; word 3 of a record is set to 1 when it was solved
+__global__ void k_feedback(Rows Rw, const int *nrows_dev, const int *orig, int nc, float *fb) {
     int n = *nrows_dev;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int c = Rw.contact[r];
-        if (c < 0) continue;  // a ball/hinge joint's row
-        if (orig) c = orig[c];
+        if (c < 0) c = nc + (-1 - c);  // joint k's row: owner -1 - k
+        else if (orig) c = orig[c];
         const int2 b = Rw.body[r];
         const float l = Rw.lambda[r] / Rw.Ad[r];
         float4 a = Rw.J1l[r], d = Rw.J1a[r];
@@ -2355,16 +2356,17 @@ int copy_last_rows(Workspace &ws, float *rows, int cap, cudaStream_t s) {
     return n;
 }
 
-void contact_feedback(Workspace &ws, int ncontacts, std::vector<float> &out, cudaStream_t s) {
-    out.assign((size_t)ncontacts * 16, 0.f);
-    if (ncontacts <= 0) return;
+void joint_feedback(Workspace &ws, int ncontacts, int njoints, std::vector<float> &out, cudaStream_t s) {
+    const size_t nrec = (size_t)ncontacts + (size_t)njoints;
+    out.assign(nrec * 16, 0.f);
+    if (nrec == 0) return;
     DBuf &tmp = ws.res_f;
-    tmp.ensure((size_t)ncontacts * 64);
-    cudaMemsetAsync(tmp.p, 0, (size_t)ncontacts * 64, s);
+    tmp.ensure(nrec * 64);
+    cudaMemsetAsync(tmp.p, 0, nrec * 64, s);
     k_feedback<<<4 * num_sms(), 256, 0, s>>>(rows_view(ws), &ws.dc->nrows, ws.use_awake ? ws.c_orig.as<int>() : nullptr,
-                                             tmp.as<float>());
+                                             ncontacts, tmp.as<float>());
     count_launch();
-    cudaMemcpyAsync(out.data(), tmp.p, (size_t)ncontacts * 64, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(out.data(), tmp.p, nrec * 64, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
 }
 

@@ -283,3 +283,48 @@ def test_autotune_keeps_a_candidate(gblib):
     assert w.stats().residual <= 1e-4
     print(f"autotune: blocks {t.blocks}, passes {t.passes}, check every {t.check_every}, {t.ms_per_step:.3f} ms/step")
     w.close()
+
+
+def test_joint_feedback_of_a_hanging_chain(gblib):
+    """dJointFeedback on ball joints (quickstep.cpp:3108-3181), in a static
+    case: four spheres hanging straight down from the environment, each ball
+    joint carries the weight below it -- f1 (on the upper sphere) is +m g of
+    the spheres below and the joint's own sphere, f2 the opposite -- for plain
+    steps and graph-replayed steps."""
+    from ode_gb300 import ode, scenes, sim
+    L = gblib
+    n = 4
+    masses = np.array([1.0, 2.0, 1.5, 0.5], np.float32)
+    pos = np.zeros((n, 3), np.float32)
+    pos[:, 2] = 5.0 - 0.5 * np.arange(n)
+    q = np.tile(np.array([1, 0, 0, 0], np.float32), (n, 1))
+    bodies = np.zeros((n, 20), np.float32)
+    bodies[:, 0:3], bodies[:, 3:7], bodies[:, 13] = pos, q, masses
+    bodies[:, 14:17] = 0.4 * masses[:, None] * 0.1 ** 2
+    joints = np.zeros((n, scenes.JOINT_COLS), np.float32)
+    for k in range(n):
+        joints[k, 0:3] = (1, k, k - 1 if k > 0 else -1)
+        joints[k, 3:6] = (0.0, 0.0, pos[k, 2] + 0.25)
+    z = np.zeros(0, np.int32)
+    sc = scenes.Scene("hanging", bodies, z, z, np.zeros((0, 3), np.float32), np.zeros((0, 12), np.float32),
+                      np.zeros((0, 4), np.float32), dt=1 / 240, iterations=20, joints=joints)
+    w = sim.GBWorld(sc)
+    L.dWorldSetQuickStepW(w.w, 1.0)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    L.gbodeWorldSetResidualTarget(w.w, 1e-7, 5, 3000)
+    fbs = [ode.dJointFeedback() for _ in w.joints]
+    for j, fb in zip(w.joints, fbs):
+        L.dJointSetFeedback(j, ctypes.byref(fb))
+    g = abs(sc.gravity[2])
+    for label, stepper in (("plain", w.step_fused), ("graph", w.step_graph)):
+        for _ in range(60):
+            stepper()
+        for k, fb in enumerate(fbs):
+            below = float(masses[k:].sum()) * g
+            print(f"{label}: joint {k} f1 z {fb.f1[2]:.4f} N, f2 z {fb.f2[2]:.4f} N, weight carried {below:.4f} N")
+            # joint k attaches sphere k (body 1) to sphere k-1 above (body 2)
+            assert abs(fb.f1[2] - below) <= 1e-3 * below
+            if k > 0:
+                assert abs(fb.f2[2] + below) <= 1e-3 * below
+            assert abs(fb.f1[0]) < 1e-3 and abs(fb.f1[1]) < 1e-3
+    w.close()
