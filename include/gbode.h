@@ -107,6 +107,16 @@ int dWorldQuickStep(dWorldID w, dReal stepsize);
  * block per island, at most 2048 rows an island.  Contact joints from
  * dJointCreateContact only.  Returns 0 on failure (gbodeGetLastError). */
 int dWorldStep(dWorldID w, dReal stepsize);
+
+/* The dense LCP solver of dWorldStep for a batch of problems given directly
+ * (the role of the reference's internal dSolveLCP, lcp.cpp:836-1160): for
+ * each problem p, A x = b + w with A = A[p] (n x n, row-major, symmetric
+ * positive definite), the first nub variables unbounded, the rest in
+ * [lo, hi] with x = lo => w >= 0, x = hi => w <= 0, else w = 0; findex
+ * (optional) as in dWorldStep.  FP64 in and out, one thread block a problem,
+ * n <= 2048.  Host arrays; returns 0 if a problem did not solve. */
+int gbodeSolveLCPBatch(int count, int n, const double *A, const double *b, const double *lo, const double *hi, int nub,
+                       const int *findex, double *x, double *w);
 void dWorldSetQuickStepNumIterations(dWorldID w, int num);
 int dWorldGetQuickStepNumIterations(dWorldID w);
 void dWorldSetQuickStepW(dWorldID w, dReal over_relaxation);

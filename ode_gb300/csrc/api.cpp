@@ -2158,6 +2158,28 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     return 1;
 }
 
+int gbodeSolveLCPBatch(int count, int n, const double *A, const double *b, const double *lo, const double *hi, int nub,
+                       const int *findex, double *x, double *w) {
+    if (count < 0 || n < 1 || n > GB_DANTZIG_MAX_ROWS || nub < 0 || nub > n || (count > 0 && (!A || !b || !x || !w)) ||
+        (count > 0 && nub < n && (!lo || !hi))) {
+        set_error("gbodeSolveLCPBatch: bad argument");
+        return 0;
+    }
+    if (count == 0) return 1;
+    std::vector<double> zl, zh;
+    if (!lo || !hi) {  // all unbounded
+        zl.assign((size_t)count * n, -INFINITY);
+        zh.assign((size_t)count * n, INFINITY);
+        lo = zl.data();
+        hi = zh.data();
+    }
+    if (!solve_lcp_batch(count, n, A, b, lo, hi, nub, findex, x, w, 0)) {
+        set_error("gbodeSolveLCPBatch: a problem did not solve (or device allocation failed)", cudaGetLastError());
+        return 0;
+    }
+    return 1;
+}
+
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
     if (w->stats_pending) {
         cudaMemcpyAsync(w->ws.hc, w->ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream);

@@ -316,6 +316,94 @@ __global__ void __launch_bounds__(256) k_dantzig(DantzigArgs P) {
     }
 }
 
+// A batch of dense LCPs given directly (gbodeSolveLCPBatch): problem p's
+// matrix at A + p n^2 (row-major), vectors at p n; the first nub variables
+// unbounded; findex (optional, per problem) as in the reference's solver.
+struct LcpBatchArgs {
+    const double *A, *b, *lo, *hi;
+    const int *findex;
+    double *x, *w;
+    double *dscr;  // per problem: n^2 / 2 (FP32 factor) + 6 n doubles
+    int *iscr;     // per problem: 3 n
+    int n, nub;
+    unsigned *err;
+};
+
+__global__ void __launch_bounds__(256) k_lcp_batch(LcpBatchArgs P) {
+    __shared__ double red[8];
+    __shared__ int s_int[4];
+    const int n = P.n;
+    const size_t pn = (size_t)blockIdx.x * n;
+    const double *A = P.A + pn * n;
+    const double *b = P.b + pn;
+    double *x = P.x + pn, *w = P.w + pn;
+    double *D = P.dscr + (size_t)blockIdx.x * ((size_t)n * n / 2 + 1 + 6 * (size_t)n);
+    double *lo = D, *hi = lo + n, *y = hi + n, *mu = y + n;
+    float *C = (float *)(mu + n);
+    float *z = C + (size_t)n * n;
+    int *st = P.iscr + (size_t)blockIdx.x * 3 * n, *flist = st + n, *fi = flist + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        lo[i] = i < P.nub ? -INFINITY : P.lo[pn + i];
+        hi[i] = i < P.nub ? INFINITY : P.hi[pn + i];
+        mu[i] = hi[i];
+        fi[i] = P.findex ? P.findex[pn + i] : -1;
+        x[i] = 0.0;
+        if (fi[i] >= 0 || (lo[i] == 0.0 && hi[i] == 0.0)) st[i] = LCP_FIXED;
+        else st[i] = LCP_FREE;
+    }
+    __syncthreads();
+    const int max_iter = n < 500 ? 64 + 4 * n : 2064;
+    bool ok = bpp_solve(A, b, lo, hi, x, w, C, y, z, st, flist, n, max_iter, red, s_int);
+    bool any_f = false;
+    for (int i = 0; i < n; i++) any_f |= fi[i] >= 0;
+    if (ok && any_f) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            if (fi[i] < 0) continue;
+            const double xn = x[fi[i]];
+            if (xn == 0.0) { hi[i] = 0.0; lo[i] = 0.0; st[i] = LCP_FIXED; }
+            else { hi[i] = fabs(mu[i] * xn); lo[i] = -hi[i]; st[i] = LCP_FREE; }
+        }
+        __syncthreads();
+        ok = bpp_solve(A, b, lo, hi, x, w, C, y, z, st, flist, n, max_iter, red, s_int);
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(P.err, ERR_LCP_FAILED);
+    // w = A x - b (bpp_solve leaves it for its final x)
+    (void)w;
+}
+
+bool solve_lcp_batch(int count, int n, const double *A, const double *b, const double *lo, const double *hi,
+                     int nub, const int *findex, double *x, double *w, cudaStream_t s) {
+    const size_t nn = (size_t)n * n, np = (size_t)count * n;
+    DBuf dA, dv, ds, di, derr;
+    const size_t vec = np * 8;
+    if (!(dA.ensure((size_t)count * nn * 8) && dv.ensure(6 * vec) && ds.ensure((size_t)count * (nn / 2 + 1 + 6 * (size_t)n) * 8) &&
+          di.ensure((size_t)count * 3 * n * 4 + 4) && derr.ensure(4))) {
+        dA.release(); dv.release(); ds.release(); di.release(); derr.release();
+        return false;
+    }
+    double *vb = dv.as<double>(), *vlo = vb + np, *vhi = vlo + np, *vx = vhi + np, *vw = vx + np;
+    int *vf = (int *)(vw + np);
+    cudaMemcpyAsync(dA.p, A, (size_t)count * nn * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(vb, b, vec, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(vlo, lo, vec, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(vhi, hi, vec, cudaMemcpyHostToDevice, s);
+    if (findex) cudaMemcpyAsync(vf, findex, np * 4, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(derr.p, 0, 4, s);
+    LcpBatchArgs P;
+    P.A = dA.as<double>(); P.b = vb; P.lo = vlo; P.hi = vhi; P.findex = findex ? vf : nullptr;
+    P.x = vx; P.w = vw; P.dscr = ds.as<double>(); P.iscr = di.as<int>(); P.n = n; P.nub = nub;
+    P.err = derr.as<unsigned>();
+    k_lcp_batch<<<count, 256, 0, s>>>(P);
+    count_launch();
+    unsigned err = 0;
+    cudaMemcpyAsync(x, vx, vec, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(w, vw, vec, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&err, derr.p, 4, cudaMemcpyDeviceToHost, s);
+    const bool ok = cudaStreamSynchronize(s) == cudaSuccess && err == 0;
+    dA.release(); dv.release(); ds.release(); di.release(); derr.release();
+    return ok;
+}
+
 bool launch_dantzig(Workspace &ws, const std::vector<int> &order, const std::vector<int> &start, cudaStream_t s) {
     const int nisl = (int)start.size() - 1;
     if (nisl <= 0) return true;

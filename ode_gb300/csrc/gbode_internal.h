@@ -196,6 +196,9 @@ void joint_feedback(Workspace &ws, int ncontacts, int njoints, std::vector<float
 // islands' bodies; syncs
 #define GB_DANTZIG_MAX_ROWS 2048
 bool launch_dantzig(Workspace &ws, const std::vector<int> &order, const std::vector<int> &start, cudaStream_t s);
+// a batch of dense LCPs from host arrays (gbodeSolveLCPBatch; syncs)
+bool solve_lcp_batch(int count, int n, const double *A, const double *b, const double *lo, const double *hi,
+                     int nub, const int *findex, double *x, double *w, cudaStream_t s);
 // solve.cu entry points the step drivers share: the rows of a step (body pass,
 // contact and joint rows), the integration, and the rows' view
 bool assemble_step(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s);

@@ -157,6 +157,9 @@ _PROTOS = [
     ("gbodeWorldSetWarmStart", None, [ID, ctypes.c_int, dReal]),
     ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
+    ("gbodeSolveLCPBatch", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
     ("gbodeWorldAutotune", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p]),
     ("gbodeSpaceCollideContacts", ctypes.c_int, [ID, ID, ID, ctypes.POINTER(dSurfaceParameters), ctypes.c_int]),

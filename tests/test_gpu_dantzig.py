@@ -113,3 +113,125 @@ def test_dantzig_chains_follow_reference(gblib, golden):
     assert worst_p <= POS_TOL
     assert worst_a <= ANGLE_TOL
     w.close()
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def test_lcp_batch_random_problems(gblib):
+    """The reference's LCP self-test (dTestSolveLCP, lcp.cpp:1205-1335)
+    restated: random positive definite problems A = A2 A2^T (n = 100, A2
+    uniform in [-1, 1]), b = A x0 + U(-0.1, 0.1), 50 unbounded variables and
+    the rest in [-(U(0,1) + 0.01), U(0,1) + 0.01]; every solution satisfies
+    A x = b + w and the complementarity conditions (FP64 tolerances scaled by
+    the problem)."""
+    L = gblib
+    rng = np.random.default_rng(1205)
+    count, n, nub = 16, 100, 50
+    A2 = rng.uniform(-1, 1, (count, n, n))
+    A = np.einsum("pij,pkj->pik", A2, A2)
+    x0 = rng.uniform(-1, 1, (count, n))
+    b = np.einsum("pij,pj->pi", A, x0) + rng.uniform(-0.1, 0.1, (count, n))
+    lo = np.full((count, n), -np.inf)
+    hi = np.full((count, n), np.inf)
+    lo[:, nub:] = -(rng.uniform(0, 1, (count, n - nub)) + 0.01)
+    hi[:, nub:] = rng.uniform(0, 1, (count, n - nub)) + 0.01
+    A, b, lo, hi = [np.ascontiguousarray(v) for v in (A, b, lo, hi)]
+    x = np.zeros((count, n))
+    w = np.zeros((count, n))
+    assert L.gbodeSolveLCPBatch(count, n, _ptr(A), _ptr(b), _ptr(lo), _ptr(hi), nub, None, _ptr(x), _ptr(w)) == 1, \
+        L.gbodeGetLastError()
+    worst_eq, worst_c = 0.0, 0.0
+    nl = nh = nc = 0
+    for p in range(count):
+        scale = max(1.0, float(np.abs(b[p]).max()))
+        r = np.einsum("ij,j->i", A[p], x[p]) - (b[p] + w[p])
+        worst_eq = max(worst_eq, float(np.abs(r).max()) / scale)
+        tx, tw = 1e-9 * max(1.0, float(np.abs(x[p]).max())), 1e-8 * scale
+        for i in range(n):
+            if abs(x[p, i] - lo[p, i]) <= tx and w[p, i] >= -tw:
+                nl += 1
+            elif abs(x[p, i] - hi[p, i]) <= tx and w[p, i] <= tw:
+                nh += 1
+            else:
+                assert lo[p, i] - tx <= x[p, i] <= hi[p, i] + tx and abs(w[p, i]) <= tw, (p, i, x[p, i], w[p, i])
+                nc += 1
+                worst_c = max(worst_c, abs(w[p, i]) / scale)
+    print(f"{count} random LCPs (n {n}, nub {nub}): |A x - b - w| {worst_eq:.2e}, free |w| {worst_c:.2e}; "
+          f"at lo {nl}, at hi {nh}, free {nc}")
+    assert worst_eq <= 1e-9
+    assert nl > 0 and nh > 0
+
+
+def test_lcp_batch_friction_rule(gblib):
+    """findex: a normal row and two friction rows whose bounds are
+    +-mu x_normal of the problem solved without them (lcp.cpp:889-917),
+    against the same two-phase rule computed by enumeration on the host."""
+    L = gblib
+    rng = np.random.default_rng(7)
+    n = 6  # two contacts: (normal, friction, friction) x 2
+    count = 8
+    J = rng.normal(size=(count, n, 6))
+    A = np.einsum("pik,pjk->pij", J, J) + 0.05 * np.eye(n)
+    b = rng.normal(size=(count, n))
+    b[:, 0] = np.abs(b[:, 0]) + 0.5
+    b[:, 3] = np.abs(b[:, 3]) + 0.5
+    mu = 0.4
+    lo = np.tile(np.array([0, -mu, -mu, 0, -mu, -mu], float), (count, 1))
+    hi = np.tile(np.array([np.inf, mu, mu, np.inf, mu, mu]), (count, 1))
+    findex = np.tile(np.array([-1, 0, 0, -1, 3, 3], np.int32), (count, 1))
+    A, b, lo, hi = [np.ascontiguousarray(v) for v in (A, b, lo, hi)]
+    x = np.zeros((count, n))
+    w = np.zeros((count, n))
+    assert L.gbodeSolveLCPBatch(count, n, _ptr(A), _ptr(b), _ptr(lo), _ptr(hi), 0, _ptr(findex), _ptr(x), _ptr(w)) == 1
+
+    def box_lcp(A, b, lo, hi, free_mask):
+        # enumerate active sets (tiny problems): the unique solution
+        m = len(b)
+        import itertools
+        for states in itertools.product(range(3), repeat=m):
+            xs = np.zeros(m)
+            F = [i for i in range(m) if free_mask[i] and states[i] == 0]
+            for i in range(m):
+                if not free_mask[i]:
+                    xs[i] = 0.0
+                elif states[i] == 1:
+                    if not np.isfinite(lo[i]):
+                        break
+                    xs[i] = lo[i]
+                elif states[i] == 2:
+                    if not np.isfinite(hi[i]):
+                        break
+                    xs[i] = hi[i]
+            else:
+                if F:
+                    N = [i for i in range(m) if i not in F]
+                    xs[F] = np.linalg.solve(A[np.ix_(F, F)], b[F] - A[np.ix_(F, N)] @ xs[N])
+                ws = A @ xs - b
+                ok = True
+                for i in range(m):
+                    if not free_mask[i]:
+                        continue
+                    if states[i] == 0:
+                        ok &= lo[i] - 1e-12 <= xs[i] <= hi[i] + 1e-12
+                    elif states[i] == 1:
+                        ok &= ws[i] >= -1e-12
+                    else:
+                        ok &= ws[i] <= 1e-12
+                if ok:
+                    return xs
+        raise AssertionError("no solution found")
+
+    for p in range(count):
+        normal = findex[p] < 0
+        x1 = box_lcp(A[p], b[p], lo[p], hi[p], normal)
+        lo2, hi2 = lo[p].copy(), hi[p].copy()
+        for i in range(n):
+            if findex[p, i] >= 0:
+                hi2[i] = abs(mu * x1[findex[p, i]])
+                lo2[i] = -hi2[i]
+        fixed = np.array([findex[p, i] >= 0 and hi2[i] == 0 for i in range(n)])
+        x2 = box_lcp(A[p], b[p], lo2, hi2, ~fixed)
+        assert np.abs(x[p] - x2).max() <= 1e-9 * max(1.0, np.abs(x2).max()), (p, x[p], x2)
+    print("friction rule: 8 two-contact problems match the host enumeration")
