@@ -148,6 +148,41 @@ __device__ __forceinline__ bool grid_sync(GridSync *gs, unsigned *err, unsigned 
     return ok_s != 0;
 }
 
+// The same barrier in two halves: grid_arrive (block-wide __syncthreads, then
+// thread 0's release-add) and grid_wait (thread 0 polls, bounded as above;
+// then __syncthreads).  Work placed between them -- stores no other block
+// reads before a later barrier -- overlaps the wait instead of delaying the
+// release.  `target` carries the arrival's count from one half to the other.
+__device__ __forceinline__ void grid_arrive(GridSync *gs, unsigned &gen, unsigned &target) {
+    __syncthreads();
+    if (threadIdx.x == 0 && !(gen & 0x80000000u)) {
+        target = gen + gridDim.x;
+        red_release_add_u32(&gs->count, 1u);
+    }
+}
+__device__ __forceinline__ bool grid_wait(GridSync *gs, unsigned *err, unsigned &gen, unsigned target) {
+    __shared__ int ok_w;
+    if (threadIdx.x == 0) {
+        int ok = 0;
+        if (!(gen & 0x80000000u)) {
+            ok = 1;
+            long long polls = 0;
+            while ((int)(ld_acquire_u32(&gs->count) - target) < 0) {
+                if (++polls > (1ll << 22) || ((polls & 63) == 0 && (ld_acquire_u32(err) & ERR_BARRIER_TIMEOUT))) {
+                    atomicOr(err, ERR_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            gen = ok ? target : (gen | 0x80000000u);
+        }
+        ok_w = ok;
+    }
+    __syncthreads();
+    return ok_w != 0;
+}
+
 // Cache-global (L2) loads and stores for data that other SMs rewrite between
 // grid barriers (L1 is not coherent across SMs).
 __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }

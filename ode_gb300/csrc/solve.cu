@@ -1216,6 +1216,7 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
 // on chip when its barrier opens.  A slot's offset in its chunk lives in
 // bits 16-27 of its descriptor's y.
 #define GB_PGS_THREADS 256
+#define GB_STAGED_ROWS 12  // rows of a staged slot at most (4 contacts x 3, or a plain group)
 #define GB_CHUNK_ROWS 800  // rows per buffer: 2 x 100 KB of shared memory
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
@@ -1364,7 +1365,10 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // manifolds (a static second body contributes fc = 0 and is not written
 // back), loops kept rolled: the solver's inner code stays small enough for
 // the instruction caches.
-__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const float4 *buf, float *lam) {
+// The multipliers come back in lout (registers): the caller stores them after
+// its barrier arrival, so those stores do not delay the release.
+__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
+                                               float (&lout)[GB_STAGED_ROWS]) {
     const int nct = desc_rows(d) / 3, off = desc_chunk_off(d);
     const bool two = d.w >= 0;
     float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
@@ -1374,15 +1378,17 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
     float4 row[8];
 #pragma unroll 1
     for (int pass = 0; pass < A.passes; pass++) {
-#pragma unroll 1
-        for (int c = 0; c < nct; c++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if (c >= nct) break;
             const int r = off + 3 * c;
 #pragma unroll
             for (int a = 0; a < 8; a++) row[a] = buf[swz(r, a)];
             relax_fast_row<true>(row, lam[3 * c], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
         }
-#pragma unroll 1
-        for (int c = 0; c < nct; c++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if (c >= nct) break;
             const float ln = lam[3 * c];
 #pragma unroll
             for (int q = 1; q < 3; q++) {
@@ -1394,14 +1400,15 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
             }
         }
     }
-#pragma unroll 1
-    for (int k = 0; k < 3 * nct; k++) A.Rw.lambda[d.x + k] = lam[k];
+#pragma unroll
+    for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < 3 * nct ? lam[k] : 0.f;
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
 // A staged plain group (GB_DESC_PLAIN): every row in order with its own bounds.
-__device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const float4 *buf, float *lam) {
+__device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
+                                            float (&lout)[GB_STAGED_ROWS]) {
     const int n = desc_rows(d), off = desc_chunk_off(d);
     const bool two = d.w >= 0;
     float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
@@ -1418,8 +1425,8 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
             relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
         }
     }
-#pragma unroll 1
-    for (int k = 0; k < n; k++) A.Rw.lambda[d.x + k] = lam[k];
+#pragma unroll
+    for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < n ? lam[k] : 0.f;
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
@@ -1581,20 +1588,44 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             const int cn = c + 1 < ncol ? c + 1 : 0;
             const int cnn = cn + 1 < ncol ? cn + 1 : 0;
             if (threadIdx.x == 0) issue(cn);
+            float lout[GB_STAGED_ROWS];
+            int nout = 0, xout = 0;
             if (has_next) {
                 if (!staged) {
                     relax_desc(A, next);
                 } else {
                     if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
                     const float4 *buf = pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8);
-                    if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam);
-                    else relax_plain(A, next, buf, my_lam);
+                    if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
+                    else relax_plain(A, next, buf, my_lam, lout);
+                    nout = desc_rows(next);
+                    xout = next.x;
                 }
             }
             const int s = s_cstart[c], n = s_ccount[c];
             for (int k = g + nth; k < n; k += nth) relax_desc(A, __ldg(&A.desc[s + k]));
+            // arrive (the accumulators fc are out), then store the staged
+            // slot's multipliers -- read again only by this thread a sweep later
+            // and by re-formations after a later barrier -- and prefetch the
+            // next slot while the other blocks arrive.  Before a residual check
+            // (which reads every multiplier right after this barrier) they go
+            // out before the arrival.
+            const bool check_next = residual_mode && c == ncol - 1 &&
+                                    ((it + 1) % A.check_every == 0 || it + 1 == itmax);
+            if (check_next) {
+#pragma unroll
+                for (int k = 0; k < GB_STAGED_ROWS; k++)
+                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+            }
+            unsigned target = 0;
+            grid_arrive(&dc->gsync, gen, target);
+            if (!check_next) {
+#pragma unroll
+                for (int k = 0; k < GB_STAGED_ROWS; k++)
+                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+            }
             fetch(cnn);
-            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
+            if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
             // the copy for this colour has completed before its buffer's
             // mbarrier is armed again (threads with no staged slot never waited)
             if (threadIdx.x == 0) retire();
