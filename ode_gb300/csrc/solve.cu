@@ -1587,7 +1587,6 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
         for (int c = 0; c < ncol; c++) {
             const int cn = c + 1 < ncol ? c + 1 : 0;
             const int cnn = cn + 1 < ncol ? cn + 1 : 0;
-            if (threadIdx.x == 0) issue(cn);
             float lout[GB_STAGED_ROWS];
             int nout = 0, xout = 0;
             if (has_next) {
@@ -1619,6 +1618,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             }
             unsigned target = 0;
             grid_arrive(&dc->gsync, gen, target);
+            // the next colour's rows stream in while the other blocks arrive
+            if (threadIdx.x == 0) issue(cn);
             if (!check_next) {
 #pragma unroll
                 for (int k = 0; k < GB_STAGED_ROWS; k++)
