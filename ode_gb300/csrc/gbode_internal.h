@@ -76,6 +76,7 @@ struct DevCounters {
     int njoint_rows;       // scan scratch (joint rows)
     int warm_parity;       // which warm-start table holds the previous step
     int nawake;            // contacts of awake components (the solver's contacts when sleeping is on)
+    int nwaves;            // staging waves of the coloured solver
     int nasleep;           // bodies not stepped (their component sleeps)
 };
 
@@ -108,6 +109,7 @@ struct Workspace {
     DBuf r_J1l, r_J1a, r_J2l, r_J2a, r_M1l, r_M1a, r_M2l, r_M2a, r_lambda, r_Ad, r_findex, r_contact, r_body;
     // colouring / schedule
     DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc, p_rows, chunk_rows, chunk_start;
+    DBuf wv_count, wv_base, wv_col, wv_sched;  // staging waves: per (colour, block) count and first; per wave colour, slots
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state

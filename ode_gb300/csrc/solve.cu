@@ -1038,7 +1038,9 @@ struct PgsArgs {
     int nb;            // bodies
     int reform_every;  // sweeps between re-formations of fc from lambda (residual-target mode)
     const float4 *packed;                     // staged rows, chunk by chunk
-    const int *chunk_start, *chunk_rows;      // [colour][block]
+    const int *chunk_start, *chunk_rows;      // per wave: first row in `packed`, rows
+    const int *wcount, *wbase;                // per (colour, block): waves, index of the first
+    const int *sched;                         // per wave and thread: the colour slot, or -1
     int learned;      // lambda holds the learned start, lam_alt the plain one: keep the better
     float *lam_alt;
     int passes;       // passes over a manifold's rows each time it is relaxed (>= 1)
@@ -1202,77 +1204,105 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
 }
 
-// Packed staging of triplet manifolds.
+// Packed staging of the staged slots (triplet manifolds and plain groups).
 //
-// Colour slot k (k < T, the solver's thread count) belongs to block
-// b = k mod B, thread k / B.  Before the solve, the rows of every block's
-// triplet slots of a colour are packed into one contiguous chunk (colour-major,
-// then block, then thread), 128 B per row, the 8 float4 of a row stored
-// XOR-swizzled by the row's index in its chunk so that the LDS.128 of threads
-// reading different rows spread over the banks.  During the sweeps one thread
-// per block copies the chunk of the colour after the current one into the
-// other of two shared-memory buffers with a single bulk asynchronous copy
-// (TMA) completing on that buffer's mbarrier, so a colour's rows are already
-// on chip when its barrier opens.  A slot's offset in its chunk lives in
-// bits 16-27 of its descriptor's y.
+// The slots of colour c that belong to block b are k = b, b + B, b + 2B, ...
+// (B blocks; colour slots interleave over the blocks, so every colour spreads
+// over all SMs).  They are cut, in that order, into waves of at most T slots
+// (T threads a block) and GB_CHUNK_ROWS staged rows; thread t of the block
+// relaxes slot t of each wave, and the same thread relaxes the same manifold in
+// every sweep.  A colour that fits (the usual case for a single large world)
+// is one wave: slot k = b + t B for thread t.  Before the solve the rows of
+// every wave's staged slots are packed into one contiguous chunk, 128 B per
+// row, the 8 float4 of a row XOR-swizzled by the row's index in the chunk so
+// that the LDS.128 of threads reading different rows spread over the banks.
+// During the sweeps one thread per block copies the next wave's chunk into
+// the other of two shared-memory buffers with a single bulk asynchronous copy
+// (TMA) completing on that buffer's mbarrier, so a wave's rows are on chip
+// when it starts.  Waves of one colour are separated by a block barrier only;
+// colours by a grid barrier.  A slot's offset in its chunk lives in bits 16-27
+// of its descriptor's y.
 #define GB_PGS_THREADS 256
 #define GB_STAGED_ROWS 12  // rows of a staged slot at most (4 contacts x 3, or a plain group)
 #define GB_CHUNK_ROWS 800  // rows per buffer: 2 x 100 KB of shared memory
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
 
-// per (block, colour): row count of the chunk and the slots' offsets in it
-__global__ void k_chunk_offsets(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, int *chunk_rows) {
-    const int b = blockIdx.x, c = blockIdx.y, B = gridDim.x;
-    __shared__ int wsum[GB_PGS_THREADS / 32];
-    if (c >= dc->ncolours) {
-        if (threadIdx.x == 0) chunk_rows[c * B + b] = 0;
-        return;
+// The greedy cut of one (colour, block)'s slots into waves; `visit(wave, t,
+// k, offset)` for every slot (offset -1: not staged), returns the wave count.
+template <class F>
+__device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, F visit) {
+    int waves = 0, t = GB_PGS_THREADS, rows = 0;
+    for (int k = b; k < n; k += B) {
+        const int4 d = desc[s0 + k];
+        const int r = (d.y & GB_DESC_STAGED) ? desc_rows(d) : 0;
+        if (t == GB_PGS_THREADS || rows + r > GB_CHUNK_ROWS) { ++waves; t = 0; rows = 0; }
+        visit(waves - 1, t, k, r > 0 ? rows : -1);
+        rows += r;
+        ++t;
     }
-    const int k = b + threadIdx.x * B;
-    int n = 0;
-    int4 d;
-    if (k < ccount[c]) {
-        d = desc[cstart[c] + k];
-        if (d.y & GB_DESC_STAGED) n = desc_rows(d);
-    }
-    // block exclusive scan of n
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int inc = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) wsum[wid] = inc;
-    __syncthreads();
-    int before = 0, total = 0;
-    for (int w = 0; w < GB_PGS_THREADS / 32; w++) {
-        if (w < wid) before += wsum[w];
-        total += wsum[w];
-    }
-    const int off = before + inc - n;
-    if (n > 0) {
-        d.y = (d.y & ~(0xfff << 16)) | (off << 16);
-        desc[cstart[c] + k] = d;
-    }
-    if (threadIdx.x == 0) chunk_rows[c * B + b] = total;
+    return waves;
 }
 
-// copy the rows of every staged slot into its chunk (swizzled)
-__global__ void k_pack_rows(Rows Rw, const int *cstart, const int *ccount, DevCounters *dc, const int4 *desc,
-                            const int *chunk_start, float4 *packed) {
-    const int b = blockIdx.x, c = blockIdx.y, B = gridDim.x;
+// pass 1, one thread per (colour, block): waves of each (at least one, so
+// every block takes part in every colour's barrier)
+__global__ void k_wave_count(const int *cstart, const int *ccount, const DevCounters *dc, const int4 *desc,
+                             int *wcount, int B) {
+    const int cb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cb >= GB_MAX_COLOURS * B) return;
+    const int c = cb / B, b = cb % B;
+    if (c >= dc->ncolours) { wcount[cb] = 0; return; }
+    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, [](int, int, int, int) {});
+    wcount[cb] = w > 0 ? w : 1;
+}
+
+// pass 2: the chunk offsets in the descriptors, the schedule, rows per wave
+__global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, const int *wcount,
+                            const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B) {
+    const int cb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cb >= GB_MAX_COLOURS * B) return;
+    const int c = cb / B, b = cb % B;
     if (c >= dc->ncolours) return;
-    const int k = b + threadIdx.x * B;
-    if (k >= ccount[c]) return;
-    const int4 d = desc[cstart[c] + k];
-    if (!(d.y & GB_DESC_STAGED)) return;
-    const int n = desc_rows(d), off = desc_chunk_off(d);
-    float4 *dst = packed + (size_t)chunk_start[c * B + b] * 8;
-    const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
-    for (int i = 0; i < n; i++)
+    const int base = wbase[cb], nw = wcount[cb];
+    if (base + nw > wave_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); return; }
+    for (int w = 0; w < nw; w++) {
+        wrows[base + w] = 0;
+        wcol[base + w] = c;
+        for (int t = 0; t < GB_PGS_THREADS; t++) sched[(size_t)(base + w) * GB_PGS_THREADS + t] = -1;
+    }
+    const int s0 = cstart[c];
+    cut_waves(desc, s0, ccount[c], b, B, [&](int w, int t, int k, int off) {
+        sched[(size_t)(base + w) * GB_PGS_THREADS + t] = k;
+        if (off >= 0) {
+            int4 d = desc[s0 + k];
+            d.y = (d.y & ~(0xfff << 16)) | (off << 16);
+            desc[s0 + k] = d;
+            wrows[base + w] = off + desc_rows(d);
+        }
+    });
+}
+__global__ void k_wave_total(DevCounters *dc, const int *wcount, const int *wbase, int B) {
+    const int last = GB_MAX_COLOURS * B - 1;
+    dc->nwaves = wbase[last] + wcount[last];
+}
+
+// copy the rows of every staged slot into its wave's chunk (swizzled); one
+// block per wave, one thread per slot
+__global__ void k_pack_rows(Rows Rw, const int *cstart, const DevCounters *dc, const int4 *desc, const int *sched,
+                            const int *wcol, const int *chunk_start, float4 *packed) {
+    const int nw = dc->nwaves;
+    for (int wv = blockIdx.x; wv < nw; wv += gridDim.x) {
+        const int k = sched[(size_t)wv * GB_PGS_THREADS + threadIdx.x];
+        if (k < 0) continue;
+        const int4 d = desc[cstart[wcol[wv]] + k];
+        if (!(d.y & GB_DESC_STAGED)) continue;
+        const int n = desc_rows(d), off = desc_chunk_off(d);
+        float4 *dst = packed + (size_t)chunk_start[wv] * 8;
+        const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
+        for (int i = 0; i < n; i++)
 #pragma unroll
-        for (int a = 0; a < 8; a++) dst[swz(off + i, a)] = arr[a][d.x + i];
+            for (int a = 0; a < 8; a++) dst[swz(off + i, a)] = arr[a][d.x + i];
+    }
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -1443,8 +1473,7 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
 __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
     DevCounters *dc = A.dc;
-    __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS];
-    __shared__ int s_chunk_start[GB_MAX_COLOURS], s_chunk_rows[GB_MAX_COLOURS];
+    __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS], s_wcount[GB_MAX_COLOURS], s_wbase[GB_MAX_COLOURS];
     __shared__ unsigned long long s_mbar[2];
     __shared__ float s_lam[GB_PGS_THREADS * 13];  // per thread: the next manifold's multipliers
     extern __shared__ float4 pgs_smem[];  // two buffers of GB_CHUNK_ROWS rows
@@ -1453,8 +1482,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
         s_cstart[c] = A.cstart[c];
         s_ccount[c] = A.ccount[c];
-        s_chunk_start[c] = A.chunk_start[c * gridDim.x + blockIdx.x];
-        s_chunk_rows[c] = min(A.chunk_rows[c * gridDim.x + blockIdx.x], GB_CHUNK_ROWS);
+        s_wcount[c] = A.wcount[c * gridDim.x + blockIdx.x];
+        s_wbase[c] = A.wbase[c * gridDim.x + blockIdx.x];
     }
     if (threadIdx.x == 0) {
         mbar_init(&s_mbar[0]);
@@ -1532,18 +1561,34 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     } else if (A.warm) {
         if (!form_fc(false)) return;
     }
-    // Buffer q & 1 holds colour number q (counted over all sweeps); its use
-    // number q >> 1 is the mbarrier phase to wait for.
+    // The sweep is a sequence of steps (colour c, wave w): the waves of a
+    // colour in order, then the next colour.  Buffer q & 1 holds step number q
+    // (counted over all sweeps); its use number q >> 1 is the mbarrier phase to
+    // wait for.
+    struct Step { int c, w; };
+    auto step_after = [&](Step t) -> Step {
+        if (t.w + 1 < s_wcount[t.c]) return Step{t.c, t.w + 1};
+        return Step{t.c + 1 < ncol ? t.c + 1 : 0, 0};
+    };
     unsigned q = 0;
-    unsigned nissued = 0, nwaited = 0;  // thread 0: chunk copies issued / waited for, in colour order
-    auto issue = [&](int c) {           // thread 0: the copy for colour number nissued
+    unsigned nissued = 0, nwaited = 0;  // thread 0: chunk copies issued / waited for, in step order
+    // thread 0: the chunk (first row, rows) of the step to issue next, loaded
+    // one issue ahead so that no global load sits in front of a copy
+    int pend_start = 0, pend_rows = 0;
+    auto chunk_of = [&](Step t) {  // loads only: nothing uses them before the next issue
+        const int wv = s_wbase[t.c] + t.w;
+        pend_start = __ldg(&A.chunk_start[wv]);
+        pend_rows = __ldg(&A.chunk_rows[wv]);
+    };
+    auto issue = [&](Step t) {  // thread 0: the copy for step number nissued (t); loads t's successor's chunk
         const unsigned qq = nissued++;
         unsigned long long *m = &s_mbar[qq & 1];
-        const unsigned bytes = 128u * (unsigned)s_chunk_rows[c];
-        // the block's reads of this buffer (two colours ago) come before the copy's writes
+        const unsigned bytes = 128u * (unsigned)min(pend_rows, GB_CHUNK_ROWS);
+        // the block's reads of this buffer (two steps ago) come before the copy's writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(m, bytes);
-        if (bytes) bulk_g2s(pgs_smem + (qq & 1) * (GB_CHUNK_ROWS * 8), A.packed + (size_t)s_chunk_start[c] * 8, bytes, m);
+        if (bytes) bulk_g2s(pgs_smem + (qq & 1) * (GB_CHUNK_ROWS * 8), A.packed + (size_t)pend_start * 8, bytes, m);
+        chunk_of(step_after(t));
     };
     auto retire = [&]() {  // thread 0: wait for the oldest copy not yet waited for
         const unsigned qq = nwaited++;
@@ -1555,16 +1600,20 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             while (nwaited < nissued) retire();
     };
     float *my_lam = s_lam + threadIdx.x * 13;
-    // Two-deep descriptor pipeline: `ahead` (the slot of the colour after the
-    // next one) is loaded a colour early, so the multiplier copies for `next`
+    // Two-deep descriptor pipeline: `ahead` (the slot of the step after the
+    // next one) is loaded a step early, so the multiplier copies for `next`
     // can be issued at once, without waiting for a descriptor load.
     int4 next = make_int4(0, 0, -1, -1), ahead = next;
     bool has_next = false, staged = false, has_ahead = false;
-    auto load_ahead = [&](int c) {
-        has_ahead = g < s_ccount[c];
-        if (has_ahead) ahead = __ldg(&A.desc[s_cstart[c] + g]);
+    auto load_ahead = [&](Step t) {
+        // a colour in one wave: slot b + t B for thread t (no schedule load)
+        int k = blockIdx.x + threadIdx.x * (int)gridDim.x;
+        if (s_wcount[t.c] == 1) k = k < s_ccount[t.c] ? k : -1;
+        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * GB_PGS_THREADS + threadIdx.x]);
+        has_ahead = k >= 0;
+        if (has_ahead) ahead = __ldg(&A.desc[s_cstart[t.c] + k]);
     };
-    auto fetch = [&](int c_after) {
+    auto fetch = [&](Step t_after) {
         has_next = has_ahead;
         next = ahead;
         staged = false;
@@ -1576,17 +1625,26 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                 cp_async_commit();
             }
         }
-        load_ahead(c_after);
+        load_ahead(t_after);
     };
     if (ncol > 0) {
-        if (threadIdx.x == 0) issue(0);
-        load_ahead(0);
-        fetch(ncol > 1 ? 1 : 0);
+        const Step s0{0, 0};
+        if (threadIdx.x == 0) {
+            chunk_of(s0);
+            issue(s0);
+        }
+        load_ahead(s0);
+        fetch(step_after(s0));
     }
     for (; it < itmax && ncol > 0;) {
-        for (int c = 0; c < ncol; c++) {
-            const int cn = c + 1 < ncol ? c + 1 : 0;
-            const int cnn = cn + 1 < ncol ? cn + 1 : 0;
+        Step cur{0, 0};
+        for (;;) {
+            const Step nxt = step_after(cur), nnx = step_after(nxt);
+            const bool last_wave = cur.w + 1 == s_wcount[cur.c];
+            // inside a colour the next wave's rows stream in while this one is
+            // relaxed (its buffer was last read two steps ago, before a barrier);
+            // after a colour's last wave they are issued once the block arrives
+            if (threadIdx.x == 0 && !last_wave) issue(nxt);
             float lout[GB_STAGED_ROWS];
             int nout = 0, xout = 0;
             if (has_next) {
@@ -1601,36 +1659,46 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                     xout = next.x;
                 }
             }
-            const int s = s_cstart[c], n = s_ccount[c];
-            for (int k = g + nth; k < n; k += nth) relax_desc(A, __ldg(&A.desc[s + k]));
-            // arrive (the accumulators fc are out), then store the staged
-            // slot's multipliers -- read again only by this thread a sweep later
-            // and by re-formations after a later barrier -- and prefetch the
-            // next slot while the other blocks arrive.  Before a residual check
-            // (which reads every multiplier right after this barrier) they go
-            // out before the arrival.
-            const bool check_next = residual_mode && c == ncol - 1 &&
-                                    ((it + 1) % A.check_every == 0 || it + 1 == itmax);
-            if (check_next) {
+            const bool sweep_end = last_wave && cur.c == ncol - 1;
+            if (!last_wave) {
+                // another wave of this colour follows: a block barrier (the
+                // colour's slots share no body, so no other block waits on these)
 #pragma unroll
                 for (int k = 0; k < GB_STAGED_ROWS; k++)
                     if (k < nout) A.Rw.lambda[xout + k] = lout[k];
-            }
-            unsigned target = 0;
-            grid_arrive(&dc->gsync, gen, target);
-            // the next colour's rows stream in while the other blocks arrive
-            if (threadIdx.x == 0) issue(cn);
-            if (!check_next) {
+                fetch(nnx);
+                __syncthreads();
+            } else {
+                // arrive (the accumulators fc are out), then store the staged
+                // slot's multipliers -- read again only by this thread a sweep
+                // later and by re-formations after a later barrier -- and
+                // prefetch the next slot while the other blocks arrive.  Before a
+                // residual check (which reads every multiplier right after this
+                // barrier) they go out before the arrival.
+                const bool check_next = residual_mode && sweep_end &&
+                                        ((it + 1) % A.check_every == 0 || it + 1 == itmax);
+                if (check_next) {
 #pragma unroll
-                for (int k = 0; k < GB_STAGED_ROWS; k++)
-                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                    for (int k = 0; k < GB_STAGED_ROWS; k++)
+                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                }
+                unsigned target = 0;
+                grid_arrive(&dc->gsync, gen, target);
+                if (threadIdx.x == 0) issue(nxt);
+                if (!check_next) {
+#pragma unroll
+                    for (int k = 0; k < GB_STAGED_ROWS; k++)
+                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                }
+                fetch(nnx);
+                if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
             }
-            fetch(cnn);
-            if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
-            // the copy for this colour has completed before its buffer's
-            // mbarrier is armed again (threads with no staged slot never waited)
+            // the copy for this step has completed before its buffer's mbarrier
+            // is armed again (threads with no staged slot never waited)
             if (threadIdx.x == 0) retire();
             ++q;
+            if (sweep_end) break;
+            cur = nxt;
         }
         ++it;
         if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
@@ -2192,21 +2260,33 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.c_mcount.as<int>(), ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc,
                                          ws.m_desc.as<int4>(), ws.j_rstart.as<int>(), ws.j_m.as<int>(),
                                          ws.grp_body.as<int2>());
-    // pack the triplet slots' rows chunk by chunk for the solver's blocks
+    // cut every (colour, block)'s slots into waves and pack their rows chunk by
+    // chunk for the solver's blocks
     const int pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
-    const size_t nchunks = (size_t)GB_MAX_COLOURS * pgs_blocks;
-    if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.chunk_rows.ensure(nchunks * 4) &&
-          ws.chunk_start.ensure(nchunks * 4)))
+    const int ncb = GB_MAX_COLOURS * pgs_blocks;
+    // waves: one per (colour, block) at least, plus one per T slots and per
+    // GB_CHUNK_ROWS - 12 staged rows
+    const size_t ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
+    const size_t wave_cap = 2 * (size_t)ncb + ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (GB_CHUNK_ROWS - 12) + 16;
+    if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.wv_count.ensure((size_t)ncb * 4) &&
+          ws.wv_base.ensure((size_t)ncb * 4 + 4) && ws.chunk_rows.ensure(wave_cap * 4) &&
+          ws.chunk_start.ensure(wave_cap * 4) && ws.wv_col.ensure(wave_cap * 4) &&
+          ws.wv_sched.ensure(wave_cap * GB_PGS_THREADS * 4)))
         return false;
     {
-        dim3 cg(pgs_blocks, GB_MAX_COLOURS);
-        k_chunk_offsets<<<cg, GB_PGS_THREADS, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc,
-                                                      ws.m_desc.as<int4>(), ws.chunk_rows.as<int>());
-        scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), nullptr, (int)nchunks, nullptr, ws, s);
-        k_pack_rows<<<cg, GB_PGS_THREADS, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc,
-                                                  ws.m_desc.as<int4>(), ws.chunk_start.as<int>(),
-                                                  ws.p_rows.as<float4>());
-        count_launch(2);
+        const int g1 = (ncb + 127) / 128;
+        k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
+                                        ws.wv_count.as<int>(), pgs_blocks);
+        scan_exclusive(ws.wv_count.as<int>(), ws.wv_base.as<int>(), nullptr, ncb, nullptr, ws, s);
+        k_wave_total<<<1, 1, 0, s>>>(ws.dc, ws.wv_count.as<int>(), ws.wv_base.as<int>(), pgs_blocks);
+        k_wave_fill<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
+                                       ws.wv_count.as<int>(), ws.wv_base.as<int>(), ws.wv_sched.as<int>(),
+                                       ws.chunk_rows.as<int>(), ws.wv_col.as<int>(), (int)wave_cap, pgs_blocks);
+        scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), &ws.dc->nwaves, (int)wave_cap, nullptr, ws, s);
+        k_pack_rows<<<grid, GB_PGS_THREADS, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
+                                                    ws.wv_sched.as<int>(), ws.wv_col.as<int>(),
+                                                    ws.chunk_start.as<int>(), ws.p_rows.as<float4>());
+        count_launch(4);
     }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
@@ -2235,6 +2315,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.packed = ws.p_rows.as<float4>();
         A.chunk_start = ws.chunk_start.as<int>();
         A.chunk_rows = ws.chunk_rows.as<int>();
+        A.wcount = ws.wv_count.as<int>();
+        A.wbase = ws.wv_base.as<int>();
+        A.sched = ws.wv_sched.as<int>();
         // one block per SM (the grid barrier's cost grows with the block count;
         // the chunk packing above assumes exactly pgs_blocks blocks)
         const int threads = GB_PGS_THREADS;
