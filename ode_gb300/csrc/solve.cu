@@ -1463,12 +1463,12 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
 
 // The coloured SOR sweeps, one persistent cooperative launch.
 //
-// Slot k of a colour belongs to thread (k mod T) with the blocks interleaved
-// (T threads in all), so a colour's manifolds spread over every SM and the
-// same thread relaxes the same manifold in every sweep.  While a colour is
-// relaxed, the block's chunk of the next colour streams into the other
-// shared-memory buffer, and each thread loads its next manifold's descriptor
-// and multipliers before the barrier; after the barrier only the body
+// Colour slots interleave over the blocks and are cut per block into waves
+// (see the staging comment above), so a colour's manifolds spread over every
+// SM and the same thread relaxes the same manifold in every sweep.  While a
+// wave is relaxed the block's next chunk streams into the other shared-memory
+// buffer, and each thread loads its next manifold's descriptor and
+// multipliers while it waits at the barrier; after the barrier only the body
 // accumulators fc (written by the previous colour) are read through L2.
 __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
