@@ -20,6 +20,9 @@
 
 #include <algorithm>
 
+#include <map>
+#include <mutex>
+
 #include "gbode_internal.h"
 
 namespace gb {
@@ -2092,15 +2095,19 @@ static Rows rows_view(Workspace &ws) {
 }
 
 static int coop_blocks(const void *kernel, int block, int max_per_sm) {
-    // queried once per kernel (the answer does not change; no query runs while a step is captured)
-    static const void *k_cached = nullptr;
-    static int per_sm_cached = 0;
+    // queried once per (kernel, block size): the answer does not change, and no
+    // query then runs while a step is recorded into a graph
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
     int per_sm = 0;
-    if (k_cached == kernel) per_sm = per_sm_cached;
-    else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-        k_cached = kernel;
-        per_sm_cached = per_sm;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find({kernel, block});
+        if (it != cache.end()) per_sm = it->second;
+        else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+            cache[{kernel, block}] = per_sm;
+        }
     }
     if (per_sm < 1) per_sm = 1;
     if (per_sm > max_per_sm) per_sm = max_per_sm;
@@ -2322,13 +2329,13 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         // the chunk packing above assumes exactly pgs_blocks blocks)
         const int threads = GB_PGS_THREADS;
         const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;  // two chunk buffers, 200 KB
-        static bool smem_set = false;
-        if (!smem_set) {
+        // the shared-memory opt-in and the occupancy query, once (thread-safe static initialisation)
+        static const int per_sm = [&]() {
             cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            smem_set = true;
-        }
-        static int per_sm = -1;  // queried once
-        if (per_sm < 0) cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, (const void *)k_pgs, threads, smem, 0);
+            int v = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&v, (const void *)k_pgs, threads, smem, 0);
+            return v;
+        }();
         if (per_sm < 1) return false;
         const int blocks = pgs_blocks;
         void *args[] = {(void *)&A};
