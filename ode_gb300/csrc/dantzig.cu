@@ -65,27 +65,88 @@ __device__ __forceinline__ double block_max(double v, double *red) {
     return s;
 }
 
-// In-place Cholesky (lower triangle, column by column) of the n x n matrix C
-// (row-major, leading dimension n), in FP32: FP64 arithmetic runs at a small
-// fraction of FP32's rate on this GPU, and the FP64 refinement of the solve
-// below recovers the digits.  Returns false on a non-positive pivot.
+// In-place Cholesky (lower triangle) of the n x n matrix C (row-major, leading
+// dimension n), in FP32: FP64 arithmetic runs at a small fraction of FP32's
+// rate on this GPU, and the FP64 refinement of the solve below recovers the
+// digits.  Blocked right-looking, 32-column panels: the diagonal block is
+// factored in shared memory, the panel below it solved row by row, and the
+// trailing lower triangle updated tile by tile (32 x 32), one tile per warp
+// at a time -- lane a holds row a of the panel tile in registers, the warp's
+// partner tile sits in shared memory -- so the trailing matrix is read once
+// per panel instead of once per column.  Returns false on a non-positive pivot.
+#define CH_TB 32
 __device__ bool block_cholesky(float *C, int n, int *s_ok) {
-    for (int k = 0; k < n; k++) {
-        if (threadIdx.x == 0) {
-            const float d = C[(size_t)k * n + k];
-            *s_ok = d > 0.f;
-            C[(size_t)k * n + k] = d > 0.f ? sqrtf(d) : 1.f;
+    __shared__ float Dk[CH_TB][CH_TB + 1];
+    __shared__ float Tj[8][CH_TB][CH_TB + 1];  // one partner tile per warp (256 threads)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int k0 = 0; k0 < n; k0 += CH_TB) {
+        const int kb = min(CH_TB, n - k0);
+        // 1. the diagonal block, factored in shared memory
+        for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+            const int i = t / kb, j = t % kb;
+            Dk[i][j] = C[(size_t)(k0 + i) * n + k0 + j];
         }
         __syncthreads();
-        if (!*s_ok) return false;
-        const float lkk = C[(size_t)k * n + k];
-        for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) C[(size_t)i * n + k] /= lkk;
+        for (int k = 0; k < kb; k++) {
+            if (threadIdx.x == 0) {
+                const float d = Dk[k][k];
+                *s_ok = d > 0.f;
+                Dk[k][k] = d > 0.f ? sqrtf(d) : 1.f;
+            }
+            __syncthreads();
+            if (!*s_ok) return false;
+            for (int i = k + 1 + threadIdx.x; i < kb; i += blockDim.x) Dk[i][k] /= Dk[k][k];
+            __syncthreads();
+            for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+                const int i = t / kb, j = t % kb;
+                if (i > k && j > k && j <= i) Dk[i][j] -= Dk[i][k] * Dk[j][k];
+            }
+            __syncthreads();
+        }
+        for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+            const int i = t / kb, j = t % kb;
+            if (j <= i) C[(size_t)(k0 + i) * n + k0 + j] = Dk[i][j];
+        }
+        // 2. the panel below: L_rk = A_rk L_kk^-T, one row per thread
+        const int r0 = k0 + kb;
+        for (int r = r0 + threadIdx.x; r < n; r += blockDim.x) {
+            float *row = C + (size_t)r * n + k0;
+            for (int j = 0; j < kb; j++) {
+                float v = row[j];
+                for (int m = 0; m < j; m++) v -= row[m] * Dk[j][m];
+                row[j] = v / Dk[j][j];
+            }
+        }
         __syncthreads();
-        // trailing update of the lower triangle, one row per thread and step
-        for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
-            const float lik = C[(size_t)i * n + k];
-            float *ri = C + (size_t)i * n;
-            for (int j = k + 1; j <= i; j++) ri[j] -= lik * C[(size_t)j * n + k];
+        // 3. the trailing lower triangle, tile pairs (I, J <= I), one per warp
+        const int nt = (n - r0 + CH_TB - 1) / CH_TB;
+        const int npairs = nt * (nt + 1) / 2;
+        for (int p = warp; p < npairs; p += nwarps) {
+            int I = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
+            while ((I + 1) * (I + 2) / 2 <= p) I++;
+            while (I * (I + 1) / 2 > p) I--;
+            const int J = p - I * (I + 1) / 2;
+            const int i0 = r0 + I * CH_TB, j0 = r0 + J * CH_TB;
+            const int ib = min(CH_TB, n - i0), jb = min(CH_TB, n - j0);
+            // partner tile rows (j0 + b) of the panel into shared memory
+            for (int b = 0; b < jb; b++)
+                Tj[warp][b][lane] = lane < kb ? C[(size_t)(j0 + b) * n + k0 + lane] : 0.f;
+            __syncwarp();
+            if (lane < ib) {
+                float ti[CH_TB];
+                const float *ri = C + (size_t)(i0 + lane) * n + k0;
+#pragma unroll
+                for (int m = 0; m < CH_TB; m++) ti[m] = m < kb ? ri[m] : 0.f;
+                float *out = C + (size_t)(i0 + lane) * n + j0;
+                for (int b = 0; b < jb; b++) {
+                    if (j0 + b > i0 + lane) break;  // lower triangle only
+                    float acc = 0.f;
+#pragma unroll
+                    for (int m = 0; m < CH_TB; m++) acc += ti[m] * Tj[warp][b][m];
+                    out[b] -= acc;
+                }
+            }
+            __syncwarp();
         }
         __syncthreads();
     }
