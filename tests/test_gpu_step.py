@@ -152,3 +152,33 @@ def test_fused_pile_steps_are_sane(gblib):
     assert s.rows == 3 * s.contacts and s.contacts > 20000
     assert 2 <= s.colours <= 128
     w.close()
+
+
+def test_staging_waves_give_the_same_solution(gblib):
+    """The coloured solver on one thread block instead of one per SM: every
+    colour of a 2,048-body pile is then cut into many waves of at most 256
+    slots and 800 staged rows (block barriers between them) instead of one
+    wave per block.  A colour's manifolds share no body, so the order within a
+    colour cannot change the result: the states after 250 steps (the pile
+    landed, ~15k rows) are equal to the bit."""
+    from ode_gb300 import scenes, sim
+    L = gblib
+    sc = scenes.pile(2048, seed=7)
+    worlds = [sim.GBWorld(sc), sim.GBWorld(sc)]
+    L.gbodeWorldSetSolverBlocks(worlds[1].w, 1)
+    assert L.gbodeWorldGetSolverBlocks(worlds[1].w) == 1
+    for w in worlds:
+        L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.dWorldSetQuickStepNumIterations(w.w, 30)
+    for _ in range(250):
+        for w in worlds:
+            w.step_fused()
+    a, b = worlds[0].state(), worlds[1].state()
+    s0, s1 = worlds[0].stats(), worlds[1].stats()
+    print(f"one block vs {L.gbodeWorldGetSolverBlocks(worlds[0].w)}: {s1.iterations} vs {s0.iterations} sweeps, "
+          f"{s0.rows} rows, {s0.colours} colours")
+    assert np.isfinite(a).all() and s0.rows > 10000
+    assert np.array_equal(a, b), float(np.abs(a - b).max())
+    for w in worlds:
+        w.close()
