@@ -1962,19 +1962,24 @@ int dWorldStep(dWorldID w, dReal stepsize) {
     P.learned = 0;
     P.learn_capture = 0;
     cudaStream_t s = w->stream;
-    if (w->device_contacts) {
-        set_error("dWorldStep: steps contact joints made by dJointCreateContact, not device contacts");
-        return 0;
-    }
+    const bool dev = w->device_contacts;  // contacts from gbodeSpaceCollideContacts, on the device
     std::vector<dxJoint *> js;
     for (dxJoint *j : w->joints) if (j->attached && j->type == dJointTypeContact) js.push_back(j);
+    if (dev && !js.empty()) {
+        set_error("dWorldStep: a step mixes dJointCreateContact joints with gbodeSpaceCollideContacts contacts");
+        return 0;
+    }
     if (!upload_joint_table(w)) { set_error("dWorldStep: joint table upload"); return 0; }
-    if (!upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
+    if (!dev && !upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
+    if (dev && ws.contact_cap <= 0) {
+        ws.contacts.ensure(sizeof(Contact));
+        ws.contact_cap = 1;
+    }
     if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
     const int nb = (int)w->bodies.size();
     std::vector<dxJoint *> awake_js;
     const std::vector<dxJoint *> *solved = &js;
-    if (ws.sleep_on) {
+    if (ws.sleep_on && !dev) {
         if (!launch_sleep(ws, nb, stepsize, s)) { set_error("dWorldStep: sleep stage", cudaGetLastError()); return 0; }
         std::vector<int> asleep(nb > 0 ? nb : 1);
         if (nb > 0) cudaMemcpyAsync(asleep.data(), ws.b_asleep.p, 4 * (size_t)nb, cudaMemcpyDeviceToHost, s);
@@ -1992,9 +1997,28 @@ int dWorldStep(dWorldID w, dReal stepsize) {
     // row ranges: contacts in order (rows per contact from getInfo1), then the
     // joints' rows after all contact rows (row counts from the device)
     const std::vector<dxJoint *> &sj = *solved;
-    const int nc = (int)sj.size(), nj = ws.njoints;
-    std::vector<int> crs(nc + 1, 0);
-    for (int k = 0; k < nc; k++) crs[k + 1] = crs[k] + host_contact_m(sj[k]->contact.surface);
+    std::vector<int2> cbody;  // per contact: bodies (static -1)
+    std::vector<int> crow, cm;  // per contact: first row, rows
+    int nc;
+    if (dev) {
+        nc = download_solver_contacts(ws, cbody, crow, cm, s);
+        if (nc < 0) { set_error("dWorldStep: contacts"); return 0; }
+    } else {
+        nc = (int)sj.size();
+        cbody.resize(nc > 0 ? nc : 1);
+        crow.assign(nc > 0 ? nc : 1, 0);
+        cm.assign(nc > 0 ? nc : 1, 0);
+        int r = 0;
+        for (int k = 0; k < nc; k++) {
+            cbody[k] = make_int2(sj[k]->b1 ? sj[k]->b1->index : -1, sj[k]->b2 ? sj[k]->b2->index : -1);
+            crow[k] = r;
+            cm[k] = host_contact_m(sj[k]->contact.surface);
+            r += cm[k];
+        }
+    }
+    int ncrows = 0;
+    for (int k = 0; k < nc; k++) ncrows = crow[k] + cm[k] > ncrows ? crow[k] + cm[k] : ncrows;
+    const int nj = ws.njoints;
     std::vector<int> jm(nj > 0 ? nj : 1), jr(nj > 0 ? nj : 1);
     std::vector<int4> jinfo(nj > 0 ? nj : 1);
     if (nj > 0) {
@@ -2015,23 +2039,22 @@ int dWorldStep(dWorldID w, dReal stepsize) {
         a = find(a); b = find(b);
         if (a != b) parent[a > b ? a : b] = a > b ? b : a;
     };
-    for (const dxJoint *j : sj) unite(j->b1 ? j->b1->index : -1, j->b2 ? j->b2->index : -1);
+    for (int k = 0; k < nc; k++) unite(cbody[k].x, cbody[k].y);
     for (int k = 0; k < nj; k++)
         if (jm[k] > 0) unite(jinfo[k].y, jinfo[k].z);
     std::vector<std::vector<int>> rows_of(nb > 0 ? nb : 1);
     for (int k = 0; k < nc; k++) {
-        const dxJoint *j = sj[k];
-        const int b = j->b1 ? j->b1->index : (j->b2 ? j->b2->index : -1);
+        const int b = cbody[k].x >= 0 ? cbody[k].x : cbody[k].y;
         if (b < 0) continue;
         auto &v = rows_of[find(b)];
-        for (int r = crs[k]; r < crs[k + 1]; r++) v.push_back(r);
+        for (int r = crow[k]; r < crow[k] + cm[k]; r++) v.push_back(r);
     }
     for (int k = 0; k < nj; k++) {
         if (jm[k] <= 0) continue;
         const int b = jinfo[k].y >= 0 ? jinfo[k].y : jinfo[k].z;
         if (b < 0) continue;
         auto &v = rows_of[find(b)];
-        for (int r = 0; r < jm[k]; r++) v.push_back(crs[nc] + jr[k] + r);
+        for (int r = 0; r < jm[k]; r++) v.push_back(ncrows + jr[k] + r);
     }
     std::vector<int> order, start(1, 0);
     for (int i = 0; i < nb; i++) {

@@ -206,6 +206,8 @@ bool solve_lcp_batch(int count, int n, const double *A, const double *b, const d
 bool assemble_step(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s);
 bool launch_integrate(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s);
 Rows rows_view_public(Workspace &ws);
+int download_solver_contacts(Workspace &ws, std::vector<int2> &bodies, std::vector<int> &rstart,
+                             std::vector<int> &mcount, cudaStream_t s);
 
 // ---- sleep.cu: auto-disable state buffers; the sleep stage of a step
 bool ensure_sleep(Workspace &ws, int nb, int samples);

@@ -1972,7 +1972,10 @@ __global__ void k_feedback(Rows Rw, const int *nrows_dev, const int *orig, int n
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int c = Rw.contact[r];
         if (c < 0) c = nc + (-1 - c);  // joint k's row: owner -1 - k
-        else if (orig) c = orig[c];
+        else {
+            if (orig) c = orig[c];
+            if (c >= nc) continue;  // contacts without a record (made on the device): no feedback
+        }
         const int2 b = Rw.body[r];
         const float l = Rw.lambda[r] / Rw.Ad[r];
         float4 a = Rw.J1l[r], d = Rw.J1a[r];
@@ -2226,6 +2229,27 @@ bool launch_integrate(Workspace &ws, int nb, const SolverParams &P, cudaStream_t
     return cudaGetLastError() == cudaSuccess;
 }
 Rows rows_view_public(Workspace &ws) { return rows_view(ws); }
+
+// The solver's contacts of the last assembly (all of them, or those of awake
+// components), with their bodies (static: -1) and row ranges; syncs.
+int download_solver_contacts(Workspace &ws, std::vector<int2> &bodies, std::vector<int> &rstart,
+                             std::vector<int> &mcount, cudaStream_t s) {
+    int nc = 0;
+    cudaMemcpyAsync(&nc, solve_count(ws), 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    std::vector<Contact> C(nc > 0 ? nc : 1);
+    rstart.assign(nc > 0 ? nc : 1, 0);
+    mcount.assign(nc > 0 ? nc : 1, 0);
+    if (nc > 0) {
+        cudaMemcpyAsync(C.data(), solve_contacts(ws), (size_t)nc * sizeof(Contact), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(rstart.data(), ws.c_rstart.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(mcount.data(), ws.c_mcount.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    }
+    bodies.resize(nc > 0 ? nc : 1);
+    for (int k = 0; k < nc; k++) bodies[k] = make_int2(C[k].b1, C[k].b2);
+    return nc;
+}
 
 bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStream_t s, cudaEvent_t ev0,
                       cudaEvent_t ev1) {

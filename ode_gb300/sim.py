@@ -223,10 +223,25 @@ class GBWorld:
             raise RuntimeError(L.gbodeGetLastError().decode())
         return 1
 
-    def step_dantzig(self):
-        """One dWorldStep (a dense LCP per island) on the joints alone: no
-        collision (for jointed scenes without geoms)."""
-        return self.L.dWorldStep(self.w, self.scene.dt)
+    def step_dantzig(self, collide: str | None = None):
+        """One dWorldStep (a dense LCP per island).  `collide`: None steps the
+        joints alone (jointed scenes without geoms); "host" makes contact
+        joints through dSpaceCollide and dCollide; "device" makes the contacts
+        on the device (gbodeSpaceCollideContacts)."""
+        L = self.L
+        if collide == "host":
+            self.made = []
+            L.dSpaceCollide(self.space, None, self._cb)
+        elif collide == "device":
+            if not L.gbodeSpaceCollideContacts(self.space, self.w, self.group, ctypes.byref(self.surface),
+                                               self.scene.maxc):
+                raise RuntimeError(L.gbodeGetLastError().decode())
+        elif collide is not None:
+            raise ValueError(f"collide: {collide!r}")
+        ok = L.dWorldStep(self.w, self.scene.dt)
+        if collide is not None:
+            L.dJointGroupEmpty(self.group)
+        return ok
 
     def autotune(self, steps: int = 3, graph: bool = True) -> ode.gbodeTuning:
         """gbodeWorldAutotune on the fused step (the tuning steps advance the world)."""
