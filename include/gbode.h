@@ -104,8 +104,10 @@ int dWorldQuickStep(dWorldID w, dReal stepsize);
  * A = J M^-1 J^T + diag(cfm), solved exactly on the device as the reference's
  * Dantzig solver defines it (friction rows bounded by the normal multipliers
  * of the problem without them), FP64 with FP32 factorisations; one thread
- * block per island, at most 2048 rows an island.  Contact joints from
- * dJointCreateContact only.  Returns 0 on failure (gbodeGetLastError). */
+ * block per island, at most 2048 rows an island.  The contacts are the
+ * attached contact joints (dJointCreateContact) or the device's own from
+ * gbodeSpaceCollideContacts, not both in one step.  Returns 0 on failure
+ * (gbodeGetLastError). */
 int dWorldStep(dWorldID w, dReal stepsize);
 
 /* The dense LCP solver of dWorldStep for a batch of problems given directly
