@@ -5,6 +5,8 @@
 #include "ode_port.h"
 
 #include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1127,6 +1129,8 @@ struct port_world {
     real premature_delta, extra_delta;
     unsigned max_extra;
     int dyn_enabled;
+    int threads;       /* SOR threads (1: the reference's default self-threaded stepping) */
+    int mt_min_rows;   /* islands with fewer rows iterate on one thread */
 };
 
 /* contact joint as dJointCreateContact + dJointAttach leave it (ode.cpp:1192-1200, 1383-1439) */
@@ -1198,6 +1202,8 @@ port_world *port_world_create(int nb, const float *bin, const float *params, int
     w->erp = params[4]; w->cfm = params[5]; w->w = params[6]; w->max_vel = params[7]; w->min_depth = params[8];
     w->iterations = iterations;
     w->reorder = reorder;
+    w->threads = 1;
+    w->mt_min_rows = 4096;
     /* objects.h:451-475 defaults; objects.cpp:78-91 */
     w->premature_delta = dyn ? 1e-8f : 0.0f;
     w->extra_delta = 1e-2f;
@@ -1225,6 +1231,11 @@ void port_world_set_dyn(port_world *w, float premature, float extra_factor, floa
     w->extra_delta = extra_delta;
     w->max_extra = (unsigned)((real)w->iterations * extra_factor);
     w->dyn_enabled = w->max_extra != 0 || w->premature_delta != 0;
+}
+
+void port_world_set_threads(port_world *w, int threads, int min_rows) {
+    w->threads = threads > 1 ? threads : 1;
+    w->mt_min_rows = min_rows > 0 ? min_rows : 1;
 }
 
 void port_world_get(const port_world *w, float *out) {
@@ -1388,6 +1399,228 @@ static void contact_info2(const port_world *w, pjoint *j, real fps, real erp_wor
 
 /* quickstep.cpp:1112-3439 dxQuickStepIsland, single-threaded path.
  * body_ids/joint_ids: the island in DFS order; rows_out/lambda in joint terms. */
+/* ------------------------------------------------------------------ SOR */
+/* The rows of one island as the SOR sweep reads them. */
+typedef struct {
+    const real *J, *iMJ;
+    const int *jb1, *jb2, *findex;
+    real *lambda, *fc, *fa;
+} sor_rows;
+
+/* Stage4LCP_IterationStep (quickstep.cpp:2917-3033): one row's projected
+ * Gauss-Seidel update of lambda and of its bodies' fc (and the dynamic
+ * iteration's per-body maximum adjustments fa). */
+static inline void sor_row(const sor_rows *S, int index) {
+    const real *Jr = S->J + 16 * index;
+    real *lambda = S->lambda;
+    real old_lambda = lambda[index];
+    real delta = Jr[6] - old_lambda * Jr[7];
+    int b1 = S->jb1[index], b2 = S->jb2[index];
+    real *f1 = S->fc + 6 * b1, *f2 = NULL;
+    delta -= f1[0] * Jr[0] + f1[1] * Jr[1] + f1[2] * Jr[2] + f1[3] * Jr[3] + f1[4] * Jr[4] + f1[5] * Jr[5];
+    if (b2 != -1) {
+        f2 = S->fc + 6 * b2;
+        delta -= f2[0] * Jr[8] + f2[1] * Jr[9] + f2[2] * Jr[10] + f2[3] * Jr[11] + f2[4] * Jr[12] + f2[5] * Jr[13];
+    }
+    real hi_act, lo_act;
+    const int fi = S->findex[index];
+    if (fi != -1) { hi_act = fabsf(Jr[15] * lambda[fi]); lo_act = -hi_act; }
+    else { hi_act = Jr[15]; lo_act = Jr[14]; }
+    real new_lambda = old_lambda + delta;
+    if (new_lambda < lo_act) { delta = lo_act - old_lambda; lambda[index] = lo_act; }
+    else if (new_lambda > hi_act) { delta = hi_act - old_lambda; lambda[index] = hi_act; }
+    else lambda[index] = new_lambda;
+    if (delta != 0) {
+        const real *o = S->iMJ + 14 * index;
+        int pos_ = delta > 0;
+        for (int k = 0; k < 6; k++) f1[k] += delta * o[k];
+        S->fa[2 * b1 + pos_] += delta * o[6];
+        if (f2) {
+            S->fa[2 * b2 + pos_] += delta * o[13];
+            for (int k = 0; k < 6; k++) f2[k] += delta * o[7 + k];
+        }
+    }
+}
+
+/* IsSORConstraintsReorderRequiredForIteration (quickstep.cpp:1080-1109) and
+ * the random shuffle of ConstraintsShuffling (quickstep.cpp:2578-2618). */
+static int sor_reorder_due(const port_world *w, unsigned iteration) {
+    return w->reorder == 1 && iteration >= 8u && iteration % 8u == 0u;
+}
+static void sor_shuffle(int *order, int m) {
+    for (int idx = 1; idx < m; ++idx) {
+        int sw = port_rand_int(idx + 1);
+        int t = order[idx]; order[idx] = order[sw]; order[sw] = t;
+    }
+}
+
+/* The iteration driver's exit rule (quickstep.cpp:1823-1856) and the dynamic
+ * iteration check (CheckForMaximumToBeLessThanLimitAndResetMaxAdjustments,
+ * quickstep.cpp:3253-3285), after one sweep: 1 when the sweeps end. */
+typedef struct { unsigned iteration, extra; real premature; } sor_driver;
+static int sor_after_sweep(const port_world *w, sor_driver *d, real *fa, int nb) {
+    ++d->iteration;
+    if (d->iteration - d->extra == (unsigned)w->iterations) {
+        if (d->extra != 0 || w->max_extra == 0) return 1;
+        d->extra = w->max_extra;
+        d->premature = w->extra_delta;
+    }
+    if (w->dyn_enabled) {
+        int hit = 0;
+        if (d->premature == 0) { memset(fa, 0, sizeof(real) * 2 * nb); hit = 1; }
+        else {
+            for (int i = 0; i < nb; i++) {
+                if (!(fa[2 * i + 1] < d->premature) || !(-fa[2 * i] < d->premature)) {
+                    memset(fa + 2 * i, 0, sizeof(real) * 2 * (nb - i));
+                    hit = 1;
+                    break;
+                }
+                fa[2 * i] = 0; fa[2 * i + 1] = 0;
+            }
+        }
+        if (!hit) return 1;
+    }
+    return 0;
+}
+
+/* Multi-threaded sweeps: the reference's opt-in threaded iteration
+ * (dWorldSetStepThreadingImplementation, ode.cpp:1814-1825; the dependency
+ * map of quickstep.cpp:2661-2742 and MTIteration, :2807-2890) runs a row once
+ * the rows before it in the order that share one of its bodies have run.  This
+ * restatement groups the rows of an order into levels -- a row's level is one
+ * above the highest level of the earlier rows on its bodies, so the rows of a
+ * level share no body -- and runs the levels one after another, each level's
+ * rows split over the threads, with a spin barrier between levels.  A
+ * friction row's normal row belongs to the same contact, so it is ordered by
+ * the shared bodies too.  Every row then reads the body accumulators the
+ * sequential order gives it: the multipliers are the sequential ones to the
+ * bit (the reference's tree releases a row after the later of its two
+ * predecessors only, and waits for fewer).  The level map is rebuilt by one
+ * thread after every reorder, as the reference rebuilds its map. */
+typedef struct {
+    sor_rows S;
+    const port_world *w;
+    int m, nb, nthreads;
+    int *order, *lev_start, *lev_rows, *lev_of, *blev;
+    int nlev, serial;
+    sor_driver drv;
+    int stop;
+    atomic_int bar_count, bar_sense, go;
+} sor_mt;
+
+typedef struct { sor_mt *C; int tid; } sor_mt_arg;
+
+static void sor_barrier(sor_mt *C, int *sense) {
+    const int s = !*sense;
+    *sense = s;
+    if (atomic_fetch_add(&C->bar_count, 1) == C->nthreads - 1) {
+        atomic_store(&C->bar_count, 0);
+        atomic_store(&C->bar_sense, s);
+    } else {
+        while (atomic_load(&C->bar_sense) != s) {
+        }
+    }
+}
+
+static void sor_levels(sor_mt *C) {
+    const int m = C->m;
+    memset(C->blev, 0, sizeof(int) * (C->nb > 0 ? C->nb : 1));
+    int nlev = 0;
+    for (int ii = 0; ii < m; ii++) {
+        const int index = C->order[ii];
+        const int b1 = C->S.jb1[index], b2 = C->S.jb2[index];
+        int l = C->blev[b1];
+        if (b2 != -1 && C->blev[b2] > l) l = C->blev[b2];
+        C->blev[b1] = l + 1;
+        if (b2 != -1) C->blev[b2] = l + 1;
+        C->lev_of[index] = l;
+        if (l + 1 > nlev) nlev = l + 1;
+    }
+    memset(C->lev_start, 0, sizeof(int) * (nlev + 1));
+    for (int r = 0; r < m; r++) C->lev_start[C->lev_of[r] + 1]++;
+    for (int l = 0; l < nlev; l++) C->lev_start[l + 1] += C->lev_start[l];
+    /* a level's rows are independent: they are listed by row index (the
+     * order of memory), lev_start[l] running to the end of level l */
+    for (int r = 0; r < m; r++) C->lev_rows[C->lev_start[C->lev_of[r]]++] = r;
+    for (int l = nlev; l > 0; l--) C->lev_start[l] = C->lev_start[l - 1];
+    C->lev_start[0] = 0;
+    C->nlev = nlev;
+    /* an order whose levels hold fewer than 8 rows a thread on average (the
+     * initial order: contacts of a body next to each other, chained through
+     * their bodies) is swept by one thread in order */
+    C->serial = (long long)nlev * 8 * C->nthreads > (long long)m;
+}
+
+static void *sor_mt_run(void *argp) {
+    sor_mt_arg *a = (sor_mt_arg *)argp;
+    sor_mt *C = a->C;
+    while (!atomic_load(&C->go)) {
+    }
+    const int tid = a->tid, T = C->nthreads;
+    int sense = 0;
+    for (;;) {
+        if (C->serial) {
+            if (tid == 0)
+                for (int ii = 0; ii < C->m; ii++) sor_row(&C->S, C->order[ii]);
+            sor_barrier(C, &sense);
+        } else {
+            for (int l = 0; l < C->nlev; l++) {
+                const int s0 = C->lev_start[l], n = C->lev_start[l + 1] - s0;
+                const int lo = s0 + (int)((long long)n * tid / T), hi = s0 + (int)((long long)n * (tid + 1) / T);
+                for (int k = lo; k < hi; k++) sor_row(&C->S, C->lev_rows[k]);
+                sor_barrier(C, &sense);
+            }
+        }
+        if (tid == 0) {
+            C->stop = sor_after_sweep(C->w, &C->drv, C->S.fa, C->nb);
+            if (!C->stop && sor_reorder_due(C->w, C->drv.iteration)) {
+                sor_shuffle(C->order, C->m);
+                sor_levels(C);
+            }
+        }
+        sor_barrier(C, &sense);
+        if (C->stop) break;
+    }
+    return NULL;
+}
+
+static void sor_sweeps_mt(const port_world *w, const sor_rows *S, int *order, int m, int nb) {
+    sor_mt C;
+    memset(&C, 0, sizeof C);
+    C.S = *S;
+    C.w = w;
+    C.m = m;
+    C.nb = nb;
+    C.nthreads = w->threads;
+    C.order = order;
+    C.lev_start = (int *)malloc(sizeof(int) * (m + 2));
+    C.lev_rows = (int *)malloc(sizeof(int) * (m + 1));
+    C.lev_of = (int *)malloc(sizeof(int) * (m + 1));
+    C.blev = (int *)malloc(sizeof(int) * (nb + 1));
+    C.drv.premature = w->premature_delta;
+    atomic_init(&C.bar_count, 0);
+    atomic_init(&C.bar_sense, 0);
+    atomic_init(&C.go, 0);
+    const int asked = w->threads;
+    sor_mt_arg *args = (sor_mt_arg *)malloc(sizeof(sor_mt_arg) * asked);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * asked);
+    int started = 1;
+    for (int t = 0; t < asked; t++) { args[t].C = &C; args[t].tid = t; }
+    for (int t = 1; t < asked; t++) {
+        if (pthread_create(&th[t], NULL, sor_mt_run, &args[t]) != 0) break;
+        started++;
+    }
+    /* the threads read the count only after the gate opens: a failed
+     * pthread_create leaves fewer threads, with tids 0 .. started-1 */
+    C.nthreads = started;
+    sor_levels(&C);
+    atomic_store(&C.go, 1);
+    sor_mt_run(&args[0]);
+    for (int t = 1; t < started; t++) pthread_join(th[t], NULL);
+    free(th); free(args);
+    free(C.blev); free(C.lev_of); free(C.lev_rows); free(C.lev_start);
+}
+
 static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint *joints, const int *joint_ids,
                              int nj_in, const int *joint_cidx, float *lambda_out, float *rows_out, int row_base) {
     const real h = w->dt;
@@ -1543,68 +1776,16 @@ static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint 
             for (int i = 0; i < m; i++) { if (findex[i] == -1) order[head++] = i; else order[tail++] = i; }
         }
         /* iteration driver :1823-1856 */
-        unsigned num_iterations = (unsigned)w->iterations;
-        real prematureExitDelta = w->premature_delta;
-        for (unsigned iteration = 0, extra = 0;;) {
-            /* IsSORConstraintsReorderRequiredForIteration :1080-1109 + ConstraintsShuffling :2578-2618 */
-            if (w->reorder == 1 && iteration >= 8u && iteration % 8u == 0u) {
-                for (int idx = 1; idx < m; ++idx) {
-                    int sw = port_rand_int(idx + 1);
-                    int t = order[idx]; order[idx] = order[sw]; order[sw] = t;
-                }
-            }
-            /* Stage4LCP_IterationStep :2917-3033 */
-            for (int ii = 0; ii < m; ii++) {
-                int index = order[ii];
-                const real *Jr = J + 16 * index;
-                real old_lambda = lambda[index];
-                real delta = Jr[6] - old_lambda * Jr[7];
-                int b1 = jb1[index], b2 = jb2[index];
-                real *f1 = fc + 6 * b1, *f2 = NULL;
-                delta -= f1[0] * Jr[0] + f1[1] * Jr[1] + f1[2] * Jr[2] + f1[3] * Jr[3] + f1[4] * Jr[4] + f1[5] * Jr[5];
-                if (b2 != -1) {
-                    f2 = fc + 6 * b2;
-                    delta -= f2[0] * Jr[8] + f2[1] * Jr[9] + f2[2] * Jr[10] + f2[3] * Jr[11] + f2[4] * Jr[12] + f2[5] * Jr[13];
-                }
-                real hi_act, lo_act;
-                if (findex[index] != -1) { hi_act = fabsf(Jr[15] * lambda[findex[index]]); lo_act = -hi_act; }
-                else { hi_act = Jr[15]; lo_act = Jr[14]; }
-                real new_lambda = old_lambda + delta;
-                if (new_lambda < lo_act) { delta = lo_act - old_lambda; lambda[index] = lo_act; }
-                else if (new_lambda > hi_act) { delta = hi_act - old_lambda; lambda[index] = hi_act; }
-                else lambda[index] = new_lambda;
-                if (delta != 0) {
-                    const real *o = iMJ + 14 * index;
-                    int pos_ = delta > 0;
-                    for (int k = 0; k < 6; k++) f1[k] += delta * o[k];
-                    fa[2 * b1 + pos_] += delta * o[6];
-                    if (f2) {
-                        fa[2 * b2 + pos_] += delta * o[13];
-                        for (int k = 0; k < 6; k++) f2[k] += delta * o[7 + k];
-                    }
-                }
-            }
-            ++iteration;
-            if (iteration - extra == num_iterations) {
-                if (extra != 0 || w->max_extra == 0) break;
-                extra = w->max_extra;
-                prematureExitDelta = w->extra_delta;
-            }
-            if (w->dyn_enabled) {
-                /* CheckForMaximumToBeLessThanLimitAndResetMaxAdjustments :3253-3285 */
-                int hit = 0;
-                if (prematureExitDelta == 0) { memset(fa, 0, sizeof(real) * 2 * nb); hit = 1; }
-                else {
-                    for (int i = 0; i < nb; i++) {
-                        if (!(fa[2 * i + 1] < prematureExitDelta) || !(-fa[2 * i] < prematureExitDelta)) {
-                            memset(fa + 2 * i, 0, sizeof(real) * 2 * (nb - i));
-                            hit = 1;
-                            break;
-                        }
-                        fa[2 * i] = 0; fa[2 * i + 1] = 0;
-                    }
-                }
-                if (!hit) break;
+        sor_rows S = {J, iMJ, jb1, jb2, findex, lambda, fc, fa};
+        if (w->threads > 1 && m >= w->mt_min_rows) {
+            sor_sweeps_mt(w, &S, order, m, nb);
+        } else {
+            sor_driver drv = {0u, 0u, w->premature_delta};
+            for (;;) {
+                if (sor_reorder_due(w, drv.iteration)) sor_shuffle(order, m);
+                /* Stage4LCP_IterationStep :2917-3033 */
+                for (int ii = 0; ii < m; ii++) sor_row(&S, order[ii]);
+                if (sor_after_sweep(w, &drv, fa, nb)) break;
             }
         }
         /* Stage4b :3082-3182 */

@@ -46,6 +46,10 @@ void port_world_destroy(port_world *w);
 void port_world_get(const port_world *w, float *out /* [nb][25] pos q R lvel avel */);
 void port_world_set_state(port_world *w, const float *state /* [nb][25] */);
 void port_world_set_dyn(port_world *w, float premature_delta, float extra_factor, float extra_delta);
+/* SOR sweeps on `threads` host threads for islands of at least `min_rows`
+ * rows (the reference's opt-in multi-threaded stepping); the multipliers stay
+ * those of the single-threaded sweep, to the bit. */
+void port_world_set_threads(port_world *w, int threads, int min_rows);
 void port_rand_set_seed(unsigned long s);
 unsigned long port_rand_get_seed(void);
 /* One dWorldQuickStep with the given contact joints attached in order.

@@ -20,7 +20,8 @@ def build(force: bool = False) -> str:
     """Compile the oracle with the flags that keep the reference's float order."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
             os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "ode_port.h"))):
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB, SRC, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-o", LIB, SRC,
+                               "-lm"])
     return LIB
 
 
@@ -50,6 +51,7 @@ class Port:
         L.port_world_get.argtypes = [ctypes.c_void_p, _F]
         L.port_world_set_state.argtypes = [ctypes.c_void_p, _F]
         L.port_world_set_dyn.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+        L.port_world_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.port_world_quickstep.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, _I, _F, _F, _F, _I]
         L.port_sim_create.restype = ctypes.c_void_p
         L.port_sim_create.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, _I, _F, _F, _F, ctypes.c_int,
@@ -132,6 +134,11 @@ class PortWorld:
 
     def set_dyn(self, premature, factor, extra_delta):
         self.port.lib.port_world_set_dyn(self.h, premature, factor, extra_delta)
+
+    def set_threads(self, threads: int, min_rows: int = 4096):
+        """SOR sweeps of islands with at least `min_rows` rows on `threads`
+        host threads (same multipliers as one thread, to the bit)."""
+        self.port.lib.port_world_set_threads(self.h, int(threads), int(min_rows))
 
     def quickstep(self, cb, mode, cs, want_rows=False):
         nc = cb.shape[0]

@@ -82,6 +82,46 @@ def test_full_loop_trajectory(port, golden, name, stock):
             np.testing.assert_array_equal(st[:, 0:3], traj[s // every, :, 0:3])
 
 
+@pytest.mark.parametrize("name", ["box_stack", "pile256", "capsule_pile96"])
+def test_threaded_sweeps_follow_reference(port, golden, name):
+    """The oracle's multi-threaded SOR sweeps (levels of rows that share no
+    body, three threads, every island threaded) on the stock build's golden
+    trajectory (random row shuffling, dynamic iteration counts): bit-exact,
+    as the single-threaded sweep is."""
+    g = golden(f"step_{name}.npz")
+    iters, maxc, mode, nsteps = [int(x) for x in g["ints"]]
+    every = int(g["traj_every"][0])
+    port.lib.port_rand_set_seed(0)
+    w = port.world(g["bodies0"], g["params"], iters, dyn=1, reorder=1)
+    w.set_threads(3, 1)
+    w.attach_space(g["geom_cls"], g["geom_body"], g["geom_pos"], g["geom_R"], g["geom_dims"], (-3, 10), maxc, mode,
+                   g["surface"])
+    for s in range(nsteps):
+        w.sim_step()
+        if s % every == 0:
+            np.testing.assert_array_equal(w.state()[:, 0:3], g["traj_stock"][s // every, :, 0:3])
+
+
+def test_threaded_sweeps_on_a_pile():
+    """A 2048-body pile, 70 steps of 24 shuffled sweeps: the oracle's
+    threaded sweeps (4 threads) give the single-threaded state to the bit."""
+    from oracle.port.port import Port
+    from ode_gb300 import scenes
+    P = Port()
+    sc = scenes.pile(2048, seed=1)
+    out = []
+    for threads in (1, 4):
+        P.lib.port_rand_set_seed(0)
+        w = P.world(sc.bodies.copy(), sc.world_params(), 24, dyn=0, reorder=1)
+        w.set_threads(threads, 256)
+        w.attach_space(sc.geom_cls, sc.geom_body, sc.geom_pos, sc.geom_R, sc.geom_dims, sc.hash_levels, sc.maxc,
+                       sc.surface_mode, sc.surface())
+        nc = sum(w.sim_step() for _ in range(70))
+        out.append((nc, w.state()))
+    assert out[0][0] == out[1][0] > 2000
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_rand_known_answers():
     """misc.cpp:64-74 dTestRand golden LCG outputs, through the oracle's LCG."""
     from oracle.port.port import Port
