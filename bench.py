@@ -93,9 +93,19 @@ def host_threads(args) -> int:
     if args.ref_threads > 0:
         return args.ref_threads
     try:
-        return max(1, len(os.sched_getaffinity(0)))
+        n = len(os.sched_getaffinity(0))
     except AttributeError:
-        return max(1, os.cpu_count() or 1)
+        n = os.cpu_count() or 1
+    # a CPU quota below the visible cores (cgroup v2 cpu.max "quota period")
+    # would deschedule spinning threads: stay within it
+    try:
+        with open("/sys/fs/cgroup/cpu.max") as f:
+            quota, period = f.read().split()[:2]
+        if quota != "max":
+            n = min(n, max(1, int(int(quota) // int(period))))
+    except (OSError, ValueError):
+        pass
+    return max(1, n)
 
 
 class ClockSampler:
