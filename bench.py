@@ -311,6 +311,10 @@ def run_gbode(args, ws, rank, local):
         w.step_fused()
     w.sync()
     settled = w.state()
+    # the e2e and learned legs rerun the timed steps from this state (bodies
+    # and warm-start cache, gbodeWorldSaveSnapshot)
+    if not args.save_settled and L.gbodeWorldSaveSnapshot(w.w) != 1:
+        raise RuntimeError(L.gbodeGetLastError().decode())
     if args.save_settled:
         np.savez_compressed(args.save_settled, pos=settled[:, 0:3], q=settled[:, 3:7], lvel=settled[:, 19:22],
                             avel=settled[:, 22:25], seed=1 + rank, settle=args.settle + args.warmup)
@@ -345,6 +349,7 @@ def run_gbode(args, ws, rank, local):
     # e2e through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
+        restore_snapshot(L, w)
         host = w.state()
         h2d = 240 * sc.nb   # pos, q, R, lvel, avel, facc, tacc, I, invI as uploaded by the library
         d2h = 112 * sc.nb   # pos, q, R, lvel, avel as downloaded
@@ -361,7 +366,7 @@ def run_gbode(args, ws, rank, local):
     # learned warm start: the same settled state, the same timed loop
     learned = None
     if not args.no_learned:
-        learned = learned_leg(args, w, L, stream, flush, settled, T, sc.nb, ws, dev)
+        learned = learned_leg(args, w, L, stream, flush, T, sc.nb, ws, dev)
     # batched independent worlds: capsule chains with hinge/ball joints
     batched = None
     if not args.no_batched and ws == 1:
@@ -409,6 +414,11 @@ def run_gbode(args, ws, rank, local):
     print(json.dumps(line))
 
 
+def restore_snapshot(L, w):
+    if L.gbodeWorldRestoreSnapshot(w.w) != 1:
+        raise RuntimeError(L.gbodeGetLastError().decode())
+
+
 def batched_leg(args, L, stream, dev, kind):
     """Thousands of independent worlds as islands of one step, stepped by one
     fused step (one persistent PGS launch) and timed like the pile:
@@ -430,6 +440,9 @@ def batched_leg(args, L, stream, dev, kind):
         if not w.step_fused():
             raise RuntimeError(L.gbodeGetLastError().decode())
     w.sync()
+    # every leg runs the same steps: from this state (gbodeWorldSaveSnapshot)
+    if L.gbodeWorldSaveSnapshot(w.w) != 1:
+        raise RuntimeError(L.gbodeGetLastError().decode())
     setup_s = time.perf_counter() - t0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     out = {"workload": f"{kind}{args.chains if kind == 'chains' else args.vehicles}", "bodies": sc.nb,
@@ -439,6 +452,7 @@ def batched_leg(args, L, stream, dev, kind):
                                  ("residual", args.target, False), ("residual_graph", args.target, True)):
         if target > 0:
             L.gbodeWorldSetResidualTarget(w.w, target, args.check_every, args.max_iters)
+        restore_snapshot(L, w)
         for _ in range(args.warmup):
             if graph:
                 w.step_graph()
@@ -453,7 +467,9 @@ def batched_leg(args, L, stream, dev, kind):
                       "contacts_per_step": float(np.mean(T["contacts"])), "colours": int(np.median(T["colours"])),
                       "steps_at_target": ok}
     # solver settings tuned on the running world (gbodeWorldAutotune), then the residual leg again
+    restore_snapshot(L, w)
     tu = w.autotune(steps=3, graph=True)
+    restore_snapshot(L, w)
     for _ in range(args.warmup):
         w.step_graph()
     w.sync()
@@ -469,7 +485,9 @@ def batched_leg(args, L, stream, dev, kind):
     out["note"] = ("value counts steps at the residual target (residual) or every step at the configured 20 "
                    "sweeps (iterations20); the chains are islands of one world, solved by the same coloured "
                    "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused); "
-                   "*_tuned: after gbodeWorldAutotune chose the solver blocks, passes per group and check interval")
+                   "*_tuned: after gbodeWorldAutotune chose the solver blocks, passes per group and check interval; "
+                   "every leg starts from the same state (gbodeWorldRestoreSnapshot): W warm-up steps, then the "
+                   "same K timed steps")
     w.close()
     return out
 
@@ -505,22 +523,24 @@ def timed_steps(w, stream, flush, steps, graph=False):
     return out
 
 
-def learned_leg(args, w, L, stream, flush, settled, plain, nb, ws, dev):
-    """Learned warm start from the same settled state as the plain leg: W
-    untimed steps, then the same timed loop; residual target and counting
-    rules unchanged."""
+def learned_leg(args, w, L, stream, flush, plain, nb, ws, dev):
+    """Learned warm start on the plain leg's timed steps: W untimed steps
+    with the network, then the world's snapshot of the plain leg's start
+    (bodies and warm-start cache) is restored and the same timed loop runs;
+    residual target and counting rules unchanged."""
     import ctypes as C
     from ode_gb300 import learned
     path = args.weights or learned.WEIGHTS
     if not os.path.exists(path):
         return {"unavailable": f"no trained parameters at {os.path.relpath(path, ROOT)}"}
     params = learned.load(path)
-    w.set_state(settled)
+    restore_snapshot(L, w)
     if L.gbodeWorldSetLearnedWarmStart(w.w, params.ctypes.data_as(C.POINTER(C.c_float)), 1) != 1:
         return {"unavailable": L.gbodeGetLastError().decode()}
     for _ in range(args.warmup):
         w.step_fused()
     w.sync()
+    restore_snapshot(L, w)
     chosen, r_mlp, r_plain = [], [], []
     st = np.zeros(3, np.float32)
     T = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours")}

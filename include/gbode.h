@@ -443,6 +443,17 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */
 void gbodeWorldSetTiming(dWorldID w, int enabled);
 
+/* A device-side copy of the world's simulation state -- bodies, the
+ * warm-start cache, the joints' multipliers, the auto-disable state -- to
+ * rerun the same steps (benchmarks, tuning, rollback).  Save replaces the
+ * world's one snapshot; Restore puts it back (0 with gbodeGetLastError when
+ * bodies were added or removed, a device buffer grew, or the host changed a
+ * body, since the save); Drop frees it (dWorldDestroy does too).  Contacts,
+ * rows and space state are rebuilt by every step and are not part of it. */
+int gbodeWorldSaveSnapshot(dWorldID w);
+int gbodeWorldRestoreSnapshot(dWorldID w);
+void gbodeWorldDropSnapshot(dWorldID w);
+
 /* Solver settings tuned on the running world.  gbodeWorldAutotune makes one
  * plain fused step, copies the device-side state aside, and for each
  * candidate -- solver blocks: one per SM or half as many; passes over a

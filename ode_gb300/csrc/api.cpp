@@ -192,7 +192,82 @@ struct dxWorld {
     bool stats_pending = false;
     int last_host_contacts = 0;
     std::vector<dxJoint *> table_joints;  // the ball/hinge/hinge2 joints in device-table order
+    struct DevSnapshot *snapshot = nullptr;  // gbodeWorldSaveSnapshot
 };
+
+// A copy of a world's device-side simulation state: bodies, the warm-start
+// tables, the joints' multipliers, the auto-disable state and the counters.
+// Everything else on the device is rebuilt by every step.
+struct DevSnapshot {
+    std::vector<DBuf> copies;
+    std::vector<size_t> sizes;  // each source buffer's size at the save (0: not allocated)
+    int nbodies = 0;
+    bool warm_valid = false;
+    unsigned warm_mask = 0;
+    bool valid = false;
+    void release() {
+        for (DBuf &c : copies) c.release();
+        copies.clear();
+        sizes.clear();
+        valid = false;
+    }
+};
+
+static int snapshot_sources(Workspace &ws, DBuf **out) {
+    DBuf *keep[] = {&ws.b_pos, &ws.b_q, &ws.b_R, &ws.b_lvel, &ws.b_avel, &ws.b_facc, &ws.b_tacc, &ws.w_keys,
+                    &ws.w_lambda, &ws.j_lam, &ws.b_adis_i, &ws.b_adis_f, &ws.b_adis_buf};
+    const int n = (int)(sizeof keep / sizeof keep[0]);
+    for (int k = 0; k < n; k++) out[k] = keep[k];
+    return n;
+}
+static const int SNAP_MAX = 16;
+
+// Copies the state aside on the world's stream and waits for the copies.
+static bool snapshot_save(dxWorld *w, DevSnapshot &S) {
+    Workspace &ws = w->ws;
+    DBuf *src[SNAP_MAX];
+    const int n = snapshot_sources(ws, src);
+    S.valid = false;
+    S.copies.resize(n + 1);
+    S.sizes.assign(n, 0);
+    for (int k = 0; k < n; k++) {
+        if (!src[k]->p) continue;
+        S.sizes[k] = src[k]->bytes;
+        if (!S.copies[k].ensure(src[k]->bytes)) return false;
+        cudaMemcpyAsync(S.copies[k].p, src[k]->p, src[k]->bytes, cudaMemcpyDeviceToDevice, w->stream);
+    }
+    if (!S.copies[n].ensure(sizeof(DevCounters))) return false;
+    cudaMemcpyAsync(S.copies[n].p, ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
+    S.nbodies = (int)w->bodies.size();
+    S.warm_valid = ws.warm_valid;
+    S.warm_mask = ws.warm_mask;
+    S.valid = cudaStreamSynchronize(w->stream) == cudaSuccess;
+    return S.valid;
+}
+
+// false (nothing restored) when a buffer was allocated or resized since the save
+static bool snapshot_fits(dxWorld *w, const DevSnapshot &S) {
+    DBuf *src[SNAP_MAX];
+    const int n = snapshot_sources(w->ws, src);
+    if (!S.valid || (int)S.sizes.size() != n || S.nbodies != (int)w->bodies.size()) return false;
+    for (int k = 0; k < n; k++)
+        if ((src[k]->p ? src[k]->bytes : 0) != S.sizes[k]) return false;
+    return true;
+}
+
+static bool snapshot_restore(dxWorld *w, const DevSnapshot &S) {
+    if (!snapshot_fits(w, S)) return false;
+    Workspace &ws = w->ws;
+    DBuf *src[SNAP_MAX];
+    const int n = snapshot_sources(ws, src);
+    for (int k = 0; k < n; k++)
+        if (S.sizes[k]) cudaMemcpyAsync(src[k]->p, S.copies[k].p, S.sizes[k], cudaMemcpyDeviceToDevice, w->stream);
+    cudaMemcpyAsync(ws.dc, S.copies[n].p, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
+    if (cudaStreamSynchronize(w->stream) != cudaSuccess) return false;
+    ws.warm_valid = S.warm_valid && ws.warm_mask == S.warm_mask;
+    w->host_valid = false;
+    return true;
+}
 
 static dxWorld *g_default_world = nullptr;
 static std::vector<dxWorld *> g_worlds;
@@ -599,6 +674,7 @@ void dWorldDestroy(dWorldID w) {
     }
     if (w->stream) cudaStreamSynchronize(w->stream);
     drop_graph(w);
+    if (w->snapshot) { w->snapshot->release(); delete w->snapshot; }
     for (int i = 0; i < 4; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
     w->ws.release();
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
@@ -2097,38 +2173,14 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     // at the end, so the world leaves the tuner as it entered it
     if (!world_upload(w)) return 0;
     if (!w->host_valid) world_download(w);
-    Workspace &ws = w->ws;
-    DBuf *keep[] = {&ws.b_pos, &ws.b_q, &ws.b_R, &ws.b_lvel, &ws.b_avel, &ws.b_facc, &ws.b_tacc, &ws.w_keys,
-                    &ws.w_lambda, &ws.j_lam, &ws.b_adis_i, &ws.b_adis_f, &ws.b_adis_buf};
-    const int nkeep = (int)(sizeof keep / sizeof keep[0]);
-    std::vector<DBuf> copies(nkeep + 1);
-    const bool warm_valid = ws.warm_valid;
-    const unsigned warm_mask = ws.warm_mask;
-    auto save = [&]() -> bool {
-        for (int k = 0; k < nkeep; k++) {
-            if (!keep[k]->p) continue;
-            if (!copies[k].ensure(keep[k]->bytes)) return false;
-            cudaMemcpyAsync(copies[k].p, keep[k]->p, keep[k]->bytes, cudaMemcpyDeviceToDevice, w->stream);
-        }
-        if (!copies[nkeep].ensure(sizeof(DevCounters))) return false;
-        cudaMemcpyAsync(copies[nkeep].p, ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
-        return cudaStreamSynchronize(w->stream) == cudaSuccess;
-    };
-    auto restore = [&]() {
-        for (int k = 0; k < nkeep; k++)
-            if (keep[k]->p && copies[k].p && keep[k]->bytes == copies[k].bytes)
-                cudaMemcpyAsync(keep[k]->p, copies[k].p, keep[k]->bytes, cudaMemcpyDeviceToDevice, w->stream);
-        cudaMemcpyAsync(ws.dc, copies[nkeep].p, sizeof(DevCounters), cudaMemcpyDeviceToDevice, w->stream);
-        cudaStreamSynchronize(w->stream);
-        ws.warm_valid = warm_valid && ws.warm_mask == warm_mask;
-        w->host_valid = false;
-    };
-    auto release = [&]() { for (DBuf &c : copies) c.release(); };
+    DevSnapshot snap;
+    auto restore = [&]() { snapshot_restore(w, snap); };
+    auto release = [&]() { snap.release(); };
     // one plain step settles buffer sizes (a later reallocation would not be restored)
     const SolverParams saved = w->P;
     if (!gbodeWorldStepFused(w, space, group, sp, maxc, dt, 0)) return 0;
     if (cudaStreamSynchronize(w->stream) != cudaSuccess) return 0;
-    if (!save()) { set_error("gbodeWorldAutotune: device allocation"); release(); return 0; }
+    if (!snapshot_save(w, snap)) { set_error("gbodeWorldAutotune: device allocation"); release(); return 0; }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -2179,6 +2231,35 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     best->ms_per_step = best_ms;
     best->candidates = (int)cands.size();
     return 1;
+}
+
+int gbodeWorldSaveSnapshot(dWorldID w) {
+    if (!w) { set_error("gbodeWorldSaveSnapshot: no world"); return 0; }
+    if (!world_init_device(w) || !world_upload(w)) return 0;
+    if (!w->snapshot) w->snapshot = new DevSnapshot();
+    if (!snapshot_save(w, *w->snapshot)) {
+        w->snapshot->release();
+        set_error("gbodeWorldSaveSnapshot: device allocation", cudaGetLastError());
+        return 0;
+    }
+    return 1;
+}
+
+int gbodeWorldRestoreSnapshot(dWorldID w) {
+    if (!w || !w->snapshot || !w->snapshot->valid) { set_error("gbodeWorldRestoreSnapshot: no snapshot"); return 0; }
+    if (w->dev_dirty) {
+        set_error("gbodeWorldRestoreSnapshot: the host changed the world since the snapshot");
+        return 0;
+    }
+    if (!snapshot_restore(w, *w->snapshot)) {
+        set_error("gbodeWorldRestoreSnapshot: the world's bodies or device buffers changed since the snapshot");
+        return 0;
+    }
+    return 1;
+}
+
+void gbodeWorldDropSnapshot(dWorldID w) {
+    if (w && w->snapshot) w->snapshot->release();
 }
 
 int gbodeSolveLCPBatch(int count, int n, const double *A, const double *b, const double *lo, const double *hi, int nub,

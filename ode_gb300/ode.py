@@ -162,6 +162,8 @@ _PROTOS = [
                                           ctypes.c_void_p]),
     ("gbodeWorldAutotune", ctypes.c_int, [ID, ID, ID, ctypes.c_void_p, ctypes.c_int, dReal, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p]),
+    ("gbodeWorldSaveSnapshot", ctypes.c_int, [ID]), ("gbodeWorldRestoreSnapshot", ctypes.c_int, [ID]),
+    ("gbodeWorldDropSnapshot", None, [ID]),
     ("gbodeSpaceCollideContacts", ctypes.c_int, [ID, ID, ID, ctypes.POINTER(dSurfaceParameters), ctypes.c_int]),
     ("gbodeHashSpaceSetExactPairs", None, [ID, ctypes.c_int]),
     ("gbodeWorldSetStream", None, [ID, ctypes.c_void_p]), ("gbodeWorldGetStream", ctypes.c_void_p, [ID]),

@@ -182,3 +182,36 @@ def test_staging_waves_give_the_same_solution(gblib):
     assert np.array_equal(a, b), float(np.abs(a - b).max())
     for w in worlds:
         w.close()
+
+
+def test_snapshot_reruns_the_same_steps(gblib):
+    """gbodeWorldSaveSnapshot / gbodeWorldRestoreSnapshot: a 2,048-body pile
+    with the warm-start cache on, 60 fused steps, a snapshot, 10 steps; the
+    restore and the same 10 steps again give the same state to the bit (the
+    fused step is deterministic and the snapshot holds the bodies and the
+    warm-start cache).  A restore after a body was added fails with a message
+    and changes nothing."""
+    from ode_gb300 import scenes, sim
+    L = gblib
+    sc = scenes.pile(2048, seed=7)
+    w = sim.GBWorld(sc)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    for _ in range(60):
+        w.step_fused()
+    assert L.gbodeWorldSaveSnapshot(w.w) == 1, L.gbodeGetLastError()
+    start = w.state()
+    for _ in range(10):
+        w.step_fused()
+    a = w.state()
+    assert L.gbodeWorldRestoreSnapshot(w.w) == 1, L.gbodeGetLastError()
+    np.testing.assert_array_equal(w.state(), start)
+    for _ in range(10):
+        w.step_fused()
+    b = w.state()
+    assert np.abs(a - start).max() > 1e-4  # the pile moved
+    np.testing.assert_array_equal(a, b)
+    L.dBodyCreate(w.w)
+    assert L.gbodeWorldRestoreSnapshot(w.w) == 0
+    assert b"changed" in L.gbodeGetLastError()
+    L.gbodeWorldDropSnapshot(w.w)
+    w.close()
