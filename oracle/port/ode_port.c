@@ -1991,20 +1991,32 @@ int port_sim_step(port_sim *s) {
     for (int k = 0; k < s->nj; k++) cidx[k] = k;
     int *stepped = (int *)malloc(sizeof(int) * (w->nb > 0 ? w->nb : 1));
     world_quickstep(w, s->joints, s->nj, cidx, NULL, NULL, NULL, stepped);
-    /* dGeomMoved for each stepped body's geom: move to the list head if clean
-     * (collision_space.cpp:49-75, 205-209) */
+    /* dGeomMoved for each stepped body's geom: a clean geom is marked dirty
+     * and moved to the head of the space's list (collision_space.cpp:49-75,
+     * 205-209).  The moves are applied at once: the moved geoms, last moved
+     * first, then the others in their previous order -- the list the
+     * one-at-a-time moves leave, in O(geoms) instead of O(geoms^2). */
     int *geom_of = (int *)malloc(sizeof(int) * (w->nb > 0 ? w->nb : 1));
+    int *moved = (int *)malloc(sizeof(int) * (s->ng > 0 ? s->ng : 1));
+    unsigned char *was_moved = (unsigned char *)calloc(s->ng > 0 ? s->ng : 1, 1);
+    int *list2 = (int *)malloc(sizeof(int) * (s->ng > 0 ? s->ng : 1));
     for (int i = 0; i < w->nb; i++) geom_of[i] = -1;
     for (int g = 0; g < s->ng; g++) if (s->body[g] >= 0) geom_of[s->body[g]] = g;
+    int nmoved = 0;
     for (int k = 0; k < w->nb; k++) {
         int g = geom_of[stepped[k]];
         if (g < 0 || s->dirty[g]) continue;
         s->dirty[g] = 1;
-        int p = 0;
-        while (s->list[p] != g) p++;
-        memmove(s->list + 1, s->list, sizeof(int) * p);
-        s->list[0] = g;
+        was_moved[g] = 1;
+        moved[nmoved++] = g;
     }
+    if (nmoved > 0) {
+        int p = 0;
+        for (int k = nmoved - 1; k >= 0; k--) list2[p++] = moved[k];
+        for (int k = 0; k < s->ng; k++) if (!was_moved[s->list[k]]) list2[p++] = s->list[k];
+        memcpy(s->list, list2, sizeof(int) * s->ng);
+    }
+    free(list2); free(was_moved); free(moved);
     free(geom_of); free(stepped); free(cidx);
     return s->nj;
 }
