@@ -480,16 +480,59 @@ def batched_leg(args, L, stream, dev, kind):
                                    "sweeps_per_step": float(np.mean(T["sweeps"])), "steps_at_target": ok,
                                    "tuning": {"blocks": tu.blocks, "passes": tu.passes,
                                               "check_every": tu.check_every, "candidates": tu.candidates}}
+    if kind == "vehicles" and not args.no_learned:
+        out["residual_learned_tuned_graph"] = learned_batched(args, L, w, stream, flush, sc.nb)
     r64, _, ml = w.last_residual()
     out["fp64_residual_last_step"] = r64 / max(1.0, ml)
     out["note"] = ("value counts steps at the residual target (residual) or every step at the configured 20 "
                    "sweeps (iterations20); the chains are islands of one world, solved by the same coloured "
                    "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused); "
                    "*_tuned: after gbodeWorldAutotune chose the solver blocks, passes per group and check interval; "
+                   "*_learned_*: the learned warm start with the plain start as fallback (per step, whichever "
+                   "start has the lower residual), on the tuned settings; "
                    "every leg starts from the same state (gbodeWorldRestoreSnapshot): W warm-up steps, then the "
                    "same K timed steps")
     w.close()
     return out
+
+
+def learned_batched(args, L, w, stream, flush, nb):
+    """The residual leg of a batched workload with the learned warm start
+    (the plain previous-step start as fallback), graph-replayed: W untimed
+    steps, the world's snapshot restored, the same K timed steps as the other
+    legs."""
+    import ctypes as C
+    from ode_gb300 import learned
+    path = args.weights or learned.WEIGHTS
+    if not os.path.exists(path):
+        return {"unavailable": f"no trained parameters at {os.path.relpath(path, ROOT)}"}
+    params = learned.load(path)
+    try:
+        restore_snapshot(L, w)
+        if L.gbodeWorldSetLearnedWarmStart(w.w, params.ctypes.data_as(C.POINTER(C.c_float)), 1) != 1:
+            return {"unavailable": L.gbodeGetLastError().decode()}
+        for _ in range(args.warmup):
+            w.step_graph()
+        w.sync()
+        restore_snapshot(L, w)
+        st = np.zeros(3, np.float32)
+        chosen = []
+        T = {k: [] for k in ("step_ms", "sweeps", "resid")}
+        for _ in range(args.steps):
+            t = timed_steps(w, stream, flush, 1, graph=True)
+            for k in T:
+                T[k] += t[k]
+            L.gbodeWorldGetLearnedStats(w.w, st.ctypes.data_as(C.POINTER(C.c_float)))
+            chosen.append(float(st[0]))
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    finally:
+        L.gbodeWorldSetLearnedWarmStart(w.w, None, 0)
+    ms = sum(T["step_ms"])
+    ok = sum(1 for r in T["resid"] if r <= args.target)
+    return {"body_steps_per_s": nb * ok / (ms / 1e3), "ms_per_step": ms / args.steps,
+            "sweeps_per_step": float(np.mean(T["sweeps"])), "steps_at_target": ok,
+            "mlp_start_chosen": float(np.mean(chosen)), "weights": os.path.relpath(path, ROOT)}
 
 
 def timed_steps(w, stream, flush, steps, graph=False):
