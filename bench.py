@@ -498,9 +498,9 @@ def batched_leg(args, L, stream, dev, kind):
 
 def learned_batched(args, L, w, stream, flush, nb):
     """The residual leg of a batched workload with the learned warm start
-    (the plain previous-step start as fallback), graph-replayed: W untimed
-    steps, the world's snapshot restored, the same K timed steps as the other
-    legs."""
+    (the plain previous-step start as fallback), graph-replayed: like the
+    other legs, the world's snapshot restored, W untimed steps (they also
+    record the graph), then the same K timed steps."""
     import ctypes as C
     from ode_gb300 import learned
     path = args.weights or learned.WEIGHTS
@@ -514,7 +514,6 @@ def learned_batched(args, L, w, stream, flush, nb):
         for _ in range(args.warmup):
             w.step_graph()
         w.sync()
-        restore_snapshot(L, w)
         st = np.zeros(3, np.float32)
         chosen = []
         T = {k: [] for k in ("step_ms", "sweeps", "resid")}
