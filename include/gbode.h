@@ -305,6 +305,8 @@ void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z);        /* objec
 void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* objects.h:1977 */
 void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);       /* objects.h:1983 */
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);         /* objects.h:1991 */
+/* the axis, with the current relative rotation taken as the given angle */
+void dJointSetHingeAxisOffset(dJointID j, dReal x, dReal y, dReal z, dReal angle); /* objects.h:2021 */
 void dJointSetHingeParam(dJointID j, int parameter, dReal value);        /* objects.h:2027 */
 void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* objects.h:2555 */
 dReal dJointGetBallParam(dJointID j, int parameter);                      /* objects.h:2573 */
@@ -319,6 +321,8 @@ void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z);             /*
 void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z);             /* objects.h:2104 */
 void dJointSetHinge2Param(dJointID j, int parameter, dReal value);             /* objects.h:2110 */
 void dJointGetHinge2Anchor(dJointID j, dVector3 result);                       /* objects.h:2663 */
+void dJointGetHinge2Axis1(dJointID j, dVector3 result);                        /* objects.h:2679 */
+void dJointGetHinge2Axis2(dJointID j, dVector3 result);                        /* objects.h:2685 */
 dReal dJointGetHinge2Param(dJointID j, int parameter);                          /* objects.h:2691 */
 dReal dJointGetHinge2Angle1(dJointID j);                                        /* objects.h:2697 */
 
@@ -332,6 +336,10 @@ void dRSetIdentity(dMatrix3 R);
 void dRFromAxisAndAngle(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal angle);
 void dRfromQ(dMatrix3 R, const dQuaternion q);
 void dQFromAxisAndAngle(dQuaternion q, dReal ax, dReal ay, dReal az, dReal angle);
+/* odemath.h:521-523: scale to unit length by the largest component; a zero
+ * vector is left as it is (dSafeNormalize3 returns 0 for it) */
+int dSafeNormalize3(dVector3 a);
+void dNormalize3(dVector3 a);
 
 /* ======================================================================
  * gbode extensions (no ODE counterpart)

@@ -1373,6 +1373,15 @@ static bool safe_normalize3(float *a) {
     a[idx] = copysignf(l, a[idx]);
     return true;
 }
+// odemath.cpp:37-50: dSafeNormalize3 / dNormalize3 (the reference's dNormalize3
+// asserts on a zero vector; here it is left unchanged)
+int dSafeNormalize3(dVector3 a) {
+    float v[3] = {(float)a[0], (float)a[1], (float)a[2]};
+    const bool ok = safe_normalize3(v);
+    a[0] = v[0]; a[1] = v[1]; a[2] = v[2];
+    return ok ? 1 : 0;
+}
+void dNormalize3(dVector3 a) { dSafeNormalize3(a); }
 // joint.cpp:325-360 setAxes: either target may be null
 static void set_axes(dxJoint *j, float x, float y, float z, float *ax1, float *ax2) {
     world_download(j->world);
@@ -1441,6 +1450,22 @@ void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z) {
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z) {
     set_axes(j, x, y, z, j->axis1, j->axis2);
     hinge_qrel(j);
+}
+// hinge.cpp:211-228: the axis, then the initial relative rotation turned by
+// the angle about it (dQMultiply3(qrel, q_angle, qrel), rotation.cpp:221-228)
+void dJointSetHingeAxisOffset(dJointID j, dReal x, dReal y, dReal z, dReal dangle) {
+    set_axes(j, x, y, z, j->axis1, j->axis2);
+    hinge_qrel(j);
+    if (!j->b1 && j->b2) dangle = -dangle;  // dJOINT_REVERSE
+    dQuaternion qa;
+    dQFromAxisAndAngle(qa, x, y, z, dangle);
+    const float *qc = j->qrel;
+    const float q0 = qa[0] * qc[0] - qa[1] * qc[1] - qa[2] * qc[2] - qa[3] * qc[3];
+    const float q1 = -qa[0] * qc[1] - qa[1] * qc[0] + qa[2] * qc[3] - qa[3] * qc[2];
+    const float q2 = -qa[0] * qc[2] - qa[2] * qc[0] + qa[3] * qc[1] - qa[1] * qc[3];
+    const float q3 = -qa[0] * qc[3] - qa[3] * qc[0] + qa[1] * qc[2] - qa[2] * qc[1];
+    j->qrel[0] = q0; j->qrel[1] = q1; j->qrel[2] = q2; j->qrel[3] = q3;
+    j->world->joints_dirty = true;
 }
 // joint.cpp:363-393 getAnchor: anchor1 in world coordinates (reverse: anchor2 from node 1)
 static void anchor_world(dxJoint *j, dVector3 out, const float *a, bool second) {
@@ -1578,6 +1603,18 @@ dReal dJointGetHinge2Param(dJointID j, int parameter) {
 void dJointGetHinge2Anchor(dJointID j, dVector3 out) {
     bool rev = !j->b1 && j->b2;
     anchor_world(j, out, rev ? j->anchor2 : j->anchor1, rev);
+}
+// hinge2.cpp:377-411: the axes in world coordinates from the first and the
+// second attached body (zero without that body)
+void dJointGetHinge2Axis1(dJointID j, dVector3 out) {
+    world_download(j->world);
+    if (j->node0()) mul0_331h(out, j->node0()->R, j->axis1);
+    else out[0] = out[1] = out[2] = 0;
+}
+void dJointGetHinge2Axis2(dJointID j, dVector3 out) {
+    world_download(j->world);
+    if (j->node1()) mul0_331h(out, j->node1()->R, j->axis2);
+    else out[0] = out[1] = out[2] = 0;
 }
 // hinge2.cpp:33-51 measureAngle1
 dReal dJointGetHinge2Angle1(dJointID j) {

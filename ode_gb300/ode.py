@@ -185,6 +185,9 @@ _PROTOS = [
     ("dJointSetBallParam", None, [ID, ctypes.c_int, dReal]),
     ("dJointSetHingeAnchor", None, [ID, dReal, dReal, dReal]),
     ("dJointSetHingeAxis", None, [ID, dReal, dReal, dReal]),
+    ("dJointSetHingeAxisOffset", None, [ID, dReal, dReal, dReal, dReal]),
+    ("dJointGetHinge2Axis1", None, [ID, _F]), ("dJointGetHinge2Axis2", None, [ID, _F]),
+    ("dSafeNormalize3", ctypes.c_int, [_F]), ("dNormalize3", None, [_F]),
     ("dJointSetHingeParam", None, [ID, ctypes.c_int, dReal]),
     ("dJointGetBallAnchor", None, [ID, _F]), ("dJointGetBallParam", dReal, [ID, ctypes.c_int]),
     ("dJointGetHingeAnchor", None, [ID, _F]), ("dJointGetHingeAxis", None, [ID, _F]),

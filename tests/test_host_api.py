@@ -1,0 +1,209 @@
+"""Host-side behaviour of the C ABI that needs no GPU: joint geometry set and
+read on the host (anchors, axes, hinge angle with an axis offset), world
+defaults copied into new bodies, and the error returns of calls without the
+state they need.  The hinge cases restate the reference's own unit tests
+(tests/joints/hinge.cpp:103-784): a hinge between two bodies, or one body
+and the static environment, an axis along +X or -X, one body turned about
+X; the angle reads back the turn with the sign the axis and the body give,
+dJointSetHingeAxisOffset with that angle keeps it, and turning the body back
+reads 0 (tolerance 1e-4, as there)."""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def L():
+    from ode_gb300 import build, ode
+    return ode.load(build.build())
+
+
+def _vec(n=4):
+    return (ctypes.c_float * n)()
+
+
+def _turn(L, body, angle):
+    R = _vec(12)
+    L.dRFromAxisAndAngle(R, 1.0, 0.0, 0.0, angle)
+    L.dBodySetRotation(body, R)
+
+
+# (bodies attached, axis x, turned body, turn angle, angle read back);
+# "b1b2": dJointAttach(j, b1, b2), "b1": (j, b1, NULL), "b2": (j, NULL, b2)
+HALF_PI = math.pi / 2
+HINGE_CASES = [
+    ("b1b2", +1, "b2", +HALF_PI, -HALF_PI),
+    ("b1b2", +1, "b2", -HALF_PI, +HALF_PI),
+    ("b1b2", +1, "b1", +0.23, +0.23),
+    ("b1b2", +1, "b1", -0.23, -0.23),
+    ("b1b2", -1, "b2", +HALF_PI, +HALF_PI),
+    ("b1b2", -1, "b2", -HALF_PI, -HALF_PI),
+    ("b1b2", -1, "b1", +0.23, -0.23),
+    ("b1b2", -1, "b1", -0.23, +0.23),
+    ("b1", +1, "b1", +HALF_PI, +HALF_PI),
+    ("b1", +1, "b1", -0.23, -0.23),
+    ("b1", -1, "b1", +HALF_PI, -HALF_PI),
+    ("b1", -1, "b1", -0.23, +0.23),
+    ("b2", +1, "b2", +HALF_PI, -HALF_PI),
+    ("b2", +1, "b2", -0.23, +0.23),
+]
+
+
+@pytest.mark.parametrize("attach,ax,turned,angle,expect", HINGE_CASES)
+def test_hinge_angle_and_axis_offset(L, attach, ax, turned, angle, expect):
+    w = L.dWorldCreate()
+    b1 = L.dBodyCreate(w) if "b1" in attach else None
+    b2 = L.dBodyCreate(w) if "b2" in attach else None
+    if b1:
+        L.dBodySetPosition(b1, 0.0, -1.0 if b2 else 0.0, 0.0)
+    if b2:
+        L.dBodySetPosition(b2, 0.0, 1.0 if b1 else 0.0, 0.0)
+    j = L.dJointCreateHinge(w, None)
+    L.dJointAttach(j, b1, b2)
+    L.dJointSetHingeAnchor(j, 0.0, 0.0, 0.0)
+    L.dJointSetHingeAxis(j, float(ax), 0.0, 0.0)
+    body = b1 if turned == "b1" else b2
+    assert abs(L.dJointGetHingeAngle(j)) < 1e-4
+    _turn(L, body, angle)
+    assert abs(L.dJointGetHingeAngle(j) - expect) < 1e-4
+    L.dJointSetHingeAxisOffset(j, float(ax), 0.0, 0.0, expect)
+    assert abs(L.dJointGetHingeAngle(j) - expect) < 1e-4
+    _turn(L, body, 0.0)
+    assert abs(L.dJointGetHingeAngle(j)) < 1e-4
+    L.dWorldDestroy(w)
+
+
+def test_hinge_default_axis_is_x(L):
+    """tests/joints/hinge.cpp:103-133: without dJointSetHingeAxis the axis is
+    +X (hinge.cpp:46-63); turning the second body by +90 deg reads -90."""
+    w = L.dWorldCreate()
+    b1, b2 = L.dBodyCreate(w), L.dBodyCreate(w)
+    L.dBodySetPosition(b1, 0.0, -1.0, 0.0)
+    j = L.dJointCreateHinge(w, None)
+    L.dJointAttach(j, b1, b2)
+    L.dJointSetHingeAnchor(j, 0.0, 0.0, 0.0)
+    _turn(L, b2, HALF_PI)
+    assert abs(L.dJointGetHingeAngle(j) + HALF_PI) < 1e-4
+    L.dJointSetHingeAxisOffset(j, 1.0, 0.0, 0.0, -HALF_PI)
+    assert abs(L.dJointGetHingeAngle(j) + HALF_PI) < 1e-4
+    _turn(L, b2, 0.0)
+    assert abs(L.dJointGetHingeAngle(j)) < 1e-4
+    L.dWorldDestroy(w)
+
+
+def _turned_pair(L, w):
+    """tests/joints/ball.cpp:41-90, hinge2.cpp:36-85: two bodies at
+    (-1, -2, -3) and (11, 22, 33), each turned 27 deg about its own axis."""
+    a, b = L.dBodyCreate(w), L.dBodyCreate(w)
+    L.dBodySetPosition(a, -1.0, -2.0, -3.0)
+    L.dBodySetPosition(b, 11.0, 22.0, 33.0)
+    for body, axis in ((a, (0.53, -0.71, 0.43)), (b, (1.2, 0.87, -0.33))):
+        v = _vec(4)
+        v[0], v[1], v[2] = axis
+        L.dNormalize3(v)
+        R = _vec(12)
+        L.dRFromAxisAndAngle(R, v[0], v[1], v[2], 0.47123)
+        L.dBodySetRotation(body, R)
+    return a, b
+
+
+def test_ball_anchor_set_to_itself(L):
+    """A ball joint's anchor read back and set again reads the same anchor and
+    leaves the bodies where they were (the set-up of tests/joints/ball.cpp)."""
+    w = L.dWorldCreate()
+    a, b = _turned_pair(L, w)
+    j = L.dJointCreateBall(w, None)
+    L.dJointAttach(j, a, b)
+    q0 = np.array(L.dBodyGetQuaternion(a)[:4]), np.array(L.dBodyGetQuaternion(b)[:4])
+    anc = _vec()
+    L.dJointGetBallAnchor(j, anc)
+    L.dJointSetBallAnchor(j, anc[0], anc[1], anc[2])
+    anc2 = _vec()
+    L.dJointGetBallAnchor(j, anc2)
+    assert np.allclose(anc[:3], anc2[:3], atol=1e-4)
+    assert np.allclose(q0[0], L.dBodyGetQuaternion(a)[:4]) and np.allclose(q0[1], L.dBodyGetQuaternion(b)[:4])
+    L.dWorldDestroy(w)
+
+
+def test_hinge2_axes_set_to_themselves(L):
+    """tests/joints/hinge2.cpp:101-114: a hinge2's anchor and axes read back
+    and set again (both axes, the first alone, the second alone) read the
+    same; the axes are unit vectors in world coordinates."""
+    w = L.dWorldCreate()
+    a, b = _turned_pair(L, w)
+    j = L.dJointCreateHinge2(w, None)
+    L.dJointAttach(j, a, b)
+    L.dJointSetHinge2Axis1(j, 0.0, 0.0, 1.0)
+    L.dJointSetHinge2Axis2(j, 0.0, 1.0, 0.0)
+    anc = _vec()
+    L.dJointGetHinge2Anchor(j, anc)
+    L.dJointSetHinge2Anchor(j, anc[0], anc[1], anc[2])
+    x1, x2 = _vec(), _vec()
+    L.dJointGetHinge2Axis1(j, x1)
+    L.dJointGetHinge2Axis2(j, x2)
+    assert np.allclose(x1[:3], [0, 0, 1], atol=1e-5) and np.allclose(x2[:3], [0, 1, 0], atol=1e-5)
+    for first, second in ((x1, x2), (x1, None), (None, x2)):
+        L.dJointSetHinge2Axes(j, first, second)
+        y1, y2 = _vec(), _vec()
+        L.dJointGetHinge2Axis1(j, y1)
+        L.dJointGetHinge2Axis2(j, y2)
+        assert np.allclose(y1[:3], x1[:3], atol=1e-5) and np.allclose(y2[:3], x2[:3], atol=1e-5)
+    L.dWorldDestroy(w)
+
+
+def test_safe_normalize3(L):
+    """odemath.cpp:95-165: unit length by the largest component, sign kept;
+    a zero vector stays zero and returns 0."""
+    v = _vec()
+    v[0], v[1], v[2] = 3.0, -4.0, 0.0
+    assert L.dSafeNormalize3(v) == 1
+    assert np.allclose(v[:3], [0.6, -0.8, 0.0], atol=1e-6)
+    z = _vec()
+    assert L.dSafeNormalize3(z) == 0 and list(z[:3]) == [0.0, 0.0, 0.0]
+
+
+def test_world_defaults_reach_new_bodies(L):
+    """A body takes the world's auto-disable and damping settings when it is
+    created (objects.cpp:55-69, ode.cpp:265-285 dBodySetAutoDisableDefaults,
+    dBodySetDampingDefaults); bodies made before keep theirs."""
+    w = L.dWorldCreate()
+    before = L.dBodyCreate(w)
+    L.dWorldSetAutoDisableFlag(w, 1)
+    L.dWorldSetAutoDisableSteps(w, 7)
+    L.dWorldSetLinearDamping(w, 0.25)
+    L.dWorldSetAngularDamping(w, 0.5)
+    after = L.dBodyCreate(w)
+    assert L.dBodyGetAutoDisableFlag(before) == 0 and L.dBodyGetAutoDisableFlag(after) == 1
+    assert L.dBodyGetAutoDisableSteps(after) == 7
+    assert abs(L.dBodyGetLinearDamping(after) - 0.25) < 1e-7 and abs(L.dBodyGetAngularDamping(after) - 0.5) < 1e-7
+    assert L.dBodyGetLinearDamping(before) == 0.0
+    L.dWorldDestroy(w)
+
+
+def test_connected_bodies(L):
+    """ode.cpp dAreConnected / dAreConnectedExcluding through a ball joint."""
+    w = L.dWorldCreate()
+    a, b, c = L.dBodyCreate(w), L.dBodyCreate(w), L.dBodyCreate(w)
+    j = L.dJointCreateBall(w, None)
+    L.dJointAttach(j, a, b)
+    assert L.dAreConnected(a, b) and L.dAreConnected(b, a) and not L.dAreConnected(a, c)
+    from ode_gb300 import ode
+    assert not L.dAreConnectedExcluding(a, b, ode.dJointTypeBall)
+    assert L.dAreConnectedExcluding(a, b, ode.dJointTypeContact)
+    L.dWorldDestroy(w)
+
+
+def test_snapshot_calls_without_a_snapshot(L):
+    """gbodeWorldRestoreSnapshot without a saved snapshot (or without a world)
+    returns 0 with a message and touches nothing."""
+    w = L.dWorldCreate()
+    assert L.gbodeWorldRestoreSnapshot(w) == 0
+    assert b"no snapshot" in L.gbodeGetLastError()
+    assert L.gbodeWorldRestoreSnapshot(None) == 0
+    L.gbodeWorldDropSnapshot(w)
+    L.gbodeWorldDropSnapshot(None)
+    L.dWorldDestroy(w)
