@@ -207,3 +207,29 @@ def test_snapshot_calls_without_a_snapshot(L):
     L.gbodeWorldDropSnapshot(w)
     L.gbodeWorldDropSnapshot(None)
     L.dWorldDestroy(w)
+
+
+def test_hinge_axis_and_anchor_set_to_themselves(L):
+    """tests/joints/hinge.cpp:848-865: a hinge between two turned bodies with
+    its axis and anchor read back and set again keeps the bodies' poses, the
+    axis, the anchor and a zero angle (the stepping half of that test needs
+    the device)."""
+    w = L.dWorldCreate()
+    a, b = _turned_pair(L, w)
+    j = L.dJointCreateHinge(w, None)
+    L.dJointAttach(j, a, b)
+    q0 = [np.array(L.dBodyGetQuaternion(x)[:4]) for x in (a, b)]
+    ax, anc = _vec(), _vec()
+    L.dJointGetHingeAxis(j, ax)
+    L.dJointSetHingeAxis(j, ax[0], ax[1], ax[2])
+    L.dJointGetHingeAnchor(j, anc)
+    L.dJointSetHingeAnchor(j, anc[0], anc[1], anc[2])
+    ax2, anc2 = _vec(), _vec()
+    L.dJointGetHingeAxis(j, ax2)
+    L.dJointGetHingeAnchor(j, anc2)
+    assert np.allclose(ax[:3], ax2[:3], atol=1e-6) and np.allclose(anc[:3], anc2[:3], atol=1e-5)
+    assert abs(np.linalg.norm(np.array(ax2[:3])) - 1.0) < 1e-6
+    for x, q in zip((a, b), q0):
+        assert np.allclose(L.dBodyGetQuaternion(x)[:4], q, atol=1e-6)
+    assert abs(L.dJointGetHingeAngle(j)) < 1e-4
+    L.dWorldDestroy(w)
