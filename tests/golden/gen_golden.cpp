@@ -14,10 +14,16 @@
 //   loop IN OUT        the full user loop (dSpaceCollide -> near callback ->
 //                      dCollide -> dJointCreateContact -> dWorldQuickStep ->
 //                      dJointGroupEmpty) with per-step states and snapshots
+//   timing IN OUT      the full user loop on a large scene with the reference's
+//                      opt-in multi-threaded stepping (built-in thread pool,
+//                      dWorldSetStepThreadingImplementation): wall-clock seconds
+//                      of dSpaceCollide + contact joints and of dWorldQuickStep
+//                      per step (a timing of the reference itself, not a golden)
 //   chain IN OUT       bodies linked by ball and hinge joints (hinge limits),
 //                      no geoms, stepped with dWorldQuickStep: per-step body
 //                      poses and hinge angles (dJointGetHingeAngle)
 #include <ode/ode.h>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -434,6 +440,86 @@ static void mode_chain() {
     dWorldDestroy(w);
 }
 
+// ---------------------------------------------------------------- timing
+struct TimingCtx { dWorldID world; dJointGroupID group; int maxc; int mode; float surf[8]; int made; };
+static void timing_cb(void *data, dGeomID o1, dGeomID o2) {
+    TimingCtx *T = (TimingCtx *)data;
+    dBodyID b1 = dGeomGetBody(o1), b2 = dGeomGetBody(o2);
+    dContact contact[16];
+    for (int i = 0; i < T->maxc; i++) {
+        memset(&contact[i], 0, sizeof(dContact));
+        contact[i].surface.mode = T->mode;
+        contact[i].surface.mu = T->surf[0]; contact[i].surface.mu2 = T->surf[1];
+        contact[i].surface.bounce = T->surf[2]; contact[i].surface.bounce_vel = T->surf[3];
+        contact[i].surface.soft_erp = T->surf[4]; contact[i].surface.soft_cfm = T->surf[5];
+    }
+    int n = dCollide(o1, o2, T->maxc, &contact[0].geom, sizeof(dContact));
+    for (int i = 0; i < n; i++) {
+        dJointID c = dJointCreateContact(T->world, T->group, &contact[i]);
+        dJointAttach(c, b1, b2);
+    }
+    T->made += n;
+}
+static void mode_timing() {
+    int nb = rdi(), ng = rdi(), nsteps = rdi(), iters = rdi(), threads = rdi(), maxc = rdi(), mode = rdi();
+    int minlevel = rdi(), maxlevel = rdi();
+    WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
+    float surf[8]; rd(surf, 8);
+    std::vector<float> bodies(BODY_IN * nb); rd(bodies.data(), bodies.size());
+    std::vector<int> gcls(ng), gbody(ng);
+    std::vector<float> gpos(3 * ng), gR(12 * ng), gdims(4 * ng);
+    rd(gcls.data(), ng); rd(gbody.data(), ng); rd(gpos.data(), gpos.size()); rd(gR.data(), gR.size()); rd(gdims.data(), gdims.size());
+
+    dWorldID w = dWorldCreate();
+    apply_params(w, P, iters, 0);
+    dThreadingImplementationID impl = 0;
+    dThreadingThreadPoolID pool = 0;
+    if (threads > 1) {
+        impl = dThreadingAllocateMultiThreadedImplementation();
+        pool = dThreadingAllocateThreadPool(threads, 0, dAllocateFlagBasicData, NULL);
+        dThreadingThreadPoolServeMultiThreadedImplementation(pool, impl);
+        dWorldSetStepIslandsProcessingMaxThreadCount(w, threads);
+        dWorldSetStepThreadingImplementation(w, dThreadingImplementationGetFunctions(impl), impl);
+    }
+    std::vector<dBodyID> b(nb);
+    for (int i = 0; i < nb; i++) { b[i] = dBodyCreate(w); set_body(b[i], &bodies[BODY_IN * i]); }
+    dSpaceID sp = dHashSpaceCreate(0);
+    dHashSpaceSetLevels(sp, minlevel, maxlevel);
+    for (int i = 0; i < ng; i++) {
+        dGeomID g = make_geom(sp, gcls[i], &gpos[3 * i], &gR[12 * i], &gdims[4 * i]);
+        if (gbody[i] >= 0) dGeomSetBody(g, b[gbody[i]]);
+    }
+    TimingCtx T; T.world = w; T.group = dJointGroupCreate(0); T.maxc = maxc; T.mode = mode;
+    memcpy(T.surf, surf, sizeof surf);
+    std::vector<double> out;
+    typedef std::chrono::steady_clock clk;
+    for (int s = 0; s < nsteps; s++) {
+        T.made = 0;
+        const clk::time_point t0 = clk::now();
+        dSpaceCollide(sp, &T, &timing_cb);
+        const clk::time_point t1 = clk::now();
+        dWorldQuickStep(w, P.dt);
+        dJointGroupEmpty(T.group);
+        const clk::time_point t2 = clk::now();
+        out.push_back(std::chrono::duration<double>(t1 - t0).count());
+        out.push_back(std::chrono::duration<double>(t2 - t1).count());
+        out.push_back((double)T.made);
+    }
+    wr(out.data(), out.size());
+    std::vector<float> st(BODY_OUT * nb);
+    for (int i = 0; i < nb; i++) get_body(b[i], &st[BODY_OUT * i]);
+    wr(st.data(), st.size());
+    dJointGroupDestroy(T.group);
+    if (impl) {
+        dThreadingImplementationShutdownProcessing(impl);
+        dThreadingFreeThreadPool(pool);
+        dWorldSetStepThreadingImplementation(w, NULL, NULL);
+        dThreadingFreeImplementation(impl);
+    }
+    dSpaceDestroy(sp);
+    dWorldDestroy(w);
+}
+
 int main(int argc, char **argv) {
     if (argc != 4) { fprintf(stderr, "usage: gen_golden MODE IN OUT\n"); return 2; }
     fin = fopen(argv[2], "rb"); fout = fopen(argv[3], "wb");
@@ -445,6 +531,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[1], "loop")) mode_loop();
     else if (!strcmp(argv[1], "chain")) mode_chain();
     else if (!strcmp(argv[1], "sleep")) mode_sleep();
+    else if (!strcmp(argv[1], "timing")) mode_timing();
     else { fprintf(stderr, "bad mode\n"); return 2; }
     dCloseODE();
     fclose(fin); fclose(fout);
