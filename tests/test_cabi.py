@@ -61,3 +61,51 @@ def test_rand_known_answers(lib_path):
     L = ode.load(lib_path)
     L.dRandSetSeed(0)
     assert [L.dRand() for _ in range(5)] == [0x3c6ef35f, 0x47502932, 0xd1ccf6e9, 0xaaf95334, 0x6252e503]
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include "gbode.h"
+int main(void) {
+    dInitODE2(0);
+    dWorldID w = dWorldCreate();
+    dBodyID a = dBodyCreate(w), b = dBodyCreate(w);
+    dBodySetPosition(a, 0, -1, 0);
+    dBodySetPosition(b, 0, 1, 0);
+    dMass m;
+    dMassSetBox(&m, 2.0f, 1.0f, 2.0f, 3.0f);
+    dBodySetMass(a, &m);
+    dJointID j = dJointCreateHinge(w, 0);
+    dJointAttach(j, a, b);
+    dJointSetHingeAnchor(j, 0, 0, 0);
+    dJointSetHingeAxis(j, 1, 0, 0);
+    dMatrix3 R;
+    dRFromAxisAndAngle(R, 1, 0, 0, 0.23f);
+    dBodySetRotation(a, R);
+    printf("%.5f %.3f %d\n", (double)dJointGetHingeAngle(j), (double)m.mass, dAreConnected(a, b));
+    dWorldDestroy(w);
+    dCloseODE();
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c99"), ("g++", "-std=c++17")])
+def test_header_builds_a_c_program(lib_path, tmp_path, compiler, std):
+    """An ODE-style C program compiles against include/gbode.h as strict C99
+    and as C++17 (no warnings with -Wall -Wextra -pedantic), links -lgbode and
+    runs its host-side calls (no GPU work: world, bodies, mass, hinge
+    geometry)."""
+    src = tmp_path / "prog.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "prog"
+    libdir = os.path.dirname(lib_path)
+    lang = ["-x", "c++"] if compiler == "g++" else []
+    cc = subprocess.run([compiler, std, "-Wall", "-Wextra", "-pedantic", "-Werror", *lang,
+                         f"-I{os.path.join(ROOT, 'include')}", str(src), f"-L{libdir}", "-lgbode",
+                         f"-Wl,-rpath,{libdir}", "-lm", "-o", str(exe)], capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    angle, mass, connected = out.stdout.split()
+    assert abs(float(angle) - 0.23) < 1e-4 and abs(float(mass) - 12.0) < 1e-3 and connected == "1"
