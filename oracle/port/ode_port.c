@@ -6,6 +6,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <sched.h>
 #include <stdatomic.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -1517,8 +1518,10 @@ static void sor_barrier(sor_mt *C, int *sense) {
         atomic_store(&C->bar_count, 0);
         atomic_store(&C->bar_sense, s);
     } else {
-        while (atomic_load(&C->bar_sense) != s) {
-        }
+        /* spin, then give the core away: with more threads than free cores a
+         * pure spin would wait for a descheduled thread's whole time slice */
+        for (unsigned spins = 0; atomic_load(&C->bar_sense) != s; spins++)
+            if (spins >= 2048u) sched_yield();
     }
 }
 
@@ -1554,8 +1557,7 @@ static void sor_levels(sor_mt *C) {
 static void *sor_mt_run(void *argp) {
     sor_mt_arg *a = (sor_mt_arg *)argp;
     sor_mt *C = a->C;
-    while (!atomic_load(&C->go)) {
-    }
+    while (!atomic_load(&C->go)) sched_yield();
     const int tid = a->tid, T = C->nthreads;
     int sense = 0;
     for (;;) {
