@@ -1262,11 +1262,15 @@ dJointID dJointCreateContact(dWorldID w, dJointGroupID group, const dContact *c)
     if (group) group->joints.push_back(j);
     return j;
 }
+static void set_relative_values(dxJoint *j);
 void dJointAttach(dJointID j, dBodyID body1, dBodyID body2) {
     j->b1 = body1;
     j->b2 = body2;
     j->attached = body1 || body2;
-    if (j->type != dJointTypeContact) j->world->joints_dirty = true;
+    if (j->type != dJointTypeContact) {
+        j->world->joints_dirty = true;
+        if (j->attached) set_relative_values(j);  // ode.cpp:1434-1438
+    }
 }
 void dJointDestroy(dJointID j) {
     dxWorld *w = j->world;
@@ -1615,6 +1619,29 @@ void dJointGetHinge2Axis2(dJointID j, dVector3 out) {
     world_download(j->world);
     if (j->node1()) mul0_331h(out, j->node1()->R, j->axis2);
     else out[0] = out[1] = out[2] = 0;
+}
+// setRelativeValues, run by dJointAttach: the anchor and the axes as they read
+// in world coordinates with the new bodies, set again, so that the body-frame
+// values follow the bodies just attached (ball.cpp:178-183, hinge.cpp:362-372,
+// hinge2.cpp:521-545; a hinge2 needs both bodies for its axis information)
+static void set_relative_values(dxJoint *j) {
+    dVector3 a, x1, x2;
+    if (j->type == dJointTypeBall) {
+        dJointGetBallAnchor(j, a);
+        dJointSetBallAnchor(j, a[0], a[1], a[2]);
+    } else if (j->type == dJointTypeHinge) {
+        dJointGetHingeAnchor(j, a);
+        set_anchors(j, a[0], a[1], a[2], j->anchor1, j->anchor2);
+        x1[0] = x1[1] = x1[2] = 0;
+        dJointGetHingeAxis(j, x1);
+        dJointSetHingeAxis(j, x1[0], x1[1], x1[2]);
+    } else if (j->type == dJointTypeHinge2) {
+        dJointGetHinge2Anchor(j, a);
+        set_anchors(j, a[0], a[1], a[2], j->anchor1, j->anchor2);
+        dJointGetHinge2Axis1(j, x1);
+        dJointGetHinge2Axis2(j, x2);
+        dJointSetHinge2Axes(j, x1, j->node1() ? x2 : nullptr);
+    }
 }
 // hinge2.cpp:33-51 measureAngle1
 dReal dJointGetHinge2Angle1(dJointID j) {

@@ -233,3 +233,32 @@ def test_hinge_axis_and_anchor_set_to_themselves(L):
         assert np.allclose(L.dBodyGetQuaternion(x)[:4], q, atol=1e-6)
     assert abs(L.dJointGetHingeAngle(j)) < 1e-4
     L.dWorldDestroy(w)
+
+
+def test_attach_takes_relative_values(L):
+    """dJointAttach recomputes a joint's body-frame anchor and axes from their
+    world values with the bodies just attached (ode.cpp:1434-1438,
+    setRelativeValues in ball.cpp:178-183, hinge.cpp:362-372,
+    hinge2.cpp:521-545): a joint attached with nothing set has its anchor at
+    the first body's centre (the second body's anchor is set to the same
+    point), and the hinge axis is the first body's x axis; the initial
+    relative rotation is the bodies' current one (angle 0)."""
+    w = L.dWorldCreate()
+    a, b = _turned_pair(L, w)
+    pa = np.array(L.dBodyGetPosition(a)[:3])
+    for create, get_anchor in ((L.dJointCreateBall, L.dJointGetBallAnchor),
+                               (L.dJointCreateHinge, L.dJointGetHingeAnchor),
+                               (L.dJointCreateHinge2, L.dJointGetHinge2Anchor)):
+        j = create(w, None)
+        L.dJointAttach(j, a, b)
+        anc = _vec()
+        get_anchor(j, anc)
+        assert np.allclose(anc[:3], pa, atol=1e-5)
+    h = L.dJointCreateHinge(w, None)
+    L.dJointAttach(h, a, b)
+    ax = _vec()
+    L.dJointGetHingeAxis(h, ax)
+    Ra = np.array(L.dBodyGetRotation(a)[:12]).reshape(3, 4)
+    assert np.allclose(ax[:3], Ra[:, 0], atol=1e-6)
+    assert abs(L.dJointGetHingeAngle(h)) < 1e-6
+    L.dWorldDestroy(w)
