@@ -262,3 +262,34 @@ def test_attach_takes_relative_values(L):
     assert np.allclose(ax[:3], Ra[:, 0], atol=1e-6)
     assert abs(L.dJointGetHingeAngle(h)) < 1e-6
     L.dWorldDestroy(w)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("value", [1.0, 0.1, 1e-20, -1.0, -0.1, -1e-20])
+def test_safe_normalize3_axis_vectors(L, axis, value):
+    """The reference's dSafeNormalize3 unit test (tests/odemath.cpp:31-182):
+    a vector along one axis, of length 1, 0.1 or 1e-20 and either sign,
+    becomes that axis's unit vector with the sign kept, of length exactly 1
+    in single precision."""
+    v = _vec()
+    v[axis] = value
+    assert L.dSafeNormalize3(v) == 1
+    e = np.zeros(3, np.float32)
+    e[axis] = math.copysign(1.0, value)
+    assert list(v[:3]) == list(e)
+    x = np.array(v[:3], np.float32)
+    assert np.sqrt(np.float32(x @ x)) == np.float32(1.0)
+
+
+def test_safe_normalize3_large_components(L):
+    """tests/odemath.cpp:164-181: (1e10, 0, 1e-20) normalises to length
+    exactly 1; (1e10, 9999, 9) to length 1 within 1e-3."""
+    v = _vec()
+    v[0], v[1], v[2] = 9999999999.0, 0.0, 1e-20
+    L.dSafeNormalize3(v)
+    x = np.array(v[:3], np.float32)
+    assert np.sqrt(np.float32(x @ x)) == np.float32(1.0)
+    v[0], v[1], v[2] = 9999999999.0, 9999.0, 9.0
+    L.dSafeNormalize3(v)
+    x = np.array(v[:3], np.float32)
+    assert abs(float(np.sqrt(x @ x)) - 1.0) < 1e-3
