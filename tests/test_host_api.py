@@ -293,3 +293,26 @@ def test_safe_normalize3_large_components(L):
     L.dSafeNormalize3(v)
     x = np.array(v[:3], np.float32)
     assert abs(float(np.sqrt(x @ x)) - 1.0) < 1e-3
+
+
+def test_reattach_with_one_or_no_body(L):
+    """tests/joint.cpp:2986-3053 (host half): a hinge attached to two bodies
+    is attached again to the first body alone, to the second alone and to
+    none; each attach takes the joint's relative values from its current
+    anchor (the stepping half needs the device)."""
+    w = L.dWorldCreate()
+    b1, b2 = L.dBodyCreate(w), L.dBodyCreate(w)
+    L.dBodySetPosition(b1, 0.0, -1.0, 0.0)
+    L.dBodySetPosition(b2, 0.0, 1.0, 0.0)
+    j = L.dJointCreateHinge(w, None)
+    L.dJointAttach(j, b1, b2)
+    anc = _vec()
+    for first, second, body in ((b1, None, b1), (None, b2, b2)):
+        L.dJointAttach(j, first, second)
+        assert L.dJointGetBody(j, 0) == body and not L.dJointGetBody(j, 1)
+        L.dJointGetHingeAnchor(j, anc)
+        assert all(math.isfinite(x) for x in anc[:3])
+        assert abs(L.dJointGetHingeAngle(j)) < 1e-6
+    L.dJointAttach(j, None, None)
+    assert not L.dJointGetBody(j, 0) and not L.dJointGetBody(j, 1)
+    L.dWorldDestroy(w)
