@@ -109,3 +109,26 @@ def test_header_builds_a_c_program(lib_path, tmp_path, compiler, std):
     assert out.returncode == 0, out.stderr
     angle, mass, connected = out.stdout.split()
     assert abs(float(angle) - 0.23) < 1e-4 and abs(float(mass) - 12.0) < 1e-3 and connected == "1"
+
+
+@pytest.mark.parametrize("direction", [1, 2, 3])
+def test_capsule_mass_matches_reference_formula(lib_path, direction):
+    """mass.cpp:141-162 dMassSetCapsule: cylinder plus the two caps, the
+    inertia about the capsule's axis on `direction`, the other two equal."""
+    import ctypes
+    import math
+    from ode_gb300 import ode
+    L = ode.load(lib_path)
+    m = ode.dMass()
+    rho, r, length = 700.0, 0.05, 0.3
+    L.dMassSetCapsule(ctypes.byref(m), rho, direction, r, length)
+    m1 = math.pi * r * r * length * rho
+    m2 = 4.0 / 3.0 * math.pi * r ** 3 * rho
+    ia = m1 * (0.25 * r * r + length * length / 12.0) + m2 * (0.4 * r * r + 0.375 * r * length + 0.25 * length ** 2)
+    ib = (0.5 * m1 + 0.4 * m2) * r * r
+    assert abs(m.mass - (m1 + m2)) <= 1e-5 * (m1 + m2)
+    diag = [m.I[0], m.I[5], m.I[10]]
+    for k in range(3):
+        want = ib if k == direction - 1 else ia
+        assert abs(diag[k] - want) <= 1e-5 * want
+    assert m.I[1] == m.I[2] == m.I[4] == m.I[6] == m.I[8] == m.I[9] == 0.0
