@@ -132,3 +132,21 @@ def test_capsule_mass_matches_reference_formula(lib_path, direction):
         want = ib if k == direction - 1 else ia
         assert abs(diag[k] - want) <= 1e-5 * want
     assert m.I[1] == m.I[2] == m.I[4] == m.I[6] == m.I[8] == m.I[9] == 0.0
+
+
+def test_total_mass_variants(lib_path):
+    """mass.cpp dMassSetSphereTotal / dMassSetBoxTotal: the density form
+    rescaled to the given total (dMassAdjust), so the inertia scales with it:
+    sphere I = 2/5 m r^2, box I = m (b^2 + c^2) / 12."""
+    import ctypes
+    from ode_gb300 import ode
+    L = ode.load(lib_path)
+    m = ode.dMass()
+    L.dMassSetSphereTotal(ctypes.byref(m), 3.0, 0.5)
+    assert abs(m.mass - 3.0) < 1e-6 and abs(m.I[0] - 0.4 * 3.0 * 0.25) < 1e-6
+    L.dMassSetBoxTotal(ctypes.byref(m), 6.0, 1.0, 2.0, 3.0)
+    assert abs(m.mass - 6.0) < 1e-6
+    assert abs(m.I[0] - 6.0 * (4 + 9) / 12) < 1e-5 and abs(m.I[5] - 6.0 * (1 + 9) / 12) < 1e-5
+    assert abs(m.I[10] - 6.0 * (1 + 4) / 12) < 1e-5
+    L.dMassSetZero(ctypes.byref(m))
+    assert m.mass == 0.0 and all(x == 0.0 for x in m.I)
