@@ -316,3 +316,34 @@ def test_reattach_with_one_or_no_body(L):
     L.dJointAttach(j, None, None)
     assert not L.dJointGetBody(j, 0) and not L.dJointGetBody(j, 1)
     L.dWorldDestroy(w)
+
+
+def test_rotation_helpers_agree(L):
+    """rotation.cpp: dRFromAxisAndAngle is dRfromQ of dQFromAxisAndAngle
+    (rotation.cpp:160-188, 236-254) and equals Rodrigues' formula; a body
+    given that rotation reports a unit quaternion of the same rotation
+    (dBodySetRotation -> dQfromR, rotation.cpp:257-307)."""
+    rng = np.random.default_rng(7)
+    w = L.dWorldCreate()
+    b = L.dBodyCreate(w)
+    for _ in range(20):
+        ax = rng.normal(size=3)
+        ang = float(rng.uniform(-3.0, 3.0))
+        R = _vec(12)
+        L.dRFromAxisAndAngle(R, *map(float, ax), ang)
+        q = _vec(4)
+        L.dQFromAxisAndAngle(q, *map(float, ax), ang)
+        R2 = _vec(12)
+        L.dRfromQ(R2, q)
+        assert np.allclose(R[:12], R2[:12], atol=1e-6)
+        k = ax / np.linalg.norm(ax)
+        K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+        rod = np.eye(3) + math.sin(ang) * K + (1 - math.cos(ang)) * K @ K
+        assert np.allclose(np.array(R[:12]).reshape(3, 4)[:, :3], rod, atol=2e-6)
+        L.dBodySetRotation(b, R)
+        qb = np.array(L.dBodyGetQuaternion(b)[:4])
+        assert abs(np.linalg.norm(qb) - 1.0) < 1e-6
+        R3 = _vec(12)
+        L.dRfromQ(R3, (ctypes.c_float * 4)(*map(float, qb)))
+        assert np.allclose(R3[:12], R[:12], atol=2e-6)
+    L.dWorldDestroy(w)
