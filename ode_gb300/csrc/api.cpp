@@ -1087,7 +1087,14 @@ void dGeomGetAABB(dGeomID g, dReal aabb[6]) {
     } else if (g->cls == dCapsuleClass) {
         for (int i = 0; i < 3; i++) r[i] = fabsf(R[4 * i + 2] * d[1]) * 0.5f + d[0];
     } else {
+        // plane.cpp:80-107: unbounded, or the half space below an axis-aligned plane
         for (int i = 0; i < 6; i++) aabb[i] = (i & 1) ? INFINITY : -INFINITY;
+        const int ax = (d[1] == 0.0f && d[2] == 0.0f) ? 0 : (d[0] == 0.0f && d[2] == 0.0f) ? 1
+                     : (d[0] == 0.0f && d[1] == 0.0f) ? 2 : -1;
+        if (ax >= 0) {
+            aabb[2 * ax] = d[ax] > 0 ? -INFINITY : -d[3];
+            aabb[2 * ax + 1] = d[ax] > 0 ? d[3] : INFINITY;
+        }
         return;
     }
     for (int i = 0; i < 3; i++) { aabb[2 * i] = p[i] - r[i]; aabb[2 * i + 1] = p[i] + r[i]; }

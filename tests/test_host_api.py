@@ -347,3 +347,38 @@ def test_rotation_helpers_agree(L):
         L.dRfromQ(R3, (ctypes.c_float * 4)(*map(float, qb)))
         assert np.allclose(R3[:12], R[:12], atol=2e-6)
     L.dWorldDestroy(w)
+
+
+def test_geom_aabbs(L):
+    """dGeomGetAABB as the reference's computeAABB gives it: sphere
+    (sphere.cpp), box with a rotation (box.cpp: half sides through |R|),
+    capsule along its z axis (capsule.cpp), and planes (plane.cpp:80-107:
+    the half space below an axis-aligned plane, else unbounded)."""
+    inf = float("inf")
+    sp = L.dHashSpaceCreate(None)
+    a = _vec(6)
+    g = L.dCreateSphere(sp, 0.5)
+    L.dGeomSetPosition(g, 1.0, 2.0, 3.0)
+    L.dGeomGetAABB(g, a)
+    assert list(a[:6]) == [0.5, 1.5, 1.5, 2.5, 2.5, 3.5]
+    R = _vec(12)
+    L.dRFromAxisAndAngle(R, 0.0, 0.0, 1.0, 0.5)
+    g = L.dCreateBox(sp, 1.0, 2.0, 3.0)
+    L.dGeomSetRotation(g, R)
+    L.dGeomGetAABB(g, a)
+    Rm = np.abs(np.array(R[:12]).reshape(3, 4)[:, :3])
+    half = 0.5 * Rm @ np.array([1.0, 2.0, 3.0])
+    assert np.allclose(a[1:6:2], half, atol=1e-6) and np.allclose(a[0:6:2], -half, atol=1e-6)
+    g = L.dCreateCapsule(sp, 0.1, 0.8)
+    L.dGeomSetRotation(g, R)
+    L.dGeomGetAABB(g, a)
+    ext = Rm[:, 2] * 0.4 + 0.1
+    assert np.allclose(a[1:6:2], ext, atol=1e-6)
+    for (pa, pb, pc, pd), want in (((0, 0, 1, 0), [-inf, inf, -inf, inf, -inf, 0.0]),
+                                   ((-1, 0, 0, -5), [5.0, inf, -inf, inf, -inf, inf]),
+                                   ((0, 2, 0, 4), [-inf, inf, -inf, 2.0, -inf, inf]),
+                                   ((1, 1, 0, 0), [-inf, inf, -inf, inf, -inf, inf])):
+        g = L.dCreatePlane(sp, float(pa), float(pb), float(pc), float(pd))
+        L.dGeomGetAABB(g, a)
+        assert list(a[:6]) == want
+    L.dSpaceDestroy(sp)
