@@ -265,6 +265,8 @@ void dGeomSetRotation(dGeomID geom, const dMatrix3 R);
 const dReal *dGeomGetPosition(dGeomID geom);
 const dReal *dGeomGetRotation(dGeomID geom);
 int dGeomGetClass(dGeomID geom);
+/* minx maxx miny maxy minz maxz; a plane is unbounded except below an
+ * axis-aligned one (plane.cpp:80-107) */
 void dGeomGetAABB(dGeomID geom, dReal aabb[6]);
 /* include/ode/collision.h:792 */
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom *contact, int skip);
@@ -278,6 +280,9 @@ dJointGroupID dJointGroupCreate(int max_size);
 void dJointGroupDestroy(dJointGroupID group);
 void dJointGroupEmpty(dJointGroupID group);
 dJointID dJointCreateContact(dWorldID w, dJointGroupID group, const dContact *c);
+/* attaching a ball, hinge or hinge2 joint re-derives its body-frame anchor
+ * and axes from their world values with the new bodies (the reference's
+ * setRelativeValues, ode.cpp:1434-1438) */
 void dJointAttach(dJointID j, dBodyID body1, dBodyID body2);
 void dJointDestroy(dJointID j);
 void dJointSetFeedback(dJointID j, dJointFeedback *fb);
