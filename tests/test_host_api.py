@@ -382,3 +382,17 @@ def test_geom_aabbs(L):
         L.dGeomGetAABB(g, a)
         assert list(a[:6]) == want
     L.dSpaceDestroy(sp)
+
+
+def test_body_quaternion_is_normalised(L):
+    """ode.cpp:379-387 dBodySetQuaternion: the quaternion is normalised and
+    the rotation matrix derived from it."""
+    w = L.dWorldCreate()
+    b = L.dBodyCreate(w)
+    L.dBodySetQuaternion(b, (ctypes.c_float * 4)(2.0, 0.0, 0.0, 0.0))
+    assert list(L.dBodyGetQuaternion(b)[:4]) == [1.0, 0.0, 0.0, 0.0]
+    L.dBodySetQuaternion(b, (ctypes.c_float * 4)(0.0, 0.0, 0.0, 3.0))
+    assert list(L.dBodyGetQuaternion(b)[:4]) == [0.0, 0.0, 0.0, 1.0]
+    R = np.array(L.dBodyGetRotation(b)[:12]).reshape(3, 4)[:, :3]
+    assert np.allclose(R, np.diag([-1.0, -1.0, 1.0]), atol=1e-7)
+    L.dWorldDestroy(w)
