@@ -263,7 +263,7 @@ def run_reference(args, ws, rank):
                        "sor_threads": threads,
                        "threads_note": "the oracle's threaded sweeps (levels of rows that share no body, a "
                                        "barrier between levels) give the single-threaded result to the bit "
-                                       "and ran 5.9x faster on 8 cores than the reference's own threaded "
+                                       "and ran 5.3x faster on 8 cores than the reference's own threaded "
                                        "mode at its best (one thread) where the reference compiles",
                        "start": settle_note, "contacts_per_step": nc / steps,
                        "fp64_residual_last_step": rel, "residual_target": args.target,
