@@ -406,7 +406,7 @@ def run_gbode(args, ws, rank, local):
         "roofline": {"bound": "hbm", "kernel": "gb::k_pgs", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": PGS_TRAFFIC,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean of two k_pgs "
-                                       "launches from the settled pile (profiles/k_pgs_pile32768_dram.md)",
+                                       "launches from the settled pile",
                      "algorithmic_bytes_per_launch": pgs_bytes / args.steps},
         "clocks": clk,
         "gpu_launches": launches,

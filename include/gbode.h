@@ -581,9 +581,11 @@ void gbodeWorldGetLearnedStats(dWorldID w, float *out3);
  * device: for pair p, geoms[pairs[2p]] against geoms[pairs[2p+1]], with the
  * same colliders, rejections (a geom with itself, two geoms on one body) and
  * normal orientation as dCollide, and at most flags & 0xffff contacts per
- * pair (capped at 8).  All pointers are DEVICE pointers the caller owns:
+ * pair (capped at 8).  Only those low 16 bits of flags are used; higher flag
+ * bits are ignored.  All pointers are DEVICE pointers the caller owns:
  *   geoms     [ngeoms] gbodePairGeom records
- *   pairs     [npairs][2] geom indices
+ *   pairs     [npairs][2] geom indices, 8-byte aligned (a pair is read as
+ *             one 8-byte load; a misaligned pointer is rejected)
  *   contacts  [capacity][8] out: pos xyz, depth, normal xyz, 0 -- pair p's
  *             contacts are rows first[p] .. first[p+1]-1 (rows at or beyond
  *             capacity are not written)
@@ -607,6 +609,10 @@ void gbodeWorldGetLearnedStats(dWorldID w, float *out3);
  * array's device address with cudaGetSymbolAddress, which can load the
  * library's device code on that device; make that first call before any
  * stream capture begins.
+ *
+ * An error already pending on the calling thread from earlier, unrelated CUDA
+ * work is cleared before the launches, so that a launch error reported here
+ * is this call's own.
  *
  * Returns 1 when the work was enqueued, 0 on a rejected argument or launch
  * error (gbodeGetLastError() has the message). */

@@ -1,6 +1,7 @@
 """Builds libgbode.so in-tree with nvcc for sm_103a.
 
-Six translation units compiled in parallel, then linked; the link also
+Every translation unit under csrc/ (SOURCES) is compiled in parallel, then
+linked; the link also
 pulls in the CUDA runtime statically so the library loads without a
 particular libcudart on the library path.  Flags that matter for results:
 -fmad=false -prec-div=true -prec-sqrt=true keep every float operation
@@ -48,9 +49,6 @@ def build(force: bool = False, verbose: bool = False) -> str:
     def compile_one(src):
         obj = os.path.join(obj_dir, src + ".o")
         cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
-        if src.endswith(".cpp"):
-            cmd = [cc, *NVCC_FLAGS, "-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj] if False else \
-                  [cc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

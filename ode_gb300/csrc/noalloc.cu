@@ -16,6 +16,7 @@
 // the fixed array instead of workspace buffers, followed by a one-block
 // exclusive scan of the per-pair counts and a compaction into the caller's
 // contact array, all enqueued on the caller's stream.
+#include <cstdint>
 #include <mutex>
 
 #include "colliders.cuh"
@@ -152,6 +153,12 @@ extern "C" int gbodeCollidePairsNoAlloc(const gbodePairGeom *geoms, int ngeoms, 
         report_error("gbodeCollidePairsNoAlloc: null buffer or negative size");
         return 0;
     }
+    // the kernel reads a pair as one 8-byte int2; a misaligned pointer would
+    // fault on the device, so it is refused here
+    if (((uintptr_t)pairs & 7) != 0) {
+        report_error("gbodeCollidePairsNoAlloc: pairs must be 8-byte aligned");
+        return 0;
+    }
     const char *why = "";
     float4 *scratch = scratch_ptr(&why);
     if (!scratch) {
@@ -165,6 +172,9 @@ extern "C" int gbodeCollidePairsNoAlloc(const gbodePairGeom *geoms, int ngeoms, 
     int maxc = flags & GB_NUMC_MASK;
     if (maxc > NA_SLOTS) maxc = NA_SLOTS;
     const int grid = npairs > 0 ? (npairs + 127) / 128 : 1;
+    // an error left pending on this thread by unrelated earlier work would
+    // otherwise be reported (and cleared) as this call's launch failure
+    (void)cudaGetLastError();
     // every count[p] and slot this call reads is written by this call first:
     // nothing in the scratch has to start at zero
     if (npairs > 0) {

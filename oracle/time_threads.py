@@ -83,11 +83,14 @@ def time_oracle(sc, bodies, threads, steps, sweeps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ODE_REFERENCE_DIR"),
+                    help="reference source tree (default: $ODE_REFERENCE_DIR)")
     ap.add_argument("--threads", type=int, nargs="+", default=[1, 8])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--sweeps", type=int, default=200)
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("--ref or ODE_REFERENCE_DIR must name the reference source tree")
     exe = reference_exe(args.ref)
     sc, bodies = settled_pile()
     print(f"pile{sc.nb}, {args.sweeps} sweeps per step, {args.steps} timed steps after one untimed")

@@ -4,7 +4,7 @@ The reference is built from its own sources by oracle/ref_build/Makefile into
 oracle/_ref/<variant>/libode.a; this script compiles tests/golden/gen_golden.cpp
 against it, writes seeded inputs, runs it and packs the outputs as .npz.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference source tree>
 
 Only this container has the reference sources; the fixtures it writes are
 committed so that tests elsewhere need neither the reference nor this script.
@@ -461,9 +461,12 @@ def gen_sleep(exes):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ODE_REFERENCE_DIR"),
+                    help="reference source tree (default: $ODE_REFERENCE_DIR)")
     ap.add_argument("--only", default="")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("--ref or ODE_REFERENCE_DIR must name the reference source tree")
     exes = build(a.ref)
     if a.only in ("", "colliders"):
         gen_colliders(exes)

@@ -122,6 +122,55 @@ def test_no_alloc_collide_matches_dcollide_twice(gblib, golden):
           f"{len(sel)} reversed pairs -> {t2} contacts (worst {w2:.3g})")
 
 
+def test_no_alloc_collide_leaves_free_memory_unchanged(gblib, golden):
+    """The property the entry point is named for: once the buffers exist, a
+    call takes no device memory (the device's free bytes are the same before
+    and after it)."""
+    import torch
+    L = gblib
+    g = golden("colliders.npz")
+    rec = _records(g)
+    n = len(g["count"])
+    dev = torch.device("cuda", 0)
+    geoms_d = torch.from_numpy(rec.view(np.uint8).copy()).to(dev)
+    pairs = np.stack([2 * np.arange(n), 2 * np.arange(n) + 1], axis=1).astype(np.int32)
+    pairs_d = torch.from_numpy(pairs).to(dev)
+    out_d = torch.zeros((8 * n, 8), dtype=torch.float32, device=dev)
+    first_d = torch.zeros((n + 1,), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def call():
+        ok = L.gbodeCollidePairsNoAlloc(geoms_d.data_ptr(), len(rec), pairs_d.data_ptr(), n, 4, out_d.data_ptr(),
+                                        8 * n, first_d.data_ptr(), stream.cuda_stream)
+        assert ok == 1, L.gbodeGetLastError()
+        stream.synchronize()
+
+    call()  # the first call on the device may do its one-time set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, (free0, free1)
+    assert int(first_d[n].item()) > 1000
+
+
+def test_no_alloc_collide_rejects_misaligned_pairs(gblib):
+    """A pair is read as one 8-byte load: a pairs pointer that is only 4-byte
+    aligned is refused on the host before anything is launched."""
+    import torch
+    L = gblib
+    dev = torch.device("cuda", 0)
+    buf = torch.zeros(8, dtype=torch.int32, device=dev)
+    geoms = torch.zeros(96, dtype=torch.uint8, device=dev)
+    out = torch.zeros((8, 8), dtype=torch.float32, device=dev)
+    first = torch.zeros(2, dtype=torch.int32, device=dev)
+    assert L.gbodeCollidePairsNoAlloc(geoms.data_ptr(), 1, buf.data_ptr() + 4, 1, 4, out.data_ptr(), 8,
+                                      first.data_ptr(), None) == 0
+    assert "aligned" in L.gbodeGetLastError().decode()
+
+
 def test_no_alloc_collide_rejects_oversized_batch(gblib):
     L = gblib
     from ode_gb300 import ode
