@@ -400,7 +400,10 @@ def run_gbode(args, ws, rank, local):
                    "rows_per_step": m_mean, "contacts_per_step": float(np.mean(contacts)),
                    "colours": int(np.median(colours)), "sweeps_per_step": float(np.mean(sweeps)),
                    "steps_at_target": ok_steps, "fp32_residual_max": float(max(resid)),
-                   "fp64_residual_last_step": fp64_rel, "complementarity_last_step": ce,
+                   "fp64_residual_last_step": fp64_rel,
+                   "complementarity_last_step": ce / max(1.0, ml),
+                   "normalisation": "residual and complementarity (min-map form, in the units of lambda) "
+                                    "relative to max(1, max|lambda|) of the step's own solution",
                    "contact_rows_per_s": float(np.sum(rows)) / (total_ms / 1e3),
                    "solve_share": pgs_s * 1e3 / total_ms},
         "roofline": {"bound": "hbm", "kernel": "gb::k_pgs", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -490,7 +490,11 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
 /* FP64 LCP residual and complementarity error of the last step's solution,
  * evaluated on the device from the step's FP32 rows (unscaled) and lambda:
  * max_i |lambda_i - proj_[lo,hi](lambda_i - (A lambda - b)_i / A_ii)|, not
- * normalised; *max_lambda receives max|lambda|.  Synchronises the stream. */
+ * normalised; *complementarity receives the min-map complementarity error
+ * max_i max(min(lambda_i - lo_i, w_i+ / A_ii), min(hi_i - lambda_i, w_i- / A_ii))
+ * with w_i = (A lambda - b)_i, w+ = max(w, 0), w- = max(-w, 0) -- in the units
+ * of lambda, like the residual; *max_lambda receives max|lambda|.  Divide the first two by
+ * max(1, max|lambda_ref|) for relative figures.  Synchronises the stream. */
 double gbodeWorldLastResidual(dWorldID w, double *complementarity, double *max_lambda);
 
 /* Copies of the last step's rows and lambda for checking: rows [nrows][20]

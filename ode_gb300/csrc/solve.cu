@@ -1951,11 +1951,11 @@ __global__ void k_res_rows(Rows Rw, Bodies B, const int *nrows_dev, const double
         double t = lam - w / D;
         t = fmin(fmax(t, lo), hi);
         rmax = fmax(rmax, fabs(lam - t));
-        double c;
-        if (lam <= lo) c = w < 0 ? -w : 0;
-        else if (lam >= hi) c = w > 0 ? w : 0;
-        else c = fabs(w);
-        cmax = fmax(cmax, c);
+        // complementarity, min-map form in the units of lambda (w / A_ii):
+        // max(min(lambda - lo, w+ / D), min(hi - lambda, w- / D))
+        const double wp = fmax(w, 0.0) / D, wm = fmax(-w, 0.0) / D;
+        const double c = fmax(fmin(lam - lo, wp), fmin(hi - lam, wm));
+        cmax = fmax(cmax, fabs(c));
         lmax = fmax(lmax, fabs(lam));
     }
     atomic_max_d(&out[0], rmax);

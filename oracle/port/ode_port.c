@@ -1623,6 +1623,9 @@ static void sor_sweeps_mt(const port_world *w, const sor_rows *S, int *order, in
     free(C.blev); free(C.lev_of); free(C.lev_rows); free(C.lev_start);
 }
 
+/* set only while port_world_quickstep_map runs: receives each recorded row's contact slot */
+static int *g_row_slot = NULL;
+
 static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint *joints, const int *joint_ids,
                              int nj_in, const int *joint_cidx, float *lambda_out, float *rows_out, int row_base) {
     const real h = w->dt;
@@ -1803,6 +1806,13 @@ static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint 
                 for (int r = 0; r < im && r < 3; r++) lambda_out[3 * ci + r] = lambda[ofs + r];
             }
         }
+        if (g_row_slot) {  /* row -> 3 * contact + row of the contact (port_world_quickstep_map) */
+            for (int ji = 0; ji < nj; ji++) {
+                int ofs = mindex[ji], im = mindex[ji + 1] - ofs;
+                int ci = joint_cidx[jl[ji]];
+                for (int r = 0; r < im; r++) g_row_slot[row_base + ofs + r] = 3 * ci + r;
+            }
+        }
         free(order); free(iMJ); free(fa); free(fc); free(lambda); free(rhs_tmp);
         free(jb2); free(jb1); free(findex); free(J);
     }
@@ -1887,6 +1897,14 @@ static void fill_joint(pjoint *j, int b1, int b2, int mode, const float *s) {
     j->normal[0] = s[3]; j->normal[1] = s[4]; j->normal[2] = s[5];
     j->depth = s[6]; j->mu = s[7]; j->mu2 = s[8]; j->bounce = s[9]; j->bounce_vel = s[10];
     j->soft_erp = s[11]; j->soft_cfm = s[12]; j->slip1 = s[13]; j->slip2 = s[14];
+}
+
+int port_world_quickstep_map(port_world *w, int nc, const int *cb, const int *mode, const float *cs, float *lambda,
+                             float *rows_out, int *nrows_out, int *row_slot) {
+    g_row_slot = row_slot;
+    int r = port_world_quickstep(w, nc, cb, mode, cs, lambda, rows_out, nrows_out);
+    g_row_slot = NULL;
+    return r;
 }
 
 int port_world_quickstep(port_world *w, int nc, const int *cb, const int *mode, const float *cs, float *lambda,
@@ -2078,13 +2096,10 @@ double port_lcp_residual(int m, const float *rows, int nb, const double *invm, c
         if (t > hi) t = hi;
         double e = fabs(li - t);
         if (e > res) res = e;
-        /* complementarity: at lo w>=0, at hi w<=0, inside w==0 */
-        double c;
-        if (li <= lo) c = w_i < 0 ? -w_i : 0;
-        else if (li >= hi) c = w_i > 0 ? w_i : 0;
-        else c = fabs(w_i);
-        double cl = fabs(fmin(li - lo, hi - li));
-        double cc = fmin(c, cl > 0 ? c : c);
+        /* complementarity, min-map form in the units of lambda (w / A_ii) */
+        double wp = w_i > 0 ? w_i / D : 0, wm = w_i < 0 ? -w_i / D : 0;
+        double cc = fmax(fmin(li - lo, wp), fmin(hi - li, wm));
+        cc = fabs(cc);
         if (cc > ce) ce = cc;
     }
     if (compl_err) *compl_err = ce;

@@ -75,11 +75,20 @@ int port_sim_step(port_sim *s);
 /* Contacts made in the last step: cb [nc][2], cs [nc][16] (pos normal depth ...). */
 int port_sim_last_contacts(const port_sim *s, int *cb, float *cs, int cap);
 
+/* port_world_quickstep that also writes, for every recorded row (rows_out
+ * order: islands in the reference's order), 3 * contact index + the row's
+ * place in its contact (0 normal, 1 and 2 friction) to row_slot [m].  Not
+ * thread-safe (test use). */
+int port_world_quickstep_map(port_world *w, int nc, const int *cb, const int *mode, const float *cs, float *lambda,
+                             float *rows_out, int *nrows_out, int *row_slot);
+
 /* FP64 LCP residual of a solution lambda (per row, [m]) for rows in the
  * layout of port_world_quickstep's rows_out, with the body inverse masses / world-frame
  * inverse inertias (invm [nb], invI [nb][9]).  Returns the natural-map
  * residual max_i |lambda_i - proj(lambda_i - (A lambda - b)_i / A_ii)|
- * (unnormalised) and writes the complementarity error. */
+ * (unnormalised) and writes the min-map complementarity error
+ * max_i max(min(lambda_i - lo_i, w_i+ / A_ii), min(hi_i - lambda_i, w_i- / A_ii)),
+ * w = A lambda - b (unnormalised, in the units of lambda). */
 double port_lcp_residual(int m, const float *rows, int nb, const double *invm, const double *invI,
                          const float *lambda, double *compl_err);
 

@@ -59,6 +59,7 @@ class Port:
         L.port_sim_destroy.argtypes = [ctypes.c_void_p]
         L.port_sim_step.argtypes = [ctypes.c_void_p]
         L.port_sim_last_contacts.argtypes = [ctypes.c_void_p, _I, _F, ctypes.c_int]
+        L.port_world_quickstep_map.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, _I, _F, _F, _F, _I, _I]
         L.port_lcp_residual.restype = ctypes.c_double
         L.port_lcp_residual.argtypes = [ctypes.c_int, _F, ctypes.c_int, _D, _D, _F, _D]
         L.port_rand_set_seed.argtypes = [ctypes.c_ulong]
@@ -154,6 +155,31 @@ class PortWorld:
         if want_rows:
             return lam[:nc], rows[:nrows.value]
         return lam[:nc]
+
+    def quickstep_contact_rows(self, cb, mode, cs):
+        """One quickstep with the rows recorded and put in contact order (3
+        rows per contact: normal, friction 1, friction 2; findex and body
+        columns renumbered to that order).  Returns (lambda [nc,3], rows [3nc,20])."""
+        nc = cb.shape[0]
+        lam = np.zeros((max(nc, 1), 3), np.float32)
+        rows = np.zeros((max(3 * nc, 1) * 2, 20), np.float32)
+        slot = np.full(max(3 * nc, 1) * 2, -1, np.int32)
+        nrows = ctypes.c_int(0)
+        cb = np.ascontiguousarray(cb, np.int32)
+        mode = np.ascontiguousarray(mode, np.int32)
+        cs = np.ascontiguousarray(cs, np.float32)
+        self.port.lib.port_world_quickstep_map(self.h, nc, cb.ctypes.data_as(_I), mode.ctypes.data_as(_I),
+                                               cs.ctypes.data_as(_F), lam.ctypes.data_as(_F),
+                                               rows.ctypes.data_as(_F), ctypes.byref(nrows),
+                                               slot.ctypes.data_as(_I))
+        m = nrows.value
+        assert m == 3 * nc, "contact rows in three-row form only"
+        slot = slot[:m]
+        out = np.zeros((m, 20), np.float32)
+        out[slot] = rows[:m]
+        f = out[:, 18] >= 0
+        out[f, 18] = slot[out[f, 18].astype(np.int64)]
+        return lam[:nc], out
 
     def attach_space(self, geom_cls, geom_body, geom_pos, geom_R, geom_dims, levels, maxc, mode, surface):
         self._gkeep = [np.ascontiguousarray(geom_cls, np.int32), np.ascontiguousarray(geom_body, np.int32),

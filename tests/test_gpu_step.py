@@ -135,6 +135,104 @@ def test_coloured_solver_reaches_residual(gblib, port, golden, target):
     w.close()
 
 
+# coloured solver against the FP64 oracle (see the test's docstring)
+FP64_TARGET = 1e-6          # FP32 in-kernel residual target of the solve
+FP64_RESID_TOL = 1e-5       # section 8(d) residual of the result, relative to max|lambda_dantzig|
+EXACT_LAMBDA_TOL = 2e-2     # |lambda - lambda_exact| / max|lambda_exact| (redundant contacts)
+EXACT_DV_TOL = 2e-3         # |M^-1 J^T (lambda - lambda_exact)| / max|M^-1 J^T lambda_exact|
+
+
+@pytest.mark.parametrize("name", ["box_stack", "pile256", "capsule_pile96"])
+def test_coloured_solver_against_fp64_dantzig(gblib, golden, name):
+    """The throughput solver (coloured PGS, k_pgs) against the FP64 oracle on
+    every snapshot of the step goldens (except the one where the reference's
+    Dantzig solver itself gave up).
+
+    The oracle is the reference's dDOUBLE dWorldStep (Dantzig,
+    lcp.cpp:836-1160) on the same contacts (`s{k}_lambda_dantzig`).  Dantzig
+    sets the friction rows' bounds once, from the normal multipliers of a
+    first pass with friction held at zero, while quickstep's LCP -- the one
+    PGS solves -- bounds friction by the final normals
+    (quickstep.cpp:2972-2978).  The two solutions therefore differ wherever
+    friction acts; tests/golden/lcp_exact.npz holds, per snapshot, the
+    reference's two-phase solution restated in FP64 (oracle/lcp_exact.py,
+    within 8e-6 of the reference's own multipliers) and that solution
+    continued to an exact solution of quickstep's LCP (natural-map residual
+    <= 1e-9).  Checked here, with lambda_oracle = the reference's Dantzig
+    multipliers as the section 8(d) normalisation:
+    * residual r(lambda) / max(1, max|lambda_oracle|) <= 1e-5 after a solve
+      to an FP32 residual of 1e-6, and the complementarity error (in the
+      units of lambda) likewise;
+    * lambda within 2e-2 of max|lambda_exact| of the exact solution, and the
+      velocity change M^-1 J^T lambda within 2e-3 of its largest entry (the
+      piles and the stack have four coplanar contacts per face, redundant
+      rows whose split PGS converges slowly, while the net force on each
+      body converges fast);
+    * against the reference's Dantzig multipliers lambda differs by no more
+      than the exact solution does (the friction-bound model) plus that
+      solver tolerance."""
+    from oracle import lcp_exact as X
+    from oracle.port.port import world_inv_inertia
+    from ode_gb300 import sim
+    L = gblib
+    g = golden(f"step_{name}.npz")
+    ex = golden("lcp_exact.npz")
+    mode = int(g["ints"][2])
+    report = []
+    for k in range(len(g["snaps"])):
+        if g[f"s{k}_dantzig_lcp_error"][1]:
+            continue
+        pre, cb, cs = g[f"s{k}_pre"], g[f"s{k}_cb"], g[f"s{k}_cs"]
+        sc = snapshot_scene(g, pre, name)
+        w = sim.GBWorld(sc)
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.gbodeWorldSetResidualTarget(w.w, FP64_TARGET, 10, 100000)
+        assert sim.step_contacts(w, cb, cs, mode) == 1, L.gbodeGetLastError()
+        w.sync()
+        st = w.stats()
+        rows = w.last_rows()
+        lam = rows[:, 19].astype(np.float64)
+        invI, invm = world_inv_inertia(pre, sc.bodies)
+        A, b, lo, hi, fi = X.dense_problem(rows, invm, invI)
+        ref = g[f"s{k}_lambda_dantzig"].reshape(-1).astype(np.float64)
+        exact = ex[f"{name}_s{k}_exact"].reshape(-1)
+        scale = max(1.0, float(np.abs(ref).max()))
+        r = X.natural_residual(A, b, lo, hi, fi, lam) / scale
+        c = X.complementarity(A, b, lo, hi, fi, lam) / scale
+        escale = max(1.0, float(np.abs(exact).max()))
+        d_exact = float(np.abs(lam - exact).max()) / escale
+        # velocity change per body: M^-1 J^T lambda, from A's off-diagonal-free pieces
+        J = np.zeros((len(lam), 6 * len(invm)))
+        b1, b2 = rows[:, 16].astype(int), rows[:, 17].astype(int)
+        for i in range(len(lam)):
+            J[i, 6 * b1[i]:6 * b1[i] + 6] = rows[i, 0:6]
+            if b2[i] >= 0:
+                J[i, 6 * b2[i]:6 * b2[i] + 6] = rows[i, 6:12]
+
+        def dv(x):
+            f = (J.T @ x).reshape(-1, 6)
+            v = np.empty_like(f)
+            v[:, 0:3] = f[:, 0:3] * invm[:, None]
+            v[:, 3:6] = np.einsum("bij,bj->bi", invI.reshape(-1, 3, 3), f[:, 3:6])
+            return v
+        dv_exact = dv(exact)
+        d_dv = float(np.abs(dv(lam) - dv_exact).max()) / max(1e-12, float(np.abs(dv_exact).max()))
+        d_ref = float(np.abs(lam - ref).max()) / scale
+        d_model = float(np.abs(exact - ref).max()) / scale
+        dp = float(np.abs(w.state()[:, 0:3] - g[f"s{k}_post_dantzig"][:, 0:3]).max())
+        report.append(f"s{k}: {len(lam)} rows, {st.iterations} sweeps, residual {r:.1e}, complementarity {c:.1e}, "
+                      f"lambda vs exact {d_exact:.1e} (dv {d_dv:.1e}), vs reference Dantzig {d_ref:.2e} "
+                      f"(exact vs reference {d_model:.2e}), positions vs reference Dantzig {dp:.1e} m")
+        assert r <= FP64_RESID_TOL, report[-1]
+        assert c <= FP64_RESID_TOL, report[-1]
+        assert d_exact <= EXACT_LAMBDA_TOL, report[-1]
+        assert d_dv <= EXACT_DV_TOL, report[-1]
+        assert d_ref <= d_model + EXACT_LAMBDA_TOL * escale / scale, report[-1]
+        L.dJointGroupEmpty(w.group)
+        w.close()
+    print(f"{name}:\n  " + "\n  ".join(report))
+
+
 def test_fused_pile_steps_are_sane(gblib):
     """Full-size pile, fused path: finite state, bodies stay in the container,
     contact and row counts in the expected range, colours valid."""
