@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
     ap.add_argument("--pgs-blocks", type=int, default=0, help="thread blocks of the PGS kernel (0: one per SM)")
     ap.add_argument("--passes", type=int, default=1, help="passes over a manifold's rows per visit")
+    ap.add_argument("--two-level", type=int, default=0,
+                    help="two-level sweep of the pile's solver with this many interior phases a sweep "
+                         "(gbodeWorldSetTwoLevelSweep; 0: off)")
     ap.add_argument("--from-settled", action="store_true",
                     help="start the pile from ode_gb300/data/pile32768_settled.npz instead of settling (profiling)")
     ap.add_argument("--ref-sweeps", type=int, default=1500,
@@ -305,6 +308,7 @@ def run_gbode(args, ws, rank, local):
             w.step_fused()
     w.sync()
     L.gbodeWorldSetResidualTarget(w.w, args.target, args.check_every, args.max_iters)
+    L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
     L.gbodeWorldSetTiming(w.w, 1)
     if args.profile_steps:
         for _ in range(args.profile_steps):
@@ -395,7 +399,11 @@ def run_gbode(args, ws, rank, local):
                    "settle_steps": args.settle, "residual_target": args.target, "check_every": args.check_every,
                    "max_sweeps": args.max_iters, "l2": "256 MB flush before every timed step (outside the events)",
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                   "solver": f"coloured PGS (W {args.sor_w}), persistent cooperative kernel",
+                   "solver": f"coloured PGS (W {args.sor_w}), persistent cooperative kernel"
+                             + (f", two-level sweep ({args.two_level} interior phases a sweep)"
+                                if args.two_level else ""),
+                   "interior_rows_per_step": float(np.mean(T["interior_rows"])),
+                   "interior_colours": int(np.median(T["interior_colours"])),
                    "warm_start": f"previous-step lambda x {args.warm_scale}" if args.warm_scale > 0 else "cold",
                    "rows_per_step": m_mean, "contacts_per_step": float(np.mean(contacts)),
                    "colours": int(np.median(colours)), "sweeps_per_step": float(np.mean(sweeps)),
@@ -545,7 +553,8 @@ def timed_steps(w, stream, flush, steps, graph=False):
     """`steps` fused steps, each bracketed by CUDA events on the world's stream
     (L2 flushed before each, outside the events); per-step statistics."""
     import torch
-    out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours")}
+    out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours",
+                           "interior_rows", "interior_colours")}
     torch.cuda.nvtx.range_push("timed")
     for _ in range(steps):
         with torch.cuda.stream(stream):
@@ -567,6 +576,8 @@ def timed_steps(w, stream, flush, steps, graph=False):
         out["rows"].append(st.rows)
         out["contacts"].append(st.contacts)
         out["colours"].append(st.colours)
+        out["interior_rows"].append(st.interior_rows)
+        out["interior_colours"].append(st.interior_colours)
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     return out

@@ -388,6 +388,18 @@ int gbodeWorldGetSolverBlocks(dWorldID w);
 void gbodeWorldSetManifoldPasses(dWorldID w, int passes);
 int gbodeWorldGetManifoldPasses(dWorldID w);
 
+/* Two-level sweep of the coloured solver (0 off; k >= 1 on, up to 8).  The
+ * bodies are split into one spatial column per solver block; contact
+ * manifolds inside one column are relaxed from the block's shared memory,
+ * colour by colour with block barriers only, and only the manifolds that
+ * cross columns are coloured globally with a grid barrier per colour.  A
+ * sweep relaxes the interior manifolds k times (interior passes cost no grid
+ * barrier), then the crossing ones once.  Same LCP, another Gauss-Seidel
+ * order (deterministic).  Columns whose manifolds do not fit in shared memory
+ * fall back to the global colours. */
+void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases);
+int gbodeWorldGetTwoLevelSweep(dWorldID w);
+
 /* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
  * creation without leaving the device.  Equivalent to dSpaceCollide with a near
  * callback that calls dCollide(o1, o2, maxc, ...) and makes one contact joint
@@ -451,6 +463,8 @@ typedef struct gbodeStepStats {
     float solve_ms;        /* device time of the PGS sweeps, if timing is on */
     float step_ms;         /* device time of the whole dWorldQuickStep, if timing is on */
     int sleeping;          /* bodies not stepped: their component is disabled (auto-disable) */
+    int interior_colours;  /* two-level sweep: colours of the columns' interior manifolds (0: off) */
+    int interior_rows;     /* two-level sweep: rows relaxed from shared memory (0: off) */
 } gbodeStepStats;
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */

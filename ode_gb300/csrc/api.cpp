@@ -61,7 +61,9 @@ void Workspace::release() {
                    &r_J1a, &r_J2l, &r_J2a, &r_M1l, &r_M1a, &r_M2l, &r_M2a, &r_lambda, &r_Ad, &r_findex, &r_contact,
                    &r_body, &m_head, &m_id, &m_start, &m_colour, &m_mask, &m_claim, &m_tent, &col_count, &col_start,
                    &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &wv_count, &wv_base, &wv_col, &wv_sched, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &d_off, &d_scr, &d_iscr, &d_rloc, &w_keys, &w_lambda,
-                   &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp};
+                   &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp, &s_bw, &s_part, &s_blocal, &s_pbcount,
+                   &s_pbody, &s_prow, &s_pgrp, &s_gpart, &s_gdesc, &s_pccount, &s_pcstart, &s_pcfill, &s_ilist,
+                   &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
     if (hc) cudaFreeHost(hc);
@@ -718,6 +720,10 @@ void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode 
 void gbodeWorldSetSolverBlocks(dWorldID w, int blocks) { w->P.pgs_blocks = blocks > 0 ? blocks : 0; }
 void gbodeWorldSetManifoldPasses(dWorldID w, int passes) { w->P.pgs_passes = passes > 1 ? (passes > 16 ? 16 : passes) : 1; }
 int gbodeWorldGetManifoldPasses(dWorldID w) { return w->P.pgs_passes > 1 ? w->P.pgs_passes : 1; }
+void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases) {
+    w->P.pgs_two_level = interior_phases < 0 ? 0 : (interior_phases > 8 ? 8 : interior_phases);
+}
+int gbodeWorldGetTwoLevelSweep(dWorldID w) { return w->P.pgs_two_level; }
 int gbodeWorldGetSolverBlocks(dWorldID w) { return w->P.pgs_blocks > 0 && w->P.pgs_blocks < num_sms() ? w->P.pgs_blocks : num_sms(); }
 
 int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
@@ -2366,6 +2372,8 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         w->stats.iterations = h.iterations;
         w->stats.residual = h.resid;
         w->stats.sleeping = w->ws.sleep_on ? h.nasleep : 0;
+        w->stats.interior_colours = h.nicolours;
+        w->stats.interior_rows = h.slab_rows;
         w->stats.solve_ms = 0;
         w->stats.step_ms = 0;
         if (w->timing) {

@@ -39,6 +39,7 @@ struct SolverParams {
     int learn_capture;  // record the per-contact features of each step
     int pgs_blocks;     // thread blocks of the coloured solver (0: one per SM)
     int pgs_passes;     // passes over a manifold's rows per visit (0 or 1: one)
+    int pgs_two_level;  // two-level sweep: parts' interior groups in shared memory, cross groups coloured globally
 };
 
 // learned warm start network (parameter layout in mlp.cu)
@@ -78,6 +79,9 @@ struct DevCounters {
     int nawake;            // contacts of awake components (the solver's contacts when sleeping is on)
     int nwaves;            // staging waves of the coloured solver
     int nasleep;           // bodies not stepped (their component sleeps)
+    int nicolours;         // two-level sweep: colours of the parts' interior groups
+    int slab_box[4];       // two-level sweep: body x / y range (order-preserving ints)
+    int slab_rows;         // two-level sweep: interior rows of the last solve
 };
 
 // auto-disable state per body, int4: x flags, y idle steps, z steps left,
@@ -110,6 +114,11 @@ struct Workspace {
     // colouring / schedule
     DBuf m_head, m_id, m_start, m_colour, m_mask, m_claim, m_tent, col_count, col_start, col_fill, col_list, m_desc, p_rows, chunk_rows, chunk_start;
     DBuf wv_count, wv_base, wv_col, wv_sched;  // staging waves: per (colour, block) count and first; per wave colour, slots
+    // two-level sweep: body weights, parts, per-part body lists and counts,
+    // group classes and descriptors, per-(part, colour) interior lists, the
+    // interior rows packed part by part, partition histograms
+    DBuf s_bw, s_part, s_blocal, s_pbcount, s_pbody, s_prow, s_pgrp, s_gpart, s_gdesc;
+    DBuf s_pccount, s_pcstart, s_pcfill, s_ilist, s_irown, s_irowoff, s_idesc, s_ipack, s_hist, s_binpart;
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state

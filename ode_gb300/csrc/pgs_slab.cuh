@@ -1,0 +1,630 @@
+// Two-level coloured SOR sweep (included by solve.cu after k_pgs).
+//
+// The coloured solver's cost on a large connected pile is the number of grid
+// barriers a sweep needs (one per colour, ~1.3 us each on 152 SMs) times the
+// sweeps, while the relaxation itself is short.  Here the dynamic bodies are
+// split into one spatial part per thread block: SX strips in x, each cut into
+// SY parts in y, SX * SY = blocks, every cut placed so that the parts carry
+// about the same number of contact ends (a column through the whole pile per
+// part).  A constraint group whose bodies lie in one part (the static world
+// belongs to every part) is interior to it; the others cross parts.  One sweep
+// is then
+//   1. the interior phase (repeated `ipasses` times): every block relaxes its
+//      part's interior groups, colour by colour under block barriers only,
+//      with the rows (80 bytes a row, loaded once per step), their
+//      multipliers and the part's body accumulators fc resident in shared
+//      memory;
+//   2. the part's fc published to global memory, one grid barrier;
+//   3. the cross groups in their own global colours, exactly as k_pgs relaxes
+//      colours (staged waves, one grid barrier per colour);
+//   4. the part's fc read back from global memory.
+// Both phases are Gauss-Seidel in a fixed order (no two groups of one colour
+// share a body), so a sweep is deterministic.  The interior and the cross
+// groups are coloured independently (k_colour with a class per group).  A
+// part whose interior rows, groups or bodies exceed the shared-memory
+// capacity gives all its groups to the cross phase, so any world runs; worlds
+// of many small islands spread over all blocks keep the one-level k_pgs.
+//
+// quickstep.cpp:2917-3033 is the row update; the order of the rows inside a
+// contact manifold (normal rows first, then the friction pairs) is that of
+// relax_triplets.
+
+#define GB_SLAB_NBIN 1024      // histogram bins per axis of the partition
+#define GB_SLAB_XCHUNK 128     // cross-phase staging rows per buffer
+#define GB_SLAB_ROW_F4 5       // float4 per interior row (80 bytes)
+#define GB_SLAB_COLOURS 64     // interior colours (64 + c in the shared colouring)
+
+__device__ __forceinline__ int ord_f(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float unord_f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ int slab_bin(float v, int lo_o, int hi_o) {
+    const float lo = unord_f(lo_o), hi = unord_f(hi_o);
+    const float span = hi - lo;
+    int b = span > 0.f ? (int)((v - lo) / span * (float)GB_SLAB_NBIN) : 0;
+    return b < 0 ? 0 : (b >= GB_SLAB_NBIN ? GB_SLAB_NBIN - 1 : b);
+}
+
+// contact ends per body: the weight the partition balances
+__global__ void k_slab_weight(const Contact *C, const int *nc_dev, int *bw, DevCounters *dc) {
+    const int nc = *nc_dev;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        dc->slab_box[0] = 0x7fffffff; dc->slab_box[1] = (int)0x80000000;
+        dc->slab_box[2] = 0x7fffffff; dc->slab_box[3] = (int)0x80000000;
+    }
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const Contact k = C[c];
+        if (k.b1 >= 0) atomicAdd(&bw[k.b1], 1);
+        if (k.b2 >= 0) atomicAdd(&bw[k.b2], 1);
+    }
+}
+
+// x / y range of the weighted bodies
+__global__ void k_slab_range(Bodies B, const int *bw, DevCounters *dc) {
+    int x0 = 0x7fffffff, x1 = (int)0x80000000, y0 = 0x7fffffff, y1 = (int)0x80000000;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
+        if (bw[b] <= 0) continue;
+        const float4 p = B.pos[b];
+        x0 = min(x0, ord_f(p.x)); x1 = max(x1, ord_f(p.x));
+        y0 = min(y0, ord_f(p.y)); y1 = max(y1, ord_f(p.y));
+    }
+    x0 = __reduce_min_sync(0xffffffffu, x0); x1 = __reduce_max_sync(0xffffffffu, x1);
+    y0 = __reduce_min_sync(0xffffffffu, y0); y1 = __reduce_max_sync(0xffffffffu, y1);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&dc->slab_box[0], x0); atomicMax(&dc->slab_box[1], x1);
+        atomicMin(&dc->slab_box[2], y0); atomicMax(&dc->slab_box[3], y1);
+    }
+}
+
+// hist[0 .. NBIN): weight by x bin; hist[NBIN + strip * NBIN + ybin] (axis 1):
+// weight by y bin within each x strip (binpart of the x histogram known)
+__global__ void k_slab_hist(Bodies B, const int *bw, const DevCounters *dc, const int *binpart, int *hist, int axis) {
+    const int bx0 = dc->slab_box[0], bx1 = dc->slab_box[1], by0 = dc->slab_box[2], by1 = dc->slab_box[3];
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
+        const int w = bw[b];
+        if (w <= 0) continue;
+        const float4 p = B.pos[b];
+        const int xb = slab_bin(p.x, bx0, bx1);
+        if (axis == 0) atomicAdd(&hist[xb], w);
+        else atomicAdd(&hist[GB_SLAB_NBIN + binpart[xb] * GB_SLAB_NBIN + slab_bin(p.y, by0, by1)], w);
+    }
+}
+
+// One block of GB_SLAB_NBIN threads per histogram row: bin -> part by the
+// cumulative weight at the bin's start, floor(parts * before / total).
+__global__ void k_slab_cut(const int *hist, int *binpart, int parts) {
+    __shared__ int wsum[32];
+    const int row = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int v = hist[row * GB_SLAB_NBIN + t];
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += x;
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int x = wsum[lane];
+        int xi = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += y;
+        }
+        wsum[lane] = xi - x;  // exclusive, per warp
+    }
+    __syncthreads();
+    const long long before = (long long)wsum[wid] + inc - v;
+    __shared__ long long total_s;
+    if (t == GB_SLAB_NBIN - 1) total_s = before + v;
+    __syncthreads();
+    const long long total = total_s;
+    int p = total > 0 ? (int)(before * parts / total) : 0;
+    binpart[row * GB_SLAB_NBIN + t] = p < parts ? p : parts - 1;
+}
+
+// part of every weighted body (strip * sy + y part), its index in the part,
+// the part's body list (first bcap)
+__global__ void k_slab_assign(Bodies B, const int *bw, const DevCounters *dc, const int *binpart, int sy,
+                              int *part, int *blocal, int *pbcount, int *pbody, int bcap) {
+    const int bx0 = dc->slab_box[0], bx1 = dc->slab_box[1], by0 = dc->slab_box[2], by1 = dc->slab_box[3];
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B.n; b += gridDim.x * blockDim.x) {
+        if (bw[b] <= 0) { part[b] = -1; continue; }
+        const float4 p = B.pos[b];
+        const int strip = binpart[slab_bin(p.x, bx0, bx1)];
+        const int q = strip * sy + binpart[GB_SLAB_NBIN + strip * GB_SLAB_NBIN + slab_bin(p.y, by0, by1)];
+        const int l = atomicAdd(&pbcount[q], 1);
+        part[b] = q;
+        blocal[b] = l;
+        if (l < bcap) pbody[(size_t)q * bcap + l] = b;
+    }
+}
+
+// interior (its part) or cross (-1) for every group; interior rows and
+// groups counted per part.  Only triplet manifolds (contacts under
+// dContactApprox1 with friction) have the compact interior row form.
+__global__ void k_slab_classify(const int4 *gdesc, const DevCounters *dc, const int *part, int *gpart, int *prow,
+                                int *pgrp) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int4 d = gdesc[e];
+        int p = -1;
+        if (d.y & GB_DESC_TRIPLETS) {
+            const int p0 = part[d.z], p1 = d.w >= 0 ? part[d.w] : p0;
+            if (p0 >= 0 && p0 == p1) p = p0;
+        }
+        gpart[e] = p;
+        if (p >= 0) {
+            atomicAdd(&prow[p], desc_rows(d));
+            atomicAdd(&pgrp[p], 1);
+        }
+    }
+}
+
+// a part over any shared-memory capacity hands all its groups to the cross phase
+__global__ void k_slab_demote(const DevCounters *dc, const int *prow, const int *pgrp, const int *pbcount, int rcap,
+                              int gcap, int bcap, int *gpart) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int p = gpart[e];
+        if (p >= 0 && (prow[p] > rcap || pgrp[p] > gcap || pbcount[p] > bcap)) gpart[e] = -1;
+    }
+}
+
+__global__ void k_slab_count(const DevCounters *dc, const int *gpart, const int *colour, int *pccount) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int p = gpart[e];
+        if (p < 0) continue;
+        const int c = colour[e] - 64;
+        if (c >= 0 && c < GB_SLAB_COLOURS) atomicAdd(&pccount[p * GB_SLAB_COLOURS + c], 1);
+    }
+}
+
+// interior groups listed part by part, colour by colour (order within one
+// (part, colour) is free: those groups share no body)
+__global__ void k_slab_fill(const DevCounters *dc, const int *gpart, const int *colour, const int4 *gdesc,
+                            const int *pcstart, int *pcfill, int *ilist, int *irown) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int p = gpart[e];
+        if (p < 0) continue;
+        const int c = colour[e] - 64;
+        if (c < 0 || c >= GB_SLAB_COLOURS) continue;
+        const int k = p * GB_SLAB_COLOURS + c;
+        const int pos = pcstart[k] + atomicAdd(&pcfill[k], 1);
+        ilist[pos] = e;
+        irown[pos] = desc_rows(gdesc[e]);
+    }
+}
+
+// The interior descriptors (first global row, row count and flags, local
+// bodies b1 | (b2 + 1) << 16, first row in the part's block of rows) and rows:
+//   q0 J1l' (xyz, rhs')   q1 J1a' (xyz, cfm')   q2 J2a' (xyz, hi)
+//   q3 M1a (xyz, invm1 / Ad)   q4 M2a (xyz, invm2 / Ad)
+// A contact row's second linear Jacobian is the negated first one (J2l' =
+// -J1l', exactly), and M^-1 J^T's linear parts are invm * J / Ad, so 80 bytes
+// hold the row.  Normal rows have lo = 0; friction rows +-|hi * lambda_normal|.
+__global__ void k_slab_pack(Rows Rw, Bodies B, const int *gpart, const int4 *gdesc, const int *ilist,
+                            const int *irowoff, const int *irown, const int *pcstart, const int *blocal,
+                            int total_slot, int4 *idesc, float4 *ipack, DevCounters *dc) {
+    const int total = pcstart[total_slot];
+    if (blockIdx.x == 0 && threadIdx.x == 0) dc->slab_rows = total > 0 ? irowoff[total - 1] + irown[total - 1] : 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int e = ilist[i];
+        const int4 d = gdesc[e];
+        const int p = gpart[e];
+        const int off = irowoff[i] - irowoff[pcstart[p * GB_SLAB_COLOURS]];
+        const int lb1 = blocal[d.z], lb2 = d.w >= 0 ? blocal[d.w] : -1;
+        idesc[i] = make_int4(d.x, d.y, lb1 | ((lb2 + 1) << 16), off);
+        const float im1 = B.pos[d.z].w, im2 = d.w >= 0 ? B.pos[d.w].w : 0.f;
+        const int n = desc_rows(d);
+        for (int k = 0; k < n; k++) {
+            const int r = d.x + k;
+            const float ad = Rw.Ad[r];
+            const float4 m1a = Rw.M1a[r], m2a = Rw.M2a[r];
+            float4 *o = ipack + (size_t)(irowoff[i] + k) * GB_SLAB_ROW_F4;
+            o[0] = Rw.J1l[r];
+            o[1] = Rw.J1a[r];
+            o[2] = Rw.J2a[r];
+            o[3] = make_float4(m1a.x, m1a.y, m1a.z, im1 / ad);
+            o[4] = make_float4(m2a.x, m2a.y, m2a.z, im2 / ad);
+        }
+    }
+}
+
+// quickstep.cpp:2917-3033 on one 80-byte row (the second body's
+// accumulators are zero and unused for a one-body contact)
+__device__ __forceinline__ void relax_slab_row(const float4 *row, float &lam, float lo, float hi, float4 &f1l,
+                                               float4 &f1a, float4 &f2l, float4 &f2a) {
+    const float4 q0 = row[0], q1 = row[1], q2 = row[2];
+    const float dx = f1l.x - f2l.x, dy = f1l.y - f2l.y, dz = f1l.z - f2l.z;
+    float a = fmaf(dx, q0.x, dy * q0.y);
+    float b = fmaf(dz, q0.z, f1a.x * q1.x);
+    float c = fmaf(f1a.y, q1.y, f1a.z * q1.z);
+    a = fmaf(f2a.x, q2.x, a);
+    b = fmaf(f2a.y, q2.y, b);
+    c = fmaf(f2a.z, q2.z, c);
+    const float old = lam;
+    float delta = fmaf(-old, q1.w, q0.w) - ((a + b) + c);
+    const float nl = old + delta;
+    const float cl = fminf(fmaxf(nl, lo), hi);
+    if (cl != nl) delta = cl - old;
+    lam = cl;
+    const float4 q3 = row[3], q4 = row[4];
+    const float d1 = delta * q3.w, d2 = delta * q4.w;
+    f1l.x = fmaf(d1, q0.x, f1l.x); f1l.y = fmaf(d1, q0.y, f1l.y); f1l.z = fmaf(d1, q0.z, f1l.z);
+    f1a.x = fmaf(delta, q3.x, f1a.x); f1a.y = fmaf(delta, q3.y, f1a.y); f1a.z = fmaf(delta, q3.z, f1a.z);
+    f2l.x = fmaf(-d2, q0.x, f2l.x); f2l.y = fmaf(-d2, q0.y, f2l.y); f2l.z = fmaf(-d2, q0.z, f2l.z);
+    f2a.x = fmaf(delta, q4.x, f2a.x); f2a.y = fmaf(delta, q4.y, f2a.y); f2a.z = fmaf(delta, q4.z, f2a.z);
+}
+
+// one interior triplet manifold, all in shared memory
+__device__ __forceinline__ void relax_slab(int4 d, const float4 *rows, float *lam, float4 *fc, int passes) {
+    const int nct = desc_rows(d) / 3, off = d.w;
+    const int lb1 = d.z & 0xffff, lb2 = (d.z >> 16) - 1;
+    float4 f1l = fc[2 * lb1], f1a = fc[2 * lb1 + 1];
+    float4 f2l = make_float4(0.f, 0.f, 0.f, 0.f), f2a = f2l;
+    if (lb2 >= 0) { f2l = fc[2 * lb2]; f2a = fc[2 * lb2 + 1]; }
+    const float4 *R = rows + (size_t)off * GB_SLAB_ROW_F4;
+    float *L = lam + off;
+#pragma unroll 1
+    for (int pass = 0; pass < passes; pass++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if (c >= nct) break;
+            relax_slab_row(R + 3 * c * GB_SLAB_ROW_F4, L[3 * c], 0.f, R[3 * c * GB_SLAB_ROW_F4 + 2].w, f1l, f1a, f2l,
+                           f2a);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if (c >= nct) break;
+            const float ln = L[3 * c];
+#pragma unroll
+            for (int q = 1; q < 3; q++) {
+                const float4 *row = R + (3 * c + q) * GB_SLAB_ROW_F4;
+                const float hi = fabsf(row[2].w * ln);
+                relax_slab_row(row, L[3 * c + q], -hi, hi, f1l, f1a, f2l, f2a);
+            }
+        }
+    }
+    fc[2 * lb1] = f1l; fc[2 * lb1 + 1] = f1a;
+    if (lb2 >= 0) { fc[2 * lb2] = f2l; fc[2 * lb2 + 1] = f2a; }
+}
+
+struct SlabArgs {
+    PgsArgs A;
+    const int *pcstart;   // [parts * 64 + 1]: interior groups per (part, colour), exclusive scan
+    const int *irowoff;   // [interior groups]: first row of each in ipack
+    const int *irown;     // [interior groups]: rows of each
+    const int4 *idesc;    // [interior groups]
+    const float4 *ipack;  // interior rows, 5 float4 each, part by part
+    const int *pbody, *pbcount;
+    int bcap, rcap, gcap;  // per-part capacities: bodies, interior rows, interior groups
+    int chunk_cap;         // cross-phase staging rows per buffer
+    int ipasses;           // interior phases per sweep (>= 1)
+};
+
+// Shared memory of k_pgs_slab: two cross staging buffers (chunk_cap rows of
+// 128 B), the part's interior rows (rcap x 80 B), body accumulators
+// ((bcap + 1) x 32 B, the last slot zero), interior descriptors (gcap x
+// 16 B), interior multipliers (rcap x 4 B), global body ids (bcap x 4 B).
+__host__ __device__ __forceinline__ size_t slab_smem_bytes(int chunk_cap, int rcap, int bcap, int gcap) {
+    return (size_t)2 * chunk_cap * 128 + (size_t)rcap * 80 + (size_t)(bcap + 1) * 32 + (size_t)gcap * 16 +
+           (size_t)rcap * 4 + (size_t)bcap * 4;
+}
+
+__global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
+    const PgsArgs &A = S.A;
+    unsigned gen = 0;
+    DevCounters *dc = A.dc;
+    __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS], s_wcount[GB_MAX_COLOURS],
+        s_wbase[GB_MAX_COLOURS];
+    __shared__ int s_icol[GB_SLAB_COLOURS + 1];
+    __shared__ int s_nic, s_g0, s_ng, s_row0, s_nrows, s_nb;
+    __shared__ unsigned long long s_mbar[3];
+    __shared__ float s_lam[GB_PGS_THREADS * 13];
+    extern __shared__ float4 pgs_smem[];
+    float4 *xbuf = pgs_smem;                                         // 2 x chunk_cap x 8
+    float4 *irows = xbuf + (size_t)2 * S.chunk_cap * 8;              // rcap x 5
+    float4 *ifc = irows + (size_t)S.rcap * GB_SLAB_ROW_F4;           // (bcap + 1) x 2
+    int4 *idesc = (int4 *)(ifc + (size_t)(S.bcap + 1) * 2);          // gcap
+    float *ilam = (float *)(idesc + S.gcap);                         // rcap
+    int *ibid = (int *)(ilam + S.rcap);                              // bcap
+    const int ncol = dc->ncolours;   // cross colours
+    const int nicol = dc->nicolours; // interior colours (global)
+    const int nrows = dc->nrows;
+    const int part = blockIdx.x;
+    for (int c = threadIdx.x; c < GB_MAX_COLOURS; c += blockDim.x) {
+        s_cstart[c] = A.cstart[c];
+        s_ccount[c] = A.ccount[c];
+        s_wcount[c] = c < ncol ? A.wcount[c * gridDim.x + blockIdx.x] : 1;
+        s_wbase[c] = c < ncol ? A.wbase[c * gridDim.x + blockIdx.x] : 0;
+    }
+    if (threadIdx.x <= GB_SLAB_COLOURS) {
+        const int base = S.pcstart[part * GB_SLAB_COLOURS];
+        s_icol[threadIdx.x] = S.pcstart[part * GB_SLAB_COLOURS + threadIdx.x] - base;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&s_mbar[0]);
+        mbar_init(&s_mbar[1]);
+        mbar_init(&s_mbar[2]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        const int g0 = S.pcstart[part * GB_SLAB_COLOURS], g1 = S.pcstart[(part + 1) * GB_SLAB_COLOURS];
+        s_g0 = g0;
+        s_ng = g1 - g0;
+        s_row0 = g1 > g0 ? S.irowoff[g0] : 0;
+        s_nrows = g1 > g0 ? S.irowoff[g1 - 1] + S.irown[g1 - 1] - s_row0 : 0;
+        s_nb = min(S.pbcount[part], S.bcap);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int c = 0; c < GB_SLAB_COLOURS; c++)
+            if (s_icol[c + 1] > s_icol[c]) n = c + 1;
+        s_nic = n;
+    }
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const bool residual_mode = A.target > 0;
+    const int itmax = nrows > 0 ? (residual_mode ? A.max_iterations : A.iterations) : 0;
+    int it = 0, check = 0, last_reform = 0;
+    float *slots = dc->racc;
+    // fc = M^-1 J^T lambda over every group (cross colours, then interior colours), from global lambda
+    auto form_fc = [&](bool zero) -> bool {
+        if (zero) {
+            for (int b = tid; b < A.nb; b += nth) {
+                stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
+                stcg4(&A.fc[2 * b + 1], make_float4(0.f, 0.f, 0.f, 0.f));
+            }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+        }
+        for (int cc = 0; cc < ncol + nicol; cc++) {
+            const int c = cc < ncol ? cc : 64 + (cc - ncol);
+            for (int k = tid; k < s_ccount[c]; k += nth) apply_desc(A, __ldg(&A.desc[s_cstart[c] + k]));
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+        }
+        return true;
+    };
+    auto residual_rel = [&](float &rel) -> bool {
+        float *acc = slots + 2 * (check & 1);
+        float rmax = 0.f, lmax = 0.f;
+        for (int r = tid; r < nrows; r += nth) {
+            rmax = fmaxf(rmax, row_residual(A.Rw, A.fc, r, A.w_sor));
+            lmax = fmaxf(lmax, fabsf(__ldcg(&A.Rw.lambda[r])));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+            lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        }
+        if ((threadIdx.x & 31) == 0) { atomic_max_pos(&acc[0], rmax); atomic_max_pos(&acc[1], lmax); }
+        if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+        const float rr = __ldcg(&acc[0]), ll = __ldcg(&acc[1]);
+        rel = rr / fmaxf(1.0f, ll);
+        if (tid == 0) {
+            float *other = slots + 2 * ((check + 1) & 1);
+            other[0] = 0.f; other[1] = 0.f;
+            dc->resid = rel; dc->maxlam = ll;
+            if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
+        }
+        ++check;
+        return true;
+    };
+    auto swap_alt = [&]() -> bool {
+        for (int r = tid; r < nrows; r += nth) {
+            const float a = __ldcg(&A.Rw.lambda[r]), b = __ldcg(&A.lam_alt[r]);
+            __stcg(&A.Rw.lambda[r], b);
+            __stcg(&A.lam_alt[r], a);
+        }
+        return grid_sync(&dc->gsync, &dc->err, gen);
+    };
+    // the part's interior rows stream in while the start is formed
+    if (threadIdx.x == 0) {
+        const unsigned bytes = 80u * (unsigned)min(s_nrows, S.rcap);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&s_mbar[2], bytes);
+        if (bytes) bulk_g2s(irows, S.ipack + (size_t)s_row0 * GB_SLAB_ROW_F4, bytes, &s_mbar[2]);
+    }
+    for (int i = threadIdx.x; i < s_ng && i < S.gcap; i += blockDim.x) idesc[i] = S.idesc[s_g0 + i];
+    for (int l = threadIdx.x; l < s_nb; l += blockDim.x) ibid[l] = S.pbody[(size_t)part * S.bcap + l];
+    if (threadIdx.x < 2) ifc[2 * S.bcap + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool ok = true;
+    if (A.learned) {
+        float r_mlp = 0.f, r_plain = 0.f;
+        ok = form_fc(true) && residual_rel(r_mlp) && swap_alt() && form_fc(true) && residual_rel(r_plain);
+        const bool use = ok && r_mlp < r_plain;
+        if (ok && use) ok = swap_alt() && form_fc(true);
+        if (ok && tid == 0) {
+            dc->learn_stats[0] = use ? 1.f : 0.f;
+            dc->learn_stats[1] = r_mlp;
+            dc->learn_stats[2] = r_plain;
+        }
+    } else if (A.warm) {
+        ok = form_fc(false);
+    }
+    // the copy of the interior rows ends before the block can exit
+    if (threadIdx.x == 0) mbar_wait(&s_mbar[2], 0, &dc->err);
+    __syncthreads();
+    if (!ok) return;
+    // interior multipliers and the part's accumulators into shared memory
+    auto load_part = [&](bool with_lambda) {
+        for (int l = threadIdx.x; l < s_nb; l += blockDim.x) {
+            const int b = ibid[l];
+            ifc[2 * l] = ldcg4(&A.fc[2 * b]);
+            ifc[2 * l + 1] = ldcg4(&A.fc[2 * b + 1]);
+        }
+        if (with_lambda)
+            for (int i = threadIdx.x; i < s_ng; i += blockDim.x) {
+                const int4 d = idesc[i];
+                for (int k = 0; k < desc_rows(d); k++) ilam[d.w + k] = __ldcg(&A.Rw.lambda[d.x + k]);
+            }
+    };
+    auto publish_fc = [&]() {
+        for (int l = threadIdx.x; l < s_nb; l += blockDim.x) {
+            const int b = ibid[l];
+            stcg4(&A.fc[2 * b], ifc[2 * l]);
+            stcg4(&A.fc[2 * b + 1], ifc[2 * l + 1]);
+        }
+    };
+    auto publish_lambda = [&]() {
+        for (int i = threadIdx.x; i < s_ng; i += blockDim.x) {
+            const int4 d = idesc[i];
+            for (int k = 0; k < desc_rows(d); k++) __stcg(&A.Rw.lambda[d.x + k], ilam[d.w + k]);
+        }
+    };
+    load_part(true);
+    __syncthreads();
+    // The sweep is a sequence of steps: the interior phase (c = -1), then the
+    // cross colours' waves.  Buffer q & 1 holds step number q's cross chunk
+    // (the interior step copies nothing); its use number q >> 1 is the
+    // mbarrier phase to wait for.
+    struct Step { int c, w; };
+    auto step_after = [&](Step t) -> Step {
+        if (t.c < 0) return Step{ncol > 0 ? 0 : -1, 0};
+        if (t.w + 1 < s_wcount[t.c]) return Step{t.c, t.w + 1};
+        return Step{t.c + 1 < ncol ? t.c + 1 : -1, 0};
+    };
+    unsigned q = 0;
+    unsigned nissued = 0, nwaited = 0;
+    int pend_start = 0, pend_rows = 0;
+    auto chunk_of = [&](Step t) {
+        if (t.c < 0) { pend_start = 0; pend_rows = 0; return; }
+        const int wv = s_wbase[t.c] + t.w;
+        pend_start = __ldg(&A.chunk_start[wv]);
+        pend_rows = __ldg(&A.chunk_rows[wv]);
+    };
+    auto issue = [&](Step t) {
+        const unsigned qq = nissued++;
+        unsigned long long *m = &s_mbar[qq & 1];
+        const unsigned bytes = 128u * (unsigned)min(pend_rows, S.chunk_cap);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(m, bytes);
+        if (bytes) bulk_g2s(xbuf + (qq & 1) * (S.chunk_cap * 8), A.packed + (size_t)pend_start * 8, bytes, m);
+        chunk_of(step_after(t));
+    };
+    auto retire = [&]() {
+        const unsigned qq = nwaited++;
+        return mbar_wait(&s_mbar[qq & 1], (qq >> 1) & 1, &dc->err);
+    };
+    auto drain = [&]() {
+        cp_async_wait_all();
+        if (threadIdx.x == 0)
+            while (nwaited < nissued) retire();
+    };
+    float *my_lam = s_lam + threadIdx.x * 13;
+    int4 next = make_int4(0, 0, -1, -1), ahead = next;
+    bool has_next = false, staged = false, has_ahead = false;
+    auto load_ahead = [&](Step t) {
+        if (t.c < 0) { has_ahead = false; return; }
+        int k = blockIdx.x + threadIdx.x * (int)gridDim.x;
+        if (s_wcount[t.c] == 1) k = k < s_ccount[t.c] ? k : -1;
+        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * GB_PGS_THREADS + threadIdx.x]);
+        has_ahead = k >= 0;
+        if (has_ahead) ahead = __ldg(&A.desc[s_cstart[t.c] + k]);
+    };
+    auto fetch = [&](Step t_after) {
+        has_next = has_ahead;
+        next = ahead;
+        staged = false;
+        if (has_next) {
+            const int n = desc_rows(next);
+            staged = (next.y & GB_DESC_STAGED) && desc_chunk_off(next) + n <= S.chunk_cap;
+            if (staged) {
+                for (int k = 0; k < n; k++) cp_async4(&my_lam[k], &A.Rw.lambda[next.x + k]);
+                cp_async_commit();
+            }
+        }
+        load_ahead(t_after);
+    };
+    {
+        const Step s0{-1, 0};
+        if (threadIdx.x == 0) {
+            chunk_of(s0);
+            issue(s0);
+        }
+        load_ahead(s0);
+        fetch(step_after(s0));
+    }
+    for (; it < itmax;) {
+        Step cur{-1, 0};
+        const bool check_this = residual_mode && ((it + 1) % A.check_every == 0 || it + 1 == itmax);
+        for (;;) {
+            const Step nxt = step_after(cur), nnx = step_after(nxt);
+            const bool interior = cur.c < 0;
+            const bool last_wave = interior || cur.w + 1 == s_wcount[cur.c];
+            if (threadIdx.x == 0 && !last_wave) issue(nxt);
+            float lout[GB_STAGED_ROWS];
+            int nout = 0, xout = 0;
+            if (interior) {
+                for (int rep = 0; rep < S.ipasses; rep++)
+                    for (int c = 0; c < s_nic; c++) {
+                        for (int i = s_icol[c] + threadIdx.x; i < s_icol[c + 1]; i += blockDim.x)
+                            relax_slab(idesc[i], irows, ilam, ifc, A.passes);
+                        __syncthreads();
+                    }
+                publish_fc();
+                if (check_this) publish_lambda();
+            } else if (has_next) {
+                if (!staged) {
+                    relax_desc(A, next);
+                } else {
+                    if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
+                    const float4 *buf = xbuf + (q & 1) * (S.chunk_cap * 8);
+                    if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
+                    else relax_plain(A, next, buf, my_lam, lout);
+                    nout = desc_rows(next);
+                    xout = next.x;
+                }
+            }
+            const bool sweep_end = last_wave && nxt.c < 0;
+            if (!last_wave) {
+#pragma unroll
+                for (int k = 0; k < GB_STAGED_ROWS; k++)
+                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                fetch(nnx);
+                __syncthreads();
+            } else {
+                const bool check_next = check_this && sweep_end;
+                if (check_next) {
+#pragma unroll
+                    for (int k = 0; k < GB_STAGED_ROWS; k++)
+                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                }
+                unsigned target = 0;
+                grid_arrive(&dc->gsync, gen, target);
+                if (threadIdx.x == 0) issue(nxt);
+                if (!check_next) {
+#pragma unroll
+                    for (int k = 0; k < GB_STAGED_ROWS; k++)
+                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                }
+                fetch(nnx);
+                if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
+            }
+            if (threadIdx.x == 0) retire();
+            ++q;
+            if (sweep_end) break;
+            cur = nxt;
+        }
+        ++it;
+        if (check_this) {
+            if (it - last_reform >= A.reform_every || it == itmax) {
+                last_reform = it;
+                if (!form_fc(true)) { drain(); return; }
+            }
+            float rel;
+            if (!residual_rel(rel)) { drain(); return; }
+            if (rel <= A.target) break;
+        }
+        // every block's cross updates of the part's bodies are out (the last
+        // barrier of the sweep, or of the check): the accumulators come back
+        load_part(false);
+        __syncthreads();
+    }
+    // The global accumulators are current here (read back after the last
+    // sweep's barrier, or formed at the check that ended the solve); the
+    // interior multipliers go out for the integration and the warm-start store.
+    publish_lambda();
+    drain();
+    if (tid == 0) dc->iterations = it;
+}

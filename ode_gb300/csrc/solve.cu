@@ -902,8 +902,13 @@ __global__ void k_groups_total(DevCounters *dc, int nj) {
 // Speculative first-fit colouring (rounds of: pick the lowest colour free at
 // both bodies; per (body, colour) the lowest manifold index wins; losers
 // retry).  One cooperative launch; every barrier is bounded.
+// With `cls` (two-level sweep) the groups form two classes coloured
+// independently: cross groups (cls < 0) take colours 0-63, a part's interior
+// groups (cls >= 0) 64-127; dc->ncolours counts the first, dc->nicolours the
+// second.  Interior groups of different parts share no body, so one colouring
+// serves every part.
 __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long *mask, int *claim, int *colour,
-                         int *tent, int nb) {
+                         int *tent, int nb, const int *cls) {
     unsigned gen = 0;
     const int nm = dc->nmanifolds;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -921,7 +926,12 @@ __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long 
             if (n1 >= 0) { m1 = __ldcg(&mask[2 * n1]); m1b = __ldcg(&mask[2 * n1 + 1]); }
             unsigned long long lo = m0 | m1, hi = m0b | m1b;
             int c;
-            if (~lo) c = __ffsll(~lo) - 1;
+            if (cls) {
+                const bool in = cls[e] >= 0;
+                const unsigned long long used = in ? hi : lo;
+                if (~used) c = (in ? 64 : 0) + __ffsll(~used) - 1;
+                else { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); c = in ? GB_MAX_COLOURS - 1 : 63; }
+            } else if (~lo) c = __ffsll(~lo) - 1;
             else if (~hi) c = 64 + __ffsll(~hi) - 1;
             else { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); c = GB_MAX_COLOURS - 1; }
             tent[e] = c;
@@ -942,7 +952,8 @@ __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long 
                 unsigned long long bit = 1ull << (c & 63);
                 atomicOr(&mask[2 * n0 + (c >> 6)], bit);
                 if (n1 >= 0) atomicOr(&mask[2 * n1 + (c >> 6)], bit);
-                atomicMax(&dc->ncolours, c + 1);
+                if (cls && c >= 64) atomicMax(&dc->nicolours, c - 63);
+                else atomicMax(&dc->ncolours, c + 1);
             }
         }
         if (!grid_sync(&dc->gsync, &dc->err, gen)) return;
@@ -1063,32 +1074,46 @@ struct PgsArgs {
 #define GB_DESC_STAGED (GB_DESC_TRIPLETS | GB_DESC_PLAIN)
 __device__ __forceinline__ int desc_rows(int4 d) { return d.y & 0xffff; }
 
+// The descriptor of constraint group e (a contact manifold, or a ball/hinge
+// joint whose rows follow the contact rows).
+__device__ __forceinline__ int4 group_desc(int e, const int *mstart, const int *rstart, const int *mcount,
+                                           const int2 *rbody, const int *findex, const DevCounters *dc,
+                                           const int *jrstart, const int *jm, const int2 *gbody) {
+    const int ncm = dc->ncmanifolds;
+    if (e >= ncm) {
+        const int k = e - ncm;
+        const int2 b = gbody[e];
+        return make_int4(dc->nrows_contacts + jrstart[k], jm[k] | GB_DESC_PLAIN, b.x, b.y);
+    }
+    const int c0 = mstart[e], c1 = mstart[e + 1];
+    const int r0 = rstart[c0];
+    const int r1 = rstart[c1 - 1] + mcount[c1 - 1];
+    const int2 b = rbody[r0];
+    bool tri = c1 - c0 <= 4;
+    for (int c = c0; c < c1 && tri; c++) {
+        const int r = r0 + 3 * (c - c0);
+        tri = mcount[c] == 3 && rstart[c] == r && findex[r] < 0 && findex[r + 1] == r && findex[r + 2] == r;
+    }
+    bool plain = !tri && r1 - r0 <= 12;
+    for (int r = r0; r < r1 && plain; r++) plain = findex[r] < 0;
+    return make_int4(r0, (r1 - r0) | (tri ? GB_DESC_TRIPLETS : 0) | (plain ? GB_DESC_PLAIN : 0), b.x, b.y);
+}
+
 __global__ void k_manifold_desc(const int *clist, const int *mstart, const int *rstart, const int *mcount,
                                 const int2 *rbody, const int *findex, DevCounters *dc, int4 *desc,
                                 const int *jrstart, const int *jm, const int2 *gbody) {
     const int total = dc->colour_total;
-    const int ncm = dc->ncmanifolds;
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
-        const int e = clist[j];
-        if (e >= ncm) {  // a ball or hinge joint: its rows follow the contact rows
-            const int k = e - ncm;
-            const int2 b = gbody[e];
-            desc[j] = make_int4(dc->nrows_contacts + jrstart[k], jm[k] | GB_DESC_PLAIN, b.x, b.y);
-            continue;
-        }
-        const int c0 = mstart[e], c1 = mstart[e + 1];
-        const int r0 = rstart[c0];
-        const int r1 = rstart[c1 - 1] + mcount[c1 - 1];
-        const int2 b = rbody[r0];
-        bool tri = c1 - c0 <= 4;
-        for (int c = c0; c < c1 && tri; c++) {
-            const int r = r0 + 3 * (c - c0);
-            tri = mcount[c] == 3 && rstart[c] == r && findex[r] < 0 && findex[r + 1] == r && findex[r + 2] == r;
-        }
-        bool plain = !tri && r1 - r0 <= 12;
-        for (int r = r0; r < r1 && plain; r++) plain = findex[r] < 0;
-        desc[j] = make_int4(r0, (r1 - r0) | (tri ? GB_DESC_TRIPLETS : 0) | (plain ? GB_DESC_PLAIN : 0), b.x, b.y);
-    }
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x)
+        desc[j] = group_desc(clist[j], mstart, rstart, mcount, rbody, findex, dc, jrstart, jm, gbody);
+}
+
+// the same descriptors indexed by group (the two-level sweep classifies groups before colouring)
+__global__ void k_group_desc(const int *mstart, const int *rstart, const int *mcount, const int2 *rbody,
+                             const int *findex, DevCounters *dc, int4 *gdesc, const int *jrstart, const int *jm,
+                             const int2 *gbody) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x)
+        gdesc[e] = group_desc(e, mstart, rstart, mcount, rbody, findex, dc, jrstart, jm, gbody);
 }
 
 // Prefetch a manifold's rows into L1.  The row arrays are read-only while the
@@ -1234,12 +1259,12 @@ __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row 
 // The greedy cut of one (colour, block)'s slots into waves; `visit(wave, t,
 // k, offset)` for every slot (offset -1: not staged), returns the wave count.
 template <class F>
-__device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, F visit) {
+__device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, int chunk_cap, F visit) {
     int waves = 0, t = GB_PGS_THREADS, rows = 0;
     for (int k = b; k < n; k += B) {
         const int4 d = desc[s0 + k];
         const int r = (d.y & GB_DESC_STAGED) ? desc_rows(d) : 0;
-        if (t == GB_PGS_THREADS || rows + r > GB_CHUNK_ROWS) { ++waves; t = 0; rows = 0; }
+        if (t == GB_PGS_THREADS || rows + r > chunk_cap) { ++waves; t = 0; rows = 0; }
         visit(waves - 1, t, k, r > 0 ? rows : -1);
         rows += r;
         ++t;
@@ -1250,18 +1275,19 @@ __device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, F visit)
 // pass 1, one thread per (colour, block): waves of each (at least one, so
 // every block takes part in every colour's barrier)
 __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCounters *dc, const int4 *desc,
-                             int *wcount, int B) {
+                             int *wcount, int B, int chunk_cap) {
     const int cb = blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
     if (c >= dc->ncolours) { wcount[cb] = 0; return; }
-    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, [](int, int, int, int) {});
+    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, [](int, int, int, int) {});
     wcount[cb] = w > 0 ? w : 1;
 }
 
 // pass 2: the chunk offsets in the descriptors, the schedule, rows per wave
 __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, const int *wcount,
-                            const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B) {
+                            const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B,
+                            int chunk_cap) {
     const int cb = blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
@@ -1274,7 +1300,7 @@ __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *d
         for (int t = 0; t < GB_PGS_THREADS; t++) sched[(size_t)(base + w) * GB_PGS_THREADS + t] = -1;
     }
     const int s0 = cstart[c];
-    cut_waves(desc, s0, ccount[c], b, B, [&](int w, int t, int k, int off) {
+    cut_waves(desc, s0, ccount[c], b, B, chunk_cap, [&](int w, int t, int k, int off) {
         sched[(size_t)(base + w) * GB_PGS_THREADS + t] = k;
         if (off >= 0) {
             int4 d = desc[s0 + k];
@@ -1722,6 +1748,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     if (tid == 0) dc->iterations = it;
 }
 
+#include "pgs_slab.cuh"
+
 // ------------------------------------------------------------------ reference-order islands
 // One block per island, rows relaxed by thread 0 in the reference's order
 // (island joint order, findex<0 rows first: quickstep.cpp:2329-2355), with
@@ -2117,6 +2145,36 @@ static int coop_blocks(const void *kernel, int block, int max_per_sm) {
     return per_sm * num_sms();
 }
 
+// Per-part capacities of the two-level sweep from the shared memory a block
+// may opt into (once; thread-safe static initialisation): bodies and groups
+// fixed, the rest for interior rows.  Sized for the 32,768-body pile on 152
+// columns (per column at most ~240 bodies, ~520 interior manifolds and ~1,920
+// interior rows), whose every column then keeps its interior manifolds.
+struct SlabCaps {
+    int bcap, gcap, rcap;
+    size_t smem;
+};
+static SlabCaps slab_caps() {
+    static const SlabCaps caps = []() {
+        SlabCaps c{288, 560, 0, 0};
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, (const void *)k_pgs_slab) != cudaSuccess) return c;
+        const long long fixed = (long long)fa.sharedSizeBytes + (long long)slab_smem_bytes(GB_SLAB_XCHUNK, 0, c.bcap, c.gcap);
+        const long long room = (long long)optin - fixed - 256;  // a little kept for the runtime's own use
+        c.rcap = room > 0 ? (int)(room / 84) : 0;
+        c.smem = slab_smem_bytes(GB_SLAB_XCHUNK, c.rcap, c.bcap, c.gcap);
+        if (c.rcap > 0 &&
+            cudaFuncSetAttribute((const void *)k_pgs_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem) !=
+                cudaSuccess)
+            c.rcap = 0;
+        return c;
+    }();
+    return caps;
+}
+
 static bool ensure_warm(Workspace &ws) {
     unsigned want = 1024;
     while (want < 2u * (unsigned)(ws.contact_cap > 0 ? ws.contact_cap : 1) && want < (1u << 23)) want <<= 1;
@@ -2266,10 +2324,58 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                   ws.grp_body.as<int2>());
     k_groups_total<<<1, 1, 0, s>>>(ws.dc, ws.njoints);
     count_launch(2);
+    const int pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
+    // two-level sweep: parts, interior / cross classes of the groups
+    const SlabCaps caps = slab_caps();
+    const bool slab = P.pgs_two_level && pgs_blocks >= 2 && caps.rcap > 0;
+    const size_t ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
+    int sx = 1, sy = pgs_blocks;
+    if (slab) {
+        for (int d = 1; d * d <= pgs_blocks; d++)
+            if (pgs_blocks % d == 0) sx = d;
+        sy = pgs_blocks / sx;
+        const size_t nbb = nb > 0 ? nb : 1, npc = (size_t)pgs_blocks * GB_SLAB_COLOURS;
+        const size_t nh = (size_t)GB_SLAB_NBIN * (1 + sx);
+        if (!(ws.s_bw.ensure(nbb * 4) && ws.s_part.ensure(nbb * 4) && ws.s_blocal.ensure(nbb * 4) &&
+              ws.s_pbcount.ensure((size_t)pgs_blocks * 4) && ws.s_pbody.ensure((size_t)pgs_blocks * caps.bcap * 4) &&
+              ws.s_prow.ensure((size_t)pgs_blocks * 4) && ws.s_pgrp.ensure((size_t)pgs_blocks * 4) &&
+              ws.s_gpart.ensure((ngroups + 1) * 4) && ws.s_gdesc.ensure((ngroups + 1) * 16) &&
+              ws.s_pccount.ensure(npc * 4) && ws.s_pcstart.ensure((npc + 1) * 4) && ws.s_pcfill.ensure(npc * 4) &&
+              ws.s_ilist.ensure((ngroups + 1) * 4) && ws.s_irown.ensure((ngroups + 1) * 4) &&
+              ws.s_irowoff.ensure((ngroups + 1) * 4) && ws.s_idesc.ensure((ngroups + 1) * 16) &&
+              ws.s_ipack.ensure((size_t)ws.row_cap * 80) && ws.s_hist.ensure(nh * 4) && ws.s_binpart.ensure(nh * 4)))
+            return false;
+        Bodies B = bodies_view(ws, nb);
+        cudaMemsetAsync(ws.s_bw.p, 0, nbb * 4, s);
+        cudaMemsetAsync(ws.s_hist.p, 0, nh * 4, s);
+        cudaMemsetAsync(ws.s_pbcount.p, 0, (size_t)pgs_blocks * 4, s);
+        cudaMemsetAsync(ws.s_prow.p, 0, (size_t)pgs_blocks * 4, s);
+        cudaMemsetAsync(ws.s_pgrp.p, 0, (size_t)pgs_blocks * 4, s);
+        k_group_desc<<<grid, 256, 0, s>>>(ws.m_start.as<int>(), ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
+                                          ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc, ws.s_gdesc.as<int4>(),
+                                          ws.j_rstart.as<int>(), ws.j_m.as<int>(), ws.grp_body.as<int2>());
+        k_slab_weight<<<grid, 256, 0, s>>>(C, ncp, ws.s_bw.as<int>(), ws.dc);
+        k_slab_range<<<grid, 256, 0, s>>>(B, ws.s_bw.as<int>(), ws.dc);
+        k_slab_hist<<<grid, 256, 0, s>>>(B, ws.s_bw.as<int>(), ws.dc, ws.s_binpart.as<int>(), ws.s_hist.as<int>(), 0);
+        k_slab_cut<<<1, GB_SLAB_NBIN, 0, s>>>(ws.s_hist.as<int>(), ws.s_binpart.as<int>(), sx);
+        k_slab_hist<<<grid, 256, 0, s>>>(B, ws.s_bw.as<int>(), ws.dc, ws.s_binpart.as<int>(), ws.s_hist.as<int>(), 1);
+        k_slab_cut<<<sx, GB_SLAB_NBIN, 0, s>>>(ws.s_hist.as<int>() + GB_SLAB_NBIN,
+                                               ws.s_binpart.as<int>() + GB_SLAB_NBIN, sy);
+        k_slab_assign<<<grid, 256, 0, s>>>(B, ws.s_bw.as<int>(), ws.dc, ws.s_binpart.as<int>(), sy,
+                                           ws.s_part.as<int>(), ws.s_blocal.as<int>(), ws.s_pbcount.as<int>(),
+                                           ws.s_pbody.as<int>(), caps.bcap);
+        k_slab_classify<<<grid, 256, 0, s>>>(ws.s_gdesc.as<int4>(), ws.dc, ws.s_part.as<int>(), ws.s_gpart.as<int>(),
+                                             ws.s_prow.as<int>(), ws.s_pgrp.as<int>());
+        k_slab_demote<<<grid, 256, 0, s>>>(ws.dc, ws.s_prow.as<int>(), ws.s_pgrp.as<int>(), ws.s_pbcount.as<int>(),
+                                           caps.rcap, caps.gcap, caps.bcap, ws.s_gpart.as<int>());
+        count_launch(10);
+    }
     // colouring
     cudaMemsetAsync(ws.m_mask.p, 0, (size_t)(nb > 0 ? nb : 1) * 16, s);
     cudaMemsetAsync(ws.m_claim.p, 0x7f, (size_t)(nb > 0 ? nb : 1) * GB_MAX_COLOURS * 4, s);
     cudaMemsetAsync(&ws.dc->ncolours, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->nicolours, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->slab_rows, 0, 4, s);
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     {
         int blocks = coop_blocks((const void *)k_colour, 256, 2);
@@ -2277,8 +2383,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         int *claim = ws.m_claim.as<int>(), *colour = ws.m_colour.as<int>(), *tent = ws.m_tent.as<int>();
         const int2 *gbody = ws.grp_body.as<int2>();
         DevCounters *dc = ws.dc;
+        const int *cls = slab ? ws.s_gpart.as<int>() : nullptr;
         void *args[] = {(void *)&gbody, (void *)&dc, (void *)&mask, (void *)&claim, (void *)&colour, (void *)&tent,
-                        (void *)&nb};
+                        (void *)&nb, (void *)&cls};
         if (cudaLaunchCooperativeKernel((const void *)k_colour, blocks, 256, args, 0, s) != cudaSuccess) return false;
     }
     cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
@@ -2293,12 +2400,11 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.grp_body.as<int2>());
     // cut every (colour, block)'s slots into waves and pack their rows chunk by
     // chunk for the solver's blocks
-    const int pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
     const int ncb = GB_MAX_COLOURS * pgs_blocks;
+    const int chunk_cap = slab ? GB_SLAB_XCHUNK : GB_CHUNK_ROWS;
     // waves: one per (colour, block) at least, plus one per T slots and per
-    // GB_CHUNK_ROWS - 12 staged rows
-    const size_t ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
-    const size_t wave_cap = 2 * (size_t)ncb + ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (GB_CHUNK_ROWS - 12) + 16;
+    // chunk_cap - 12 staged rows
+    const size_t wave_cap = 2 * (size_t)ncb + ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (chunk_cap - 12) + 16;
     if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.wv_count.ensure((size_t)ncb * 4) &&
           ws.wv_base.ensure((size_t)ncb * 4 + 4) && ws.chunk_rows.ensure(wave_cap * 4) &&
           ws.chunk_start.ensure(wave_cap * 4) && ws.wv_col.ensure(wave_cap * 4) &&
@@ -2307,17 +2413,35 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     {
         const int g1 = (ncb + 127) / 128;
         k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
-                                        ws.wv_count.as<int>(), pgs_blocks);
+                                        ws.wv_count.as<int>(), pgs_blocks, chunk_cap);
         scan_exclusive(ws.wv_count.as<int>(), ws.wv_base.as<int>(), nullptr, ncb, nullptr, ws, s);
         k_wave_total<<<1, 1, 0, s>>>(ws.dc, ws.wv_count.as<int>(), ws.wv_base.as<int>(), pgs_blocks);
         k_wave_fill<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                        ws.wv_count.as<int>(), ws.wv_base.as<int>(), ws.wv_sched.as<int>(),
-                                       ws.chunk_rows.as<int>(), ws.wv_col.as<int>(), (int)wave_cap, pgs_blocks);
+                                       ws.chunk_rows.as<int>(), ws.wv_col.as<int>(), (int)wave_cap, pgs_blocks,
+                                       chunk_cap);
         scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), &ws.dc->nwaves, (int)wave_cap, nullptr, ws, s);
         k_pack_rows<<<grid, GB_PGS_THREADS, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                                     ws.wv_sched.as<int>(), ws.wv_col.as<int>(),
                                                     ws.chunk_start.as<int>(), ws.p_rows.as<float4>());
         count_launch(4);
+    }
+    if (slab) {
+        // interior groups part by part, colour by colour; their rows packed
+        const int npc = pgs_blocks * GB_SLAB_COLOURS;
+        int *pcstart = ws.s_pcstart.as<int>();
+        cudaMemsetAsync(ws.s_pccount.p, 0, (size_t)npc * 4, s);
+        cudaMemsetAsync(ws.s_pcfill.p, 0, (size_t)npc * 4, s);
+        k_slab_count<<<grid, 256, 0, s>>>(ws.dc, ws.s_gpart.as<int>(), ws.m_colour.as<int>(), ws.s_pccount.as<int>());
+        scan_exclusive(ws.s_pccount.as<int>(), pcstart, nullptr, npc, pcstart + npc, ws, s);
+        k_slab_fill<<<grid, 256, 0, s>>>(ws.dc, ws.s_gpart.as<int>(), ws.m_colour.as<int>(), ws.s_gdesc.as<int4>(),
+                                         pcstart, ws.s_pcfill.as<int>(), ws.s_ilist.as<int>(), ws.s_irown.as<int>());
+        scan_exclusive(ws.s_irown.as<int>(), ws.s_irowoff.as<int>(), pcstart + npc, (int)ngroups, nullptr, ws, s);
+        k_slab_pack<<<grid, 256, 0, s>>>(rows_view(ws), bodies_view(ws, nb), ws.s_gpart.as<int>(),
+                                         ws.s_gdesc.as<int4>(), ws.s_ilist.as<int>(), ws.s_irowoff.as<int>(),
+                                         ws.s_irown.as<int>(), pcstart, ws.s_blocal.as<int>(), npc,
+                                         ws.s_idesc.as<int4>(), ws.s_ipack.as<float4>(), ws.dc);
+        count_launch(3);
     }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
@@ -2362,8 +2486,28 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         }();
         if (per_sm < 1) return false;
         const int blocks = pgs_blocks;
-        void *args[] = {(void *)&A};
-        if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, threads, args, smem, s) != cudaSuccess) return false;
+        if (slab) {
+            SlabArgs SA;
+            SA.A = A;
+            SA.pcstart = ws.s_pcstart.as<int>();
+            SA.irowoff = ws.s_irowoff.as<int>();
+            SA.irown = ws.s_irown.as<int>();
+            SA.idesc = ws.s_idesc.as<int4>();
+            SA.ipack = ws.s_ipack.as<float4>();
+            SA.pbody = ws.s_pbody.as<int>();
+            SA.pbcount = ws.s_pbcount.as<int>();
+            SA.bcap = caps.bcap; SA.rcap = caps.rcap; SA.gcap = caps.gcap;
+            SA.chunk_cap = GB_SLAB_XCHUNK;
+            SA.ipasses = P.pgs_two_level;
+            void *args[] = {(void *)&SA};
+            if (cudaLaunchCooperativeKernel((const void *)k_pgs_slab, blocks, threads, args, caps.smem, s) !=
+                cudaSuccess)
+                return false;
+        } else {
+            void *args[] = {(void *)&A};
+            if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, threads, args, smem, s) != cudaSuccess)
+                return false;
+        }
     }
     if (ev1) cudaEventRecord(ev1, s);
     if (P.warm_mode) warm_store(ws, s);

@@ -57,7 +57,8 @@ class gbodeTuning(ctypes.Structure):
 class gbodeStepStats(ctypes.Structure):
     _fields_ = [("contacts", ctypes.c_int), ("rows", ctypes.c_int), ("colours", ctypes.c_int),
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
-                ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int)]
+                ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int),
+                ("interior_colours", ctypes.c_int), ("interior_rows", ctypes.c_int)]
 
 
 dNearCallback = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ID, ID)
@@ -157,6 +158,7 @@ _PROTOS = [
     ("gbodeWorldSetWarmStart", None, [ID, ctypes.c_int, dReal]),
     ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
+    ("gbodeWorldSetTwoLevelSweep", None, [ID, ctypes.c_int]), ("gbodeWorldGetTwoLevelSweep", ctypes.c_int, [ID]),
     ("gbodeSolveLCPBatch", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
