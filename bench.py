@@ -46,9 +46,11 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s at LCP residual \u22641e-4: plain GPU PGS vs learned warm start, 1 GB300"
 B_ROW = 132        # algorithmic bytes per PGS row-iteration
 B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
-# DRAM bytes per k_pgs launch on the settled 32,768-body pile, measured with ncu (mean of two
-# launches: 238.0 + 2.4 MB and 203.9 + 0.3 MB): the rows stay in L2 across sweeps
-PGS_TRAFFIC = 2.223e8
+# DRAM bytes (read + write) per launch of the sweep kernel on the settled 32,768-body pile,
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches):
+# k_pgs_slab (two-level sweep, kernel of commit e119748): 77.7 and 76.3 MB;
+# k_pgs (one-level): 240.4 and 204.2 MB.  The rows stay in L2 / shared memory across sweeps.
+PGS_TRAFFIC = {"gb::k_pgs_slab": 7.703e7, "gb::k_pgs": 2.223e8}
 
 
 def parse():
@@ -77,7 +79,7 @@ def parse():
     ap.add_argument("--save-settled", default=None, help="write the settled state (.npz) and exit")
     ap.add_argument("--pgs-blocks", type=int, default=0, help="thread blocks of the PGS kernel (0: one per SM)")
     ap.add_argument("--passes", type=int, default=1, help="passes over a manifold's rows per visit")
-    ap.add_argument("--two-level", type=int, default=0,
+    ap.add_argument("--two-level", type=int, default=2,
                     help="two-level sweep of the pile's solver with this many interior phases a sweep "
                          "(gbodeWorldSetTwoLevelSweep; 0: off)")
     ap.add_argument("--from-settled", action="store_true",
@@ -349,9 +351,13 @@ def run_gbode(args, ws, rank, local):
     # FP64 residual of the last step's solution, evaluated on the device
     r64, ce, ml = w.last_residual()
     fp64_rel = r64 / max(1.0, ml)
-    # roofline of the dominant kernel (the persistent PGS sweep kernel)
+    # roofline of the dominant kernel (the persistent PGS sweep kernel): every
+    # row relaxation counts B_ROW, the interior rows of the two-level sweep once
+    # per interior phase
     checks = [int(np.ceil(s / args.check_every)) for s in sweeps]
-    pgs_bytes = sum(s * m * B_ROW + c * m * B_ROW_CHECK for s, m, c in zip(sweeps, rows, checks))
+    extra = max(0, args.two_level - 1)
+    pgs_bytes = sum(s * (m + extra * mi) * B_ROW + c * m * B_ROW_CHECK
+                    for s, m, mi, c in zip(sweeps, rows, T["interior_rows"], checks))
     pgs_s = sum(solve_ms) / 1e3
     achieved = pgs_bytes / pgs_s / 1e9 if pgs_s > 0 else 0.0
     # e2e through the C ABI with host buffers
@@ -414,10 +420,12 @@ def run_gbode(args, ws, rank, local):
                                     "relative to max(1, max|lambda|) of the step's own solution",
                    "contact_rows_per_s": float(np.sum(rows)) / (total_ms / 1e3),
                    "solve_share": pgs_s * 1e3 / total_ms},
-        "roofline": {"bound": "hbm", "kernel": "gb::k_pgs", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": PGS_TRAFFIC,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean of two k_pgs "
-                                       "launches from the settled pile",
+        "roofline": {"bound": "hbm", "kernel": "gb::k_pgs_slab" if args.two_level else "gb::k_pgs",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": PGS_TRAFFIC["gb::k_pgs_slab" if args.two_level else "gb::k_pgs"],
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches "
+                                       "of the same kernel from the settled pile",
                      "algorithmic_bytes_per_launch": pgs_bytes / args.steps},
         "clocks": clk,
         "gpu_launches": launches,
