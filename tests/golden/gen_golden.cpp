@@ -167,6 +167,10 @@ static void contact_lambda(const dContact &c, bool reversed, const dJointFeedbac
     lam[2] = (float)dCalcVectorDot3(fb.f1, t2);
 }
 
+// dyn 0: the dynamic iteration rule off; 1: on at the reference's defaults;
+// 2: on with the parameters in g_dynp (premature exit delta, extra factor,
+// extra iteration delta), read by the step mode
+static dReal g_dynp[3] = {0, 0, 0};
 static void apply_params(dWorldID w, const WorldParams &P, int iters, int dyn) {
     dWorldSetGravity(w, P.g[0], P.g[1], P.g[2]);
     dWorldSetERP(w, P.erp);
@@ -178,6 +182,8 @@ static void apply_params(dWorldID w, const WorldParams &P, int iters, int dyn) {
     if (!dyn) {
         dReal zero = 0;
         dWorldSetQuickStepDynamicIterationParameters(w, &zero, &zero, NULL);
+    } else if (dyn == 2) {
+        dWorldSetQuickStepDynamicIterationParameters(w, &g_dynp[0], &g_dynp[1], &g_dynp[2]);
     }
 }
 
@@ -185,6 +191,11 @@ static void apply_params(dWorldID w, const WorldParams &P, int iters, int dyn) {
 static void mode_step() {
     int nb = rdi(), nc = rdi(), iters = rdi(), dyn = rdi(), stepper = rdi();
     WorldParams P; rd((float *)&P, sizeof(P) / sizeof(float));
+    if (dyn == 2) {
+        float d3[3];
+        rd(d3, 3);
+        for (int i = 0; i < 3; i++) g_dynp[i] = d3[i];
+    }
     std::vector<float> bodies(BODY_IN * nb);
     rd(bodies.data(), bodies.size());
     std::vector<int> cb(2 * nc), cmode(nc);

@@ -262,11 +262,12 @@ def bodies_from_state(state, sc: scenes.Scene):
     return b
 
 
-def run_step(exe, sc, bodies, cb, cs, iters, dyn, stepper, messages=None):
+def run_step(exe, sc, bodies, cb, cs, iters, dyn, stepper, messages=None, dynp=None):
     nb, nc = bodies.shape[0], cb.shape[0]
     hdr = np.array([nb, nc, iters, dyn, stepper], np.int32)
     mode = np.full(nc, sc.surface_mode, np.int32)
-    r = Reader(run(exe, "step", [hdr, sc.world_params(), bodies, cb.astype(np.int32), mode, cs], messages))
+    extra = [np.asarray(dynp, np.float32)] if dyn == 2 else []
+    r = Reader(run(exe, "step", [hdr, sc.world_params(), *extra, bodies, cb.astype(np.int32), mode, cs], messages))
     ok = int(r.take(np.int32, 1)[0])
     lam = r.take(np.float32, 3 * nc).reshape(nc, 3)
     raw = r.take(np.float32, 12 * nc).reshape(nc, 12)
@@ -308,6 +309,50 @@ def gen_steps(exes):
             print(f"{name} step {s['step']}: {len(s['cb'])} contacts, replay drift {drift:.2e}, "
                   f"max|lambda| {np.abs(lam).max() if len(lam) else 0:.3g}")
         np.savez_compressed(os.path.join(HERE, f"step_{name}.npz"), **out)
+
+
+# two more sets of dynamic iteration parameters (premature exit delta, extra
+# factor, extra iteration delta): under the first the solves stop early
+# (the box stack after 11 of 20 sweeps), under the second between the regular
+# count and twice it (the pile after 47 of 30 + 30)
+DYN_SETS = (("dyn2", (30.0, 1.0, 1e9)), ("dyn3", (100.0, 1.0, 1000.0)))
+
+
+def gen_steps_dyn(exes):
+    """The step goldens' snapshots stepped once more by the no-reorder
+    reference with its dynamic iteration rule on (quickstep.cpp:1823-1856,
+    :3253-3285): at the defaults (premature exit below 1e-8, up to
+    `iterations` extra sweeps while an adjustment is >= 1e-2) into
+    s{k}_lambda_dyn / s{k}_post_dyn, and with each of DYN_SETS into
+    s{k}_lambda_<tag> / s{k}_post_<tag>.  The rule only decides when the sweeps
+    stop, so its multipliers equal, to the bit, those of a fixed count of
+    sweeps; that count (per contact, the smallest fixed count giving its three
+    multipliers; the maximum over contacts is the largest island's) is
+    s{k}_sweeps_<tag>.  Adds keys to the existing step_*.npz files."""
+    for name in ("box_stack", "pile256", "capsule_pile96"):
+        path = os.path.join(HERE, f"step_{name}.npz")
+        g = dict(np.load(path))
+        sc = {"box_stack": scenes.box_stack(seed=0), "pile256": scenes.pile(256, seed=3),
+              "capsule_pile96": scenes.capsule_pile(96, seed=2)}[name]
+        iters = int(g["ints"][0])
+        for k in range(len(g["snaps"])):
+            bodies = bodies_from_state(g[f"s{k}_pre"], sc)
+            cb, cs = g[f"s{k}_cb"], g[f"s{k}_cs"]
+            fixed = [run_step(exes["single_noreorder"], sc, bodies, cb, cs, n, 0, 0)[0]
+                     for n in range(1, 2 * iters + 2)]
+            for dyn, tag, dynp in ((1, "dyn", None),) + tuple((2, t, p) for t, p in DYN_SETS):
+                lam, _, post = run_step(exes["single_noreorder"], sc, bodies, cb, cs, iters, dyn, 0, dynp=dynp)
+                sweeps = np.zeros(len(cb), np.int32)
+                for n, ln in enumerate(fixed, start=1):
+                    hit = (sweeps == 0) & np.all(ln == lam, axis=1)
+                    sweeps[hit] = n
+                assert np.all(sweeps > 0), (name, k, tag)
+                g[f"s{k}_lambda_{tag}"], g[f"s{k}_post_{tag}"], g[f"s{k}_sweeps_{tag}"] = lam, post, sweeps
+                print(f"{name} snapshot {k} ({tag}): stopped after {sweeps.max()} sweeps "
+                      f"(fixed count {iters}); max|lambda| {np.abs(lam).max():.3g}")
+        for t, p in DYN_SETS:
+            g[f"{t}_params"] = np.array(p, np.float32)
+        np.savez_compressed(path, **g)
 
 
 def gen_space_pile(exes):
@@ -488,6 +533,8 @@ def main():
         gen_chain_step(exes)
     if a.only in ("", "dantzig32"):
         gen_step_dantzig32(exes)
+    if a.only in ("", "steps_dyn"):
+        gen_steps_dyn(exes)
 
 
 if __name__ == "__main__":

@@ -59,6 +59,49 @@ def test_reference_order_lambda_parity(gblib, golden, name):
         w.close()
 
 
+@pytest.mark.parametrize("name", ["box_stack", "pile256", "capsule_pile96"])
+def test_reference_order_dynamic_iterations(gblib, golden, name):
+    """The reference's dynamic iteration rule (quickstep.cpp:1823-1856,
+    :3253-3285) in the reference-order solver (k_islands), rows not
+    reordered, on every step snapshot under three parameter sets: the
+    defaults (every solve runs its extra sweeps), and two under which solves
+    exit early (the box stack after 4-14 of 20 sweeps) or stop between the
+    regular and the doubled count (the 256-body pile after 47 of 30 + 30).
+    lambda within 1e-3 of max(1, max|lambda|) of the reference, positions
+    within 1e-4 m, and the sweeps performed (the largest island's) equal to the
+    reference's (tests/golden/make_golden.py gen_steps_dyn: the fixed sweep
+    count whose multipliers equal the dynamic solve's to the bit)."""
+    import ctypes
+    from ode_gb300 import ode, sim
+    g = golden(f"step_{name}.npz")
+    mode = int(g["ints"][2])
+    report = []
+    for tag in ("dyn", "dyn2", "dyn3"):
+        worst, sweeps = 0.0, []
+        for k in range(len(g["snaps"])):
+            pre, cb, cs = g[f"s{k}_pre"], g[f"s{k}_cb"], g[f"s{k}_cs"]
+            w = sim.GBWorld(snapshot_scene(g, pre, name), solver=ode.GBODE_SOLVER_REFERENCE_ORDER, dyn=True)
+            if tag != "dyn":
+                pe, mf, ed = (ctypes.c_float(float(x)) for x in g[f"{tag}_params"])
+                w.L.dWorldSetQuickStepDynamicIterationParameters(w.w, ctypes.byref(pe), ctypes.byref(mf),
+                                                                 ctypes.byref(ed))
+            assert sim.step_contacts(w, cb, cs, mode) == 1
+            w.sync()
+            lam = contact_lambdas(w.last_rows(), len(cb))
+            ref = g[f"s{k}_lambda_{tag}"]
+            d = float(np.abs(lam - ref).max()) / max(1.0, float(np.abs(ref).max()))
+            worst = max(worst, d)
+            assert d <= LAMBDA_RTOL, (tag, k, d)
+            assert np.abs(w.state()[:, 0:3] - g[f"s{k}_post_{tag}"][:, 0:3]).max() <= POS_ATOL
+            ref_sweeps = int(g[f"s{k}_sweeps_{tag}"].max())
+            sweeps.append((w.stats().iterations, ref_sweeps))
+            assert w.stats().iterations == ref_sweeps, (tag, k, w.stats().iterations, ref_sweeps)
+            w.L.dJointGroupEmpty(w.group)
+            w.close()
+        report.append(f"{tag}: sweeps (device, reference) {sweeps}, lambda within {worst:.1e}")
+    print(f"{name}: " + "; ".join(report))
+
+
 @pytest.mark.parametrize("name", ["box_stack", "pile256"])
 def test_reference_order_matches_oracle_bitwise(gblib, port, golden, name):
     """The device relaxes rows in the reference's order with the reference's

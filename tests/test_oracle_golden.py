@@ -139,3 +139,34 @@ def test_hash_space_settled_pile(port, golden):
     ng = len(g["cls"])
     pairs = port.hash_pairs(g["cls"], g["body"], g["pos"], g["R"], g["dims"], np.arange(ng)[::-1].copy())
     assert {tuple(sorted(p)) for p in pairs.tolist()} == {tuple(p) for p in g["pairs"].tolist()}
+
+
+DYN_TAGS = ("dyn", "dyn2", "dyn3")
+
+
+@pytest.mark.parametrize("name", ["box_stack", "pile256", "capsule_pile96"])
+def test_dynamic_iterations_follow_reference(port, golden, name):
+    """The reference's dynamic iteration rule (quickstep.cpp:1823-1856,
+    :3253-3285) with row reordering off, on every step snapshot: at the
+    default parameters (s{k}_*_dyn: every solve runs its extra sweeps) and at
+    two sets under which solves exit early or stop between the regular and the
+    doubled count (s{k}_*_dyn2 / dyn3, parameters in dyn2_params /
+    dyn3_params).  The oracle's post-step state equals the reference's to the
+    bit; its multipliers match the ones recovered from the reference's
+    feedback forces to 1e-6 of max|lambda|."""
+    g = golden(f"step_{name}.npz")
+    iters, _, mode, _ = [int(x) for x in g["ints"]]
+    for k in range(len(g["snaps"])):
+        pre, cb, cs = g[f"s{k}_pre"], g[f"s{k}_cb"], g[f"s{k}_cs"]
+        bodies = g["bodies0"].copy()
+        bodies[:, 0:3], bodies[:, 3:7] = pre[:, 0:3], pre[:, 3:7]
+        bodies[:, 7:10], bodies[:, 10:13] = pre[:, 19:22], pre[:, 22:25]
+        for tag in DYN_TAGS:
+            w = port.world(bodies, g["params"], iters, dyn=1, reorder=0)
+            if tag != "dyn":
+                pe, mf, ed = (float(x) for x in g[f"{tag}_params"])
+                w.set_dyn(pe, mf, ed)
+            lam = w.quickstep(cb, np.full(len(cb), mode, np.int32), cs)
+            ref = g[f"s{k}_lambda_{tag}"]
+            assert np.abs(lam - ref).max() / max(1.0, float(np.abs(ref).max())) < 1e-6, (name, k, tag)
+            np.testing.assert_array_equal(w.state(), g[f"s{k}_post_{tag}"], err_msg=f"{name} s{k} {tag}")
