@@ -533,6 +533,37 @@ const char *gbodeGetLastError(void);
 /* Number of kernel launches the library has issued since load. */
 long long gbodeKernelLaunchCount(void);
 
+/* Fault injection for error-path tests (no counterpart in the reference).
+ * Process-wide, host-side; nothing is made to fault:
+ *   GBODE_TEST_BARRIER   value != 0: the next solver launch's grid-barrier
+ *                        counter starts one arrival short, so its bounded
+ *                        wait runs out (a second or two): the kernel returns
+ *                        and gbodeWorldSynchronize reports ERR bit 0x1
+ *   GBODE_TEST_STAGE     value != 0: the next solver launch's first staging
+ *                        wait names a copy that is never issued (bounded):
+ *                        ERR bit 0x100 (and 0x1 from blocks left waiting)
+ *   GBODE_TEST_ALLOC     after `value` more device allocations succeed, the
+ *                        next `count` fail as cudaMalloc would
+ *   GBODE_TEST_CONTACT_CAP, GBODE_TEST_ROW_CAP, GBODE_TEST_COLOUR_CAP
+ *                        capacities the kernels see, below what is allocated
+ *                        (0: off): contacts of the narrow phase, contact rows
+ *                        of the assembly (worlds without ball/hinge joints),
+ *                        colours of the colouring; the kernels clamp and set
+ *                        ERR bits 0x4 / 0x8 / 0x10
+ *   GBODE_TEST_ALLOC_PENDING  returns 1 while an injected allocation
+ *                        failure has not happened yet, else 0
+ *   GBODE_TEST_OFF       clears everything
+ * Returns 1, or 0 for an unknown kind. */
+#define GBODE_TEST_OFF 0
+#define GBODE_TEST_BARRIER 1
+#define GBODE_TEST_STAGE 2
+#define GBODE_TEST_ALLOC 3
+#define GBODE_TEST_CONTACT_CAP 4
+#define GBODE_TEST_ROW_CAP 5
+#define GBODE_TEST_COLOUR_CAP 6
+#define GBODE_TEST_ALLOC_PENDING 7
+int gbodeTestInject(int kind, int value, int count);
+
 /* Bulk state access for batched drivers: [nb][25] pos q R lvel avel in body
  * creation order (index = order of dBodyCreate among live bodies). */
 int gbodeWorldGetBodyCount(dWorldID w);

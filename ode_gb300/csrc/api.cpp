@@ -37,14 +37,30 @@ int num_sms() {
     }
     return n;
 }
+TestFaults g_test;
+
+// an injected allocation failure (gbodeTestInject), as cudaMalloc failing
+static bool injected_alloc_failure() {
+    if (g_test.alloc_skip < 0) return false;
+    if (g_test.alloc_skip > 0) { --g_test.alloc_skip; return false; }
+    if (--g_test.alloc_fail <= 0) g_test.alloc_skip = -1;
+    return true;
+}
+
+// The new block is allocated before the old one is released: a failed grow
+// leaves the buffer (and its contents) as it was.
 bool DBuf::ensure(size_t want) {
     if (want <= bytes && p) return true;
     size_t nb = bytes ? bytes : 256;
     while (nb < want) nb = nb + nb / 2 + 256;
+    if (injected_alloc_failure()) return false;
+    void *np = nullptr;
+    if (cudaMalloc(&np, nb) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
     if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    if (cudaMalloc(&p, nb) != cudaSuccess) { p = nullptr; return false; }
+    p = np;
     bytes = nb;
     return true;
 }
@@ -544,6 +560,23 @@ void dCloseODE(void) {}
 
 const char *gbodeGetLastError(void) { return g_err.c_str(); }
 long long gbodeKernelLaunchCount(void) { return g_launches.load(); }
+
+int gbodeTestInject(int kind, int value, int count) {
+    switch (kind) {
+    case GBODE_TEST_OFF: g_test = TestFaults(); return 1;
+    case GBODE_TEST_BARRIER: g_test.barrier = value != 0; return 1;
+    case GBODE_TEST_STAGE: g_test.stage = value != 0; return 1;
+    case GBODE_TEST_ALLOC:
+        g_test.alloc_skip = count > 0 && value >= 0 ? value : -1;
+        g_test.alloc_fail = count > 0 ? count : 0;
+        return 1;
+    case GBODE_TEST_CONTACT_CAP: g_test.contact_cap = value > 0 ? value : 0; return 1;
+    case GBODE_TEST_ROW_CAP: g_test.row_cap = value > 0 ? value : 0; return 1;
+    case GBODE_TEST_COLOUR_CAP: g_test.colour_cap = value > 0 ? value : 0; return 1;
+    case GBODE_TEST_ALLOC_PENDING: return g_test.alloc_skip >= 0 ? 1 : 0;
+    default: set_error("gbodeTestInject: unknown kind"); return 0;
+    }
+}
 
 // misc.cpp:35-135 dRand / dRandInt
 static uint32_t g_seed = 0;
@@ -1975,10 +2008,10 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     if (!w->device_contacts) {
         if (!upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
     } else if (ws.contact_cap <= 0) {
-        ws.contacts.ensure(sizeof(Contact));
+        if (!ws.contacts.ensure(sizeof(Contact))) { set_error("device allocation (contacts)"); return 0; }
         ws.contact_cap = 1;
     }
-    if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
+    if (!ws.surfaces.p && !ws.surfaces.ensure(sizeof(Surface))) { set_error("device allocation (surfaces)"); return 0; }
     // the contact joints whose index the rows carry (feedback below)
     std::vector<dxJoint *> awake_js;
     const std::vector<dxJoint *> *solved = &js;
@@ -2125,10 +2158,10 @@ int dWorldStep(dWorldID w, dReal stepsize) {
     if (!upload_joint_table(w)) { set_error("dWorldStep: joint table upload"); return 0; }
     if (!dev && !upload_host_contacts(w, js)) { set_error("upload contacts"); return 0; }
     if (dev && ws.contact_cap <= 0) {
-        ws.contacts.ensure(sizeof(Contact));
+        if (!ws.contacts.ensure(sizeof(Contact))) { set_error("device allocation (contacts)"); return 0; }
         ws.contact_cap = 1;
     }
-    if (!ws.surfaces.p) ws.surfaces.ensure(sizeof(Surface));
+    if (!ws.surfaces.p && !ws.surfaces.ensure(sizeof(Surface))) { set_error("device allocation (surfaces)"); return 0; }
     const int nb = (int)w->bodies.size();
     std::vector<dxJoint *> awake_js;
     const std::vector<dxJoint *> *solved = &js;

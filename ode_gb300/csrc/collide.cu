@@ -486,9 +486,11 @@ bool launch_narrowphase(Workspace &ws, int maxc, int surf, bool append, cudaStre
         cudaStreamSynchronize(s);
         base = nc;
     }
+    // the capacity the compaction sees (lowered only by the error-path tests)
+    const int cap = g_test.contact_cap > 0 && g_test.contact_cap < ws.contact_cap ? g_test.contact_cap : ws.contact_cap;
     k_compact<<<grid, 128, 0, s>>>(&ws.dc->npairs, ws.c_count.as<int>(), ws.c_start.as<int>(), ws.c_slots.as<Contact>(),
-                                   ws.contacts.as<Contact>(), base, ws.dc, ws.contact_cap);
-    k_contacts_total<<<1, 1, 0, s>>>(ws.dc, base, ws.contact_cap);
+                                   ws.contacts.as<Contact>(), base, ws.dc, cap);
+    k_contacts_total<<<1, 1, 0, s>>>(ws.dc, base, cap);
     count_launch(3);
     return cudaGetLastError() == cudaSuccess;
 }

@@ -147,6 +147,23 @@ struct Workspace {
     void release();
 };
 
+// ---- fault injection for the error-path tests (gbodeTestInject; host-side
+// state, consumed by the next launch it applies to).  Nothing faults: a
+// barrier counter starts one arrival short or a staging wait names a copy
+// that is never issued (bounded waits run out and report), allocations fail
+// as cudaMalloc failing would, and capacities the kernels see are lowered
+// below what is allocated (the kernels clamp and report).
+struct TestFaults {
+    int barrier = 0;      // next solver launch: grid barrier counter one arrival short
+    int stage = 0;        // next solver launch: its first staging wait names a copy never issued
+    int alloc_skip = -1;  // device allocations that still succeed (-1: injection off)
+    int alloc_fail = 0;   // then this many fail
+    int contact_cap = 0;  // contact capacity the narrow phase sees (0: the allocated one)
+    int row_cap = 0;      // row capacity the contact assembly sees (0: the allocated one; worlds without joints)
+    int colour_cap = 0;   // colours the colouring may use (0: all)
+};
+extern TestFaults g_test;
+
 // ---- scan (scan.cu): exclusive prefix sum of n ints (n read from *n_dev if
 // non-null, else n_host), writing the total to *total_dev.
 void scan_exclusive(const int *in, int *out, const int *n_dev, int n_cap, int *total_dev, Workspace &ws,

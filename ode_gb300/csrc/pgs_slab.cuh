@@ -323,7 +323,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
         s_wbase[GB_MAX_COLOURS];
     __shared__ int s_icol[GB_SLAB_COLOURS + 1];
     __shared__ int s_nic, s_g0, s_ng, s_row0, s_nrows, s_nb;
-    __shared__ unsigned long long s_mbar[3];
+    __shared__ unsigned long long s_mbar[4];  // two cross buffers, the interior rows, [3] never armed (poison_stage)
+    __shared__ int s_abort;                   // a staging wait of this block ran out
     __shared__ float s_lam[GB_PGS_THREADS * 13];
     extern __shared__ float4 pgs_smem[];
     float4 *xbuf = pgs_smem;                                         // 2 x chunk_cap x 8
@@ -350,6 +351,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
         mbar_init(&s_mbar[0]);
         mbar_init(&s_mbar[1]);
         mbar_init(&s_mbar[2]);
+        mbar_init(&s_mbar[3]);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         const int g0 = S.pcstart[part * GB_SLAB_COLOURS], g1 = S.pcstart[(part + 1) * GB_SLAB_COLOURS];
         s_g0 = g0;
@@ -567,13 +570,15 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
             } else if (has_next) {
                 if (!staged) {
                     relax_desc(A, next);
-                } else {
-                    if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
+                } else if (A.poison_stage ? mbar_wait(&s_mbar[3], 0, &dc->err, 16)
+                                          : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
                     const float4 *buf = xbuf + (q & 1) * (S.chunk_cap * 8);
                     if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
                     else relax_plain(A, next, buf, my_lam, lout);
                     nout = desc_rows(next);
                     xout = next.x;
+                } else {
+                    s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
             const bool sweep_end = last_wave && nxt.c < 0;
@@ -583,6 +588,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
                     if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 fetch(nnx);
                 __syncthreads();
+                if (s_abort) { drain(); return; }
             } else {
                 const bool check_next = check_this && sweep_end;
                 if (check_next) {
@@ -599,7 +605,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
                         if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 }
                 fetch(nnx);
-                if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
+                if (!grid_wait(&dc->gsync, &dc->err, gen, target) || s_abort) { drain(); return; }
             }
             if (threadIdx.x == 0) retire();
             ++q;

@@ -73,11 +73,36 @@ __global__ void k_scan_add(int *out, const int *n_dev, int n_host, const int *bl
     if (i < n) out[i] += block_sums[blockIdx.x];
 }
 
+// One block, no scratch: the same exclusive scan in SCAN_BLOCK-element
+// tiles with a carry (used when the scratch of the fast path cannot grow).
+__global__ void k_scan_single(const int *in, int *out, const int *n_dev, int n_host, int *total_dev) {
+    const int n = n_dev ? *n_dev : n_host;
+    __shared__ int carry_s;
+    __shared__ int tot;
+    if (threadIdx.x == 0) carry_s = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += SCAN_BLOCK) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? in[i] : 0;
+        const int e = block_excl_scan(v, &tot);
+        const int carry = carry_s;
+        if (i < n) out[i] = e + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry_s = carry + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total_dev) *total_dev = carry_s;
+}
+
 void scan_exclusive(const int *in, int *out, const int *n_dev, int n_cap, int *total_dev, Workspace &ws,
                     cudaStream_t s) {
     int nblocks = (n_cap + SCAN_BLOCK - 1) / SCAN_BLOCK;
     if (nblocks < 1) nblocks = 1;
-    ws.scan_tmp.ensure(sizeof(int) * (size_t)(nblocks + 1));
+    if (!ws.scan_tmp.ensure(sizeof(int) * (size_t)(nblocks + 1))) {
+        k_scan_single<<<1, SCAN_BLOCK, 0, s>>>(in, out, n_dev, n_cap, total_dev);
+        count_launch();
+        return;
+    }
     int *sums = ws.scan_tmp.as<int>();
     k_scan_blocks<<<nblocks, SCAN_BLOCK, 0, s>>>(in, out, n_dev, n_cap, sums);
     k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(sums, n_dev, n_cap, total_dev);

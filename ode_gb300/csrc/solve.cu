@@ -156,8 +156,21 @@ __global__ void k_contact_m(const Contact *C, const Surface *S, const int *nc_de
     }
 }
 
-__global__ void k_rows_total(DevCounters *dc, int row_cap) {
-    if (dc->nrows > row_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); dc->nrows = row_cap; }
+// Rows over the capacity: the step keeps the first contacts whose rows fit
+// (the solver's contact count is lowered with them), so every later stage
+// sees one consistent, smaller problem, and ERR_ROW_OVERFLOW is reported.
+__global__ void k_rows_total(DevCounters *dc, int row_cap, const int *rstart, const int *mcount, int *nc_dev) {
+    if (dc->nrows > row_cap) {
+        atomicOr(&dc->err, ERR_ROW_OVERFLOW);
+        int lo = 0, hi = *nc_dev;  // the most leading contacts whose rows end within the capacity
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (rstart[mid - 1] + mcount[mid - 1] <= row_cap) lo = mid;
+            else hi = mid - 1;
+        }
+        *nc_dev = lo;
+        dc->nrows = lo > 0 ? rstart[lo - 1] + mcount[lo - 1] : 0;
+    }
     dc->step_contacts = dc->ncontacts;
 }
 
@@ -908,7 +921,7 @@ __global__ void k_groups_total(DevCounters *dc, int nj) {
 // second.  Interior groups of different parts share no body, so one colouring
 // serves every part.
 __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long *mask, int *claim, int *colour,
-                         int *tent, int nb, const int *cls) {
+                         int *tent, int nb, const int *cls, int climit) {
     unsigned gen = 0;
     const int nm = dc->nmanifolds;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -926,14 +939,21 @@ __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long 
             if (n1 >= 0) { m1 = __ldcg(&mask[2 * n1]); m1b = __ldcg(&mask[2 * n1 + 1]); }
             unsigned long long lo = m0 | m1, hi = m0b | m1b;
             int c;
+            // climit: the colours a class may use (GB_MAX_COLOURS, or 64 a
+            // class; lower only in the error-path tests).  Past it the last
+            // colour is reused and ERR_COLOUR_OVERFLOW reported.
             if (cls) {
                 const bool in = cls[e] >= 0;
                 const unsigned long long used = in ? hi : lo;
-                if (~used) c = (in ? 64 : 0) + __ffsll(~used) - 1;
-                else { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); c = in ? GB_MAX_COLOURS - 1 : 63; }
-            } else if (~lo) c = __ffsll(~lo) - 1;
-            else if (~hi) c = 64 + __ffsll(~hi) - 1;
-            else { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); c = GB_MAX_COLOURS - 1; }
+                const int lim = climit < 64 ? climit : 64;
+                int k = ~used ? __ffsll(~used) - 1 : 64;
+                if (k >= lim) { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); k = lim - 1; }
+                c = (in ? 64 : 0) + k;
+            } else {
+                int k = ~lo ? __ffsll(~lo) - 1 : (~hi ? 64 + __ffsll(~hi) - 1 : GB_MAX_COLOURS);
+                if (k >= climit) { atomicOr(&dc->err, ERR_COLOUR_OVERFLOW); k = climit - 1; }
+                c = k;
+            }
             tent[e] = c;
             atomicMin(&claim[n0 * GB_MAX_COLOURS + c], e);
             if (n1 >= 0) atomicMin(&claim[n1 * GB_MAX_COLOURS + c], e);
@@ -1058,6 +1078,7 @@ struct PgsArgs {
     int learned;      // lambda holds the learned start, lam_alt the plain one: keep the better
     float *lam_alt;
     int passes;       // passes over a manifold's rows each time it is relaxed (>= 1)
+    int poison_stage; // error-path tests: the staging waits name a copy that is never issued
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -1356,11 +1377,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                  "l"(src), "r"(bytes), "r"(smem_u32(m))
                  : "memory");
 }
-// bounded wait for a phase of an mbarrier
-__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, unsigned *err) {
+// bounded wait for a phase of an mbarrier (at most 2^limit_log2 tries)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, unsigned *err, int limit_log2 = 22) {
     long long tries = 0;
     while (!mbar_try_wait(m, parity)) {
-        if (++tries > (1ll << 22)) {
+        if (++tries > (1ll << limit_log2)) {
             atomicOr(err, ERR_STAGE_TIMEOUT);
             return false;
         }
@@ -1503,7 +1524,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
     DevCounters *dc = A.dc;
     __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS], s_wcount[GB_MAX_COLOURS], s_wbase[GB_MAX_COLOURS];
-    __shared__ unsigned long long s_mbar[2];
+    __shared__ unsigned long long s_mbar[3];  // two chunk buffers; [2] is never armed (poison_stage)
+    __shared__ int s_abort;                   // a staging wait of this block ran out
     __shared__ float s_lam[GB_PGS_THREADS * 13];  // per thread: the next manifold's multipliers
     extern __shared__ float4 pgs_smem[];  // two buffers of GB_CHUNK_ROWS rows
     const int ncol = dc->ncolours;
@@ -1517,6 +1539,8 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     if (threadIdx.x == 0) {
         mbar_init(&s_mbar[0]);
         mbar_init(&s_mbar[1]);
+        mbar_init(&s_mbar[2]);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -1679,13 +1703,15 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
             if (has_next) {
                 if (!staged) {
                     relax_desc(A, next);
-                } else {
-                    if (!mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) { drain(); return; }
+                } else if (A.poison_stage ? mbar_wait(&s_mbar[2], 0, &dc->err, 16)
+                                          : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
                     const float4 *buf = pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8);
                     if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
                     else relax_plain(A, next, buf, my_lam, lout);
                     nout = desc_rows(next);
                     xout = next.x;
+                } else {
+                    s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
             const bool sweep_end = last_wave && cur.c == ncol - 1;
@@ -1697,6 +1723,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                     if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 fetch(nnx);
                 __syncthreads();
+                if (s_abort) { drain(); return; }
             } else {
                 // arrive (the accumulators fc are out), then store the staged
                 // slot's multipliers -- read again only by this thread a sweep
@@ -1720,7 +1747,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                         if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 }
                 fetch(nnx);
-                if (!grid_wait(&dc->gsync, &dc->err, gen, target)) { drain(); return; }
+                if (!grid_wait(&dc->gsync, &dc->err, gen, target) || s_abort) { drain(); return; }
             }
             // the copy for this step has completed before its buffer's mbarrier
             // is armed again (threads with no staged slot never waited)
@@ -2179,9 +2206,9 @@ static bool ensure_warm(Workspace &ws) {
     unsigned want = 1024;
     while (want < 2u * (unsigned)(ws.contact_cap > 0 ? ws.contact_cap : 1) && want < (1u << 23)) want <<= 1;
     if (ws.warm_mask + 1 != want) {
+        ws.warm_valid = false;  // a grown table holds no previous step, whether or not both grow
         if (!(ws.w_keys.ensure((size_t)2 * want * 8) && ws.w_lambda.ensure((size_t)2 * want * 16))) return false;
         ws.warm_mask = want - 1;
-        ws.warm_valid = false;
     }
     return true;
 }
@@ -2215,11 +2242,83 @@ static void warm_store(Workspace &ws, cudaStream_t s) {
     ws.warm_valid = true;
 }
 
-static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s) {
-    Bodies B = bodies_view(ws, nb);
+// Sizes of the coloured solver's per-step buffers (host-known: capacities,
+// joints, blocks, the two-level sweep's partition).
+struct ColouredPlan {
+    int pgs_blocks, sx, sy, chunk_cap, ncb;
+    bool slab;
+    SlabCaps caps;
+    size_t ngroups, wave_cap;
+};
+static ColouredPlan plan_coloured(const Workspace &ws, const SolverParams &P) {
+    ColouredPlan c;
+    c.pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
+    c.caps = slab_caps();
+    c.slab = P.pgs_two_level && c.pgs_blocks >= 2 && c.caps.rcap > 0;
+    c.ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
+    c.sx = 1;
+    if (c.slab)
+        for (int d = 1; d * d <= c.pgs_blocks; d++)
+            if (c.pgs_blocks % d == 0) c.sx = d;
+    c.sy = c.pgs_blocks / c.sx;
+    c.ncb = GB_MAX_COLOURS * c.pgs_blocks;
+    c.chunk_cap = c.slab ? GB_SLAB_XCHUNK : GB_CHUNK_ROWS;
+    // waves: one per (colour, block) at least, plus one per T slots and per chunk_cap - 12 staged rows
+    c.wave_cap = 2 * (size_t)c.ncb + c.ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (c.chunk_cap - 12) + 16;
+    return c;
+}
+
+static bool ensure_coloured(Workspace &ws, int nb, const ColouredPlan &c) {
+    if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.wv_count.ensure((size_t)c.ncb * 4) &&
+          ws.wv_base.ensure((size_t)c.ncb * 4 + 4) && ws.chunk_rows.ensure(c.wave_cap * 4) &&
+          ws.chunk_start.ensure(c.wave_cap * 4) && ws.wv_col.ensure(c.wave_cap * 4) &&
+          ws.wv_sched.ensure(c.wave_cap * GB_PGS_THREADS * 4)))
+        return false;
+    if (!c.slab) return true;
+    const size_t nbb = nb > 0 ? nb : 1, npc = (size_t)c.pgs_blocks * GB_SLAB_COLOURS;
+    const size_t nh = (size_t)GB_SLAB_NBIN * (1 + c.sx), ng = c.ngroups;
+    return ws.s_bw.ensure(nbb * 4) && ws.s_part.ensure(nbb * 4) && ws.s_blocal.ensure(nbb * 4) &&
+           ws.s_pbcount.ensure((size_t)c.pgs_blocks * 4) && ws.s_pbody.ensure((size_t)c.pgs_blocks * c.caps.bcap * 4) &&
+           ws.s_prow.ensure((size_t)c.pgs_blocks * 4) && ws.s_pgrp.ensure((size_t)c.pgs_blocks * 4) &&
+           ws.s_gpart.ensure((ng + 1) * 4) && ws.s_gdesc.ensure((ng + 1) * 16) && ws.s_pccount.ensure(npc * 4) &&
+           ws.s_pcstart.ensure((npc + 1) * 4) && ws.s_pcfill.ensure(npc * 4) && ws.s_ilist.ensure((ng + 1) * 4) &&
+           ws.s_irown.ensure((ng + 1) * 4) && ws.s_irowoff.ensure((ng + 1) * 4) && ws.s_idesc.ensure((ng + 1) * 16) &&
+           ws.s_ipack.ensure((size_t)ws.row_cap * 80) && ws.s_hist.ensure(nh * 4) && ws.s_binpart.ensure(nh * 4);
+}
+
+// Every device buffer a step writes, allocated before its first kernel: an
+// allocation that fails leaves the world's state as it was (the step returns
+// 0 having launched nothing).
+static bool reserve_step(Workspace &ws, int nb, const SolverParams &P, bool coloured) {
     const int nj = ws.njoints;
     if (!ensure_rows(ws, ws.contact_cap, nj)) return false;
     if (P.warm_mode && !ensure_warm(ws)) return false;
+    const size_t nc = ws.contact_cap > 0 ? ws.contact_cap : 1;
+    if (ws.sleep_on && !(ws.c_keep.ensure(nc * 4) && ws.c_kpos.ensure(nc * 4) &&
+                         ws.c_awake.ensure(nc * sizeof(Contact)) && ws.c_orig.ensure(nc * 4)))
+        return false;
+    if ((P.learned || P.learn_capture) &&
+        !(ws.l_feat.ensure(nc * GB_MLP_IN * 4) && ws.l_scale.ensure(nc * 4) && ws.l_pred.ensure(nc * GB_MLP_OUT * 4)))
+        return false;
+    if (P.learned && !ws.l_alt.ensure((size_t)ws.row_cap * 4)) return false;
+    // the scan scratch for the longest scan of the step
+    size_t nscan = nc + 1;
+    nscan = std::max(nscan, (size_t)(nj > 0 ? nj : 1));
+    nscan = std::max(nscan, (size_t)(nb > 0 ? nb : 1));
+    nscan = std::max(nscan, (size_t)GB_MAX_COLOURS);
+    if (coloured) {
+        const ColouredPlan c = plan_coloured(ws, P);
+        if (!ensure_coloured(ws, nb, c)) return false;
+        nscan = std::max(nscan, std::max((size_t)c.ncb, c.wave_cap));
+        nscan = std::max(nscan, std::max((size_t)c.pgs_blocks * GB_SLAB_COLOURS, c.ngroups));
+    }
+    return ws.scan_tmp.ensure(sizeof(int) * ((nscan + 1023) / 1024 + 2));
+}
+
+static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t s, bool coloured = false) {
+    Bodies B = bodies_view(ws, nb);
+    const int nj = ws.njoints;
+    if (!reserve_step(ws, nb, P, coloured)) return false;
     JointTable T = joint_view(ws);
     // sleeping: the idle test and the island rule decide which bodies, joints
     // and contacts this step processes (skipped when the caller ran it already
@@ -2243,7 +2342,10 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     const Surface *S = ws.surfaces.as<Surface>();
     k_contact_m<<<grid, 256, 0, s>>>(C, S, ncp, ws.c_mcount.as<int>());
     scan_exclusive(ws.c_mcount.as<int>(), ws.c_rstart.as<int>(), ncp, ws.contact_cap, &ws.dc->nrows, ws, s);
-    k_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
+    // the capacity the assembly sees (lowered only by the error-path tests, in worlds without joints)
+    const int row_cap_seen = g_test.row_cap > 0 && nj == 0 && g_test.row_cap < ws.row_cap ? g_test.row_cap : ws.row_cap;
+    k_rows_total<<<1, 1, 0, s>>>(ws.dc, row_cap_seen, ws.c_rstart.as<int>(), ws.c_mcount.as<int>(),
+                                 const_cast<int *>(ncp));
     if (nj > 0) scan_exclusive(T.m, T.rstart, nullptr, nj, &ws.dc->njoint_rows, ws, s);
     else cudaMemsetAsync(&ws.dc->njoint_rows, 0, 4, s);
     k_joint_rows_total<<<1, 1, 0, s>>>(ws.dc, ws.row_cap);
@@ -2251,9 +2353,6 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
     const int dyn = (P.solver == 1) && (P.premature_delta != 0 || P.extra_factor != 0);
     LearnOut L = {nullptr, nullptr};
     if (P.learned || P.learn_capture) {
-        const size_t nc = ws.contact_cap > 0 ? ws.contact_cap : 1;
-        if (!(ws.l_feat.ensure(nc * GB_MLP_IN * 4) && ws.l_scale.ensure(nc * 4) && ws.l_pred.ensure(nc * GB_MLP_OUT * 4)))
-            return false;
         L.feat = ws.l_feat.as<float>();
         L.scale = ws.l_scale.as<float>();
     }
@@ -2265,7 +2364,7 @@ static bool assemble(Workspace &ws, int nb, const SolverParams &P, cudaStream_t 
         count_launch();
     }
     if (P.learned) {
-        if (!ws.mlp_wb.p || !ws.l_alt.ensure((size_t)ws.row_cap * 4)) return false;
+        if (!ws.mlp_wb.p) return false;
         if (!mlp_infer(ws.mlp_wb.as<unsigned char>(), ws.l_feat.as<float>(), 0, ncp, ws.l_pred.as<float>(),
                        &ws.dc->err, s))
             return false;
@@ -2311,7 +2410,7 @@ int download_solver_contacts(Workspace &ws, std::vector<int2> &bodies, std::vect
 
 bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStream_t s, cudaEvent_t ev0,
                       cudaEvent_t ev1) {
-    if (!assemble(ws, nb, P, s)) return false;
+    if (!assemble(ws, nb, P, s, true)) return false;
     const Contact *C = solve_contacts(ws);
     const int *ncp = solve_count(ws);
     int grid = 4 * num_sms();
@@ -2324,27 +2423,17 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                   ws.grp_body.as<int2>());
     k_groups_total<<<1, 1, 0, s>>>(ws.dc, ws.njoints);
     count_launch(2);
-    const int pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
+    // the buffers below were reserved before the step's first kernel (reserve_step)
+    const ColouredPlan plan = plan_coloured(ws, P);
+    const int pgs_blocks = plan.pgs_blocks;
     // two-level sweep: parts, interior / cross classes of the groups
-    const SlabCaps caps = slab_caps();
-    const bool slab = P.pgs_two_level && pgs_blocks >= 2 && caps.rcap > 0;
-    const size_t ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
-    int sx = 1, sy = pgs_blocks;
+    const SlabCaps caps = plan.caps;
+    const bool slab = plan.slab;
+    const size_t ngroups = plan.ngroups;
+    const int sx = plan.sx, sy = plan.sy;
     if (slab) {
-        for (int d = 1; d * d <= pgs_blocks; d++)
-            if (pgs_blocks % d == 0) sx = d;
-        sy = pgs_blocks / sx;
-        const size_t nbb = nb > 0 ? nb : 1, npc = (size_t)pgs_blocks * GB_SLAB_COLOURS;
+        const size_t nbb = nb > 0 ? nb : 1;
         const size_t nh = (size_t)GB_SLAB_NBIN * (1 + sx);
-        if (!(ws.s_bw.ensure(nbb * 4) && ws.s_part.ensure(nbb * 4) && ws.s_blocal.ensure(nbb * 4) &&
-              ws.s_pbcount.ensure((size_t)pgs_blocks * 4) && ws.s_pbody.ensure((size_t)pgs_blocks * caps.bcap * 4) &&
-              ws.s_prow.ensure((size_t)pgs_blocks * 4) && ws.s_pgrp.ensure((size_t)pgs_blocks * 4) &&
-              ws.s_gpart.ensure((ngroups + 1) * 4) && ws.s_gdesc.ensure((ngroups + 1) * 16) &&
-              ws.s_pccount.ensure(npc * 4) && ws.s_pcstart.ensure((npc + 1) * 4) && ws.s_pcfill.ensure(npc * 4) &&
-              ws.s_ilist.ensure((ngroups + 1) * 4) && ws.s_irown.ensure((ngroups + 1) * 4) &&
-              ws.s_irowoff.ensure((ngroups + 1) * 4) && ws.s_idesc.ensure((ngroups + 1) * 16) &&
-              ws.s_ipack.ensure((size_t)ws.row_cap * 80) && ws.s_hist.ensure(nh * 4) && ws.s_binpart.ensure(nh * 4)))
-            return false;
         Bodies B = bodies_view(ws, nb);
         cudaMemsetAsync(ws.s_bw.p, 0, nbb * 4, s);
         cudaMemsetAsync(ws.s_hist.p, 0, nh * 4, s);
@@ -2384,8 +2473,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         const int2 *gbody = ws.grp_body.as<int2>();
         DevCounters *dc = ws.dc;
         const int *cls = slab ? ws.s_gpart.as<int>() : nullptr;
+        int climit = g_test.colour_cap > 0 && g_test.colour_cap < GB_MAX_COLOURS ? g_test.colour_cap : GB_MAX_COLOURS;
         void *args[] = {(void *)&gbody, (void *)&dc, (void *)&mask, (void *)&claim, (void *)&colour, (void *)&tent,
-                        (void *)&nb, (void *)&cls};
+                        (void *)&nb, (void *)&cls, (void *)&climit};
         if (cudaLaunchCooperativeKernel((const void *)k_colour, blocks, 256, args, 0, s) != cudaSuccess) return false;
     }
     cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
@@ -2400,16 +2490,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.grp_body.as<int2>());
     // cut every (colour, block)'s slots into waves and pack their rows chunk by
     // chunk for the solver's blocks
-    const int ncb = GB_MAX_COLOURS * pgs_blocks;
-    const int chunk_cap = slab ? GB_SLAB_XCHUNK : GB_CHUNK_ROWS;
-    // waves: one per (colour, block) at least, plus one per T slots and per
-    // chunk_cap - 12 staged rows
-    const size_t wave_cap = 2 * (size_t)ncb + ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (chunk_cap - 12) + 16;
-    if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.wv_count.ensure((size_t)ncb * 4) &&
-          ws.wv_base.ensure((size_t)ncb * 4 + 4) && ws.chunk_rows.ensure(wave_cap * 4) &&
-          ws.chunk_start.ensure(wave_cap * 4) && ws.wv_col.ensure(wave_cap * 4) &&
-          ws.wv_sched.ensure(wave_cap * GB_PGS_THREADS * 4)))
-        return false;
+    const int ncb = plan.ncb;
+    const int chunk_cap = plan.chunk_cap;
+    const size_t wave_cap = plan.wave_cap;
     {
         const int g1 = (ncb + 127) / 128;
         k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
@@ -2445,6 +2528,12 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
+    if (g_test.barrier) {
+        // error-path tests: the counter starts one arrival short, so the
+        // solver's first grid barrier never completes and its bounded wait runs out
+        cudaMemsetAsync(&ws.dc->gsync.count, 0xff, sizeof(unsigned), s);
+        g_test.barrier = 0;
+    }
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
     cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
     cudaMemsetAsync(&ws.dc->nhist, 0, 4, s);
@@ -2467,6 +2556,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.learned = P.learned;
         A.lam_alt = P.learned ? ws.l_alt.as<float>() : nullptr;
         A.passes = P.pgs_passes > 1 ? P.pgs_passes : 1;
+        A.poison_stage = g_test.stage;
+        g_test.stage = 0;
         A.packed = ws.p_rows.as<float4>();
         A.chunk_start = ws.chunk_start.as<int>();
         A.chunk_rows = ws.chunk_rows.as<int>();
@@ -2522,13 +2613,16 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
 
 bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, const IslandSchedule &sch, cudaStream_t s,
                               cudaEvent_t ev0, cudaEvent_t ev1) {
-    if (!assemble(ws, nb, P, s)) return false;
+    // the island schedule's buffers first: nothing has run if one cannot be allocated
     int nisl = (int)sch.start.size() - 1;
     if (nisl > 0) {
         size_t no = sch.order.size() > 0 ? sch.order.size() : 1;
         if (!(ws.i_order.ensure(no * 4) && ws.i_start.ensure((nisl + 1) * 4) &&
               ws.i_bodies.ensure((sch.bodies.size() + 1) * 4) && ws.i_bstart.ensure((nisl + 1) * 4)))
             return false;
+    }
+    if (!assemble(ws, nb, P, s)) return false;
+    if (nisl > 0) {
         if (!sch.order.empty()) cudaMemcpyAsync(ws.i_order.p, sch.order.data(), sch.order.size() * 4, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(ws.i_start.p, sch.start.data(), (nisl + 1) * 4, cudaMemcpyHostToDevice, s);
         if (!sch.bodies.empty()) cudaMemcpyAsync(ws.i_bodies.p, sch.bodies.data(), sch.bodies.size() * 4, cudaMemcpyHostToDevice, s);
@@ -2561,8 +2655,12 @@ bool launch_quickstep_islands(Workspace &ws, int nb, const SolverParams &P, cons
 }
 
 double last_residual(Workspace &ws, int nb, double *compl_err, double *maxlam, cudaStream_t s) {
-    ws.res_f.ensure((size_t)(nb > 0 ? nb : 1) * 48);
-    ws.res_v.ensure((size_t)(nb > 0 ? nb : 1) * 48 + 64);
+    if (!(ws.res_f.ensure((size_t)(nb > 0 ? nb : 1) * 48) && ws.res_v.ensure((size_t)(nb > 0 ? nb : 1) * 48 + 64))) {
+        report_error("gbodeWorldLastResidual: device allocation");
+        if (compl_err) *compl_err = NAN;
+        if (maxlam) *maxlam = NAN;
+        return NAN;
+    }
     cudaMemsetAsync(ws.res_f.p, 0, (size_t)(nb > 0 ? nb : 1) * 48, s);
     double *out = (double *)((char *)ws.res_v.p + (size_t)(nb > 0 ? nb : 1) * 48);
     cudaMemsetAsync(out, 0, 24, s);
@@ -2651,7 +2749,10 @@ void joint_feedback(Workspace &ws, int ncontacts, int njoints, std::vector<float
     out.assign(nrec * 16, 0.f);
     if (nrec == 0) return;
     DBuf &tmp = ws.res_f;
-    tmp.ensure(nrec * 64);
+    if (!tmp.ensure(nrec * 64)) {  // feedback left at zero, the error reported
+        report_error("joint feedback: device allocation");
+        return;
+    }
     cudaMemsetAsync(tmp.p, 0, nrec * 64, s);
     k_feedback<<<4 * num_sms(), 256, 0, s>>>(rows_view(ws), &ws.dc->nrows, ws.use_awake ? ws.c_orig.as<int>() : nullptr,
                                              ncontacts, tmp.as<float>());

@@ -159,6 +159,7 @@ _PROTOS = [
     ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
     ("gbodeWorldSetTwoLevelSweep", None, [ID, ctypes.c_int]), ("gbodeWorldGetTwoLevelSweep", ctypes.c_int, [ID]),
+    ("gbodeTestInject", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("gbodeSolveLCPBatch", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
@@ -222,6 +223,8 @@ _PROTOS = [
 ]
 
 GBODE_NOALLOC_MAX_PAIRS = 8192  # gbodeCollidePairsNoAlloc's largest batch
+GBODE_TEST_OFF, GBODE_TEST_BARRIER, GBODE_TEST_STAGE, GBODE_TEST_ALLOC = 0, 1, 2, 3
+GBODE_TEST_CONTACT_CAP, GBODE_TEST_ROW_CAP, GBODE_TEST_COLOUR_CAP, GBODE_TEST_ALLOC_PENDING = 4, 5, 6, 7
 GBODE_MLP_NPARAMS = 35099       # learned warm start parameters
 
 dJointTypeBall, dJointTypeHinge, dJointTypeContact, dJointTypeHinge2 = 1, 2, 4, 6
