@@ -11,6 +11,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 typedef float real;
 #define R0 0.0f
@@ -1132,6 +1133,8 @@ struct port_world {
     int dyn_enabled;
     int threads;       /* SOR threads (1: the reference's default self-threaded stepping) */
     int mt_min_rows;   /* islands with fewer rows iterate on one thread */
+    int resid_on;      /* evaluate each step's FP64 LCP residual (test / benchmark bookkeeping) */
+    double res_max, lam_max;  /* of the last step: max natural-map residual, max |lambda| */
 };
 
 /* contact joint as dJointCreateContact + dJointAttach leave it (ode.cpp:1192-1200, 1383-1439) */
@@ -1623,6 +1626,57 @@ static void sor_sweeps_mt(const port_world *w, const sor_rows *S, int *order, in
     free(C.blev); free(C.lev_of); free(C.lev_rows); free(C.lev_start);
 }
 
+/* FP64 natural-map residual of one island's solution (unscaled rows Ju:
+ * J1 0-5, rhs 6, cfm 7, J2 8-13, lo 14, hi 15; findex island-local), the
+ * definition of port_lcp_residual, folded into w->res_max / w->lam_max. */
+static void island_residual(port_world *w, const real *Ju, int m, const int *jb1, const int *jb2,
+                            const int *findex, const real *lambda, const int *body_ids, int nb, const real *invI) {
+    double *f = (double *)calloc((size_t)6 * (nb > 0 ? nb : 1), sizeof(double));
+    double *v = (double *)calloc((size_t)6 * (nb > 0 ? nb : 1), sizeof(double));
+    for (int i = 0; i < m; i++) {
+        const real *r = Ju + 16 * i;
+        for (int k = 0; k < 6; k++) f[6 * jb1[i] + k] += (double)r[k] * lambda[i];
+        if (jb2[i] != -1) for (int k = 0; k < 6; k++) f[6 * jb2[i] + k] += (double)r[8 + k] * lambda[i];
+    }
+    for (int b = 0; b < nb; b++) {
+        const double im = w->b[body_ids[b]].invMass;
+        const real *I = invI + 12 * b;
+        for (int k = 0; k < 3; k++) v[6 * b + k] = im * f[6 * b + k];
+        for (int k = 0; k < 3; k++)
+            v[6 * b + 3 + k] = (double)I[4 * k] * f[6 * b + 3] + (double)I[4 * k + 1] * f[6 * b + 4] +
+                               (double)I[4 * k + 2] * f[6 * b + 5];
+    }
+    for (int i = 0; i < m; i++) {
+        const real *r = Ju + 16 * i;
+        double Av = 0, D = 0;
+        const int b1 = jb1[i], b2 = jb2[i];
+        for (int k = 0; k < 6; k++) Av += (double)r[k] * v[6 * b1 + k];
+        const double im1 = w->b[body_ids[b1]].invMass;
+        for (int k = 0; k < 3; k++) D += (double)r[k] * r[k] * im1;
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) D += (double)r[3 + a] * invI[12 * b1 + 4 * a + c] * r[3 + c];
+        if (b2 != -1) {
+            for (int k = 0; k < 6; k++) Av += (double)r[8 + k] * v[6 * b2 + k];
+            const double im2 = w->b[body_ids[b2]].invMass;
+            for (int k = 0; k < 3; k++) D += (double)r[8 + k] * r[8 + k] * im2;
+            for (int a = 0; a < 3; a++)
+                for (int c = 0; c < 3; c++) D += (double)r[11 + a] * invI[12 * b2 + 4 * a + c] * r[11 + c];
+        }
+        const double cfm = r[7], li = lambda[i];
+        const double wi = Av + cfm * li - r[6];
+        D += cfm;
+        double lo, hi;
+        if (findex[i] >= 0) { hi = fabs((double)r[15] * lambda[findex[i]]); lo = -hi; }
+        else { lo = r[14]; hi = r[15]; }
+        double t = li - wi / D;
+        if (t < lo) t = lo;
+        if (t > hi) t = hi;
+        if (fabs(li - t) > w->res_max) w->res_max = fabs(li - t);
+        if (fabs(li) > w->lam_max) w->lam_max = fabs(li);
+    }
+    free(f); free(v);
+}
+
 /* set only while port_world_quickstep_map runs: receives each recorded row's contact slot */
 static int *g_row_slot = NULL;
 
@@ -1719,6 +1773,12 @@ static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint 
             }
             Jr[6] += sum;
         }
+        /* the unscaled rows, for the step's FP64 residual after the solve */
+        real *Ju = NULL;
+        if (w->resid_on) {
+            Ju = (real *)malloc(sizeof(real) * 16 * (m > 0 ? m : 1));
+            memcpy(Ju, J, sizeof(real) * 16 * m);
+        }
         if (rows_out) {
             for (int i = 0; i < m; i++) {
                 float *o = rows_out + 20 * i;
@@ -1792,6 +1852,10 @@ static void quickstep_island(port_world *w, const int *body_ids, int nb, pjoint 
                 for (int ii = 0; ii < m; ii++) sor_row(&S, order[ii]);
                 if (sor_after_sweep(w, &drv, fa, nb)) break;
             }
+        }
+        if (Ju) {
+            island_residual(w, Ju, m, jb1, jb2, findex, lambda, body_ids, nb, invI);
+            free(Ju);
         }
         /* Stage4b :3082-3182 */
         for (int i = 0; i < nb; i++) {
@@ -1913,6 +1977,8 @@ int port_world_quickstep(port_world *w, int nc, const int *cb, const int *mode, 
     int *cidx = (int *)malloc(sizeof(int) * (nc > 0 ? nc : 1));
     for (int k = 0; k < nc; k++) { fill_joint(&joints[k], cb[2 * k], cb[2 * k + 1], mode[k], cs + 16 * k); cidx[k] = k; }
     if (lambda) memset(lambda, 0, sizeof(float) * 3 * nc);
+    w->res_max = 0;
+    w->lam_max = 0;
     world_quickstep(w, joints, nc, cidx, lambda, rows_out, nrows_out, NULL);
     free(cidx); free(joints);
     return 1;
@@ -1931,7 +1997,14 @@ struct port_sim {
     pjoint *joints; int nj, capj;
     int *made_b; float *made_cs;
     pgeom *posed;
+    double t_collide, t_step;  /* seconds of the last step: collision (dSpaceCollide + contacts), quickstep */
 };
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 port_sim *port_sim_create(port_world *w, int ng, const int *cls, const int *body, const float *pos, const float *R,
                           const float *dims, int minlevel, int maxlevel, int maxc, int mode, const float *surface) {
@@ -1990,6 +2063,7 @@ static void sim_cb(void *ctx, int g1, int g2) {
 
 int port_sim_step(port_sim *s) {
     port_world *w = s->w;
+    const double t0 = now_s();
     /* geoms take their body's pose (collision_kernel.cpp recomputePosr) */
     real *aabbs = (real *)malloc(sizeof(real) * 6 * (s->ng > 0 ? s->ng : 1));
     for (int i = 0; i < s->ng; i++) {
@@ -2010,7 +2084,12 @@ int port_sim_step(port_sim *s) {
     int *cidx = (int *)malloc(sizeof(int) * (s->nj > 0 ? s->nj : 1));
     for (int k = 0; k < s->nj; k++) cidx[k] = k;
     int *stepped = (int *)malloc(sizeof(int) * (w->nb > 0 ? w->nb : 1));
+    const double t1 = now_s();
+    w->res_max = 0;
+    w->lam_max = 0;
     world_quickstep(w, s->joints, s->nj, cidx, NULL, NULL, NULL, stepped);
+    s->t_collide = t1 - t0;
+    s->t_step = now_s() - t1;
     /* dGeomMoved for each stepped body's geom: a clean geom is marked dirty
      * and moved to the head of the space's list (collision_space.cpp:49-75,
      * 205-209).  The moves are applied at once: the moved geoms, last moved
@@ -2040,6 +2119,16 @@ int port_sim_step(port_sim *s) {
     free(geom_of); free(stepped); free(cidx);
     return s->nj;
 }
+
+void port_sim_last_stats(const port_sim *s, double *out4) {
+    out4[0] = s->t_collide;
+    out4[1] = s->t_step;
+    out4[2] = s->w->res_max;
+    out4[3] = s->w->lam_max;
+}
+
+void port_world_set_residual(port_world *w, int on) { w->resid_on = on != 0; }
+void port_world_last_residual(const port_world *w, double *out2) { out2[0] = w->res_max; out2[1] = w->lam_max; }
 
 int port_sim_last_contacts(const port_sim *s, int *cb, float *cs, int cap) {
     int n = s->nj < cap ? s->nj : cap;

@@ -75,6 +75,16 @@ int port_sim_step(port_sim *s);
 /* Contacts made in the last step: cb [nc][2], cs [nc][16] (pos normal depth ...). */
 int port_sim_last_contacts(const port_sim *s, int *cb, float *cs, int cap);
 
+/* Evaluate each step's FP64 natural-map LCP residual (the definition of
+ * port_lcp_residual, over the step's unscaled rows) while stepping. */
+void port_world_set_residual(port_world *w, int on);
+/* Of the last port_sim_step: seconds of collision (geom poses, hash space,
+ * contacts) and of the quickstep, the step's residual (with
+ * port_world_set_residual on; else 0) and max |lambda|. */
+void port_sim_last_stats(const port_sim *s, double *out4);
+/* The residual and max |lambda| of the world's last quickstep (residual on). */
+void port_world_last_residual(const port_world *w, double *out2);
+
 /* port_world_quickstep that also writes, for every recorded row (rows_out
  * order: islands in the reference's order), 3 * contact index + the row's
  * place in its contact (0 normal, 1 and 2 friction) to row_slot [m].  Not

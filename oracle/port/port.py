@@ -60,6 +60,9 @@ class Port:
         L.port_sim_step.argtypes = [ctypes.c_void_p]
         L.port_sim_last_contacts.argtypes = [ctypes.c_void_p, _I, _F, ctypes.c_int]
         L.port_world_quickstep_map.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, _I, _F, _F, _F, _I, _I]
+        L.port_world_set_residual.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.port_sim_last_stats.argtypes = [ctypes.c_void_p, _D]
+        L.port_world_last_residual.argtypes = [ctypes.c_void_p, _D]
         L.port_lcp_residual.restype = ctypes.c_double
         L.port_lcp_residual.argtypes = [ctypes.c_int, _F, ctypes.c_int, _D, _D, _F, _D]
         L.port_rand_set_seed.argtypes = [ctypes.c_ulong]
@@ -194,6 +197,24 @@ class PortWorld:
 
     def sim_step(self):
         return self.port.lib.port_sim_step(self.sim)
+
+    def set_residual(self, on: bool = True):
+        """Evaluate every step's FP64 LCP residual while stepping."""
+        self.port.lib.port_world_set_residual(self.h, 1 if on else 0)
+
+    def last_residual(self):
+        """(FP64 residual, max |lambda|) of the last quickstep (set_residual on)."""
+        out = np.zeros(2, np.float64)
+        self.port.lib.port_world_last_residual(self.h, out.ctypes.data_as(_D))
+        return float(out[0]), float(out[1])
+
+    def last_stats(self):
+        """Of the last sim_step: (collision s, quickstep s, FP64 residual,
+        max |lambda|); the residual is relative after dividing by
+        max(1, max |lambda|)."""
+        out = np.zeros(4, np.float64)
+        self.port.lib.port_sim_last_stats(self.sim, out.ctypes.data_as(_D))
+        return float(out[0]), float(out[1]), float(out[2]), float(out[3])
 
     def last_contacts(self):
         n = self.port.lib.port_sim_last_contacts(self.sim, None, None, 0)

@@ -170,3 +170,30 @@ def test_dynamic_iterations_follow_reference(port, golden, name):
             ref = g[f"s{k}_lambda_{tag}"]
             assert np.abs(lam - ref).max() / max(1.0, float(np.abs(ref).max())) < 1e-6, (name, k, tag)
             np.testing.assert_array_equal(w.state(), g[f"s{k}_post_{tag}"], err_msg=f"{name} s{k} {tag}")
+
+
+@pytest.mark.parametrize("threads", [1, 4])
+def test_in_step_residual_matches_evaluator(port, golden, threads):
+    """The residual the oracle evaluates inside its step (the benchmark's CPU
+    legs count steps by it) agrees with the separate FP64 evaluator on the
+    same rows and multipliers to 1e-5 relative (the step uses its FP32
+    world-frame inverse inertias, the evaluator recomputes them in FP64), on
+    the 256-body pile's snapshots (one and four SOR threads, random
+    reordering)."""
+    from oracle.port.port import world_inv_inertia
+    g = golden("step_pile256.npz")
+    iters, _, mode, _ = [int(x) for x in g["ints"]]
+    for k in range(len(g["snaps"])):
+        pre, cb, cs = g[f"s{k}_pre"], g[f"s{k}_cb"], g[f"s{k}_cs"]
+        bodies = g["bodies0"].copy()
+        bodies[:, 0:3], bodies[:, 3:7] = pre[:, 0:3], pre[:, 3:7]
+        bodies[:, 7:10], bodies[:, 10:13] = pre[:, 19:22], pre[:, 22:25]
+        w = port.world(bodies, g["params"], iters, dyn=0, reorder=1)
+        w.set_threads(threads, 64)
+        w.set_residual(True)
+        _, rows = w.quickstep(cb, np.full(len(cb), mode, np.int32), cs, want_rows=True)
+        r_in, lmax = w.last_residual()
+        invI, invm = world_inv_inertia(pre, bodies)
+        r_ev, _ = port.lcp_residual(rows, invm, invI, rows[:, 19])
+        assert abs(r_in - r_ev) <= 1e-5 * max(1.0, r_ev), (k, r_in, r_ev)
+        assert lmax == float(np.abs(rows[:, 19]).max())
