@@ -513,7 +513,9 @@ def batched_leg(args, L, stream, dev, kind):
     out["residual_tuned_graph"] = {"body_steps_per_s": sc.nb * ok / (ms / 1e3), "ms_per_step": ms / args.steps,
                                    "sweeps_per_step": float(np.mean(T["sweeps"])), "steps_at_target": ok,
                                    "tuning": {"blocks": tu.blocks, "passes": tu.passes,
-                                              "check_every": tu.check_every, "candidates": tu.candidates}}
+                                              "check_every": tu.check_every, "threads_per_block": tu.threads,
+                                              "staged_rows_per_buffer": tu.chunk_rows, "two_level": tu.two_level,
+                                              "candidates": tu.candidates}}
     if kind == "vehicles" and not args.no_learned:
         out["residual_learned_tuned_graph"] = learned_batched(args, L, w, stream, flush, sc.nb)
     r64, _, ml = w.last_residual()
@@ -521,7 +523,8 @@ def batched_leg(args, L, stream, dev, kind):
     out["note"] = ("value counts steps at the residual target (residual) or every step at the configured 20 "
                    "sweeps (iterations20); the chains are islands of one world, solved by the same coloured "
                    "persistent kernel; *_graph: the fused step replayed from a CUDA graph (gbodeWorldStepFused); "
-                   "*_tuned: after gbodeWorldAutotune chose the solver blocks, passes per group and check interval; "
+                   "*_tuned: after gbodeWorldAutotune chose threads a block (colour-group tile), staged rows a "
+                   "buffer, the two-level sweep, solver blocks, passes per group and check interval; "
                    "*_learned_*: the learned warm start with the plain start as fallback (per step, whichever "
                    "start has the lower residual), on the tuned settings; "
                    "every leg starts from the same state (gbodeWorldRestoreSnapshot): W warm-up steps, then the "

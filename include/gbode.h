@@ -388,6 +388,14 @@ int gbodeWorldGetSolverBlocks(dWorldID w);
 void gbodeWorldSetManifoldPasses(dWorldID w, int passes);
 int gbodeWorldGetManifoldPasses(dWorldID w);
 
+/* Tiles of the coloured solver: threads a block of the sweep kernels (128
+ * or 256, default 256) -- the colour-group tile: a colour's slots of a block
+ * are relaxed in waves of this many -- and staged rows a shared-memory buffer
+ * of the one-level sweep (64 to 800, default 800; a wave also ends when its
+ * rows would not fit).  Other values select the defaults. */
+void gbodeWorldSetSolverTiles(dWorldID w, int threads, int chunk_rows);
+void gbodeWorldGetSolverTiles(dWorldID w, int *threads, int *chunk_rows);
+
 /* Two-level sweep of the coloured solver (0 off; k >= 1 on, up to 8).  The
  * bodies are split into one spatial column per solver block; contact
  * manifolds inside one column are relaxed from the block's shared memory,
@@ -483,9 +491,11 @@ void gbodeWorldDropSnapshot(dWorldID w);
 
 /* Solver settings tuned on the running world.  gbodeWorldAutotune makes one
  * plain fused step, copies the device-side state aside, and for each
- * candidate -- solver blocks: one per SM or half as many; passes over a
- * constraint group's rows per visit: 1, 2, 3; residual checks every 5 or 10
- * sweeps when a residual target is set -- restores that state and times
+ * candidate -- threads a solver block (128 or 256: the colour-group tile, the
+ * slots one wave of a colour relaxes at once), staged rows a shared-memory
+ * buffer (400 or 800), the two-level sweep (off, or two interior passes),
+ * residual checks every 5 or 10 sweeps when a residual target is set, and
+ * also half the solver blocks or two passes over a group's rows -- restores that state and times
  * `steps` gbodeWorldStepFused steps (after two untimed ones) with CUDA
  * events.  It keeps the candidate with the lowest median step time, leaves
  * it set, and restores the state once more: the world continues from the
@@ -497,6 +507,9 @@ typedef struct gbodeTuning {
     int check_every;  /* residual checks every this many sweeps (0: no residual target) */
     float ms_per_step;
     int candidates;   /* candidates timed */
+    int threads;      /* gbodeWorldSetSolverTiles: threads a block */
+    int chunk_rows;   /* gbodeWorldSetSolverTiles: staged rows a buffer */
+    int two_level;    /* gbodeWorldSetTwoLevelSweep */
 } gbodeTuning;
 int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *s, int maxc,
                        dReal dt, int steps, int use_graph, gbodeTuning *best);

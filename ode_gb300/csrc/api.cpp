@@ -753,6 +753,14 @@ void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode 
 void gbodeWorldSetSolverBlocks(dWorldID w, int blocks) { w->P.pgs_blocks = blocks > 0 ? blocks : 0; }
 void gbodeWorldSetManifoldPasses(dWorldID w, int passes) { w->P.pgs_passes = passes > 1 ? (passes > 16 ? 16 : passes) : 1; }
 int gbodeWorldGetManifoldPasses(dWorldID w) { return w->P.pgs_passes > 1 ? w->P.pgs_passes : 1; }
+void gbodeWorldSetSolverTiles(dWorldID w, int threads, int chunk_rows) {
+    w->P.pgs_threads = threads == 128 ? 128 : 0;
+    w->P.pgs_chunk = chunk_rows > 0 ? chunk_rows : 0;
+}
+void gbodeWorldGetSolverTiles(dWorldID w, int *threads, int *chunk_rows) {
+    if (threads) *threads = w->P.pgs_threads == 128 ? 128 : 256;
+    if (chunk_rows) *chunk_rows = w->P.pgs_chunk > 0 ? w->P.pgs_chunk : 800;
+}
 void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases) {
     w->P.pgs_two_level = interior_phases < 0 ? 0 : (interior_phases > 8 ? 8 : interior_phases);
 }
@@ -2267,16 +2275,26 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
         return 0;
     }
     if (!world_init_device(w)) return 0;
-    struct Cand { int blocks, passes, check; };
+    // candidates: threads a block (the colour-group tile: 128 or 256 slots a
+    // wave), staged rows a shared-memory buffer (400 or 800; the two-level
+    // sweep stages its crossing rows in 128-row buffers), the two-level sweep
+    // (off, or two interior passes), the residual check interval; and, as
+    // before, half the blocks and two passes over a group's rows
+    struct Cand { int blocks, passes, check, threads, chunk, two; };
     std::vector<Cand> cands;
     const int sms = num_sms();
     const bool resid = w->P.residual_target > 0;
-    for (int blocks : {sms, sms / 2})
-        for (int passes : {1, 2, 3})
-            for (int check : {5, 10}) {
-                if (!resid && check != 5) continue;
-                cands.push_back({blocks, passes, resid ? check : 0});
+    for (int threads : {256, 128})
+        for (int two : {0, 2})
+            for (int chunk : {800, 400}) {
+                if (two && chunk != 800) continue;
+                for (int check : {5, 10}) {
+                    if (!resid && check != 5) continue;
+                    cands.push_back({sms, 1, resid ? check : 0, threads, chunk, two});
+                }
             }
+    cands.push_back({sms / 2, 1, resid ? 5 : 0, 256, 800, 0});
+    cands.push_back({sms, 2, resid ? 5 : 0, 256, 800, 0});
     // every candidate starts from the same state: the device-side simulation
     // state (bodies, warm-start tables, joint multipliers, auto-disable state,
     // counters) is copied aside once and put back before each candidate and
@@ -2302,6 +2320,9 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
         restore();
         w->P.pgs_blocks = cands[i].blocks;
         w->P.pgs_passes = cands[i].passes;
+        w->P.pgs_threads = cands[i].threads == 128 ? 128 : 0;
+        w->P.pgs_chunk = cands[i].chunk;
+        w->P.pgs_two_level = cands[i].two;
         if (resid) w->P.check_every = cands[i].check;
         std::vector<float> t;
         for (int k = 0; k < steps + 2; k++) {
@@ -2334,8 +2355,14 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     const Cand &c = cands[best_i];
     w->P.pgs_blocks = c.blocks >= sms ? 0 : c.blocks;
     w->P.pgs_passes = c.passes;
+    w->P.pgs_threads = c.threads == 128 ? 128 : 0;
+    w->P.pgs_chunk = c.chunk;
+    w->P.pgs_two_level = c.two;
     if (resid) w->P.check_every = c.check;
     best->blocks = c.blocks;
+    best->threads = c.threads;
+    best->chunk_rows = c.chunk;
+    best->two_level = c.two;
     best->passes = c.passes;
     best->check_every = c.check;
     best->ms_per_step = best_ms;

@@ -40,6 +40,8 @@ struct SolverParams {
     int pgs_blocks;     // thread blocks of the coloured solver (0: one per SM)
     int pgs_passes;     // passes over a manifold's rows per visit (0 or 1: one)
     int pgs_two_level;  // two-level sweep: parts' interior groups in shared memory, cross groups coloured globally
+    int pgs_threads;    // threads a block of the sweep kernels: 128 or 256 (0: 256)
+    int pgs_chunk;      // staged rows a shared-memory buffer of the one-level sweep (0: GB_CHUNK_ROWS)
 };
 
 // learned warm start network (parameter layout in mlp.cu)

@@ -315,7 +315,8 @@ __host__ __device__ __forceinline__ size_t slab_smem_bytes(int chunk_cap, int rc
            (size_t)rcap * 4 + (size_t)bcap * 4;
 }
 
-__global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
+template <int T>
+__global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     const PgsArgs &A = S.A;
     unsigned gen = 0;
     DevCounters *dc = A.dc;
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
     __shared__ int s_nic, s_g0, s_ng, s_row0, s_nrows, s_nb;
     __shared__ unsigned long long s_mbar[4];  // two cross buffers, the interior rows, [3] never armed (poison_stage)
     __shared__ int s_abort;                   // a staging wait of this block ran out
-    __shared__ float s_lam[GB_PGS_THREADS * 13];
+    __shared__ float s_lam[T * 13];
     extern __shared__ float4 pgs_smem[];
     float4 *xbuf = pgs_smem;                                         // 2 x chunk_cap x 8
     float4 *irows = xbuf + (size_t)2 * S.chunk_cap * 8;              // rcap x 5
@@ -521,7 +522,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs_slab(SlabArgs S) {
         if (t.c < 0) { has_ahead = false; return; }
         int k = blockIdx.x + threadIdx.x * (int)gridDim.x;
         if (s_wcount[t.c] == 1) k = k < s_ccount[t.c] ? k : -1;
-        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * GB_PGS_THREADS + threadIdx.x]);
+        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * T + threadIdx.x]);
         has_ahead = k >= 0;
         if (has_ahead) ahead = __ldg(&A.desc[s_cstart[t.c] + k]);
     };

@@ -1079,6 +1079,7 @@ struct PgsArgs {
     float *lam_alt;
     int passes;       // passes over a manifold's rows each time it is relaxed (>= 1)
     int poison_stage; // error-path tests: the staging waits name a copy that is never issued
+    int chunk_cap;    // staged rows per shared-memory buffer (the waves were cut to it)
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -1271,21 +1272,21 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
 // when it starts.  Waves of one colour are separated by a block barrier only;
 // colours by a grid barrier.  A slot's offset in its chunk lives in bits 16-27
 // of its descriptor's y.
-#define GB_PGS_THREADS 256
+#define GB_PGS_THREADS 256  // threads a block of the sweep kernels by default (128 is the other instance)
 #define GB_STAGED_ROWS 12  // rows of a staged slot at most (4 contacts x 3, or a plain group)
-#define GB_CHUNK_ROWS 800  // rows per buffer: 2 x 100 KB of shared memory
+#define GB_CHUNK_ROWS 800  // staged rows per buffer by default: 2 x 100 KB of shared memory (at most)
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
 
 // The greedy cut of one (colour, block)'s slots into waves; `visit(wave, t,
 // k, offset)` for every slot (offset -1: not staged), returns the wave count.
 template <class F>
-__device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, int chunk_cap, F visit) {
-    int waves = 0, t = GB_PGS_THREADS, rows = 0;
+__device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, int chunk_cap, int T, F visit) {
+    int waves = 0, t = T, rows = 0;
     for (int k = b; k < n; k += B) {
         const int4 d = desc[s0 + k];
         const int r = (d.y & GB_DESC_STAGED) ? desc_rows(d) : 0;
-        if (t == GB_PGS_THREADS || rows + r > chunk_cap) { ++waves; t = 0; rows = 0; }
+        if (t == T || rows + r > chunk_cap) { ++waves; t = 0; rows = 0; }
         visit(waves - 1, t, k, r > 0 ? rows : -1);
         rows += r;
         ++t;
@@ -1296,19 +1297,19 @@ __device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, int chun
 // pass 1, one thread per (colour, block): waves of each (at least one, so
 // every block takes part in every colour's barrier)
 __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCounters *dc, const int4 *desc,
-                             int *wcount, int B, int chunk_cap) {
+                             int *wcount, int B, int chunk_cap, int T) {
     const int cb = blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
     if (c >= dc->ncolours) { wcount[cb] = 0; return; }
-    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, [](int, int, int, int) {});
+    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, T, [](int, int, int, int) {});
     wcount[cb] = w > 0 ? w : 1;
 }
 
 // pass 2: the chunk offsets in the descriptors, the schedule, rows per wave
 __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, const int *wcount,
                             const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B,
-                            int chunk_cap) {
+                            int chunk_cap, int T) {
     const int cb = blockIdx.x * blockDim.x + threadIdx.x;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
@@ -1318,11 +1319,11 @@ __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *d
     for (int w = 0; w < nw; w++) {
         wrows[base + w] = 0;
         wcol[base + w] = c;
-        for (int t = 0; t < GB_PGS_THREADS; t++) sched[(size_t)(base + w) * GB_PGS_THREADS + t] = -1;
+        for (int t = 0; t < T; t++) sched[(size_t)(base + w) * T + t] = -1;
     }
     const int s0 = cstart[c];
-    cut_waves(desc, s0, ccount[c], b, B, chunk_cap, [&](int w, int t, int k, int off) {
-        sched[(size_t)(base + w) * GB_PGS_THREADS + t] = k;
+    cut_waves(desc, s0, ccount[c], b, B, chunk_cap, T, [&](int w, int t, int k, int off) {
+        sched[(size_t)(base + w) * T + t] = k;
         if (off >= 0) {
             int4 d = desc[s0 + k];
             d.y = (d.y & ~(0xfff << 16)) | (off << 16);
@@ -1342,7 +1343,7 @@ __global__ void k_pack_rows(Rows Rw, const int *cstart, const DevCounters *dc, c
                             const int *wcol, const int *chunk_start, float4 *packed) {
     const int nw = dc->nwaves;
     for (int wv = blockIdx.x; wv < nw; wv += gridDim.x) {
-        const int k = sched[(size_t)wv * GB_PGS_THREADS + threadIdx.x];
+        const int k = sched[(size_t)wv * blockDim.x + threadIdx.x];
         if (k < 0) continue;
         const int4 d = desc[cstart[wcol[wv]] + k];
         if (!(d.y & GB_DESC_STAGED)) continue;
@@ -1520,14 +1521,15 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
 // buffer, and each thread loads its next manifold's descriptor and
 // multipliers while it waits at the barrier; after the barrier only the body
 // accumulators fc (written by the previous colour) are read through L2.
-__global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
+template <int T>
+__global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
     unsigned gen = 0;
     DevCounters *dc = A.dc;
     __shared__ int s_cstart[GB_MAX_COLOURS], s_ccount[GB_MAX_COLOURS], s_wcount[GB_MAX_COLOURS], s_wbase[GB_MAX_COLOURS];
     __shared__ unsigned long long s_mbar[3];  // two chunk buffers; [2] is never armed (poison_stage)
     __shared__ int s_abort;                   // a staging wait of this block ran out
-    __shared__ float s_lam[GB_PGS_THREADS * 13];  // per thread: the next manifold's multipliers
-    extern __shared__ float4 pgs_smem[];  // two buffers of GB_CHUNK_ROWS rows
+    __shared__ float s_lam[T * 13];  // per thread: the next manifold's multipliers
+    extern __shared__ float4 pgs_smem[];  // two buffers of A.chunk_cap rows
     const int ncol = dc->ncolours;
     const int nrows = dc->nrows;
     for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
@@ -1636,11 +1638,11 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
     auto issue = [&](Step t) {  // thread 0: the copy for step number nissued (t); loads t's successor's chunk
         const unsigned qq = nissued++;
         unsigned long long *m = &s_mbar[qq & 1];
-        const unsigned bytes = 128u * (unsigned)min(pend_rows, GB_CHUNK_ROWS);
+        const unsigned bytes = 128u * (unsigned)min(pend_rows, A.chunk_cap);
         // the block's reads of this buffer (two steps ago) come before the copy's writes
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(m, bytes);
-        if (bytes) bulk_g2s(pgs_smem + (qq & 1) * (GB_CHUNK_ROWS * 8), A.packed + (size_t)pend_start * 8, bytes, m);
+        if (bytes) bulk_g2s(pgs_smem + (qq & 1) * (A.chunk_cap * 8), A.packed + (size_t)pend_start * 8, bytes, m);
         chunk_of(step_after(t));
     };
     auto retire = [&]() {  // thread 0: wait for the oldest copy not yet waited for
@@ -1662,7 +1664,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
         // a colour in one wave: slot b + t B for thread t (no schedule load)
         int k = blockIdx.x + threadIdx.x * (int)gridDim.x;
         if (s_wcount[t.c] == 1) k = k < s_ccount[t.c] ? k : -1;
-        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * GB_PGS_THREADS + threadIdx.x]);
+        else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * T + threadIdx.x]);
         has_ahead = k >= 0;
         if (has_ahead) ahead = __ldg(&A.desc[s_cstart[t.c] + k]);
     };
@@ -1672,7 +1674,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
         staged = false;
         if (has_next) {
             const int n = desc_rows(next);
-            staged = (next.y & GB_DESC_STAGED) && desc_chunk_off(next) + n <= GB_CHUNK_ROWS;
+            staged = (next.y & GB_DESC_STAGED) && desc_chunk_off(next) + n <= A.chunk_cap;
             if (staged) {
                 for (int k = 0; k < n; k++) cp_async4(&my_lam[k], &A.Rw.lambda[next.x + k]);
                 cp_async_commit();
@@ -1705,7 +1707,7 @@ __global__ void __launch_bounds__(GB_PGS_THREADS, 1) k_pgs(PgsArgs A) {
                     relax_desc(A, next);
                 } else if (A.poison_stage ? mbar_wait(&s_mbar[2], 0, &dc->err, 16)
                                           : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
-                    const float4 *buf = pgs_smem + (q & 1) * (GB_CHUNK_ROWS * 8);
+                    const float4 *buf = pgs_smem + (q & 1) * (A.chunk_cap * 8);
                     if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
                     else relax_plain(A, next, buf, my_lam, lout);
                     nout = desc_rows(next);
@@ -2181,25 +2183,41 @@ struct SlabCaps {
     int bcap, gcap, rcap;
     size_t smem;
 };
-static SlabCaps slab_caps() {
+template <int T>
+static SlabCaps slab_caps_t() {
     static const SlabCaps caps = []() {
         SlabCaps c{288, 560, 0, 0};
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncAttributes fa;
-        if (cudaFuncGetAttributes(&fa, (const void *)k_pgs_slab) != cudaSuccess) return c;
+        if (cudaFuncGetAttributes(&fa, (const void *)k_pgs_slab<T>) != cudaSuccess) return c;
         const long long fixed = (long long)fa.sharedSizeBytes + (long long)slab_smem_bytes(GB_SLAB_XCHUNK, 0, c.bcap, c.gcap);
         const long long room = (long long)optin - fixed - 256;  // a little kept for the runtime's own use
         c.rcap = room > 0 ? (int)(room / 84) : 0;
         c.smem = slab_smem_bytes(GB_SLAB_XCHUNK, c.rcap, c.bcap, c.gcap);
         if (c.rcap > 0 &&
-            cudaFuncSetAttribute((const void *)k_pgs_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem) !=
-                cudaSuccess)
+            cudaFuncSetAttribute((const void *)k_pgs_slab<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)c.smem) != cudaSuccess)
             c.rcap = 0;
         return c;
     }();
     return caps;
+}
+static SlabCaps slab_caps(int threads) { return threads == 128 ? slab_caps_t<128>() : slab_caps_t<256>(); }
+
+// The one-level sweep kernel's shared-memory opt-in (two buffers of at most
+// GB_CHUNK_ROWS rows) and its co-residency, once per instance.
+template <int T>
+static int pgs_per_sm() {
+    static const int v = []() {
+        const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;
+        cudaFuncSetAttribute((const void *)k_pgs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&n, (const void *)k_pgs<T>, T, smem, 0);
+        return n;
+    }();
+    return v;
 }
 
 static bool ensure_warm(Workspace &ws) {
@@ -2245,7 +2263,7 @@ static void warm_store(Workspace &ws, cudaStream_t s) {
 // Sizes of the coloured solver's per-step buffers (host-known: capacities,
 // joints, blocks, the two-level sweep's partition).
 struct ColouredPlan {
-    int pgs_blocks, sx, sy, chunk_cap, ncb;
+    int pgs_blocks, sx, sy, chunk_cap, ncb, threads;
     bool slab;
     SlabCaps caps;
     size_t ngroups, wave_cap;
@@ -2253,7 +2271,8 @@ struct ColouredPlan {
 static ColouredPlan plan_coloured(const Workspace &ws, const SolverParams &P) {
     ColouredPlan c;
     c.pgs_blocks = P.pgs_blocks > 0 && P.pgs_blocks < num_sms() ? P.pgs_blocks : num_sms();
-    c.caps = slab_caps();
+    c.threads = P.pgs_threads == 128 ? 128 : GB_PGS_THREADS;
+    c.caps = slab_caps(c.threads);
     c.slab = P.pgs_two_level && c.pgs_blocks >= 2 && c.caps.rcap > 0;
     c.ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
     c.sx = 1;
@@ -2262,9 +2281,11 @@ static ColouredPlan plan_coloured(const Workspace &ws, const SolverParams &P) {
             if (c.pgs_blocks % d == 0) c.sx = d;
     c.sy = c.pgs_blocks / c.sx;
     c.ncb = GB_MAX_COLOURS * c.pgs_blocks;
-    c.chunk_cap = c.slab ? GB_SLAB_XCHUNK : GB_CHUNK_ROWS;
+    const int chunk = P.pgs_chunk > 0 ? (P.pgs_chunk < 64 ? 64 : (P.pgs_chunk > GB_CHUNK_ROWS ? GB_CHUNK_ROWS : P.pgs_chunk))
+                                      : GB_CHUNK_ROWS;
+    c.chunk_cap = c.slab ? GB_SLAB_XCHUNK : chunk;
     // waves: one per (colour, block) at least, plus one per T slots and per chunk_cap - 12 staged rows
-    c.wave_cap = 2 * (size_t)c.ncb + c.ngroups / GB_PGS_THREADS + (size_t)ws.row_cap / (c.chunk_cap - 12) + 16;
+    c.wave_cap = 2 * (size_t)c.ncb + c.ngroups / c.threads + (size_t)ws.row_cap / (c.chunk_cap - 12) + 16;
     return c;
 }
 
@@ -2272,7 +2293,7 @@ static bool ensure_coloured(Workspace &ws, int nb, const ColouredPlan &c) {
     if (!(ws.p_rows.ensure((size_t)ws.row_cap * 128) && ws.wv_count.ensure((size_t)c.ncb * 4) &&
           ws.wv_base.ensure((size_t)c.ncb * 4 + 4) && ws.chunk_rows.ensure(c.wave_cap * 4) &&
           ws.chunk_start.ensure(c.wave_cap * 4) && ws.wv_col.ensure(c.wave_cap * 4) &&
-          ws.wv_sched.ensure(c.wave_cap * GB_PGS_THREADS * 4)))
+          ws.wv_sched.ensure(c.wave_cap * c.threads * 4)))
         return false;
     if (!c.slab) return true;
     const size_t nbb = nb > 0 ? nb : 1, npc = (size_t)c.pgs_blocks * GB_SLAB_COLOURS;
@@ -2493,18 +2514,19 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     const int ncb = plan.ncb;
     const int chunk_cap = plan.chunk_cap;
     const size_t wave_cap = plan.wave_cap;
+    const int threads = plan.threads;
     {
         const int g1 = (ncb + 127) / 128;
         k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
-                                        ws.wv_count.as<int>(), pgs_blocks, chunk_cap);
+                                        ws.wv_count.as<int>(), pgs_blocks, chunk_cap, threads);
         scan_exclusive(ws.wv_count.as<int>(), ws.wv_base.as<int>(), nullptr, ncb, nullptr, ws, s);
         k_wave_total<<<1, 1, 0, s>>>(ws.dc, ws.wv_count.as<int>(), ws.wv_base.as<int>(), pgs_blocks);
         k_wave_fill<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                        ws.wv_count.as<int>(), ws.wv_base.as<int>(), ws.wv_sched.as<int>(),
                                        ws.chunk_rows.as<int>(), ws.wv_col.as<int>(), (int)wave_cap, pgs_blocks,
-                                       chunk_cap);
+                                       chunk_cap, threads);
         scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), &ws.dc->nwaves, (int)wave_cap, nullptr, ws, s);
-        k_pack_rows<<<grid, GB_PGS_THREADS, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
+        k_pack_rows<<<grid, threads, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                                     ws.wv_sched.as<int>(), ws.wv_col.as<int>(),
                                                     ws.chunk_start.as<int>(), ws.p_rows.as<float4>());
         count_launch(4);
@@ -2564,17 +2586,11 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.wcount = ws.wv_count.as<int>();
         A.wbase = ws.wv_base.as<int>();
         A.sched = ws.wv_sched.as<int>();
+        A.chunk_cap = chunk_cap;
         // one block per SM (the grid barrier's cost grows with the block count;
         // the chunk packing above assumes exactly pgs_blocks blocks)
-        const int threads = GB_PGS_THREADS;
-        const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;  // two chunk buffers, 200 KB
-        // the shared-memory opt-in and the occupancy query, once (thread-safe static initialisation)
-        static const int per_sm = [&]() {
-            cudaFuncSetAttribute((const void *)k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            int v = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&v, (const void *)k_pgs, threads, smem, 0);
-            return v;
-        }();
+        const size_t smem = (size_t)2 * chunk_cap * 128;  // two chunk buffers
+        const int per_sm = threads == 128 ? pgs_per_sm<128>() : pgs_per_sm<256>();
         if (per_sm < 1) return false;
         const int blocks = pgs_blocks;
         if (slab) {
@@ -2591,13 +2607,12 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             SA.chunk_cap = GB_SLAB_XCHUNK;
             SA.ipasses = P.pgs_two_level;
             void *args[] = {(void *)&SA};
-            if (cudaLaunchCooperativeKernel((const void *)k_pgs_slab, blocks, threads, args, caps.smem, s) !=
-                cudaSuccess)
-                return false;
+            const void *k = threads == 128 ? (const void *)k_pgs_slab<128> : (const void *)k_pgs_slab<256>;
+            if (cudaLaunchCooperativeKernel(k, blocks, threads, args, caps.smem, s) != cudaSuccess) return false;
         } else {
             void *args[] = {(void *)&A};
-            if (cudaLaunchCooperativeKernel((const void *)k_pgs, blocks, threads, args, smem, s) != cudaSuccess)
-                return false;
+            const void *k = threads == 128 ? (const void *)k_pgs<128> : (const void *)k_pgs<256>;
+            if (cudaLaunchCooperativeKernel(k, blocks, threads, args, smem, s) != cudaSuccess) return false;
         }
     }
     if (ev1) cudaEventRecord(ev1, s);

@@ -51,7 +51,8 @@ class dJointFeedback(ctypes.Structure):
 
 class gbodeTuning(ctypes.Structure):
     _fields_ = [("blocks", ctypes.c_int), ("passes", ctypes.c_int), ("check_every", ctypes.c_int),
-                ("ms_per_step", ctypes.c_float), ("candidates", ctypes.c_int)]
+                ("ms_per_step", ctypes.c_float), ("candidates", ctypes.c_int), ("threads", ctypes.c_int),
+                ("chunk_rows", ctypes.c_int), ("two_level", ctypes.c_int)]
 
 
 class gbodeStepStats(ctypes.Structure):
@@ -160,6 +161,8 @@ _PROTOS = [
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
     ("gbodeWorldSetTwoLevelSweep", None, [ID, ctypes.c_int]), ("gbodeWorldGetTwoLevelSweep", ctypes.c_int, [ID]),
     ("gbodeTestInject", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("gbodeWorldSetSolverTiles", None, [ID, ctypes.c_int, ctypes.c_int]),
+    ("gbodeWorldGetSolverTiles", None, [ID, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     ("gbodeSolveLCPBatch", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),

@@ -273,15 +273,22 @@ def test_autotune_keeps_a_candidate(gblib):
     twin.step_fused()
     assert np.array_equal(w.state(), twin.state())
     twin.close()
-    assert t.candidates == 12 and t.ms_per_step > 0
-    assert t.passes in (1, 2, 3) and t.check_every in (5, 10)
+    assert t.candidates == 14 and t.ms_per_step > 0
+    assert t.passes in (1, 2) and t.check_every in (5, 10)
+    assert t.threads in (128, 256) and t.chunk_rows in (400, 800) and t.two_level in (0, 2)
     assert L.gbodeWorldGetManifoldPasses(w.w) == t.passes
     assert L.gbodeWorldGetSolverBlocks(w.w) == t.blocks
+    assert L.gbodeWorldGetTwoLevelSweep(w.w) == t.two_level
+    import ctypes
+    th, ch = ctypes.c_int(0), ctypes.c_int(0)
+    L.gbodeWorldGetSolverTiles(w.w, ctypes.byref(th), ctypes.byref(ch))
+    assert (th.value, ch.value) == (t.threads, t.chunk_rows)
     for _ in range(20):
         w.step_graph()
     w.sync()
     assert w.stats().residual <= 1e-4
-    print(f"autotune: blocks {t.blocks}, passes {t.passes}, check every {t.check_every}, {t.ms_per_step:.3f} ms/step")
+    print(f"autotune: blocks {t.blocks}, passes {t.passes}, check every {t.check_every}, threads {t.threads}, "
+          f"staged rows {t.chunk_rows}, two-level {t.two_level}, {t.ms_per_step:.3f} ms/step")
     w.close()
 
 

@@ -342,6 +342,38 @@ def test_staging_waves_give_the_same_solution(gblib):
         w.close()
 
 
+@pytest.mark.parametrize("two_level", [0, 2])
+def test_solver_tiles_give_the_same_solution(gblib, two_level):
+    """gbodeWorldSetSolverTiles: 128 threads a block and 400 staged rows a
+    buffer instead of 256 and 800 cut every colour into other waves (more of
+    them, relaxed by other threads); a colour's manifolds share no body, so
+    the states after 150 steps of a 2,048-body pile are equal to the bit, with
+    the one-level and with the two-level sweep."""
+    from ode_gb300 import scenes, sim
+    import ctypes
+    L = gblib
+    sc = scenes.pile(2048, seed=7)
+    worlds = [sim.GBWorld(sc), sim.GBWorld(sc)]
+    L.gbodeWorldSetSolverTiles(worlds[1].w, 128, 400)
+    t, c = ctypes.c_int(0), ctypes.c_int(0)
+    L.gbodeWorldGetSolverTiles(worlds[1].w, ctypes.byref(t), ctypes.byref(c))
+    assert (t.value, c.value) == (128, 400)
+    for w in worlds:
+        L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.dWorldSetQuickStepNumIterations(w.w, 30)
+        L.gbodeWorldSetTwoLevelSweep(w.w, two_level)
+    for _ in range(150):
+        for w in worlds:
+            w.step_fused()
+    a, b = worlds[0].state(), worlds[1].state()
+    s0 = worlds[0].stats()
+    assert np.isfinite(a).all() and s0.rows > 10000
+    assert np.array_equal(a, b), float(np.abs(a - b).max())
+    for w in worlds:
+        w.close()
+
+
 def test_snapshot_reruns_the_same_steps(gblib):
     """gbodeWorldSaveSnapshot / gbodeWorldRestoreSnapshot: a 2,048-body pile
     with the warm-start cache on, 60 fused steps, a snapshot, 10 steps; the
