@@ -1294,41 +1294,96 @@ __device__ int cut_waves(const int4 *desc, int s0, int n, int b, int B, int chun
     return waves;
 }
 
-// pass 1, one thread per (colour, block): waves of each (at least one, so
+// The same greedy cut by one warp: the (colour, block)'s slots are taken 32
+// at a time, lane j holding slot b + (i + j) B.  With the state (slots t0 and
+// rows rows0 of the open wave) at the first unplaced lane p, a lane j >= p
+// opens a new wave iff t0 + (j - p) == T or rows0 + (rows of lanes p..j) >
+// chunk_cap -- the serial rule -- so the first such lane (a prefix sum and a
+// ballot) ends the open wave; the loop repeats from it with the state (0, 0).
+// `visit(wave, t, k, offset)` runs on each lane for its own slot; returns the
+// wave count (every lane).
+template <class F>
+__device__ int warp_cut_waves(const int4 *desc, int s0, int n, int b, int B, int chunk_cap, int T, F visit) {
+    const int lane = threadIdx.x & 31;
+    int waves = 0, t0 = T, rows0 = 0;  // t0 = T: the first slot opens a wave
+    for (int base = b; base < n; base += 32 * B) {
+        const int k = base + lane * B;
+        const bool have = k < n;
+        int4 d = make_int4(0, 0, 0, 0);
+        if (have) d = desc[s0 + k];
+        const int r = have && (d.y & GB_DESC_STAGED) ? desc_rows(d) : 0;
+        const int nl = min(32, (n - base + B - 1) / B);  // lanes holding a slot
+        int p = 0;
+        while (p < nl) {
+            // inclusive prefix of the rows of lanes p..j
+            int x = lane >= p ? r : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            const bool brk = lane >= p && lane < nl && (t0 + (lane - p) >= T || rows0 + x > chunk_cap);
+            const unsigned m = __ballot_sync(0xffffffffu, brk);
+            const int q = m ? __ffs(m) - 1 : nl;  // lanes p..q-1 join the open wave
+            if (lane >= p && lane < q) visit(waves - 1, t0 + (lane - p), k, r > 0 ? rows0 + x - r : -1);
+            const int xq = __shfl_sync(0xffffffffu, x, (q > 0 ? q : 1) - 1);  // rows of lanes p..q-1
+            if (q < nl) {
+                ++waves;  // lane q opens a new wave
+                t0 = 0;
+                rows0 = 0;
+            } else {
+                t0 += q - p;
+                rows0 += q > p ? xq : 0;
+            }
+            p = q;
+        }
+    }
+    return waves;
+}
+
+// pass 1, one warp per (colour, block): waves of each (at least one, so
 // every block takes part in every colour's barrier)
 __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCounters *dc, const int4 *desc,
                              int *wcount, int B, int chunk_cap, int T) {
-    const int cb = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cb = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
-    if (c >= dc->ncolours) { wcount[cb] = 0; return; }
-    const int w = cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, T, [](int, int, int, int) {});
-    wcount[cb] = w > 0 ? w : 1;
+    if (c >= dc->ncolours) {
+        if ((threadIdx.x & 31) == 0) wcount[cb] = 0;
+        return;
+    }
+    const int w = warp_cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, T, [](int, int, int, int) {});
+    if ((threadIdx.x & 31) == 0) wcount[cb] = w > 0 ? w : 1;
 }
 
-// pass 2: the chunk offsets in the descriptors, the schedule, rows per wave
+// pass 2, one warp per (colour, block): the chunk offsets in the
+// descriptors, the schedule, rows per wave
 __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, const int *wcount,
                             const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B,
                             int chunk_cap, int T) {
-    const int cb = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cb = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
     if (c >= dc->ncolours) return;
     const int base = wbase[cb], nw = wcount[cb];
-    if (base + nw > wave_cap) { atomicOr(&dc->err, ERR_ROW_OVERFLOW); return; }
-    for (int w = 0; w < nw; w++) {
+    if (base + nw > wave_cap) {
+        if (lane == 0) atomicOr(&dc->err, ERR_ROW_OVERFLOW);
+        return;
+    }
+    for (int w = lane; w < nw; w += 32) {
         wrows[base + w] = 0;
         wcol[base + w] = c;
-        for (int t = 0; t < T; t++) sched[(size_t)(base + w) * T + t] = -1;
     }
+    for (int i = lane; i < nw * T; i += 32) sched[(size_t)base * T + i] = -1;
+    __syncwarp();
     const int s0 = cstart[c];
-    cut_waves(desc, s0, ccount[c], b, B, chunk_cap, T, [&](int w, int t, int k, int off) {
+    warp_cut_waves(desc, s0, ccount[c], b, B, chunk_cap, T, [&](int w, int t, int k, int off) {
         sched[(size_t)(base + w) * T + t] = k;
         if (off >= 0) {
             int4 d = desc[s0 + k];
             d.y = (d.y & ~(0xfff << 16)) | (off << 16);
             desc[s0 + k] = d;
-            wrows[base + w] = off + desc_rows(d);
+            atomicMax(&wrows[base + w], off + desc_rows(d));
         }
     });
 }
@@ -2516,7 +2571,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     const size_t wave_cap = plan.wave_cap;
     const int threads = plan.threads;
     {
-        const int g1 = (ncb + 127) / 128;
+        const int g1 = (ncb * 32 + 127) / 128;  // a warp per (colour, block)
         k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                         ws.wv_count.as<int>(), pgs_blocks, chunk_cap, threads);
         scan_exclusive(ws.wv_count.as<int>(), ws.wv_base.as<int>(), nullptr, ncb, nullptr, ws, s);
