@@ -993,19 +993,41 @@ __global__ void k_colour(const int2 *gbody, DevCounters *dc, unsigned long long 
     }
 }
 
+// Colour lists: counts per colour, then every group placed in its colour's
+// list.  Each block first counts its chunk of groups in shared memory and
+// then touches each colour's global counter once (thousands of groups share a
+// colour: one global atomic each would serialise on a few addresses).  The
+// order inside a colour is free (its groups share no body).
 __global__ void k_colour_count(const int *colour, DevCounters *dc, int *ccount) {
-    int nm = dc->nmanifolds;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nm; e += gridDim.x * blockDim.x) {
-        int c = colour[e];
-        if (c >= 0) atomicAdd(&ccount[c], 1);
+    __shared__ int h[GB_MAX_COLOURS];
+    const int nm = dc->nmanifolds;
+    for (int base = blockIdx.x * blockDim.x; base < nm; base += gridDim.x * blockDim.x) {
+        for (int c = threadIdx.x; c < GB_MAX_COLOURS; c += blockDim.x) h[c] = 0;
+        __syncthreads();
+        const int e = base + threadIdx.x;
+        const int c = e < nm ? colour[e] : -1;
+        if (c >= 0) atomicAdd(&h[c], 1);
+        __syncthreads();
+        for (int k = threadIdx.x; k < GB_MAX_COLOURS; k += blockDim.x)
+            if (h[k]) atomicAdd(&ccount[k], h[k]);
+        __syncthreads();
     }
 }
 __global__ void k_colour_fill(const int *colour, DevCounters *dc, const int *cstart, int *cfill, int *list) {
-    int nm = dc->nmanifolds;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nm; e += gridDim.x * blockDim.x) {
-        int c = colour[e];
-        if (c < 0) continue;
-        list[cstart[c] + atomicAdd(&cfill[c], 1)] = e;
+    __shared__ int h[GB_MAX_COLOURS], at[GB_MAX_COLOURS];
+    const int nm = dc->nmanifolds;
+    for (int base = blockIdx.x * blockDim.x; base < nm; base += gridDim.x * blockDim.x) {
+        for (int c = threadIdx.x; c < GB_MAX_COLOURS; c += blockDim.x) h[c] = 0;
+        __syncthreads();
+        const int e = base + threadIdx.x;
+        const int c = e < nm ? colour[e] : -1;
+        const int rank = c >= 0 ? atomicAdd(&h[c], 1) : 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < GB_MAX_COLOURS; k += blockDim.x)
+            if (h[k]) at[k] = cstart[k] + atomicAdd(&cfill[k], h[k]);
+        __syncthreads();
+        if (c >= 0) list[at[c] + rank] = e;
+        __syncthreads();
     }
 }
 

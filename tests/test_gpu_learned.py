@@ -125,3 +125,60 @@ def test_learned_start_is_residual_judged(gblib):
         assert w.stats().residual <= 1e-4
     print(f"learned start chosen in {used} of 5 steps; last residuals mlp {st[1]:.3g} plain {st[2]:.3g}")
     w.close()
+
+
+# measured on the held-out pile below (one GB300): plain 368.8 mean sweeps to
+# the target, learned 332.5 (9.8 % fewer; the network's start chosen in 75 % of
+# the steps); the test asks for at least GAIN_MIN
+GAIN_MIN = 0.05
+
+
+def test_committed_network_gains_on_a_held_out_pile(gblib):
+    """What the trained network (ode_gb300/data/warmstart_mlp.npz) gains over
+    the method without it: an 8,192-body pile of a seed no training scene
+    used (7; training used 101-104, 102 and box stacks 100-115; the benchmark
+    seed 1), settled, saved (gbodeWorldSaveSnapshot); 12 steps to LCP residual
+    1e-4 with the plain previous-step start, the snapshot restored, the same
+    12 steps with the learned start (the plain start stays the fallback each
+    step).  Every step reaches the target either way; the learned start cuts
+    the mean sweeps by at least GAIN_MIN."""
+    from ode_gb300 import learned, scenes, sim
+    L = gblib
+    sc = scenes.pile(8192, seed=7)
+    w = sim.GBWorld(sc)
+    L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+    L.dWorldSetQuickStepW(w.w, 1.0)
+    L.gbodeWorldSetTwoLevelSweep(w.w, 2)
+    L.dWorldSetQuickStepNumIterations(w.w, 30)
+    for _ in range(600):
+        w.step_fused()
+    L.gbodeWorldSetResidualTarget(w.w, 1e-4, 5, 3000)
+    for _ in range(3):
+        w.step_fused()
+    w.sync()
+    assert L.gbodeWorldSaveSnapshot(w.w) == 1, L.gbodeGetLastError()
+    params = learned.load()
+    sweeps = {}
+    chosen = []
+    st = np.zeros(3, np.float32)
+    for mode in ("plain", "learned"):
+        assert L.gbodeWorldRestoreSnapshot(w.w) == 1
+        if mode == "learned":
+            assert L.gbodeWorldSetLearnedWarmStart(w.w, fp(params), 1) == 1
+        sweeps[mode] = []
+        for _ in range(12):
+            w.step_fused()
+            w.sync()
+            s = w.stats()
+            assert s.residual <= 1e-4
+            sweeps[mode].append(s.iterations)
+            if mode == "learned":
+                L.gbodeWorldGetLearnedStats(w.w, st.ctypes.data_as(F))
+                chosen.append(float(st[0]))
+    L.gbodeWorldSetLearnedWarmStart(w.w, None, 0)
+    p, q = float(np.mean(sweeps["plain"])), float(np.mean(sweeps["learned"]))
+    gain = 1.0 - q / p
+    print(f"held-out pile8192: mean sweeps to 1e-4 plain {p:.1f}, learned {q:.1f} (gain {gain:.1%}, "
+          f"network's start chosen in {np.mean(chosen):.0%} of the steps)")
+    assert gain >= GAIN_MIN, (p, q)
+    w.close()
