@@ -376,8 +376,8 @@ def run_gbode(args, ws, rank, local):
     if not args.no_e2e:
         restore_snapshot(L, w)
         host = w.state()
-        h2d = 240 * sc.nb   # pos, q, R, lvel, avel, facc, tacc, I, invI as uploaded by the library
-        d2h = 112 * sc.nb   # pos, q, R, lvel, avel as downloaded
+        h2d = 112 * sc.nb   # pos, q, R, lvel, avel (gbodeWorldSetState's pinned upload)
+        d2h = 112 * sc.nb   # pos, q, R, lvel, avel (gbodeWorldGetState's pinned download)
         n_ok, t0 = 0, time.perf_counter()
         for _ in range(args.steps):
             w.set_state(host)

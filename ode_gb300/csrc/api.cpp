@@ -211,7 +211,28 @@ struct dxWorld {
     int last_host_contacts = 0;
     std::vector<dxJoint *> table_joints;  // the ball/hinge/hinge2 joints in device-table order
     struct DevSnapshot *snapshot = nullptr;  // gbodeWorldSaveSnapshot
+    // pinned staging of the bulk state calls (pos, q, R rows, lvel, avel: 112 B a body)
+    float4 *stage_up = nullptr, *stage_down = nullptr;
+    size_t stage_up_n = 0, stage_down_n = 0;  // bodies each holds
+    cudaEvent_t stage_up_done = nullptr;      // the last upload from stage_up has been copied
 };
+
+// Pinned staging for n bodies (112 B each); false when it cannot be allocated
+// (the callers then take the path through the body records).
+static bool stage_ensure(float4 *&p, size_t &cap, size_t n, cudaEvent_t pending) {
+    if (cap >= n && p) return true;
+    if (pending) cudaEventSynchronize(pending);
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, 112 * (n > 0 ? n : 1)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        p = nullptr;
+        return false;
+    }
+    cap = n;
+    return true;
+}
 
 // A copy of a world's device-side simulation state: bodies, the warm-start
 // tables, the joints' multipliers, the auto-disable state and the counters.
@@ -711,6 +732,9 @@ void dWorldDestroy(dWorldID w) {
     drop_graph(w);
     if (w->snapshot) { w->snapshot->release(); delete w->snapshot; }
     for (int i = 0; i < 4; i++) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
+    if (w->stage_up_done) { cudaEventSynchronize(w->stage_up_done); cudaEventDestroy(w->stage_up_done); }
+    if (w->stage_up) cudaFreeHost(w->stage_up);
+    if (w->stage_down) cudaFreeHost(w->stage_down);
     w->ws.release();
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
     for (size_t k = 0; k < g_worlds.size(); k++) if (g_worlds[k] == w) { g_worlds.erase(g_worlds.begin() + k); break; }
@@ -1017,7 +1041,37 @@ int dBodyGetNumJoints(dBodyID b) {
 }
 
 int gbodeWorldGetBodyCount(dWorldID w) { return (int)w->bodies.size(); }
+// Bulk state.  While the device holds the state (after a step), Get copies
+// pos, q, R, lvel and avel straight from the device into the caller's array
+// through a pinned staging buffer and leaves the body records alone; Set packs
+// the caller's array into pinned staging and copies it to the device
+// asynchronously, the body records then read from the device when next
+// needed.  Where staging cannot be allocated, both go through the records.
 void gbodeWorldGetState(dWorldID w, float *out) {
+    const size_t nb = w->bodies.size();
+    if (!w->host_valid && nb > 0 && stage_ensure(w->stage_down, w->stage_down_n, nb, nullptr)) {
+        float4 *pos = w->stage_down, *q = pos + nb, *R = q + nb, *lv = R + 3 * nb, *av = lv + nb;
+        cudaStream_t s = w->stream;
+        cudaMemcpyAsync(pos, w->ws.b_pos.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(q, w->ws.b_q.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(R, w->ws.b_R.p, 48 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(lv, w->ws.b_lvel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(av, w->ws.b_avel.p, 16 * nb, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { set_error("gbodeWorldGetState", e); return; }
+        for (size_t i = 0; i < nb; i++) {
+            float *o = out + 25 * i;
+            o[0] = pos[i].x; o[1] = pos[i].y; o[2] = pos[i].z;
+            o[3] = q[i].x; o[4] = q[i].y; o[5] = q[i].z; o[6] = q[i].w;
+            for (int r = 0; r < 3; r++) {
+                const float4 v = R[3 * i + r];
+                o[7 + 4 * r] = v.x; o[8 + 4 * r] = v.y; o[9 + 4 * r] = v.z; o[10 + 4 * r] = 0.f;
+            }
+            o[19] = lv[i].x; o[20] = lv[i].y; o[21] = lv[i].z;
+            o[22] = av[i].x; o[23] = av[i].y; o[24] = av[i].z;
+        }
+        return;
+    }
     world_download(w);
     for (size_t i = 0; i < w->bodies.size(); i++) {
         dxBody *b = w->bodies[i];
@@ -1027,6 +1081,37 @@ void gbodeWorldGetState(dWorldID w, float *out) {
     }
 }
 void gbodeWorldSetState(dWorldID w, const float *in) {
+    const size_t nb = w->bodies.size();
+    // the direct path: every other host change is on the device first
+    if (nb > 0 && world_upload(w)) {
+        if (!w->stage_up_done && cudaEventCreateWithFlags(&w->stage_up_done, cudaEventDisableTiming) != cudaSuccess)
+            w->stage_up_done = nullptr;
+        if (w->stage_up_done && stage_ensure(w->stage_up, w->stage_up_n, nb, w->stage_up_done)) {
+            cudaEventSynchronize(w->stage_up_done);  // the previous upload has left the staging buffer
+            float4 *pos = w->stage_up, *q = pos + nb, *R = q + nb, *lv = R + 3 * nb, *av = lv + nb;
+            for (size_t i = 0; i < nb; i++) {
+                const dxBody *b = w->bodies[i];
+                const float *o = in + 25 * i;
+                pos[i] = make_float4(o[0], o[1], o[2], b->invMass);
+                q[i] = make_float4(o[3], o[4], o[5], o[6]);
+                for (int r = 0; r < 3; r++) R[3 * i + r] = make_float4(o[7 + 4 * r], o[8 + 4 * r], o[9 + 4 * r], 0.f);
+                lv[i] = make_float4(o[19], o[20], o[21], b->mass.mass);
+                const int flags = b->gyro ? 1 : 0;
+                float ff;
+                memcpy(&ff, &flags, 4);
+                av[i] = make_float4(o[22], o[23], o[24], ff);
+            }
+            cudaStream_t s = w->stream;
+            cudaMemcpyAsync(w->ws.b_pos.p, pos, 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_q.p, q, 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_R.p, R, 48 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_lvel.p, lv, 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(w->ws.b_avel.p, av, 16 * nb, cudaMemcpyHostToDevice, s);
+            cudaEventRecord(w->stage_up_done, s);
+            w->host_valid = false;  // the records read the new state from the device when next needed
+            return;
+        }
+    }
     world_download(w);
     for (size_t i = 0; i < w->bodies.size(); i++) {
         dxBody *b = w->bodies[i];
