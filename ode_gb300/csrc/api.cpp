@@ -79,7 +79,7 @@ void Workspace::release() {
                    &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &wv_count, &wv_base, &wv_col, &wv_sched, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &d_off, &d_scr, &d_iscr, &d_rloc, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp, &s_bw, &s_part, &s_blocal, &s_pbcount,
                    &s_pbody, &s_prow, &s_pgrp, &s_gpart, &s_gdesc, &s_pccount, &s_pcstart, &s_pcfill, &s_ilist,
-                   &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart};
+                   &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart, &n_perm, &n_key};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
     if (hc) cudaFreeHost(hc);

@@ -20,6 +20,7 @@
 
 #include "colliders.cuh"
 #include "gbode_internal.h"
+#include "../../include/gbode.h"
 
 namespace gb {
 
@@ -305,11 +306,71 @@ __device__ __forceinline__ bool jointed(const unsigned long long *keys, unsigned
     return false;
 }
 
+// Class-sorted batches.  The broad phase emits pairs in hash order, so the
+// 32 lanes of a warp would meet several colliders and run them one after
+// another.  The pairs are instead visited through a permutation that groups
+// them by collider class (class of g1, class of g2; the pairs the narrow phase
+// rejects form a 17th group): a warp then takes a batch of 32 pairs of one
+// class.  Each pair still writes its own slots, so the contacts, their order
+// and every result are as before; the order inside a class is free.
+#define GB_PAIR_KEYS 17
+__device__ __forceinline__ int class_slot(int c) { return c == dPlaneClass ? 3 : (c >= 0 && c < 3 ? c : 3); }
+__device__ __forceinline__ int pair_key(const Geoms &G, int2 pr, int skip_static, const unsigned long long *jkeys,
+                                        unsigned jmask) {
+    const int a = pr.x, b = pr.y;
+    const int ba = G.body[a], bb = G.body[b];
+    if (a == b || (ba == bb && ba >= 0) || (skip_static && ba < 0 && bb < 0) || jointed(jkeys, jmask, ba, bb))
+        return GB_PAIR_KEYS - 1;
+    return class_slot(G.cls[a]) * 4 + class_slot(G.cls[b]);
+}
+
+// counts per class key (a shared histogram per block, then the global counters)
+__global__ void k_pair_count(Geoms G, const int2 *pairs, const int *npairs_dev, int skip_static,
+                             const unsigned long long *jkeys, unsigned jmask, int *kcount) {
+    __shared__ int h[GB_PAIR_KEYS];
+    const int np = *npairs_dev;
+    for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+        if (threadIdx.x < GB_PAIR_KEYS) h[threadIdx.x] = 0;
+        __syncthreads();
+        const int p = base + threadIdx.x;
+        if (p < np) atomicAdd(&h[pair_key(G, pairs[p], skip_static, jkeys, jmask)], 1);
+        __syncthreads();
+        if (threadIdx.x < GB_PAIR_KEYS && h[threadIdx.x]) atomicAdd(&kcount[threadIdx.x], h[threadIdx.x]);
+        __syncthreads();
+    }
+}
+
+// perm: the pairs grouped by class key (kfill: zeroed positions per key)
+__global__ void k_pair_order(Geoms G, const int2 *pairs, const int *npairs_dev, int skip_static,
+                             const unsigned long long *jkeys, unsigned jmask, const int *kcount, int *kfill,
+                             int *perm) {
+    __shared__ int h[GB_PAIR_KEYS], at[GB_PAIR_KEYS], start[GB_PAIR_KEYS];
+    const int np = *npairs_dev;
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < GB_PAIR_KEYS; k++) { start[k] = acc; acc += kcount[k]; }
+    }
+    for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+        if (threadIdx.x < GB_PAIR_KEYS) h[threadIdx.x] = 0;
+        __syncthreads();
+        const int p = base + threadIdx.x;
+        const int key = p < np ? pair_key(G, pairs[p], skip_static, jkeys, jmask) : -1;
+        const int rank = key >= 0 ? atomicAdd(&h[key], 1) : 0;
+        __syncthreads();
+        if (threadIdx.x < GB_PAIR_KEYS && h[threadIdx.x])
+            at[threadIdx.x] = start[threadIdx.x] + atomicAdd(&kfill[threadIdx.x], h[threadIdx.x]);
+        __syncthreads();
+        if (key >= 0) perm[at[key] + rank] = p;
+        __syncthreads();
+    }
+}
+
 __global__ void k_narrow(Geoms G, const int2 *pairs, const int *npairs_dev, int np_host, int maxc, int surf,
                          Contact *slots, int *ccount, int *codes, int skip_static, const unsigned long long *jkeys,
-                         unsigned jmask) {
+                         unsigned jmask, const int *perm) {
     const int np = npairs_dev ? *npairs_dev : np_host;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int p = perm ? perm[i] : i;
         int2 pr = pairs[p];
         int a = pr.x, b = pr.y;
         int n = 0, code = -1;
@@ -470,12 +531,21 @@ static bool ensure_contact_buffers(Workspace &ws, int pair_cap, int extra) {
 
 bool launch_narrowphase(Workspace &ws, int maxc, int surf, bool append, cudaStream_t s) {
     if (!ensure_contact_buffers(ws, ws.pair_cap, 0)) return false;
+    if (!(ws.n_perm.ensure((size_t)(ws.pair_cap > 0 ? ws.pair_cap : 1) * 4) && ws.n_key.ensure(2 * GB_PAIR_KEYS * 4)))
+        return false;
     Geoms G = geoms_view(ws, 0);
     int grid = 4 * num_sms();
     if (maxc > 8) maxc = 8;
+    const unsigned long long *jk = ws.njoints > 0 ? ws.j_pairs.as<unsigned long long>() : nullptr;
+    int *kcount = ws.n_key.as<int>(), *kfill = kcount + GB_PAIR_KEYS;
+    cudaMemsetAsync(kcount, 0, 2 * GB_PAIR_KEYS * 4, s);
+    k_pair_count<<<grid, 256, 0, s>>>(G, ws.pairs.as<int2>(), &ws.dc->npairs, 1, jk, ws.j_pair_mask, kcount);
+    k_pair_order<<<grid, 256, 0, s>>>(G, ws.pairs.as<int2>(), &ws.dc->npairs, 1, jk, ws.j_pair_mask, kcount, kfill,
+                                      ws.n_perm.as<int>());
     k_narrow<<<grid, 128, 0, s>>>(G, ws.pairs.as<int2>(), &ws.dc->npairs, 0, maxc, surf, ws.c_slots.as<Contact>(),
-                                  ws.c_count.as<int>(), ws.c_code.as<int>(), 1,
-                                  ws.njoints > 0 ? ws.j_pairs.as<unsigned long long>() : nullptr, ws.j_pair_mask);
+                                  ws.c_count.as<int>(), ws.c_code.as<int>(), 1, jk, ws.j_pair_mask,
+                                  ws.n_perm.as<int>());
+    count_launch(2);
     scan_exclusive(ws.c_count.as<int>(), ws.c_start.as<int>(), &ws.dc->npairs, ws.pair_cap, &ws.dc->narrow_total, ws, s);
     // the base offset when appending is read on the host only in the compat
     // path; the fused path always starts from an empty contact list
@@ -507,7 +577,7 @@ int narrow_pairs_host(Workspace &ws, const int *pairs, int np, int maxc, std::ve
     Geoms G = geoms_view(ws, 0);
     if (maxc > 8) maxc = 8;
     k_narrow<<<grid_for(np, 128), 128, 0, s>>>(G, ws.pairs.as<int2>(), nullptr, np, maxc, 0, ws.c_slots.as<Contact>(),
-                                               ws.c_count.as<int>(), ws.c_code.as<int>(), 0, nullptr, 0u);
+                                               ws.c_count.as<int>(), ws.c_code.as<int>(), 0, nullptr, 0u, nullptr);
     count_launch();
     counts.resize(np);
     std::vector<Contact> slots((size_t)np * 8);

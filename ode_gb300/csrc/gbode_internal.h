@@ -101,6 +101,7 @@ struct Workspace {
     DBuf h_keys, h_count, h_start, h_fill, h_members, h_entry, p_count, p_start, pairs;
     // narrow phase
     DBuf c_slots, c_count, c_start, contacts, surfaces, c_mcount, c_rstart, c_code;
+    DBuf n_perm, n_key;  // narrow phase: pairs grouped by collider class, counts and fills per class
     // bodies
     DBuf b_pos, b_q, b_R, b_lvel, b_avel, b_facc, b_tacc, b_Ib, b_invIb, b_invIw, b_fc, b_rt, b_fa;
     DBuf b_damp, b_maxw;  // damping (scales, squared thresholds), angular speed cap
