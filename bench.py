@@ -63,7 +63,12 @@ def parse():
     ap.add_argument("--n", type=int, default=32768)
     ap.add_argument("--settle", type=int, default=900)
     ap.add_argument("--target", type=float, default=1e-4)
-    ap.add_argument("--check-every", type=int, default=5)
+    ap.add_argument("--check-every", type=int, default=5,
+                    help="residual checks at least this many sweeps apart (every this many with --checks fixed)")
+    ap.add_argument("--checks", choices=("predicted", "fixed"), default="predicted",
+                    help="residual-check schedule (gbodeWorldSetResidualChecks)")
+    ap.add_argument("--reform-every", type=int, default=0,
+                    help="sweeps between re-formed body accumulators (0: the library's default, 500)")
     ap.add_argument("--sor-w", type=float, default=1.0,
                     help="SOR relaxation W (dWorldSetQuickStepW); the reference's default 1.3 stalls when warm-started")
     ap.add_argument("--max-iters", type=int, default=3000)
@@ -83,6 +88,9 @@ def parse():
     ap.add_argument("--two-level", type=int, default=2,
                     help="two-level sweep of the pile's solver with this many interior phases a sweep "
                          "(gbodeWorldSetTwoLevelSweep; 0: off)")
+    ap.add_argument("--sweep-sync", choices=("neighbours", "grid"), default="neighbours",
+                    help="two-level sweep: blocks wait on the blocks sharing their bodies, or on a grid barrier "
+                         "after every step (gbodeWorldSetSweepSync)")
     ap.add_argument("--from-settled", action="store_true",
                     help="start the pile from ode_gb300/data/pile32768_settled.npz instead of settling (profiling)")
     ap.add_argument("--ref-sweeps", type=int, default=1500,
@@ -321,7 +329,10 @@ def run_gbode(args, ws, rank, local):
             w.step_fused()
     w.sync()
     L.gbodeWorldSetResidualTarget(w.w, args.target, args.check_every, args.max_iters)
+    L.gbodeWorldSetResidualChecks(w.w, ode.GBODE_CHECKS_FIXED if args.checks == "fixed" else ode.GBODE_CHECKS_PREDICTED,
+                                  args.reform_every)
     L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
+    L.gbodeWorldSetSweepSync(w.w, ode.GBODE_SYNC_GRID if args.sweep_sync == "grid" else ode.GBODE_SYNC_NEIGHBOURS)
     L.gbodeWorldSetTiming(w.w, 1)
     if args.profile_steps:
         for _ in range(args.profile_steps):
@@ -365,7 +376,7 @@ def run_gbode(args, ws, rank, local):
     # roofline of the dominant kernel (the persistent PGS sweep kernel): every
     # row relaxation counts B_ROW, the interior rows of the two-level sweep once
     # per interior phase
-    checks = [int(np.ceil(s / args.check_every)) for s in sweeps]
+    checks = T["checks"]
     extra = max(0, args.two_level - 1)
     pgs_bytes = sum(s * (m + extra * mi) * B_ROW + c * m * B_ROW_CHECK
                     for s, m, mi, c in zip(sweeps, rows, T["interior_rows"], checks))
@@ -414,10 +425,14 @@ def run_gbode(args, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"pile{sc.nb}", "bodies": sc.nb, "dt": sc.dt, "mu": sc.mu, "maxc": sc.maxc,
                    "settle_steps": args.settle, "residual_target": args.target, "check_every": args.check_every,
+                   "checks": (f"predicted (half the predicted distance, {args.check_every}-64 sweeps apart)"
+                              if args.checks == "predicted" else f"every {args.check_every} sweeps"),
+                   "checks_per_step": float(np.mean(T["checks"])),
                    "max_sweeps": args.max_iters, "l2": "256 MB flush before every timed step (outside the events)",
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
                    "solver": f"coloured PGS (W {args.sor_w}), persistent cooperative kernel"
-                             + (f", two-level sweep ({args.two_level} interior phases a sweep)"
+                             + (f", two-level sweep ({args.two_level} interior phases a sweep, "
+                                + ("neighbour waits" if min(T["neighbour_waits"]) else "grid barriers") + ")"
                                 if args.two_level else ""),
                    "interior_rows_per_step": float(np.mean(T["interior_rows"])),
                    "interior_colours": int(np.median(T["interior_colours"])),
@@ -571,12 +586,18 @@ def learned_batched(args, L, w, stream, flush, nb):
             "mlp_start_chosen": float(np.mean(chosen)), "weights": os.path.relpath(path, ROOT)}
 
 
+def ode_f32p():
+    import ctypes as C
+    return C.POINTER(C.c_float)
+
+
 def timed_steps(w, stream, flush, steps, graph=False):
     """`steps` fused steps, each bracketed by CUDA events on the world's stream
     (L2 flushed before each, outside the events); per-step statistics."""
     import torch
     out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours",
-                           "interior_rows", "interior_colours")}
+                           "interior_rows", "interior_colours", "neighbour_waits", "checks")}
+    hist = np.zeros(256, np.float32)
     torch.cuda.nvtx.range_push("timed")
     for _ in range(steps):
         with torch.cuda.stream(stream):
@@ -600,6 +621,8 @@ def timed_steps(w, stream, flush, steps, graph=False):
         out["colours"].append(st.colours)
         out["interior_rows"].append(st.interior_rows)
         out["interior_colours"].append(st.interior_colours)
+        out["neighbour_waits"].append(st.neighbour_waits)
+        out["checks"].append(w.L.gbodeWorldGetResidualHistory(w.w, hist.ctypes.data_as(ode_f32p()), 256))
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     return out

@@ -365,9 +365,22 @@ void gbodeWorldSetSolver(dWorldID w, int solver);
 int gbodeWorldGetSolver(dWorldID w);
 
 /* Iterate until the LCP residual (projected natural map, FP32, relative to
- * max(1, max|lambda|)) is <= target, checking every check_every iterations,
- * up to max_iterations.  target <= 0 restores the fixed iteration count. */
+ * max(1, max|lambda|)) is <= target, checking at least check_every
+ * iterations apart (see gbodeWorldSetResidualChecks), up to max_iterations.
+ * target <= 0 restores the fixed iteration count. */
 void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int max_iterations);
+
+/* When residual-target mode checks.  GBODE_CHECKS_PREDICTED (the default):
+ * from the last two checks' residuals the sweeps still needed are predicted
+ * (geometric decay) and the next check comes after half of them -- at least
+ * check_every, at most 64 sweeps later; check_every sweeps after a check
+ * whose residual did not fall.  GBODE_CHECKS_FIXED: every check_every sweeps.
+ * Either way the body accumulators are re-formed from the multipliers every
+ * reform_every sweeps (<= 0: 500) and before the check that ends the solve,
+ * so that check's residual is the multipliers' own. */
+#define GBODE_CHECKS_PREDICTED 0
+#define GBODE_CHECKS_FIXED 1
+void gbodeWorldSetResidualChecks(dWorldID w, int mode, int reform_every);
 
 /* Warm start: 0 = cold (lambda = 0, the reference default), 1 = previous-step
  * lambda of the same (geom pair, contact slot) scaled by `scale`. */
@@ -407,6 +420,18 @@ void gbodeWorldGetSolverTiles(dWorldID w, int *threads, int *chunk_rows);
  * fall back to the global colours. */
 void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases);
 int gbodeWorldGetTwoLevelSweep(dWorldID w);
+
+/* How the two-level sweep orders the blocks' steps (the interior phase, then
+ * each crossing colour).  GBODE_SYNC_NEIGHBOURS (the default): a crossing
+ * manifold is relaxed by the block whose column holds its first body, and a
+ * block waits only for the blocks that touch one of the same bodies to finish
+ * the previous step (nothing, in a colour where it has no manifold).
+ * GBODE_SYNC_GRID: a grid barrier after every step.  Both give the same
+ * multipliers and bodies to the bit. */
+#define GBODE_SYNC_NEIGHBOURS 0
+#define GBODE_SYNC_GRID 1
+void gbodeWorldSetSweepSync(dWorldID w, int mode);
+int gbodeWorldGetSweepSync(dWorldID w);
 
 /* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
  * creation without leaving the device.  Equivalent to dSpaceCollide with a near
@@ -473,6 +498,8 @@ typedef struct gbodeStepStats {
     int sleeping;          /* bodies not stepped: their component is disabled (auto-disable) */
     int interior_colours;  /* two-level sweep: colours of the columns' interior manifolds (0: off) */
     int interior_rows;     /* two-level sweep: rows relaxed from shared memory (0: off) */
+    int neighbour_waits;   /* two-level sweep: the blocks waited only on their neighbours (1), or on grid
+                              barriers (0: GBODE_SYNC_GRID, or a body touched by too many blocks) */
 } gbodeStepStats;
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */

@@ -79,7 +79,8 @@ void Workspace::release() {
                    &col_fill, &col_list, &m_desc, &p_rows, &chunk_rows, &chunk_start, &wv_count, &wv_base, &wv_col, &wv_sched, &l_feat, &l_scale, &l_pred, &l_alt, &mlp_P, &mlp_wb, &j_info, &j_a1, &j_a2, &j_x1, &j_x2, &j_qrel, &j_l0, &j_l1, &j_l2, &j_m, &j_rstart, &j_limit, &j_lerr, &j_lam, &grp_body, &j_pairs, &b_damp, &b_maxw, &b_adis_i, &b_adis_f, &b_adis_buf, &b_touch, &b_parent, &b_awake, &b_asleep, &c_keep, &c_kpos, &c_awake, &c_orig, &j_v1, &j_v2, &j_m0, &j_m1, &j_m2, &i_order, &i_start, &i_bodies, &i_bstart, &i_normals, &d_off, &d_scr, &d_iscr, &d_rloc, &w_keys, &w_lambda,
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp, &s_bw, &s_part, &s_blocal, &s_pbcount,
                    &s_pbody, &s_prow, &s_pgrp, &s_gpart, &s_gdesc, &s_pccount, &s_pcstart, &s_pcfill, &s_ilist,
-                   &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart, &n_perm, &n_key};
+                   &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart, &n_perm, &n_key, &x_cnt,
+                   &x_start, &x_fill, &x_accn, &x_acc, &x_adj, &x_prog};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
     if (hc) cudaFreeHost(hc);
@@ -773,6 +774,10 @@ void gbodeWorldSetResidualTarget(dWorldID w, dReal target, int check_every, int 
     w->P.check_every = check_every > 0 ? check_every : 10;
     w->P.max_iterations = max_iterations;
 }
+void gbodeWorldSetResidualChecks(dWorldID w, int mode, int reform_every) {
+    w->P.fixed_checks = mode == GBODE_CHECKS_FIXED ? 1 : 0;
+    w->P.reform_every = reform_every > 0 ? reform_every : 0;
+}
 void gbodeWorldSetWarmStart(dWorldID w, int mode, dReal scale) { w->P.warm_mode = mode; w->P.warm_scale = scale; }
 void gbodeWorldSetSolverBlocks(dWorldID w, int blocks) { w->P.pgs_blocks = blocks > 0 ? blocks : 0; }
 void gbodeWorldSetManifoldPasses(dWorldID w, int passes) { w->P.pgs_passes = passes > 1 ? (passes > 16 ? 16 : passes) : 1; }
@@ -789,6 +794,8 @@ void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases) {
     w->P.pgs_two_level = interior_phases < 0 ? 0 : (interior_phases > 8 ? 8 : interior_phases);
 }
 int gbodeWorldGetTwoLevelSweep(dWorldID w) { return w->P.pgs_two_level; }
+void gbodeWorldSetSweepSync(dWorldID w, int mode) { w->P.pgs_grid_sync = mode == GBODE_SYNC_GRID ? 1 : 0; }
+int gbodeWorldGetSweepSync(dWorldID w) { return w->P.pgs_grid_sync ? GBODE_SYNC_GRID : GBODE_SYNC_NEIGHBOURS; }
 int gbodeWorldGetSolverBlocks(dWorldID w) { return w->P.pgs_blocks > 0 && w->P.pgs_blocks < num_sms() ? w->P.pgs_blocks : num_sms(); }
 
 int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
@@ -2519,6 +2526,7 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         w->stats.sleeping = w->ws.sleep_on ? h.nasleep : 0;
         w->stats.interior_colours = h.nicolours;
         w->stats.interior_rows = h.slab_rows;
+        w->stats.neighbour_waits = h.slab_sync;
         w->stats.solve_ms = 0;
         w->stats.step_ms = 0;
         if (w->timing) {

@@ -42,6 +42,10 @@ struct SolverParams {
     int pgs_two_level;  // two-level sweep: parts' interior groups in shared memory, cross groups coloured globally
     int pgs_threads;    // threads a block of the sweep kernels: 128 or 256 (0: 256)
     int pgs_chunk;      // staged rows a shared-memory buffer of the one-level sweep (0: GB_CHUNK_ROWS)
+    int pgs_grid_sync;  // two-level sweep: 1 every cross colour ends at a grid barrier; 0 a block waits only
+                        // for the blocks that touch the same bodies (GBODE_SYNC_*)
+    int fixed_checks;   // residual-target mode: 1 a check every check_every sweeps; 0 predicted checks
+    int reform_every;   // residual-target mode: sweeps between re-formed accumulators (0: 500)
 };
 
 // learned warm start network (parameter layout in mlp.cu)
@@ -84,6 +88,8 @@ struct DevCounters {
     int nicolours;         // two-level sweep: colours of the parts' interior groups
     int slab_box[4];       // two-level sweep: body x / y range (order-preserving ints)
     int slab_rows;         // two-level sweep: interior rows of the last solve
+    int slab_nbr_over;     // two-level sweep: a body had more cross accessors than listed (grid barriers used)
+    int slab_sync;         // the last solve's two-level sweep waited on neighbour blocks (1) or grid barriers (0)
 };
 
 // auto-disable state per body, int4: x flags, y idle steps, z steps left,
@@ -122,6 +128,9 @@ struct Workspace {
     // interior rows packed part by part, partition histograms
     DBuf s_bw, s_part, s_blocal, s_pbcount, s_pbody, s_prow, s_pgrp, s_gpart, s_gdesc;
     DBuf s_pccount, s_pcstart, s_pcfill, s_ilist, s_irown, s_irowoff, s_idesc, s_ipack, s_hist, s_binpart;
+    // two-level sweep, neighbour waits: cross groups per (colour, owner block) and their first slot, the
+    // owner blocks touching each body, block adjacency bit sets, per-block step counters
+    DBuf x_cnt, x_start, x_fill, x_accn, x_acc, x_adj, x_prog;
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state

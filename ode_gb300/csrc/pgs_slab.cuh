@@ -19,7 +19,20 @@
 //      colours (staged waves, one grid barrier per colour);
 //   4. the part's fc read back from global memory.
 // Both phases are Gauss-Seidel in a fixed order (no two groups of one colour
-// share a body), so a sweep is deterministic.  The interior and the cross
+// share a body), so a sweep is deterministic.
+//
+// Neighbour waits (the default; GBODE_SYNC_NEIGHBOURS): a cross group is
+// relaxed by the block whose part holds its first body, and a block's steps
+// (the interior phase, then each cross colour) conflict only with the steps of
+// blocks that touch one of the same bodies -- the part owning a body and the
+// owners of the cross groups touching it.  Those blocks are listed once per
+// solve; every block counts its finished steps in a global counter (release),
+// and before a step that reads bodies a block waits (acquire, bounded) until
+// each listed block has finished the previous step.  A block with nothing to
+// do in a colour does not wait at all.  Every body's accumulators then see
+// the same sequence of updates as under a grid barrier per colour, so the
+// result is the same to the bit, while a colour costs only what the blocks
+// that work in it need.  The interior and the cross
 // groups are coloured independently (k_colour with a class per group).  A
 // part whose interior rows, groups or bodies exceed the shared-memory
 // capacity gives all its groups to the cross phase, so any world runs; worlds
@@ -33,6 +46,8 @@
 #define GB_SLAB_XCHUNK 128     // cross-phase staging rows per buffer
 #define GB_SLAB_ROW_F4 5       // float4 per interior row (80 bytes)
 #define GB_SLAB_COLOURS 64     // interior colours (64 + c in the shared colouring)
+#define GB_XACC 16             // owner blocks listed per body (cross groups touching it)
+#define GB_XADJ_WORDS 8        // words of a block's adjacency bit set (up to 256 blocks)
 
 __device__ __forceinline__ int ord_f(float f) {
     const int i = __float_as_int(f);
@@ -234,6 +249,70 @@ __global__ void k_slab_pack(Rows Rw, Bodies B, const int *gpart, const int4 *gde
     }
 }
 
+// ---- neighbour waits: the cross groups per (colour, owner block), the blocks
+// touching each body, the block adjacency
+
+// the block that relaxes cross group e: the part of its first body with one
+__device__ __forceinline__ int cross_owner(int2 gb, const int *part, int e, int B) {
+    const int p1 = gb.x >= 0 ? part[gb.x] : -1, p2 = gb.y >= 0 ? part[gb.y] : -1;
+    return p1 >= 0 ? p1 : (p2 >= 0 ? p2 : e % B);
+}
+__global__ void k_xown_count(const DevCounters *dc, const int *colour, const int2 *gbody, const int *part, int B,
+                             int *xcnt) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c >= 0 && c < GB_SLAB_COLOURS) atomicAdd(&xcnt[c * B + cross_owner(gbody[e], part, e, B)], 1);
+    }
+}
+// the cross colours' lists rewritten owner block by owner block: (colour c,
+// block b)'s groups take slots xstart[c B + b] .. + xcnt[c B + b] (the
+// flattened scan over (colour, block) starts colour c at its list start)
+__global__ void k_xown_fill(const DevCounters *dc, const int *colour, const int2 *gbody, const int *part, int B,
+                            const int *xstart, int *xfill, int *list) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c < 0 || c >= GB_SLAB_COLOURS) continue;
+        const int k = c * B + cross_owner(gbody[e], part, e, B);
+        list[xstart[k] + atomicAdd(&xfill[k], 1)] = e;
+    }
+}
+// owner blocks of the cross groups touching each body
+__global__ void k_xacc(DevCounters *dc, const int *colour, const int2 *gbody, const int *part, int B, int *accn,
+                       int *acc) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c < 0 || c >= GB_SLAB_COLOURS) continue;
+        const int2 gb = gbody[e];
+        const int o = cross_owner(gb, part, e, B);
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            const int x = s ? gb.y : gb.x;
+            if (x < 0) continue;
+            const int k = atomicAdd(&accn[x], 1);
+            if (k < GB_XACC) acc[(size_t)x * GB_XACC + k] = o;
+            else dc->slab_nbr_over = 1;
+        }
+    }
+}
+// every two blocks touching one body are adjacent
+__global__ void k_xadj(const int *accn, const int *acc, const int *part, int nb, unsigned *adj) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < nb; x += gridDim.x * blockDim.x) {
+        const int n = min(accn[x], GB_XACC);
+        if (n == 0) continue;
+        int L[GB_XACC + 1];
+        int m = 0;
+        if (part[x] >= 0) L[m++] = part[x];
+        for (int k = 0; k < n; k++) L[m++] = acc[(size_t)x * GB_XACC + k];
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < m; j++)
+                if (L[i] != L[j])
+                    atomicOr(&adj[(size_t)L[i] * GB_XADJ_WORDS + (L[j] >> 5)], 1u << (L[j] & 31));
+    }
+}
+
 // quickstep.cpp:2917-3033 on one 80-byte row (the second body's
 // accumulators are zero and unused for a one-body contact)
 __device__ __forceinline__ void relax_slab_row(const float4 *row, float &lam, float lo, float hi, float4 &f1l,
@@ -304,6 +383,12 @@ struct SlabArgs {
     int bcap, rcap, gcap;  // per-part capacities: bodies, interior rows, interior groups
     int chunk_cap;         // cross-phase staging rows per buffer
     int ipasses;           // interior phases per sweep (>= 1)
+    // neighbour waits (xspatial: the cross colours' groups are listed owner
+    // block by owner block; the waits run unless a body's list overflowed)
+    int xspatial;
+    const int *xcnt;       // [64 * blocks]: cross groups per (colour, block)
+    const unsigned *xadj;  // [blocks * GB_XADJ_WORDS]: adjacency bit sets
+    unsigned *xprog;       // [blocks]: steps each block has finished
 };
 
 // Shared memory of k_pgs_slab: two cross staging buffers (chunk_cap rows of
@@ -325,8 +410,10 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     __shared__ int s_icol[GB_SLAB_COLOURS + 1];
     __shared__ int s_nic, s_g0, s_ng, s_row0, s_nrows, s_nb;
     __shared__ unsigned long long s_mbar[4];  // two cross buffers, the interior rows, [3] never armed (poison_stage)
-    __shared__ int s_abort;                   // a staging wait of this block ran out
+    __shared__ int s_abort;                   // a staging or neighbour wait of this block ran out
     __shared__ float s_lam[T * 13];
+    __shared__ int s_nbr[256], s_nn;          // blocks whose steps conflict with this block's
+    __shared__ int s_xn[GB_SLAB_COLOURS];     // this block's cross groups per colour
     extern __shared__ float4 pgs_smem[];
     float4 *xbuf = pgs_smem;                                         // 2 x chunk_cap x 8
     float4 *irows = xbuf + (size_t)2 * S.chunk_cap * 8;              // rcap x 5
@@ -348,6 +435,10 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         const int base = S.pcstart[part * GB_SLAB_COLOURS];
         s_icol[threadIdx.x] = S.pcstart[part * GB_SLAB_COLOURS + threadIdx.x] - base;
     }
+    const bool nbr = S.xspatial && !dc->slab_nbr_over;  // the same on every block
+    if (blockIdx.x == 0 && threadIdx.x == 0) dc->slab_sync = nbr ? 1 : 0;
+    if (threadIdx.x < GB_SLAB_COLOURS)
+        s_xn[threadIdx.x] = S.xspatial && threadIdx.x < ncol ? S.xcnt[threadIdx.x * gridDim.x + blockIdx.x] : 1;
     if (threadIdx.x == 0) {
         mbar_init(&s_mbar[0]);
         mbar_init(&s_mbar[1]);
@@ -361,6 +452,17 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         s_row0 = g1 > g0 ? S.irowoff[g0] : 0;
         s_nrows = g1 > g0 ? S.irowoff[g1 - 1] + S.irown[g1 - 1] - s_row0 : 0;
         s_nb = min(S.pbcount[part], S.bcap);
+        int n = 0;
+        if (nbr)
+            for (int w = 0; w < GB_XADJ_WORDS; w++) {
+                unsigned m = S.xadj[(size_t)blockIdx.x * GB_XADJ_WORDS + w];
+                while (m) {
+                    const int o = w * 32 + __ffs(m) - 1;
+                    m &= m - 1;
+                    if (o != (int)blockIdx.x && o < (int)gridDim.x) s_nbr[n++] = o;
+                }
+            }
+        s_nn = n;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -373,6 +475,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     const bool residual_mode = A.target > 0;
     const int itmax = nrows > 0 ? (residual_mode ? A.max_iterations : A.iterations) : 0;
     int it = 0, check = 0, last_reform = 0;
+    CheckPlan plan;
+    plan.init(A.check_every);
     float *slots = dc->racc;
     // fc = M^-1 J^T lambda over every group (cross colours, then interior colours), from global lambda
     auto form_fc = [&](bool zero) -> bool {
@@ -521,7 +625,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     auto load_ahead = [&](Step t) {
         if (t.c < 0) { has_ahead = false; return; }
         int k = blockIdx.x + threadIdx.x * (int)gridDim.x;
-        if (s_wcount[t.c] == 1) k = k < s_ccount[t.c] ? k : -1;
+        if (s_wcount[t.c] == 1 && !S.xspatial) k = k < s_ccount[t.c] ? k : -1;
         else k = __ldg(&A.sched[(size_t)(s_wbase[t.c] + t.w) * T + threadIdx.x]);
         has_ahead = k >= 0;
         if (has_ahead) ahead = __ldg(&A.desc[s_cstart[t.c] + k]);
@@ -540,6 +644,34 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         }
         load_ahead(t_after);
     };
+    // neighbour waits: `done` counts this block's finished steps (the same
+    // sequence on every block); xprog[b] is block b's count
+    unsigned done = 0;
+    auto nbr_release = [&]() {
+        __syncthreads();  // every thread's stores of the step are issued
+        ++done;
+        if (threadIdx.x == 0) red_release_add_u32(&S.xprog[blockIdx.x], 1u);
+    };
+    // before a step that touches bodies: every conflicting block has finished
+    // as many steps as this one (bounded like a grid barrier)
+    auto nbr_wait = [&](bool work) -> bool {
+        if (work)
+            for (int i = threadIdx.x; i < s_nn; i += blockDim.x) {
+                const unsigned *p = &S.xprog[s_nbr[i]];
+                long long polls = 0;
+                while ((int)(ld_acquire_u32(p) - done) < 0) {
+                    if (++polls > (1ll << 22) ||
+                        ((polls & 63) == 0 && (ld_acquire_u32(&dc->err) & ERR_BARRIER_TIMEOUT))) {
+                        atomicOr(&dc->err, ERR_BARRIER_TIMEOUT);
+                        s_abort = 1;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+        __syncthreads();
+        return s_abort == 0;
+    };
     {
         const Step s0{-1, 0};
         if (threadIdx.x == 0) {
@@ -551,7 +683,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     }
     for (; it < itmax;) {
         Step cur{-1, 0};
-        const bool check_this = residual_mode && ((it + 1) % A.check_every == 0 || it + 1 == itmax);
+        const bool check_this = residual_mode && (it + 1 >= plan.next || it + 1 == itmax);
         for (;;) {
             const Step nxt = step_after(cur), nnx = step_after(nxt);
             const bool interior = cur.c < 0;
@@ -560,14 +692,16 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
             float lout[GB_STAGED_ROWS];
             int nout = 0, xout = 0;
             if (interior) {
-                for (int rep = 0; rep < S.ipasses; rep++)
-                    for (int c = 0; c < s_nic; c++) {
-                        for (int i = s_icol[c] + threadIdx.x; i < s_icol[c + 1]; i += blockDim.x)
-                            relax_slab(idesc[i], irows, ilam, ifc, A.passes);
-                        __syncthreads();
-                    }
-                publish_fc();
-                if (check_this) publish_lambda();
+                if (s_ng > 0) {  // a part without interior groups leaves its bodies' accumulators alone
+                    for (int rep = 0; rep < S.ipasses; rep++)
+                        for (int c = 0; c < s_nic; c++) {
+                            for (int i = s_icol[c] + threadIdx.x; i < s_icol[c + 1]; i += blockDim.x)
+                                relax_slab(idesc[i], irows, ilam, ifc, A.passes);
+                            __syncthreads();
+                        }
+                    publish_fc();
+                    if (check_this) publish_lambda();
+                }
             } else if (has_next) {
                 if (!staged) {
                     relax_desc(A, next);
@@ -598,7 +732,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                         if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 }
                 unsigned target = 0;
-                grid_arrive(&dc->gsync, gen, target);
+                if (nbr) nbr_release();
+                else grid_arrive(&dc->gsync, gen, target);
                 if (threadIdx.x == 0) issue(nxt);
                 if (!check_next) {
 #pragma unroll
@@ -606,7 +741,20 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                         if (k < nout) A.Rw.lambda[xout + k] = lout[k];
                 }
                 fetch(nnx);
-                if (!grid_wait(&dc->gsync, &dc->err, gen, target) || s_abort) { drain(); return; }
+                // the next step: a cross colour this block has groups in, or
+                // the next sweep's interior phase (its accumulators are read
+                // back first).  A residual check reads -- and may re-form --
+                // every body's accumulators: all blocks finish the sweep first.
+                bool ok;
+                if (!nbr) {
+                    ok = grid_wait(&dc->gsync, &dc->err, gen, target);
+                } else if (check_next) {
+                    grid_arrive(&dc->gsync, gen, target);
+                    ok = grid_wait(&dc->gsync, &dc->err, gen, target);
+                } else {
+                    ok = nbr_wait(sweep_end ? s_ng > 0 : s_xn[nxt.c] > 0);
+                }
+                if (!ok || s_abort) { drain(); return; }
             }
             if (threadIdx.x == 0) retire();
             ++q;
@@ -615,17 +763,27 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         }
         ++it;
         if (check_this) {
+            // as in k_pgs: re-formed accumulators every reform_every sweeps,
+            // and for the check that ends the solve
+            bool fresh = false;
             if (it - last_reform >= A.reform_every || it == itmax) {
                 last_reform = it;
+                fresh = true;
                 if (!form_fc(true)) { drain(); return; }
             }
             float rel;
             if (!residual_rel(rel)) { drain(); return; }
+            if (rel <= A.target && !fresh) {
+                last_reform = it;
+                if (!form_fc(true) || !residual_rel(rel)) { drain(); return; }
+            }
             if (rel <= A.target) break;
+            plan.after(it, rel, A.target, A.check_every, A.predict_checks);
         }
         // every block's cross updates of the part's bodies are out (the last
-        // barrier of the sweep, or of the check): the accumulators come back
-        load_part(false);
+        // barrier or neighbour wait of the sweep, or the check's barrier):
+        // the accumulators come back
+        if (s_ng > 0) load_part(false);
         __syncthreads();
     }
     // The global accumulators are current here (read back after the last

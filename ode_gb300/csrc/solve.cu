@@ -1093,6 +1093,7 @@ struct PgsArgs {
     int warm;          // lambda starts non-zero: fc = M^-1 J^T lambda is formed first
     int nb;            // bodies
     int reform_every;  // sweeps between re-formations of fc from lambda (residual-target mode)
+    int predict_checks;  // residual checks at half the predicted distance to the target (CheckPlan)
     const float4 *packed;                     // staged rows, chunk by chunk
     const int *chunk_start, *chunk_rows;      // per wave: first row in `packed`, rows
     const int *wcount, *wbase;                // per (colour, block): waves, index of the first
@@ -1362,10 +1363,25 @@ __device__ int warp_cut_waves(const int4 *desc, int s0, int n, int b, int B, int
     return waves;
 }
 
+// The slots of (colour c, block b): every B-th from b, or (xstart given: the
+// two-level sweep's cross colours listed owner block by owner block) the
+// xcnt[c B + b] slots from list position xstart[c B + b].  Returns the first
+// list position, the count and stride of the cut, and the offset from the
+// colour's first slot.
+struct SlotRange { int s0, n, b, B, koff; };
+__device__ __forceinline__ SlotRange slot_range(const int *cstart, const int *ccount, const int *xstart,
+                                                const int *xcnt, int c, int b, int B) {
+    if (xstart && c < 64) {
+        const int s0 = xstart[c * B + b];
+        return SlotRange{s0, xcnt[c * B + b], 0, 1, s0 - cstart[c]};
+    }
+    return SlotRange{cstart[c], ccount[c], b, B, 0};
+}
+
 // pass 1, one warp per (colour, block): waves of each (at least one, so
 // every block takes part in every colour's barrier)
 __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCounters *dc, const int4 *desc,
-                             int *wcount, int B, int chunk_cap, int T) {
+                             int *wcount, int B, int chunk_cap, int T, const int *xstart, const int *xcnt) {
     const int cb = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (cb >= GB_MAX_COLOURS * B) return;
     const int c = cb / B, b = cb % B;
@@ -1373,7 +1389,8 @@ __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCoun
         if ((threadIdx.x & 31) == 0) wcount[cb] = 0;
         return;
     }
-    const int w = warp_cut_waves(desc, cstart[c], ccount[c], b, B, chunk_cap, T, [](int, int, int, int) {});
+    const SlotRange r = slot_range(cstart, ccount, xstart, xcnt, c, b, B);
+    const int w = warp_cut_waves(desc, r.s0, r.n, r.b, r.B, chunk_cap, T, [](int, int, int, int) {});
     if ((threadIdx.x & 31) == 0) wcount[cb] = w > 0 ? w : 1;
 }
 
@@ -1381,7 +1398,7 @@ __global__ void k_wave_count(const int *cstart, const int *ccount, const DevCoun
 // descriptors, the schedule, rows per wave
 __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *dc, int4 *desc, const int *wcount,
                             const int *wbase, int *sched, int *wrows, int *wcol, int wave_cap, int B,
-                            int chunk_cap, int T) {
+                            int chunk_cap, int T, const int *xstart, const int *xcnt) {
     const int cb = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (cb >= GB_MAX_COLOURS * B) return;
@@ -1398,9 +1415,10 @@ __global__ void k_wave_fill(const int *cstart, const int *ccount, DevCounters *d
     }
     for (int i = lane; i < nw * T; i += 32) sched[(size_t)base * T + i] = -1;
     __syncwarp();
-    const int s0 = cstart[c];
-    warp_cut_waves(desc, s0, ccount[c], b, B, chunk_cap, T, [&](int w, int t, int k, int off) {
-        sched[(size_t)(base + w) * T + t] = k;
+    const SlotRange r = slot_range(cstart, ccount, xstart, xcnt, c, b, B);
+    const int s0 = r.s0;
+    warp_cut_waves(desc, s0, r.n, r.b, r.B, chunk_cap, T, [&](int w, int t, int k, int off) {
+        sched[(size_t)(base + w) * T + t] = k + r.koff;
         if (off >= 0) {
             int4 d = desc[s0 + k];
             d.y = (d.y & ~(0xfff << 16)) | (off << 16);
@@ -1466,6 +1484,31 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity
     }
     return true;
 }
+
+// The residual-check schedule of residual-target mode (the same on every
+// block: it depends only on the checks' results).  Fixed: every `every`
+// sweeps.  Predicted: the residual's tail decays about geometrically, so
+// from the last two checks (sweeps s0 < s1, residuals r0 > r1) the target is
+// n = ln(target / r1) / ln(r1 / r0) * (s1 - s0) sweeps away; the next check
+// comes half that distance later (at least `every`, at most 64 sweeps): a
+// rate misjudged either way costs a few checks or a few sweeps.  After a
+// check whose residual did not fall, the next is `every` sweeps later.
+struct CheckPlan {
+    int next, s_prev;
+    float r_prev;
+    __device__ void init(int every) { next = every; s_prev = -1; r_prev = 0.f; }
+    __device__ void after(int it, float r, float target, int every, bool predict) {
+        int gap = every;
+        if (predict && s_prev >= 0 && r < r_prev && r > target) {
+            const float per = logf(r / r_prev) / (float)(it - s_prev);  // < 0
+            const float n = logf(target / r) / per;                     // > 0
+            gap = max(every, min(64, (int)(0.5f * n)));
+        }
+        s_prev = it;
+        r_prev = r;
+        next = it + gap;
+    }
+};
 
 // Staged triplet manifold (GB_DESC_TRIPLETS): the rows' operations of
 // quickstep.cpp:2917-3033 with a shorter dependency chain -- the 12-term
@@ -1624,10 +1667,11 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
     }
     __syncthreads();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    const int g = threadIdx.x * gridDim.x + blockIdx.x;
     const bool residual_mode = A.target > 0;
     const int itmax = residual_mode ? A.max_iterations : A.iterations;
     int it = 0, check = 0, last_reform = 0;
+    CheckPlan plan;
+    plan.init(A.check_every);
     float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
     // fc = M^-1 J^T lambda, colour by colour so no two manifolds of a pass touch one body
     auto form_fc = [&](bool zero) -> bool {
@@ -1836,18 +1880,28 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             cur = nxt;
         }
         ++it;
-        if (residual_mode && (it % A.check_every == 0 || it == itmax)) {
+        if (residual_mode && (it >= plan.next || it == itmax)) {
             // Re-form fc = M^-1 J^T lambda from lambda every reform_every sweeps:
             // thousands of incremental FP32 updates let fc drift from the
             // multipliers it stands for, and relaxation against a drifted fc
-            // stalls at a residual of ~1e-4..1e-3 on deep piles.
+            // stalls at a residual of ~1e-4..1e-3 on deep piles.  A check
+            // that passes on accumulators not formed afresh is repeated on
+            // re-formed ones: the residual that ends the solve is the
+            // multipliers' own.
+            bool fresh = false;
             if (it - last_reform >= A.reform_every || it == itmax) {
                 last_reform = it;
+                fresh = true;
                 if (!form_fc(true)) { drain(); return; }
             }
             float rel;
             if (!residual_rel(rel)) { drain(); return; }
+            if (rel <= A.target && !fresh) {
+                last_reform = it;
+                if (!form_fc(true) || !residual_rel(rel)) { drain(); return; }
+            }
             if (rel <= A.target) break;
+            plan.after(it, rel, A.target, A.check_every, A.predict_checks);
         }
     }
     drain();  // the copy issued for the colour after the last one relaxed
@@ -2381,7 +2435,11 @@ static bool ensure_coloured(Workspace &ws, int nb, const ColouredPlan &c) {
            ws.s_gpart.ensure((ng + 1) * 4) && ws.s_gdesc.ensure((ng + 1) * 16) && ws.s_pccount.ensure(npc * 4) &&
            ws.s_pcstart.ensure((npc + 1) * 4) && ws.s_pcfill.ensure(npc * 4) && ws.s_ilist.ensure((ng + 1) * 4) &&
            ws.s_irown.ensure((ng + 1) * 4) && ws.s_irowoff.ensure((ng + 1) * 4) && ws.s_idesc.ensure((ng + 1) * 16) &&
-           ws.s_ipack.ensure((size_t)ws.row_cap * 80) && ws.s_hist.ensure(nh * 4) && ws.s_binpart.ensure(nh * 4);
+           ws.s_ipack.ensure((size_t)ws.row_cap * 80) && ws.s_hist.ensure(nh * 4) && ws.s_binpart.ensure(nh * 4) &&
+           ws.x_cnt.ensure((size_t)64 * c.pgs_blocks * 4) && ws.x_start.ensure((size_t)64 * c.pgs_blocks * 4 + 4) &&
+           ws.x_fill.ensure((size_t)64 * c.pgs_blocks * 4) && ws.x_accn.ensure(nbb * 4) &&
+           ws.x_acc.ensure(nbb * GB_XACC * 4) && ws.x_adj.ensure((size_t)c.pgs_blocks * GB_XADJ_WORDS * 4) &&
+           ws.x_prog.ensure((size_t)c.pgs_blocks * 4);
 }
 
 // Every device buffer a step writes, allocated before its first kernel: an
@@ -2562,6 +2620,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     cudaMemsetAsync(ws.m_claim.p, 0x7f, (size_t)(nb > 0 ? nb : 1) * GB_MAX_COLOURS * 4, s);
     cudaMemsetAsync(&ws.dc->ncolours, 0, 4, s);
     cudaMemsetAsync(&ws.dc->nicolours, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->slab_sync, 0, 4, s);
     cudaMemsetAsync(&ws.dc->slab_rows, 0, 4, s);
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     {
@@ -2582,6 +2641,22 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     scan_exclusive(ws.col_count.as<int>(), ws.col_start.as<int>(), nullptr, GB_MAX_COLOURS, &ws.dc->colour_total, ws, s);
     k_colour_fill<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_start.as<int>(), ws.col_fill.as<int>(),
                                        ws.col_list.as<int>());
+    // two-level sweep with neighbour waits: the cross colours' lists owner block by owner block
+    const bool xspatial = slab && !P.pgs_grid_sync;
+    const int *xstart = nullptr, *xcnt = nullptr;
+    if (xspatial) {
+        const size_t nx = (size_t)64 * pgs_blocks;
+        cudaMemsetAsync(ws.x_cnt.p, 0, nx * 4, s);
+        cudaMemsetAsync(ws.x_fill.p, 0, nx * 4, s);
+        k_xown_count<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), ws.s_part.as<int>(),
+                                          pgs_blocks, ws.x_cnt.as<int>());
+        scan_exclusive(ws.x_cnt.as<int>(), ws.x_start.as<int>(), nullptr, (int)nx, nullptr, ws, s);
+        k_xown_fill<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), ws.s_part.as<int>(),
+                                         pgs_blocks, ws.x_start.as<int>(), ws.x_fill.as<int>(), ws.col_list.as<int>());
+        count_launch(2);
+        xstart = ws.x_start.as<int>();
+        xcnt = ws.x_cnt.as<int>();
+    }
     k_manifold_desc<<<grid, 256, 0, s>>>(ws.col_list.as<int>(), ws.m_start.as<int>(), ws.c_rstart.as<int>(),
                                          ws.c_mcount.as<int>(), ws.r_body.as<int2>(), ws.r_findex.as<int>(), ws.dc,
                                          ws.m_desc.as<int4>(), ws.j_rstart.as<int>(), ws.j_m.as<int>(),
@@ -2595,13 +2670,13 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     {
         const int g1 = (ncb * 32 + 127) / 128;  // a warp per (colour, block)
         k_wave_count<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
-                                        ws.wv_count.as<int>(), pgs_blocks, chunk_cap, threads);
+                                        ws.wv_count.as<int>(), pgs_blocks, chunk_cap, threads, xstart, xcnt);
         scan_exclusive(ws.wv_count.as<int>(), ws.wv_base.as<int>(), nullptr, ncb, nullptr, ws, s);
         k_wave_total<<<1, 1, 0, s>>>(ws.dc, ws.wv_count.as<int>(), ws.wv_base.as<int>(), pgs_blocks);
         k_wave_fill<<<g1, 128, 0, s>>>(ws.col_start.as<int>(), ws.col_count.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                        ws.wv_count.as<int>(), ws.wv_base.as<int>(), ws.wv_sched.as<int>(),
                                        ws.chunk_rows.as<int>(), ws.wv_col.as<int>(), (int)wave_cap, pgs_blocks,
-                                       chunk_cap, threads);
+                                       chunk_cap, threads, xstart, xcnt);
         scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), &ws.dc->nwaves, (int)wave_cap, nullptr, ws, s);
         k_pack_rows<<<grid, threads, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                                     ws.wv_sched.as<int>(), ws.wv_col.as<int>(),
@@ -2625,12 +2700,27 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.s_idesc.as<int4>(), ws.s_ipack.as<float4>(), ws.dc);
         count_launch(3);
     }
+    if (xspatial) {
+        // the blocks touching each body, and every two of them adjacent
+        const size_t nbb = nb > 0 ? nb : 1;
+        cudaMemsetAsync(ws.x_accn.p, 0, nbb * 4, s);
+        cudaMemsetAsync(ws.x_adj.p, 0, (size_t)pgs_blocks * GB_XADJ_WORDS * 4, s);
+        cudaMemsetAsync(&ws.dc->slab_nbr_over, 0, 4, s);
+        k_xacc<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), ws.s_part.as<int>(),
+                                    pgs_blocks, ws.x_accn.as<int>(), ws.x_acc.as<int>());
+        k_xadj<<<grid, 256, 0, s>>>(ws.x_accn.as<int>(), ws.x_acc.as<int>(), ws.s_part.as<int>(), nb,
+                                    ws.x_adj.as<unsigned>());
+        cudaMemsetAsync(ws.x_prog.p, 0, (size_t)pgs_blocks * 4, s);
+        count_launch(2);
+    }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     if (g_test.barrier) {
         // error-path tests: the counter starts one arrival short, so the
         // solver's first grid barrier never completes and its bounded wait runs out
         cudaMemsetAsync(&ws.dc->gsync.count, 0xff, sizeof(unsigned), s);
+        // and every block's step counter one step short: the first neighbour wait runs out
+        if (xspatial) cudaMemsetAsync(ws.x_prog.p, 0xff, (size_t)pgs_blocks * 4, s);
         g_test.barrier = 0;
     }
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
@@ -2651,7 +2741,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.w_sor = P.w;
         A.warm = P.warm_mode != 0;
         A.nb = nb;
-        A.reform_every = 50;
+        A.reform_every = P.reform_every > 0 ? P.reform_every : 500;
+        A.predict_checks = P.fixed_checks ? 0 : 1;
         A.learned = P.learned;
         A.lam_alt = P.learned ? ws.l_alt.as<float>() : nullptr;
         A.passes = P.pgs_passes > 1 ? P.pgs_passes : 1;
@@ -2683,6 +2774,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             SA.bcap = caps.bcap; SA.rcap = caps.rcap; SA.gcap = caps.gcap;
             SA.chunk_cap = GB_SLAB_XCHUNK;
             SA.ipasses = P.pgs_two_level;
+            SA.xspatial = xspatial ? 1 : 0;
+            SA.xcnt = ws.x_cnt.as<int>();
+            SA.xadj = ws.x_adj.as<unsigned>();
+            SA.xprog = ws.x_prog.as<unsigned>();
             void *args[] = {(void *)&SA};
             const void *k = threads == 128 ? (const void *)k_pgs_slab<128> : (const void *)k_pgs_slab<256>;
             if (cudaLaunchCooperativeKernel(k, blocks, threads, args, caps.smem, s) != cudaSuccess) return false;

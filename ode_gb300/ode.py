@@ -59,7 +59,8 @@ class gbodeStepStats(ctypes.Structure):
     _fields_ = [("contacts", ctypes.c_int), ("rows", ctypes.c_int), ("colours", ctypes.c_int),
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
                 ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int),
-                ("interior_colours", ctypes.c_int), ("interior_rows", ctypes.c_int)]
+                ("interior_colours", ctypes.c_int), ("interior_rows", ctypes.c_int),
+                ("neighbour_waits", ctypes.c_int)]
 
 
 dNearCallback = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ID, ID)
@@ -160,6 +161,8 @@ _PROTOS = [
     ("gbodeWorldSetSolverBlocks", None, [ID, ctypes.c_int]), ("gbodeWorldGetSolverBlocks", ctypes.c_int, [ID]),
     ("gbodeWorldSetManifoldPasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetManifoldPasses", ctypes.c_int, [ID]),
     ("gbodeWorldSetTwoLevelSweep", None, [ID, ctypes.c_int]), ("gbodeWorldGetTwoLevelSweep", ctypes.c_int, [ID]),
+    ("gbodeWorldSetSweepSync", None, [ID, ctypes.c_int]), ("gbodeWorldGetSweepSync", ctypes.c_int, [ID]),
+    ("gbodeWorldSetResidualChecks", None, [ID, ctypes.c_int, ctypes.c_int]),
     ("gbodeTestInject", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetSolverTiles", None, [ID, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldGetSolverTiles", None, [ID, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
@@ -235,6 +238,8 @@ dParamLoStop, dParamHiStop, dParamVel, dParamFMax, dParamCFM, dParamERP = 0, 1, 
 dParamSuspensionERP, dParamSuspensionCFM = 11, 12
 dParamVel2, dParamFMax2 = 0x102, 0x105
 
+GBODE_SYNC_NEIGHBOURS, GBODE_SYNC_GRID = 0, 1  # gbodeWorldSetSweepSync
+GBODE_CHECKS_PREDICTED, GBODE_CHECKS_FIXED = 0, 1  # gbodeWorldSetResidualChecks
 GBODE_SOLVER_COLOURED = 0
 GBODE_SOLVER_REFERENCE_ORDER = 1
 

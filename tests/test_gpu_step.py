@@ -407,6 +407,47 @@ def test_snapshot_reruns_the_same_steps(gblib):
     w.close()
 
 
+@pytest.mark.parametrize("target", [1e-4, 0.0])
+def test_neighbour_waits_match_grid_barriers(gblib, target):
+    """The two-level sweep with neighbour waits (GBODE_SYNC_NEIGHBOURS: a
+    block waits only for the blocks that touch the same bodies, and not at
+    all in a colour where it has no manifold) against a grid barrier after
+    every step (GBODE_SYNC_GRID), on an 8,192-body pile that has landed: the
+    same sweeps, multipliers and bodies to the bit, step after step -- with a
+    residual target (checks every 5 sweeps under grid barriers) and with a
+    fixed 30 sweeps (no grid barrier at all in the neighbour mode)."""
+    from ode_gb300 import ode, scenes, sim
+    L = gblib
+    sc = scenes.pile(8192, seed=7)
+    worlds = [sim.GBWorld(sc) for _ in range(2)]
+    for w in worlds:
+        L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.dWorldSetQuickStepNumIterations(w.w, 30)
+    for _ in range(300):
+        for w in worlds:
+            w.step_fused()
+    for w, mode in zip(worlds, (ode.GBODE_SYNC_GRID, ode.GBODE_SYNC_NEIGHBOURS)):
+        L.gbodeWorldSetTwoLevelSweep(w.w, 2)
+        L.gbodeWorldSetSweepSync(w.w, mode)
+        assert L.gbodeWorldGetSweepSync(w.w) == mode
+        if target > 0:
+            L.gbodeWorldSetResidualTarget(w.w, target, 5, 3000)
+    for step in range(4):
+        for w in worlds:
+            assert w.step_fused() == 1, L.gbodeGetLastError()
+        g, n = (w.stats() for w in worlds)
+        assert g.neighbour_waits == 0 and n.neighbour_waits == 1
+        assert g.interior_rows > g.rows // 2 and g.colours >= 4
+        assert (g.iterations, g.rows, g.contacts) == (n.iterations, n.rows, n.contacts), step
+        a, b = (w.state() for w in worlds)
+        assert np.array_equal(a, b), f"step {step}: bodies differ by {np.abs(a - b).max():.3e}"
+    print(f"{'residual target' if target else '30 sweeps'}: {n.iterations} sweeps, {n.colours} cross colours, "
+          f"{n.interior_rows} of {n.rows} rows interior; the two modes agree to the bit")
+    for w in worlds:
+        w.close()
+
+
 def test_two_level_sweep_on_a_pile(gblib):
     """The two-level sweep (gbodeWorldSetTwoLevelSweep) on an 8,192-body
     pile that has landed: most rows are interior to a column and relaxed from
