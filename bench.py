@@ -88,6 +88,9 @@ def parse():
     ap.add_argument("--two-level", type=int, default=2,
                     help="two-level sweep of the pile's solver with this many interior phases a sweep "
                          "(gbodeWorldSetTwoLevelSweep; 0: off)")
+    ap.add_argument("--cross-classes", type=int, default=4,
+                    help="two-level sweep: crossing colours merged into this many mass-split classes "
+                         "(gbodeWorldSetCrossClasses; 0: exact colours)")
     ap.add_argument("--sweep-sync", choices=("neighbours", "grid"), default="neighbours",
                     help="two-level sweep: blocks wait on the blocks sharing their bodies, or on a grid barrier "
                          "after every step (gbodeWorldSetSweepSync)")
@@ -333,6 +336,7 @@ def run_gbode(args, ws, rank, local):
                                   args.reform_every)
     L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
     L.gbodeWorldSetSweepSync(w.w, ode.GBODE_SYNC_GRID if args.sweep_sync == "grid" else ode.GBODE_SYNC_NEIGHBOURS)
+    L.gbodeWorldSetCrossClasses(w.w, args.cross_classes)
     L.gbodeWorldSetTiming(w.w, 1)
     if args.profile_steps:
         for _ in range(args.profile_steps):
@@ -432,7 +436,9 @@ def run_gbode(args, ws, rank, local):
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
                    "solver": f"coloured PGS (W {args.sor_w}), persistent cooperative kernel"
                              + (f", two-level sweep ({args.two_level} interior phases a sweep, "
-                                + ("neighbour waits" if min(T["neighbour_waits"]) else "grid barriers") + ")"
+                                + ("neighbour waits" if min(T["neighbour_waits"]) else "grid barriers")
+                                + (f", crossing colours in {min(T['cross_classes'])} mass-split classes"
+                                   if min(T["cross_classes"]) else "") + ")"
                                 if args.two_level else ""),
                    "interior_rows_per_step": float(np.mean(T["interior_rows"])),
                    "interior_colours": int(np.median(T["interior_colours"])),
@@ -596,7 +602,7 @@ def timed_steps(w, stream, flush, steps, graph=False):
     (L2 flushed before each, outside the events); per-step statistics."""
     import torch
     out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours",
-                           "interior_rows", "interior_colours", "neighbour_waits", "checks")}
+                           "interior_rows", "interior_colours", "neighbour_waits", "checks", "cross_classes")}
     hist = np.zeros(256, np.float32)
     torch.cuda.nvtx.range_push("timed")
     for _ in range(steps):
@@ -622,6 +628,7 @@ def timed_steps(w, stream, flush, steps, graph=False):
         out["interior_rows"].append(st.interior_rows)
         out["interior_colours"].append(st.interior_colours)
         out["neighbour_waits"].append(st.neighbour_waits)
+        out["cross_classes"].append(st.cross_classes)
         out["checks"].append(w.L.gbodeWorldGetResidualHistory(w.w, hist.ctypes.data_as(ode_f32p()), 256))
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()

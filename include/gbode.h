@@ -433,6 +433,23 @@ int gbodeWorldGetTwoLevelSweep(dWorldID w);
 void gbodeWorldSetSweepSync(dWorldID w, int mode);
 int gbodeWorldGetSweepSync(dWorldID w);
 
+/* Cross classes of the two-level sweep (0 or 1: off).  With k >= 2 the
+ * crossing manifolds' colours are merged into k classes (colour c into class
+ * c mod k), each relaxed as one step instead of one step per colour.  Inside a
+ * class a body can be shared by several manifolds; they are relaxed at once
+ * (Jacobi within the class) with mass splitting: a body shared by n manifolds
+ * of the class enters each of them with 1/n of its mass, and each adds 1/n of
+ * its copy's change of the body's velocities (as fixed-point integers, so the
+ * sum does not depend on the order).  The fixed point is the same LCP
+ * solution; fewer steps a sweep, usually a few more sweeps.  The result does
+ * not depend on timing (the same to the bit run after run, and under either
+ * gbodeWorldSetSweepSync mode).  A crossing group that is not a staged
+ * manifold or joint, or that touches a body outside the columns' lists, keeps
+ * the exact colours for that step (gbodeStepStats.cross_classes reads 0). */
+#define GBODE_MAX_CROSS_CLASSES 8
+void gbodeWorldSetCrossClasses(dWorldID w, int classes);
+int gbodeWorldGetCrossClasses(dWorldID w);
+
 /* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
  * creation without leaving the device.  Equivalent to dSpaceCollide with a near
  * callback that calls dCollide(o1, o2, maxc, ...) and makes one contact joint
@@ -500,6 +517,7 @@ typedef struct gbodeStepStats {
     int interior_rows;     /* two-level sweep: rows relaxed from shared memory (0: off) */
     int neighbour_waits;   /* two-level sweep: the blocks waited only on their neighbours (1), or on grid
                               barriers (0: GBODE_SYNC_GRID, or a body touched by too many blocks) */
+    int cross_classes;     /* two-level sweep: split classes of the crossing manifolds (0: exact colours) */
 } gbodeStepStats;
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */

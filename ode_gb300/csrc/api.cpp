@@ -80,7 +80,7 @@ void Workspace::release() {
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp, &s_bw, &s_part, &s_blocal, &s_pbcount,
                    &s_pbody, &s_prow, &s_pgrp, &s_gpart, &s_gdesc, &s_pccount, &s_pcstart, &s_pcfill, &s_ilist,
                    &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart, &n_perm, &n_key, &x_cnt,
-                   &x_start, &x_fill, &x_accn, &x_acc, &x_adj, &x_prog};
+                   &x_start, &x_fill, &x_accn, &x_acc, &x_adj, &x_prog, &x_nsplit, &x_dacc, &x_smask};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
     if (hc) cudaFreeHost(hc);
@@ -796,6 +796,10 @@ void gbodeWorldSetTwoLevelSweep(dWorldID w, int interior_phases) {
 int gbodeWorldGetTwoLevelSweep(dWorldID w) { return w->P.pgs_two_level; }
 void gbodeWorldSetSweepSync(dWorldID w, int mode) { w->P.pgs_grid_sync = mode == GBODE_SYNC_GRID ? 1 : 0; }
 int gbodeWorldGetSweepSync(dWorldID w) { return w->P.pgs_grid_sync ? GBODE_SYNC_GRID : GBODE_SYNC_NEIGHBOURS; }
+void gbodeWorldSetCrossClasses(dWorldID w, int classes) {
+    w->P.pgs_split = classes < 2 ? 0 : (classes > GBODE_MAX_CROSS_CLASSES ? GBODE_MAX_CROSS_CLASSES : classes);
+}
+int gbodeWorldGetCrossClasses(dWorldID w) { return w->P.pgs_split; }
 int gbodeWorldGetSolverBlocks(dWorldID w) { return w->P.pgs_blocks > 0 && w->P.pgs_blocks < num_sms() ? w->P.pgs_blocks : num_sms(); }
 
 int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
@@ -2527,6 +2531,7 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         w->stats.interior_colours = h.nicolours;
         w->stats.interior_rows = h.slab_rows;
         w->stats.neighbour_waits = h.slab_sync;
+        w->stats.cross_classes = h.split_k;
         w->stats.solve_ms = 0;
         w->stats.step_ms = 0;
         if (w->timing) {

@@ -45,6 +45,8 @@ struct SolverParams {
     int pgs_grid_sync;  // two-level sweep: 1 every cross colour ends at a grid barrier; 0 a block waits only
                         // for the blocks that touch the same bodies (GBODE_SYNC_*)
     int fixed_checks;   // residual-target mode: 1 a check every check_every sweeps; 0 predicted checks
+    int pgs_split;      // two-level sweep: cross colours merged into this many classes, each relaxed as one
+                        // step with mass splitting (0: every cross colour its own step)
     int reform_every;   // residual-target mode: sweeps between re-formed accumulators (0: 500)
 };
 
@@ -90,6 +92,8 @@ struct DevCounters {
     int slab_rows;         // two-level sweep: interior rows of the last solve
     int slab_nbr_over;     // two-level sweep: a body had more cross accessors than listed (grid barriers used)
     int slab_sync;         // the last solve's two-level sweep waited on neighbour blocks (1) or grid barriers (0)
+    int split_off;         // two-level sweep: a cross group cannot be relaxed in a split class (exact colours)
+    int split_k;           // two-level sweep: classes of the last solve's cross phase with mass splitting (0: off)
 };
 
 // auto-disable state per body, int4: x flags, y idle steps, z steps left,
@@ -131,6 +135,8 @@ struct Workspace {
     // two-level sweep, neighbour waits: cross groups per (colour, owner block) and their first slot, the
     // owner blocks touching each body, block adjacency bit sets, per-block step counters
     DBuf x_cnt, x_start, x_fill, x_accn, x_acc, x_adj, x_prog;
+    // two-level sweep, split classes: groups per (class, body), fixed-point accumulators per (class, body)
+    DBuf x_nsplit, x_dacc, x_smask;
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state

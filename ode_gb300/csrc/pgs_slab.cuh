@@ -313,6 +313,202 @@ __global__ void k_xadj(const int *accn, const int *acc, const int *part, int nb,
     }
 }
 
+// ---- split classes (mass splitting inside a class of merged cross colours)
+
+// A crossing group can be relaxed in a split class if its rows are staged and
+// every body it moves is in a part's body list (the part folds the class
+// accumulators back into the body at the end of each sweep).
+__global__ void k_split_check(DevCounters *dc, const int *colour, const int4 *gdesc, const int2 *gbody,
+                              const int *part, const int *blocal, int bcap) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c < 0 || c >= GB_SLAB_COLOURS) continue;
+        bool bad = !(gdesc[e].y & GB_DESC_STAGED);
+        const int2 gb = gbody[e];
+        if (gb.x >= 0 && (part[gb.x] < 0 || blocal[gb.x] >= bcap)) bad = true;
+        if (gb.y >= 0 && (part[gb.y] < 0 || blocal[gb.y] >= bcap)) bad = true;
+        if (bad) dc->split_off = 1;
+    }
+}
+// classes of this solve: k, or 0 (exact colours) if a group cannot be split or
+// there are no more colours than classes
+__global__ void k_split_classes(DevCounters *dc, int k) {
+    dc->split_k = (!dc->split_off && dc->ncolours > k) ? k : 0;
+    if (dc->split_k) dc->ncolours = k;
+}
+__global__ void k_split_remap(const DevCounters *dc, int *colour) {
+    const int k = dc->split_k, ng = dc->nmanifolds;
+    if (!k) return;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c >= 0 && c < GB_SLAB_COLOURS) colour[e] = c % k;
+    }
+}
+// per body, the classes in which two or more groups touch it (bit c)
+__global__ void k_split_mask(const DevCounters *dc, const int *nsplit, int nb, int *smask) {
+    const int k = dc->split_k;
+    if (!k) return;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int m = 0;
+        for (int c = 0; c < k; c++)
+            if (nsplit[(size_t)c * nb + b] >= 2) m |= 1 << c;
+        smask[b] = m;
+    }
+}
+// groups of each class touching each body
+__global__ void k_split_count(const DevCounters *dc, const int *colour, const int2 *gbody, int nb, int *nsplit) {
+    const int ng = dc->nmanifolds;
+    if (!dc->split_k) return;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c < 0 || c >= GB_SLAB_COLOURS) continue;
+        const int2 gb = gbody[e];
+        if (gb.x >= 0) atomicAdd(&nsplit[(size_t)c * nb + gb.x], 1);
+        if (gb.y >= 0) atomicAdd(&nsplit[(size_t)c * nb + gb.y], 1);
+    }
+}
+
+// Class accumulators: per (body, class c) the fixed-point sum (2^-32 units)
+// of the changes that the groups of class c sharing the body made to its
+// accumulators fc (linear x y z, angular x y z: 48 bytes; a body's classes
+// side by side).  A group alone with a body in its class writes the body's fc
+// itself, as the exact colours do.  A group of class k reads the slots of the
+// earlier classes that shared its body (bit c of the body's mask) -- up to
+// three loads issued together -- and adds its share to slot k; the fold at
+// the end of the sweep takes every shared class back into fc.  Integer sums
+// do not depend on the order of the additions.
+#define GB_FIX_ONE 4294967296.f
+__device__ __forceinline__ long long *split_slot(long long *dacc, int stride, int b, int c) {
+    return dacc + ((size_t)b * stride + c) * 6;
+}
+__device__ __forceinline__ void split_add6(long long (&s)[6], const longlong2 *p, bool on) {
+    const longlong2 q0 = __ldcg(p), q1 = __ldcg(p + 1), q2 = __ldcg(p + 2);
+    if (on) { s[0] += q0.x; s[1] += q0.y; s[2] += q1.x; s[3] += q1.y; s[4] += q2.x; s[5] += q2.y; }
+}
+// (l, a) += the slots of the classes in `mask`
+__device__ __forceinline__ void split_sum(long long *dacc, int stride, int b, int mask, float4 &l, float4 &a) {
+    if (!mask) return;
+    long long s[6] = {0, 0, 0, 0, 0, 0};
+    const int c0 = __ffs(mask) - 1;
+    int m = mask & (mask - 1);
+    const int c1 = m ? __ffs(m) - 1 : c0;
+    const bool h1 = m != 0;
+    m &= m - 1;
+    const int c2 = m ? __ffs(m) - 1 : c0;
+    const bool h2 = m != 0;
+    m &= m - 1;
+    // three slots' loads before any sum (a missing class re-reads the first)
+    const longlong2 *p0 = (const longlong2 *)split_slot(dacc, stride, b, c0);
+    const longlong2 *p1 = (const longlong2 *)split_slot(dacc, stride, b, c1);
+    const longlong2 *p2 = (const longlong2 *)split_slot(dacc, stride, b, c2);
+    const longlong2 x0 = __ldcg(p0), x1 = __ldcg(p0 + 1), x2 = __ldcg(p0 + 2);
+    const longlong2 y0 = __ldcg(p1), y1 = __ldcg(p1 + 1), y2 = __ldcg(p1 + 2);
+    const longlong2 z0 = __ldcg(p2), z1 = __ldcg(p2 + 1), z2 = __ldcg(p2 + 2);
+    s[0] = x0.x; s[1] = x0.y; s[2] = x1.x; s[3] = x1.y; s[4] = x2.x; s[5] = x2.y;
+    if (h1) { s[0] += y0.x; s[1] += y0.y; s[2] += y1.x; s[3] += y1.y; s[4] += y2.x; s[5] += y2.y; }
+    if (h2) { s[0] += z0.x; s[1] += z0.y; s[2] += z1.x; s[3] += z1.y; s[4] += z2.x; s[5] += z2.y; }
+    while (m) {  // a fourth shared class or more
+        split_add6(s, (const longlong2 *)split_slot(dacc, stride, b, __ffs(m) - 1), true);
+        m &= m - 1;
+    }
+    const float u = 1.f / GB_FIX_ONE;
+    l.x += __ll2float_rn(s[0]) * u; l.y += __ll2float_rn(s[1]) * u; l.z += __ll2float_rn(s[2]) * u;
+    a.x += __ll2float_rn(s[3]) * u; a.y += __ll2float_rn(s[4]) * u; a.z += __ll2float_rn(s[5]) * u;
+}
+__device__ __forceinline__ void split_add1(long long *p, long long q) {
+    if (q) atomicAdd((unsigned long long *)p, (unsigned long long)q);
+}
+// the group's share of the body's change, (local copy - snapshot) / n, into
+// the slot of class c
+__device__ __forceinline__ void split_add(long long *dacc, int stride, int c, int b, float4 l, float4 a, float4 l0,
+                                          float4 a0, float n) {
+    const float r = 1.f / n;
+    long long *p = split_slot(dacc, stride, b, c);
+    split_add1(p + 0, __float2ll_rn((l.x - l0.x) * r * GB_FIX_ONE));
+    split_add1(p + 1, __float2ll_rn((l.y - l0.y) * r * GB_FIX_ONE));
+    split_add1(p + 2, __float2ll_rn((l.z - l0.z) * r * GB_FIX_ONE));
+    split_add1(p + 3, __float2ll_rn((a.x - a0.x) * r * GB_FIX_ONE));
+    split_add1(p + 4, __float2ll_rn((a.y - a0.y) * r * GB_FIX_ONE));
+    split_add1(p + 5, __float2ll_rn((a.z - a0.z) * r * GB_FIX_ONE));
+}
+
+// M^-1 J^T lambda of one group into the bodies' class-0 slot (re-formation of
+// fc with split classes, where groups of one class may share a body)
+__device__ __forceinline__ void apply_desc_fix(const PgsArgs &A, int4 d, long long *dacc, int stride) {
+    const bool two = d.w >= 0;
+    float4 f1l = make_float4(0.f, 0.f, 0.f, 0.f), f1a = f1l, f2l = f1l, f2a = f1l;
+    for (int r = d.x; r < d.x + desc_rows(d); r++) {
+        const float l = __ldcg(&A.Rw.lambda[r]);
+        if (l == 0.f) continue;
+        const float4 m1l = __ldg(&A.Rw.M1l[r]), m1a = __ldg(&A.Rw.M1a[r]);
+        f1l.x += l * m1l.x; f1l.y += l * m1l.y; f1l.z += l * m1l.z;
+        f1a.x += l * m1a.x; f1a.y += l * m1a.y; f1a.z += l * m1a.z;
+        if (two) {
+            const float4 m2l = __ldg(&A.Rw.M2l[r]), m2a = __ldg(&A.Rw.M2a[r]);
+            f2l.x += l * m2l.x; f2l.y += l * m2l.y; f2l.z += l * m2l.z;
+            f2a.x += l * m2a.x; f2a.y += l * m2a.y; f2a.z += l * m2a.z;
+        }
+    }
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    split_add(dacc, stride, 0, d.z, f1l, f1a, z, z, 1.f);
+    if (two) split_add(dacc, stride, 0, d.w, f2l, f2a, z, z, 1.f);
+}
+
+// A staged group of split class `cls`: Jacobi inside the class -- the rows
+// (packed for mass splitting) relax against the group's own copies of its
+// bodies, which start from the class's snapshot.
+__device__ __forceinline__ void relax_split(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
+                                            float (&lout)[GB_STAGED_ROWS], long long *dacc, int stride, int cls,
+                                            int classes) {
+    const int off = desc_chunk_off(d);
+    const bool two = d.w >= 0;
+    float4 s1l, s1a, s2l = make_float4(0.f, 0.f, 0.f, 0.f), s2a = s2l;
+    // the classes sharing each body (bit c) and the bodies' shares n, packed
+    // into the group's first row; a prefix slot is read only when an earlier
+    // class shared the body
+    const int m1 = __float_as_int(buf[swz(off, 4)].w), m2 = __float_as_int(buf[swz(off, 6)].w);
+    const float n1 = buf[swz(off, 5)].w, n2 = buf[swz(off, 7)].w;
+    const int before = (1 << cls) - 1;
+    const float4 b1l = ldcg4(&A.fc[2 * d.z]), b1a = ldcg4(&A.fc[2 * d.z + 1]);
+    float4 b2l = s2l, b2a = s2a;
+    if (two) { b2l = ldcg4(&A.fc[2 * d.w]); b2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    s1l = b1l; s1a = b1a; s2l = b2l; s2a = b2a;
+    split_sum(dacc, stride, d.z, m1 & before, s1l, s1a);
+    if (two) split_sum(dacc, stride, d.w, m2 & before, s2l, s2a);
+    float4 f1l = s1l, f1a = s1a, f2l = s2l, f2a = s2a;
+    cp_async_wait_all();
+    if (d.y & GB_DESC_TRIPLETS) {
+        const int nct = desc_rows(d) / 3;
+        triplet_rows(A.passes, nct, off, buf, lam, f1l, f1a, f2l, f2a);
+#pragma unroll
+        for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < 3 * nct ? lam[k] : 0.f;
+    } else {
+        plain_rows(A.passes, desc_rows(d), off, buf, lam, f1l, f1a, f2l, f2a);
+#pragma unroll
+        for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < desc_rows(d) ? lam[k] : 0.f;
+    }
+    // shared: the group's share into the later prefix slots; alone: the
+    // body's fc plus the group's change (the slots hold only shared changes)
+    if (n1 > 1.5f) {
+        split_add(dacc, stride, cls, d.z, f1l, f1a, s1l, s1a, n1);
+    } else {
+        stcg4(&A.fc[2 * d.z], make_float4(b1l.x + (f1l.x - s1l.x), b1l.y + (f1l.y - s1l.y), b1l.z + (f1l.z - s1l.z), b1l.w));
+        stcg4(&A.fc[2 * d.z + 1],
+              make_float4(b1a.x + (f1a.x - s1a.x), b1a.y + (f1a.y - s1a.y), b1a.z + (f1a.z - s1a.z), b1a.w));
+    }
+    if (two) {
+        if (n2 > 1.5f) {
+            split_add(dacc, stride, cls, d.w, f2l, f2a, s2l, s2a, n2);
+        } else {
+            stcg4(&A.fc[2 * d.w],
+                  make_float4(b2l.x + (f2l.x - s2l.x), b2l.y + (f2l.y - s2l.y), b2l.z + (f2l.z - s2l.z), b2l.w));
+            stcg4(&A.fc[2 * d.w + 1],
+                  make_float4(b2a.x + (f2a.x - s2a.x), b2a.y + (f2a.y - s2a.y), b2a.z + (f2a.z - s2a.z), b2a.w));
+        }
+    }
+}
+
 // quickstep.cpp:2917-3033 on one 80-byte row (the second body's
 // accumulators are zero and unused for a one-body contact)
 __device__ __forceinline__ void relax_slab_row(const float4 *row, float &lam, float lo, float hi, float4 &f1l,
@@ -389,6 +585,10 @@ struct SlabArgs {
     const int *xcnt;       // [64 * blocks]: cross groups per (colour, block)
     const unsigned *xadj;  // [blocks * GB_XADJ_WORDS]: adjacency bit sets
     unsigned *xprog;       // [blocks]: steps each block has finished
+    // split classes (the cross phase's steps are the classes: k_split_*)
+    int split;             // classes asked for (the solve uses dc->split_k: 0 exact colours)
+    long long *dacc;       // [bodies * split * 6]: class accumulators (zero between sweeps)
+    const int *smask;      // [bodies]: the classes whose groups share the body (bit c)
 };
 
 // Shared memory of k_pgs_slab: two cross staging buffers (chunk_cap rows of
@@ -436,6 +636,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         s_icol[threadIdx.x] = S.pcstart[part * GB_SLAB_COLOURS + threadIdx.x] - base;
     }
     const bool nbr = S.xspatial && !dc->slab_nbr_over;  // the same on every block
+    const int nsplit = S.split ? dc->split_k : 0;        // classes of the cross phase (0: exact colours)
     if (blockIdx.x == 0 && threadIdx.x == 0) dc->slab_sync = nbr ? 1 : 0;
     if (threadIdx.x < GB_SLAB_COLOURS)
         s_xn[threadIdx.x] = S.xspatial && threadIdx.x < ncol ? S.xcnt[threadIdx.x * gridDim.x + blockIdx.x] : 1;
@@ -480,6 +681,32 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     float *slots = dc->racc;
     // fc = M^-1 J^T lambda over every group (cross colours, then interior colours), from global lambda
     auto form_fc = [&](bool zero) -> bool {
+        if (nsplit) {
+            // a split class's groups may share a body: every group's share
+            // goes into class 0's integer accumulators (any order gives the
+            // same sums), which then replace (or are added to) fc; the class
+            // accumulators are zero here (folded before every check)
+            for (int cc = 0; cc < ncol + nicol; cc++) {
+                const int c = cc < ncol ? cc : 64 + (cc - ncol);
+                for (int k = tid; k < s_ccount[c]; k += nth)
+                    apply_desc_fix(A, __ldg(&A.desc[s_cstart[c] + k]), S.dacc, S.split);
+            }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
+            for (int b = tid; b < A.nb; b += nth) {
+                float4 fl = make_float4(0.f, 0.f, 0.f, 0.f), fa = fl;
+                if (!zero) { fl = ldcg4(&A.fc[2 * b]); fa = ldcg4(&A.fc[2 * b + 1]); }
+                float4 gl = make_float4(0.f, 0.f, 0.f, 0.f), ga = gl;
+                split_sum(S.dacc, S.split, b, 1, gl, ga);  // the class-0 slot
+                longlong2 *p = (longlong2 *)split_slot(S.dacc, S.split, b, 0);
+                const longlong2 zz = make_longlong2(0, 0);
+                __stcg(p, zz); __stcg(p + 1, zz); __stcg(p + 2, zz);
+                fl.x += gl.x; fl.y += gl.y; fl.z += gl.z;
+                fa.x += ga.x; fa.y += ga.y; fa.z += ga.z;
+                stcg4(&A.fc[2 * b], fl);
+                stcg4(&A.fc[2 * b + 1], fa);
+            }
+            return grid_sync(&dc->gsync, &dc->err, gen);
+        }
         if (zero) {
             for (int b = tid; b < A.nb; b += nth) {
                 stcg4(&A.fc[2 * b], make_float4(0.f, 0.f, 0.f, 0.f));
@@ -572,6 +799,35 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
             const int b = ibid[l];
             stcg4(&A.fc[2 * b], ifc[2 * l]);
             stcg4(&A.fc[2 * b + 1], ifc[2 * l + 1]);
+        }
+    };
+    // split classes: the part's bodies take their class accumulators back
+    // (fc += every class's sum, the sums zeroed) and the part's copies are
+    // refreshed; runs when every block touching the bodies is done with the
+    // sweep's last class
+    auto fold_part = [&]() {
+        for (int l = threadIdx.x; l < s_nb; l += blockDim.x) {
+            const int b = ibid[l];
+            float4 fl, fa;
+            const int m = S.smask[b];
+            if (m) {
+                fl = ldcg4(&A.fc[2 * b]);
+                fa = ldcg4(&A.fc[2 * b + 1]);
+                split_sum(S.dacc, S.split, b, m, fl, fa);  // fc + every class that shared the body
+                const longlong2 z = make_longlong2(0, 0);
+                for (int c = 0; c < nsplit; c++)
+                    if (m >> c & 1) {
+                        longlong2 *p = (longlong2 *)split_slot(S.dacc, S.split, b, c);
+                        __stcg(p, z); __stcg(p + 1, z); __stcg(p + 2, z);
+                    }
+                stcg4(&A.fc[2 * b], fl);
+                stcg4(&A.fc[2 * b + 1], fa);
+            } else {
+                fl = ldcg4(&A.fc[2 * b]);
+                fa = ldcg4(&A.fc[2 * b + 1]);
+            }
+            ifc[2 * l] = fl;
+            ifc[2 * l + 1] = fa;
         }
     };
     auto publish_lambda = [&]() {
@@ -708,7 +964,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                 } else if (A.poison_stage ? mbar_wait(&s_mbar[3], 0, &dc->err, 16)
                                           : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
                     const float4 *buf = xbuf + (q & 1) * (S.chunk_cap * 8);
-                    if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
+                    if (nsplit) relax_split(A, next, buf, my_lam, lout, S.dacc, S.split, cur.c, nsplit);
+                    else if (next.y & GB_DESC_TRIPLETS) relax_triplets(A, next, buf, my_lam, lout);
                     else relax_plain(A, next, buf, my_lam, lout);
                     nout = desc_rows(next);
                     xout = next.x;
@@ -752,7 +1009,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     grid_arrive(&dc->gsync, gen, target);
                     ok = grid_wait(&dc->gsync, &dc->err, gen, target);
                 } else {
-                    ok = nbr_wait(sweep_end ? s_ng > 0 : s_xn[nxt.c] > 0);
+                    ok = nbr_wait(sweep_end ? (nsplit ? s_nb > 0 : s_ng > 0) : s_xn[nxt.c] > 0);
                 }
                 if (!ok || s_abort) { drain(); return; }
             }
@@ -762,6 +1019,11 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
             cur = nxt;
         }
         ++it;
+        if (check_this && nsplit) {
+            // the check reads every body's accumulators: the classes' sums go back first
+            if (s_nb > 0) fold_part();
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
+        }
         if (check_this) {
             // as in k_pgs: re-formed accumulators every reform_every sweeps,
             // and for the check that ends the solve
@@ -783,7 +1045,11 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         // every block's cross updates of the part's bodies are out (the last
         // barrier or neighbour wait of the sweep, or the check's barrier):
         // the accumulators come back
-        if (s_ng > 0) load_part(false);
+        if (nsplit) {
+            if (s_nb > 0) fold_part();
+        } else if (s_ng > 0) {
+            load_part(false);
+        }
         __syncthreads();
     }
     // The global accumulators are current here (read back after the last

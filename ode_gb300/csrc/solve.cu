@@ -24,6 +24,7 @@
 #include <mutex>
 
 #include "gbode_internal.h"
+#include "../../include/gbode.h"
 
 namespace gb {
 
@@ -1433,21 +1434,64 @@ __global__ void k_wave_total(DevCounters *dc, const int *wcount, const int *wbas
 }
 
 // copy the rows of every staged slot into its wave's chunk (swizzled); one
-// block per wave, one thread per slot
+// block per wave, one thread per slot.  With split classes (nsplit: groups of
+// each class touching each body) a crossing group's rows are packed for mass
+// splitting: a body shared by n groups of the class enters each with 1/n of
+// its mass, so the row's scaled Jacobian, right-hand side and cfm (all
+// carrying Ad = W / (J M^-1 J^T + cfm)) are rescaled to W / (n1 D1 + n2 D2 +
+// cfm) -- D1, D2 the two bodies' shares of J M^-1 J^T -- and M^-1 J^T by n1
+// and n2 (the group's local copies of the bodies move n times as far); n1 and
+// n2 ride in the otherwise unused M1a.w and M2a.w, the bodies' masks of
+// shared classes (k_split_mask) in M1l.w and M2l.w.
 __global__ void k_pack_rows(Rows Rw, const int *cstart, const DevCounters *dc, const int4 *desc, const int *sched,
-                            const int *wcol, const int *chunk_start, float4 *packed) {
+                            const int *wcol, const int *chunk_start, float4 *packed, const int *nsplit,
+                            const int *smask, int nb) {
     const int nw = dc->nwaves;
+    const bool split = nsplit && dc->split_k > 0;
     for (int wv = blockIdx.x; wv < nw; wv += gridDim.x) {
         const int k = sched[(size_t)wv * blockDim.x + threadIdx.x];
         if (k < 0) continue;
-        const int4 d = desc[cstart[wcol[wv]] + k];
+        const int c = wcol[wv];
+        const int4 d = desc[cstart[c] + k];
         if (!(d.y & GB_DESC_STAGED)) continue;
         const int n = desc_rows(d), off = desc_chunk_off(d);
         float4 *dst = packed + (size_t)chunk_start[wv] * 8;
         const float4 *arr[8] = {Rw.J1l, Rw.J1a, Rw.J2l, Rw.J2a, Rw.M1l, Rw.M1a, Rw.M2l, Rw.M2a};
-        for (int i = 0; i < n; i++)
+        float n1 = 1.f, n2 = 1.f;
+        int m1 = 0, m2 = 0;
+        if (split) {
+            n1 = (float)max(1, nsplit[(size_t)c * nb + d.z]);
+            m1 = smask[d.z];
+            if (d.w >= 0) {
+                n2 = (float)max(1, nsplit[(size_t)c * nb + d.w]);
+                m2 = smask[d.w];
+            }
+        }
+        for (int i = 0; i < n; i++) {
+            float4 v[8];
 #pragma unroll
-            for (int a = 0; a < 8; a++) dst[swz(off + i, a)] = arr[a][d.x + i];
+            for (int a = 0; a < 8; a++) v[a] = arr[a][d.x + i];
+            if (split) {
+                const float ad = Rw.Ad[d.x + i];
+                const float d1 = (v[0].x * v[4].x + v[0].y * v[4].y + v[0].z * v[4].z + v[1].x * v[5].x +
+                                  v[1].y * v[5].y + v[1].z * v[5].z) / ad;
+                const float d2 = d.w >= 0 ? (v[2].x * v[6].x + v[2].y * v[6].y + v[2].z * v[6].z + v[3].x * v[7].x +
+                                             v[3].y * v[7].y + v[3].z * v[7].z) / ad
+                                          : 0.f;
+                const float cfm = v[1].w / ad;
+                const float s = (d1 + d2 + cfm) / (n1 * d1 + n2 * d2 + cfm);
+                v[0].x *= s; v[0].y *= s; v[0].z *= s; v[0].w *= s;
+                v[1].x *= s; v[1].y *= s; v[1].z *= s; v[1].w *= s;
+                v[2].x *= s; v[2].y *= s; v[2].z *= s;  // w: lo
+                v[3].x *= s; v[3].y *= s; v[3].z *= s;  // w: hi
+                v[4].x *= n1; v[4].y *= n1; v[4].z *= n1; v[4].w = __int_as_float(m1);
+                v[5].x *= n1; v[5].y *= n1; v[5].z *= n1; v[5].w = n1;
+                v[6].x *= n2; v[6].y *= n2; v[6].z *= n2; v[6].w = __int_as_float(m2);
+                v[7].x *= n2; v[7].y *= n2; v[7].z *= n2; v[7].w = n2;
+            }
+#pragma unroll
+            for (int a = 0; a < 8; a++) dst[swz(off + i, a)] = v[a];
+        }
     }
 }
 
@@ -1568,17 +1612,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // the instruction caches.
 // The multipliers come back in lout (registers): the caller stores them after
 // its barrier arrival, so those stores do not delay the release.
-__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
-                                               float (&lout)[GB_STAGED_ROWS]) {
-    const int nct = desc_rows(d) / 3, off = desc_chunk_off(d);
-    const bool two = d.w >= 0;
-    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
-    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
-    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
-    cp_async_wait_all();
+// The rows of a staged triplet manifold against the accumulators f1*, f2*.
+__device__ __forceinline__ void triplet_rows(int passes, int nct, int off, const float4 *buf, float *lam,
+                                             float4 &f1l, float4 &f1a, float4 &f2l, float4 &f2a) {
     float4 row[8];
 #pragma unroll 1
-    for (int pass = 0; pass < A.passes; pass++) {
+    for (int pass = 0; pass < passes; pass++) {
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             if (c >= nct) break;
@@ -1601,6 +1640,16 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
             }
         }
     }
+}
+__device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
+                                               float (&lout)[GB_STAGED_ROWS]) {
+    const int nct = desc_rows(d) / 3, off = desc_chunk_off(d);
+    const bool two = d.w >= 0;
+    float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
+    float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
+    if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
+    cp_async_wait_all();
+    triplet_rows(A.passes, nct, off, buf, lam, f1l, f1a, f2l, f2a);
 #pragma unroll
     for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < 3 * nct ? lam[k] : 0.f;
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
@@ -1608,6 +1657,19 @@ __device__ __forceinline__ void relax_triplets(const PgsArgs &A, int4 d, const f
 }
 
 // A staged plain group (GB_DESC_PLAIN): every row in order with its own bounds.
+__device__ __forceinline__ void plain_rows(int passes, int n, int off, const float4 *buf, float *lam,
+                                           float4 &f1l, float4 &f1a, float4 &f2l, float4 &f2a) {
+    float4 row[8];
+#pragma unroll 1
+    for (int pass = 0; pass < passes; pass++) {
+#pragma unroll 1
+        for (int k = 0; k < n; k++) {
+#pragma unroll
+            for (int a = 0; a < 8; a++) row[a] = buf[swz(off + k, a)];
+            relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
+        }
+    }
+}
 __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const float4 *buf, float *lam,
                                             float (&lout)[GB_STAGED_ROWS]) {
     const int n = desc_rows(d), off = desc_chunk_off(d);
@@ -1616,16 +1678,7 @@ __device__ __forceinline__ void relax_plain(const PgsArgs &A, int4 d, const floa
     float4 f2l = make_float4(0, 0, 0, 0), f2a = f2l;
     if (two) { f2l = ldcg4(&A.fc[2 * d.w]); f2a = ldcg4(&A.fc[2 * d.w + 1]); }
     cp_async_wait_all();
-    float4 row[8];
-#pragma unroll 1
-    for (int pass = 0; pass < A.passes; pass++) {
-#pragma unroll 1
-        for (int k = 0; k < n; k++) {
-#pragma unroll
-            for (int a = 0; a < 8; a++) row[a] = buf[swz(off + k, a)];
-            relax_fast_row<true>(row, lam[k], row[2].w, row[3].w, f1l, f1a, f2l, f2a);
-        }
-    }
+    plain_rows(A.passes, n, off, buf, lam, f1l, f1a, f2l, f2a);
 #pragma unroll
     for (int k = 0; k < GB_STAGED_ROWS; k++) lout[k] = k < n ? lam[k] : 0.f;
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
@@ -2395,6 +2448,7 @@ static void warm_store(Workspace &ws, cudaStream_t s) {
 // joints, blocks, the two-level sweep's partition).
 struct ColouredPlan {
     int pgs_blocks, sx, sy, chunk_cap, ncb, threads;
+    int split;  // split classes asked for (two-level sweep), 0: none
     bool slab;
     SlabCaps caps;
     size_t ngroups, wave_cap;
@@ -2405,6 +2459,7 @@ static ColouredPlan plan_coloured(const Workspace &ws, const SolverParams &P) {
     c.threads = P.pgs_threads == 128 ? 128 : GB_PGS_THREADS;
     c.caps = slab_caps(c.threads);
     c.slab = P.pgs_two_level && c.pgs_blocks >= 2 && c.caps.rcap > 0;
+    c.split = c.slab && P.pgs_split >= 2 ? P.pgs_split : 0;
     c.ngroups = (size_t)(ws.contact_cap > 0 ? ws.contact_cap : 1) + (ws.njoints > 0 ? ws.njoints : 0);
     c.sx = 1;
     if (c.slab)
@@ -2439,7 +2494,9 @@ static bool ensure_coloured(Workspace &ws, int nb, const ColouredPlan &c) {
            ws.x_cnt.ensure((size_t)64 * c.pgs_blocks * 4) && ws.x_start.ensure((size_t)64 * c.pgs_blocks * 4 + 4) &&
            ws.x_fill.ensure((size_t)64 * c.pgs_blocks * 4) && ws.x_accn.ensure(nbb * 4) &&
            ws.x_acc.ensure(nbb * GB_XACC * 4) && ws.x_adj.ensure((size_t)c.pgs_blocks * GB_XADJ_WORDS * 4) &&
-           ws.x_prog.ensure((size_t)c.pgs_blocks * 4);
+           ws.x_prog.ensure((size_t)c.pgs_blocks * 4) &&
+           (!c.split || (ws.x_nsplit.ensure((size_t)c.split * nbb * 4) && ws.x_dacc.ensure((size_t)c.split * nbb * 48) &&
+                         ws.x_smask.ensure(nbb * 4)));
 }
 
 // Every device buffer a step writes, allocated before its first kernel: an
@@ -2635,6 +2692,22 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                         (void *)&nb, (void *)&cls, (void *)&climit};
         if (cudaLaunchCooperativeKernel((const void *)k_colour, blocks, 256, args, 0, s) != cudaSuccess) return false;
     }
+    // split classes: the crossing colours merged into plan.split classes
+    const int nsplit = plan.split;
+    cudaMemsetAsync(&ws.dc->split_off, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->split_k, 0, 4, s);
+    if (nsplit) {
+        const size_t nbb = nb > 0 ? nb : 1;
+        k_split_check<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.s_gdesc.as<int4>(), ws.grp_body.as<int2>(),
+                                           ws.s_part.as<int>(), ws.s_blocal.as<int>(), caps.bcap);
+        k_split_classes<<<1, 1, 0, s>>>(ws.dc, nsplit);
+        k_split_remap<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>());
+        cudaMemsetAsync(ws.x_nsplit.p, 0, (size_t)nsplit * nbb * 4, s);
+        k_split_count<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), nb,
+                                           ws.x_nsplit.as<int>());
+        k_split_mask<<<grid, 256, 0, s>>>(ws.dc, ws.x_nsplit.as<int>(), nb, ws.x_smask.as<int>());
+        count_launch(5);
+    }
     cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
     cudaMemsetAsync(ws.col_fill.p, 0, GB_MAX_COLOURS * 4, s);
     k_colour_count<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_count.as<int>());
@@ -2680,7 +2753,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         scan_exclusive(ws.chunk_rows.as<int>(), ws.chunk_start.as<int>(), &ws.dc->nwaves, (int)wave_cap, nullptr, ws, s);
         k_pack_rows<<<grid, threads, 0, s>>>(rows_view(ws), ws.col_start.as<int>(), ws.dc, ws.m_desc.as<int4>(),
                                                     ws.wv_sched.as<int>(), ws.wv_col.as<int>(),
-                                                    ws.chunk_start.as<int>(), ws.p_rows.as<float4>());
+                                                    ws.chunk_start.as<int>(), ws.p_rows.as<float4>(),
+                                                    nsplit ? ws.x_nsplit.as<int>() : nullptr, ws.x_smask.as<int>(),
+                                                    nb);
         count_launch(4);
     }
     if (slab) {
@@ -2700,18 +2775,22 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
                                          ws.s_idesc.as<int4>(), ws.s_ipack.as<float4>(), ws.dc);
         count_launch(3);
     }
-    if (xspatial) {
+    if (xspatial || nsplit) {
         // the blocks touching each body, and every two of them adjacent
         const size_t nbb = nb > 0 ? nb : 1;
         cudaMemsetAsync(ws.x_accn.p, 0, nbb * 4, s);
-        cudaMemsetAsync(ws.x_adj.p, 0, (size_t)pgs_blocks * GB_XADJ_WORDS * 4, s);
         cudaMemsetAsync(&ws.dc->slab_nbr_over, 0, 4, s);
         k_xacc<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), ws.s_part.as<int>(),
                                     pgs_blocks, ws.x_accn.as<int>(), ws.x_acc.as<int>());
-        k_xadj<<<grid, 256, 0, s>>>(ws.x_accn.as<int>(), ws.x_acc.as<int>(), ws.s_part.as<int>(), nb,
-                                    ws.x_adj.as<unsigned>());
-        cudaMemsetAsync(ws.x_prog.p, 0, (size_t)pgs_blocks * 4, s);
-        count_launch(2);
+        count_launch();
+        if (xspatial) {
+            cudaMemsetAsync(ws.x_adj.p, 0, (size_t)pgs_blocks * GB_XADJ_WORDS * 4, s);
+            k_xadj<<<grid, 256, 0, s>>>(ws.x_accn.as<int>(), ws.x_acc.as<int>(), ws.s_part.as<int>(), nb,
+                                        ws.x_adj.as<unsigned>());
+            cudaMemsetAsync(ws.x_prog.p, 0, (size_t)pgs_blocks * 4, s);
+            count_launch();
+        }
+        if (nsplit) cudaMemsetAsync(ws.x_dacc.p, 0, (size_t)nsplit * nbb * 48, s);
     }
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
@@ -2778,6 +2857,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             SA.xcnt = ws.x_cnt.as<int>();
             SA.xadj = ws.x_adj.as<unsigned>();
             SA.xprog = ws.x_prog.as<unsigned>();
+            SA.split = nsplit;
+            SA.dacc = ws.x_dacc.as<long long>();
+            SA.smask = ws.x_smask.as<int>();
             void *args[] = {(void *)&SA};
             const void *k = threads == 128 ? (const void *)k_pgs_slab<128> : (const void *)k_pgs_slab<256>;
             if (cudaLaunchCooperativeKernel(k, blocks, threads, args, caps.smem, s) != cudaSuccess) return false;

@@ -60,7 +60,7 @@ class gbodeStepStats(ctypes.Structure):
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
                 ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int),
                 ("interior_colours", ctypes.c_int), ("interior_rows", ctypes.c_int),
-                ("neighbour_waits", ctypes.c_int)]
+                ("neighbour_waits", ctypes.c_int), ("cross_classes", ctypes.c_int)]
 
 
 dNearCallback = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ID, ID)
@@ -163,6 +163,7 @@ _PROTOS = [
     ("gbodeWorldSetTwoLevelSweep", None, [ID, ctypes.c_int]), ("gbodeWorldGetTwoLevelSweep", ctypes.c_int, [ID]),
     ("gbodeWorldSetSweepSync", None, [ID, ctypes.c_int]), ("gbodeWorldGetSweepSync", ctypes.c_int, [ID]),
     ("gbodeWorldSetResidualChecks", None, [ID, ctypes.c_int, ctypes.c_int]),
+    ("gbodeWorldSetCrossClasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetCrossClasses", ctypes.c_int, [ID]),
     ("gbodeTestInject", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetSolverTiles", None, [ID, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldGetSolverTiles", None, [ID, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),

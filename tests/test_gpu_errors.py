@@ -1,8 +1,9 @@
 """Error paths of the step, provoked without faulting the GPU
 (gbodeTestInject), through the C ABI.
 
-* A grid barrier whose counter starts one arrival short: every block's
-  bounded wait runs out (2^22 polls, a second or two), the solver kernel
+* A grid barrier whose counter starts one arrival short (and, under the
+  two-level sweep's neighbour waits, every block's step counter one step
+  short): every block's bounded wait runs out (2^22 polls, a second or two), the solver kernel
   returns, gbodeWorldSynchronize reports ERR_BARRIER_TIMEOUT (0x1), and the
   next step runs normally on the same context.
 * A staging wait that names a copy never issued: ERR_STAGE_TIMEOUT (0x100),
@@ -42,11 +43,12 @@ def _sync_bits(w):
     return False, int(msg.split("0x")[1].split()[0], 16)
 
 
-def _settled_pile(two_level=0, n=2048, steps=40):
+def _settled_pile(two_level=0, n=2048, steps=40, classes=0):
     from ode_gb300 import scenes, sim
     w = sim.GBWorld(scenes.pile(n, seed=11))
     w.L.dWorldSetQuickStepNumIterations(w.w, 30)
     w.L.gbodeWorldSetTwoLevelSweep(w.w, two_level)
+    w.L.gbodeWorldSetCrossClasses(w.w, classes)
     for _ in range(steps):
         w.step_fused()
     assert _sync_bits(w) == (True, 0)
@@ -61,12 +63,12 @@ def _injection_off(gblib):
     gblib.gbodeTestInject(ode.GBODE_TEST_OFF, 0, 0)
 
 
-@pytest.mark.parametrize("two_level", [0, 2])
+@pytest.mark.parametrize("two_level,classes", [(0, 0), (2, 0), (2, 4)])
 @pytest.mark.parametrize("kind,bit", [("barrier", ERR_BARRIER_TIMEOUT), ("stage", ERR_STAGE_TIMEOUT)])
-def test_bounded_waits_run_out_and_report(gblib, two_level, kind, bit):
+def test_bounded_waits_run_out_and_report(gblib, two_level, classes, kind, bit):
     from ode_gb300 import ode
     L = gblib
-    w = _settled_pile(two_level)
+    w = _settled_pile(two_level, classes=classes)
     before = w.stats().iterations
     L.gbodeTestInject(ode.GBODE_TEST_BARRIER if kind == "barrier" else ode.GBODE_TEST_STAGE, 1, 0)
     t0 = time.perf_counter()
@@ -120,8 +122,8 @@ def test_capacity_overflows_are_reported(gblib):
     w.close()
 
 
-@pytest.mark.parametrize("two_level", [0, 2])
-def test_failed_allocation_leaves_state_unchanged(gblib, two_level):
+@pytest.mark.parametrize("two_level,classes", [(0, 0), (2, 0), (2, 4)])
+def test_failed_allocation_leaves_state_unchanged(gblib, two_level, classes):
     from ode_gb300 import ode, scenes, sim
     L = gblib
     sc = scenes.pile(512, seed=13)
@@ -130,6 +132,7 @@ def test_failed_allocation_leaves_state_unchanged(gblib, two_level):
         w = sim.GBWorld(sc)
         L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
         L.gbodeWorldSetTwoLevelSweep(w.w, two_level)
+        L.gbodeWorldSetCrossClasses(w.w, classes)
         return w
 
     def fused(w):
@@ -171,6 +174,7 @@ def test_failed_allocation_leaves_state_unchanged(gblib, two_level):
         w.close()
     else:
         pytest.fail("the step kept allocating")
-    print(f"{'two-level' if two_level else 'one-level'} sweep: {failed} allocation points of a first step "
+    print(f"{'two-level' if two_level else 'one-level'} sweep{' in split classes' if classes else ''}: "
+          f"{failed} allocation points of a first step "
           f"failed in turn, each leaving the state unchanged; {tolerated} worked around with the same result")
     assert failed > 20

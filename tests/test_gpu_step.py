@@ -448,6 +448,50 @@ def test_neighbour_waits_match_grid_barriers(gblib, target):
         w.close()
 
 
+def test_split_classes_on_a_pile(gblib):
+    """Split classes (gbodeWorldSetCrossClasses): the two-level sweep's
+    crossing colours merged into 5 classes, each relaxed at once with mass
+    splitting, on an 8,192-body pile that has landed.  Every step reaches the
+    residual target, and its FP64 residual evaluated on the device confirms
+    the last one (1.5e-4: an FP32 solution at 1e-4); the class sums are integers, so two
+    worlds agree to the bit, and neighbour waits agree with grid barriers to
+    the bit; positions agree with the exact colours' solution of the same
+    steps within 1e-3 m (both are solutions to a residual of 1e-4)."""
+    from ode_gb300 import ode, scenes, sim
+    L = gblib
+    sc = scenes.pile(8192, seed=7)
+    worlds = [sim.GBWorld(sc) for _ in range(4)]
+    for w in worlds:
+        L.gbodeWorldSetWarmStart(w.w, 1, 1.0)
+        L.dWorldSetQuickStepW(w.w, 1.0)
+        L.dWorldSetQuickStepNumIterations(w.w, 30)
+    for _ in range(300):
+        for w in worlds:
+            w.step_fused()
+    for w, k, mode in zip(worlds, (0, 5, 5, 5), (0, 0, 0, ode.GBODE_SYNC_GRID)):
+        L.gbodeWorldSetTwoLevelSweep(w.w, 2)
+        L.gbodeWorldSetCrossClasses(w.w, k)
+        assert L.gbodeWorldGetCrossClasses(w.w) == k
+        L.gbodeWorldSetSweepSync(w.w, mode)
+        L.gbodeWorldSetResidualTarget(w.w, 1e-4, 5, 3000)
+    for step in range(3):
+        for w in worlds:
+            assert w.step_fused() == 1, L.gbodeGetLastError()
+        ex, a, b, c = (w.stats() for w in worlds)
+        assert ex.cross_classes == 0 and a.cross_classes == 5 and c.cross_classes == 5
+        assert a.residual <= 1e-4 and (a.iterations, a.rows) == (b.iterations, b.rows) == (c.iterations, c.rows)
+        sa, sb, scc = worlds[1].state(), worlds[2].state(), worlds[3].state()
+        assert np.array_equal(sa, sb) and np.array_equal(sa, scc), step
+    r64, _, ml = worlds[1].last_residual()
+    print(f"split classes: {a.iterations} sweeps ({ex.iterations} with exact colours, {ex.colours} colours), "
+          f"{a.colours} classes; FP64 residual {r64 / max(1.0, ml):.2e}; positions differ from the exact colours' "
+          f"by {np.abs(worlds[0].state()[:, 0:3] - sa[:, 0:3]).max():.2e} m")
+    assert r64 / max(1.0, ml) <= 1.5e-4
+    assert np.abs(worlds[0].state()[:, 0:3] - sa[:, 0:3]).max() <= 1e-3
+    for w in worlds:
+        w.close()
+
+
 def test_two_level_sweep_on_a_pile(gblib):
     """The two-level sweep (gbodeWorldSetTwoLevelSweep) on an 8,192-body
     pile that has landed: most rows are interior to a column and relaxed from
