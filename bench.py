@@ -49,9 +49,9 @@ B_ROW = 132        # algorithmic bytes per PGS row-iteration
 B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
 # DRAM bytes (read + write) per launch of the sweep kernel on the settled 32,768-body pile,
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches):
-# k_pgs_slab (two-level sweep, kernel of commit e119748): 77.7 and 76.3 MB;
+# k_pgs_slab (two-level sweep, 4 split classes, kernel of commit f71259a): 83.1 and 80.6 MB;
 # k_pgs (one-level): 240.4 and 204.2 MB.  The rows stay in L2 / shared memory across sweeps.
-PGS_TRAFFIC = {"gb::k_pgs_slab": 7.703e7, "gb::k_pgs": 2.223e8}
+PGS_TRAFFIC = {"gb::k_pgs_slab": 8.185e7, "gb::k_pgs": 2.223e8}
 
 
 def parse():
@@ -457,7 +457,7 @@ def run_gbode(args, ws, rank, local):
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": PGS_TRAFFIC["gb::k_pgs_slab" if args.two_level else "gb::k_pgs"],
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches "
-                                       "of the same kernel from the settled pile",
+                                       "of the same kernel from the settled pile (kernel of commit f71259a)",
                      "algorithmic_bytes_per_launch": pgs_bytes / args.steps},
         "clocks": clk,
         "gpu_launches": launches,
