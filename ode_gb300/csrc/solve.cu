@@ -1907,8 +1907,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
                 // prefetch the next slot while the other blocks arrive.  Before a
                 // residual check (which reads every multiplier right after this
                 // barrier) they go out before the arrival.
-                const bool check_next = residual_mode && sweep_end &&
-                                        ((it + 1) % A.check_every == 0 || it + 1 == itmax);
+                const bool check_next = residual_mode && sweep_end && (it + 1 >= plan.next || it + 1 == itmax);
                 if (check_next) {
 #pragma unroll
                     for (int k = 0; k < GB_STAGED_ROWS; k++)
