@@ -47,6 +47,8 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s at LCP residual \u22641e-4: plain GPU PGS vs learned warm start, 1 GB300"
 B_ROW = 132        # algorithmic bytes per PGS row-iteration
 B_ROW_CHECK = 80   # bytes per row of a residual sweep (J 64 + lambda + findex + bodies)
+B_ROW_MOM = 8      # momentum between sweeps: a row's previous result read and written
+B_BODY_MOM = 128   # momentum between sweeps: a body's accumulators and their previous values, read and written
 # DRAM bytes (read + write) per launch of the sweep kernel on the settled 32,768-body pile,
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches):
 # k_pgs_slab (two-level sweep, 4 split classes, kernel of commit f71259a): 83.1 and 80.6 MB;
@@ -88,9 +90,12 @@ def parse():
     ap.add_argument("--two-level", type=int, default=2,
                     help="two-level sweep of the pile's solver with this many interior phases a sweep "
                          "(gbodeWorldSetTwoLevelSweep; 0: off)")
-    ap.add_argument("--cross-classes", type=int, default=4,
+    ap.add_argument("--cross-classes", type=int, default=0,
                     help="two-level sweep: crossing colours merged into this many mass-split classes "
                          "(gbodeWorldSetCrossClasses; 0: exact colours)")
+    ap.add_argument("--momentum", type=float, default=0.8,
+                    help="momentum between the coloured solver's sweeps in the residual-target legs "
+                         "(gbodeWorldSetSweepMomentum; 0: plain sweeps)")
     ap.add_argument("--sweep-sync", choices=("neighbours", "grid"), default="neighbours",
                     help="two-level sweep: blocks wait on the blocks sharing their bodies, or on a grid barrier "
                          "after every step (gbodeWorldSetSweepSync)")
@@ -337,6 +342,7 @@ def run_gbode(args, ws, rank, local):
     L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
     L.gbodeWorldSetSweepSync(w.w, ode.GBODE_SYNC_GRID if args.sweep_sync == "grid" else ode.GBODE_SYNC_NEIGHBOURS)
     L.gbodeWorldSetCrossClasses(w.w, args.cross_classes)
+    L.gbodeWorldSetSweepMomentum(w.w, args.momentum)
     L.gbodeWorldSetTiming(w.w, 1)
     if args.profile_steps:
         for _ in range(args.profile_steps):
@@ -382,7 +388,10 @@ def run_gbode(args, ws, rank, local):
     # per interior phase
     checks = T["checks"]
     extra = max(0, args.two_level - 1)
-    pgs_bytes = sum(s * (m + extra * mi) * B_ROW + c * m * B_ROW_CHECK
+    # momentum: every sweep but the first and the checked ones moves the rows and bodies on
+    mom_bytes = sum(max(0, s - c - 1) * (m * B_ROW_MOM + sc.nb * B_BODY_MOM)
+                    for s, m, c in zip(sweeps, rows, checks)) if args.momentum > 0 else 0
+    pgs_bytes = mom_bytes + sum(s * (m + extra * mi) * B_ROW + c * m * B_ROW_CHECK
                     for s, m, mi, c in zip(sweeps, rows, T["interior_rows"], checks))
     pgs_s = sum(solve_ms) / 1e3
     achieved = pgs_bytes / pgs_s / 1e9 if pgs_s > 0 else 0.0
@@ -439,7 +448,9 @@ def run_gbode(args, ws, rank, local):
                                 + ("neighbour waits" if min(T["neighbour_waits"]) else "grid barriers")
                                 + (f", crossing colours in {min(T['cross_classes'])} mass-split classes"
                                    if min(T["cross_classes"]) else "") + ")"
-                                if args.two_level else ""),
+                                if args.two_level else "")
+                             + (f", momentum {args.momentum} between sweeps (at the end of a step: min "
+                                f"{min(T['momentum']):.3g}, max {max(T['momentum']):.3g})" if args.momentum > 0 else ""),
                    "interior_rows_per_step": float(np.mean(T["interior_rows"])),
                    "interior_colours": int(np.median(T["interior_colours"])),
                    "warm_start": f"previous-step lambda x {args.warm_scale}" if args.warm_scale > 0 else "cold",
@@ -507,6 +518,7 @@ def batched_leg(args, L, stream, dev, kind):
                                  ("residual", args.target, False), ("residual_graph", args.target, True)):
         if target > 0:
             L.gbodeWorldSetResidualTarget(w.w, target, args.check_every, args.max_iters)
+            L.gbodeWorldSetSweepMomentum(w.w, args.momentum)
         restore_snapshot(L, w)
         for _ in range(args.warmup):
             if graph:
@@ -536,6 +548,7 @@ def batched_leg(args, L, stream, dev, kind):
                                    "tuning": {"blocks": tu.blocks, "passes": tu.passes,
                                               "check_every": tu.check_every, "threads_per_block": tu.threads,
                                               "staged_rows_per_buffer": tu.chunk_rows, "two_level": tu.two_level,
+                                              "momentum": round(tu.momentum, 3),
                                               "candidates": tu.candidates}}
     if kind == "vehicles" and not args.no_learned:
         out["residual_learned_tuned_graph"] = learned_batched(args, L, w, stream, flush, sc.nb)
@@ -602,7 +615,8 @@ def timed_steps(w, stream, flush, steps, graph=False):
     (L2 flushed before each, outside the events); per-step statistics."""
     import torch
     out = {k: [] for k in ("step_ms", "solve_ms", "sweeps", "resid", "rows", "contacts", "colours",
-                           "interior_rows", "interior_colours", "neighbour_waits", "checks", "cross_classes")}
+                           "interior_rows", "interior_colours", "neighbour_waits", "checks", "cross_classes",
+                           "momentum")}
     hist = np.zeros(256, np.float32)
     torch.cuda.nvtx.range_push("timed")
     for _ in range(steps):
@@ -629,6 +643,7 @@ def timed_steps(w, stream, flush, steps, graph=False):
         out["interior_colours"].append(st.interior_colours)
         out["neighbour_waits"].append(st.neighbour_waits)
         out["cross_classes"].append(st.cross_classes)
+        out["momentum"].append(st.momentum)
         out["checks"].append(w.L.gbodeWorldGetResidualHistory(w.w, hist.ctypes.data_as(ode_f32p()), 256))
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()

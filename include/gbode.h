@@ -450,6 +450,24 @@ int gbodeWorldGetSweepSync(dWorldID w);
 void gbodeWorldSetCrossClasses(dWorldID w, int classes);
 int gbodeWorldGetCrossClasses(dWorldID w);
 
+/* Momentum between the sweeps of the coloured solver (no counterpart in the
+ * reference; 0: off, the default; clamped to [0, 0.95]).  After each sweep
+ * every multiplier moves on from the sweep's projected Gauss-Seidel result
+ * y_k to y_k + beta (y_k - y_{k-1}), and every body's velocity accumulators
+ * by the same rule, before the next sweep starts from them (the fixed-
+ * coefficient extrapolation of Nesterov's accelerated gradient method, applied
+ * to the sweep's iterates).  A solution of the LCP is a fixed point of both,
+ * so the solution is the same; on deep piles beta = 0.5 reaches a residual
+ * target in fewer sweeps.  The first and the last sweep, and every sweep that
+ * ends in a residual check, are plain, so every check and the final
+ * multipliers are Gauss-Seidel results; a check whose residual rose halves
+ * beta for the rest of the step (gbodeStepStats.momentum reads the value at
+ * the end).  On the two-level sweep a step whose crossing manifolds touch a
+ * body outside the columns' lists runs without it (momentum reads 0).  The
+ * result does not depend on timing. */
+void gbodeWorldSetSweepMomentum(dWorldID w, dReal beta);
+dReal gbodeWorldGetSweepMomentum(dWorldID w);
+
 /* The fused GPU path: hash-space broad phase, narrow phase and contact-joint
  * creation without leaving the device.  Equivalent to dSpaceCollide with a near
  * callback that calls dCollide(o1, o2, maxc, ...) and makes one contact joint
@@ -518,6 +536,7 @@ typedef struct gbodeStepStats {
     int neighbour_waits;   /* two-level sweep: the blocks waited only on their neighbours (1), or on grid
                               barriers (0: GBODE_SYNC_GRID, or a body touched by too many blocks) */
     int cross_classes;     /* two-level sweep: split classes of the crossing manifolds (0: exact colours) */
+    float momentum;        /* momentum between sweeps at the end of the solve (0: off or not used) */
 } gbodeStepStats;
 void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out);
 /* Record CUDA events around the solver and the step (adds no host syncs). */
@@ -540,7 +559,9 @@ void gbodeWorldDropSnapshot(dWorldID w);
  * slots one wave of a colour relaxes at once), staged rows a shared-memory
  * buffer (400 or 800), the two-level sweep (off, or two interior passes),
  * residual checks every 5 or 10 sweeps when a residual target is set, and
- * also half the solver blocks or two passes over a group's rows -- restores that state and times
+ * also half the solver blocks or two passes over a group's rows; each with
+ * and without the sweep momentum when a residual target and a momentum are
+ * set -- restores that state and times
  * `steps` gbodeWorldStepFused steps (after two untimed ones) with CUDA
  * events.  It keeps the candidate with the lowest median step time, leaves
  * it set, and restores the state once more: the world continues from the
@@ -555,6 +576,7 @@ typedef struct gbodeTuning {
     int threads;      /* gbodeWorldSetSolverTiles: threads a block */
     int chunk_rows;   /* gbodeWorldSetSolverTiles: staged rows a buffer */
     int two_level;    /* gbodeWorldSetTwoLevelSweep */
+    float momentum;   /* gbodeWorldSetSweepMomentum: the value set, or 0 if the sweeps were faster without */
 } gbodeTuning;
 int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dSurfaceParameters *s, int maxc,
                        dReal dt, int steps, int use_graph, gbodeTuning *best);

@@ -800,6 +800,10 @@ void gbodeWorldSetCrossClasses(dWorldID w, int classes) {
     w->P.pgs_split = classes < 2 ? 0 : (classes > GBODE_MAX_CROSS_CLASSES ? GBODE_MAX_CROSS_CLASSES : classes);
 }
 int gbodeWorldGetCrossClasses(dWorldID w) { return w->P.pgs_split; }
+void gbodeWorldSetSweepMomentum(dWorldID w, dReal beta) {
+    w->P.momentum = beta > 0.f ? (beta < 0.95f ? beta : 0.95f) : 0.f;
+}
+dReal gbodeWorldGetSweepMomentum(dWorldID w) { return w->P.momentum; }
 int gbodeWorldGetSolverBlocks(dWorldID w) { return w->P.pgs_blocks > 0 && w->P.pgs_blocks < num_sms() ? w->P.pgs_blocks : num_sms(); }
 
 int gbodeWorldSetLearnedWarmStart(dWorldID w, const float *params, int enabled) {
@@ -2376,21 +2380,28 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     // sweep stages its crossing rows in 128-row buffers), the two-level sweep
     // (off, or two interior passes), the residual check interval; and, as
     // before, half the blocks and two passes over a group's rows
-    struct Cand { int blocks, passes, check, threads, chunk, two; };
+    // and, with a residual target and momentum set (gbodeWorldSetSweepMomentum),
+    // every candidate with and without it
+    struct Cand { int blocks, passes, check, threads, chunk, two; float mom; };
     std::vector<Cand> cands;
     const int sms = num_sms();
     const bool resid = w->P.residual_target > 0;
-    for (int threads : {256, 128})
-        for (int two : {0, 2})
-            for (int chunk : {800, 400}) {
-                if (two && chunk != 800) continue;
-                for (int check : {5, 10}) {
-                    if (!resid && check != 5) continue;
-                    cands.push_back({sms, 1, resid ? check : 0, threads, chunk, two});
+    const float mom_set = w->P.momentum;
+    std::vector<float> moms{mom_set};
+    if (resid && mom_set > 0.f) moms.push_back(0.f);
+    for (float mom : moms) {
+        for (int threads : {256, 128})
+            for (int two : {0, 2})
+                for (int chunk : {800, 400}) {
+                    if (two && chunk != 800) continue;
+                    for (int check : {5, 10}) {
+                        if (!resid && check != 5) continue;
+                        cands.push_back({sms, 1, resid ? check : 0, threads, chunk, two, mom});
+                    }
                 }
-            }
-    cands.push_back({sms / 2, 1, resid ? 5 : 0, 256, 800, 0});
-    cands.push_back({sms, 2, resid ? 5 : 0, 256, 800, 0});
+        cands.push_back({sms / 2, 1, resid ? 5 : 0, 256, 800, 0, mom});
+        cands.push_back({sms, 2, resid ? 5 : 0, 256, 800, 0, mom});
+    }
     // every candidate starts from the same state: the device-side simulation
     // state (bodies, warm-start tables, joint multipliers, auto-disable state,
     // counters) is copied aside once and put back before each candidate and
@@ -2419,6 +2430,7 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
         w->P.pgs_threads = cands[i].threads == 128 ? 128 : 0;
         w->P.pgs_chunk = cands[i].chunk;
         w->P.pgs_two_level = cands[i].two;
+        w->P.momentum = cands[i].mom;
         if (resid) w->P.check_every = cands[i].check;
         std::vector<float> t;
         for (int k = 0; k < steps + 2; k++) {
@@ -2454,7 +2466,9 @@ int gbodeWorldAutotune(dWorldID w, dSpaceID space, dJointGroupID group, const dS
     w->P.pgs_threads = c.threads == 128 ? 128 : 0;
     w->P.pgs_chunk = c.chunk;
     w->P.pgs_two_level = c.two;
+    w->P.momentum = c.mom;
     if (resid) w->P.check_every = c.check;
+    best->momentum = c.mom;
     best->blocks = c.blocks;
     best->threads = c.threads;
     best->chunk_rows = c.chunk;
@@ -2532,6 +2546,7 @@ void gbodeWorldGetStepStats(dWorldID w, gbodeStepStats *out) {
         w->stats.interior_rows = h.slab_rows;
         w->stats.neighbour_waits = h.slab_sync;
         w->stats.cross_classes = h.split_k;
+        w->stats.momentum = h.mom_final;
         w->stats.solve_ms = 0;
         w->stats.step_ms = 0;
         if (w->timing) {

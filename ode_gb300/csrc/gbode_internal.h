@@ -48,6 +48,7 @@ struct SolverParams {
     int pgs_split;      // two-level sweep: cross colours merged into this many classes, each relaxed as one
                         // step with mass splitting (0: every cross colour its own step)
     int reform_every;   // residual-target mode: sweeps between re-formed accumulators (0: 500)
+    float momentum;     // coloured solvers: momentum between sweeps (0: off; see k_pgs)
 };
 
 // learned warm start network (parameter layout in mlp.cu)
@@ -94,6 +95,8 @@ struct DevCounters {
     int slab_sync;         // the last solve's two-level sweep waited on neighbour blocks (1) or grid barriers (0)
     int split_off;         // two-level sweep: a cross group cannot be relaxed in a split class (exact colours)
     int split_k;           // two-level sweep: classes of the last solve's cross phase with mass splitting (0: off)
+    int mom_off;           // two-level sweep: a group touches a body outside the columns' lists (no momentum)
+    float mom_final;       // momentum of the last solve's last sweeps (0: off)
 };
 
 // auto-disable state per body, int4: x flags, y idle steps, z steps left,
@@ -137,6 +140,8 @@ struct Workspace {
     DBuf x_cnt, x_start, x_fill, x_accn, x_acc, x_adj, x_prog;
     // two-level sweep, split classes: groups per (class, body), fixed-point accumulators per (class, body)
     DBuf x_nsplit, x_dacc, x_smask;
+    // momentum between sweeps: every row's multiplier after the previous sweep, every body's accumulators
+    DBuf m_lprev, b_fcprev;
     // learned warm start
     DBuf l_feat, l_scale, l_pred, l_alt, mlp_P, mlp_wb;
     // ball and hinge joints (uploaded when they change) and per-step joint state

@@ -331,6 +331,22 @@ __global__ void k_split_check(DevCounters *dc, const int *colour, const int4 *gd
         if (bad) dc->split_off = 1;
     }
 }
+// Momentum between sweeps needs every body that a crossing group moves in a
+// column's body list: each column moves its listed bodies' accumulators on at
+// the end of a sweep (interior groups' bodies are listed by construction).
+__global__ void k_mom_check(DevCounters *dc, const int *colour, const int2 *gbody, const int *part,
+                            const int *blocal, int bcap) {
+    const int ng = dc->nmanifolds;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ng; e += gridDim.x * blockDim.x) {
+        const int c = colour[e];
+        if (c >= 64 && c < 64 + GB_SLAB_COLOURS) continue;
+        const int2 gb = gbody[e];
+        bool bad = false;
+        if (gb.x >= 0 && (part[gb.x] < 0 || blocal[gb.x] >= bcap)) bad = true;
+        if (gb.y >= 0 && (part[gb.y] < 0 || blocal[gb.y] >= bcap)) bad = true;
+        if (bad) dc->mom_off = 1;
+    }
+}
 // classes of this solve: k, or 0 (exact colours) if a group cannot be split or
 // there are no more colours than classes
 __global__ void k_split_classes(DevCounters *dc, int k) {
@@ -678,6 +694,9 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     int it = 0, check = 0, last_reform = 0;
     CheckPlan plan;
     plan.init(A.check_every);
+    // momentum between sweeps (k_pgs): the columns move their listed bodies'
+    // accumulators on, so every body a crossing group touches must be listed
+    float mom = (A.lprev && !dc->mom_off) ? A.momentum : 0.f;
     float *slots = dc->racc;
     // fc = M^-1 J^T lambda over every group (cross colours, then interior colours), from global lambda
     auto form_fc = [&](bool zero) -> bool {
@@ -937,9 +956,45 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         load_ahead(s0);
         fetch(step_after(s0));
     }
+    // momentum: the part's interior multipliers and listed bodies after a sweep
+    // (interior groups are triplet manifolds: at most 12 rows; the previous
+    // results of a group are loaded together)
+    auto interior_momentum = [&](float beta) {
+        for (int i = threadIdx.x; i < s_ng; i += blockDim.x) {
+            const int4 d = idesc[i];
+            const int n = desc_rows(d);
+            float prev[GB_STAGED_ROWS];
+            if (beta > 0.f) {
+#pragma unroll
+                for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = k < n ? __ldcg(&A.lprev[d.x + k]) : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < GB_STAGED_ROWS; k++)
+                if (k < n) {
+                    const float out = ilam[d.w + k];
+                    if (beta > 0.f) ilam[d.w + k] = fmaf(beta, out - prev[k], out);
+                    __stcg(&A.lprev[d.x + k], out);
+                }
+        }
+    };
+    auto part_momentum = [&](float beta) {
+        for (int l = threadIdx.x; l < s_nb; l += blockDim.x) {
+            const int b = ibid[l];
+            float4 fl = ifc[2 * l], fa = ifc[2 * l + 1];
+            body_momentum(A, b, fl, fa, beta);
+            if (beta > 0.f) {
+                ifc[2 * l] = fl;
+                ifc[2 * l + 1] = fa;
+                stcg4(&A.fc[2 * b], fl);
+                stcg4(&A.fc[2 * b + 1], fa);
+            }
+        }
+    };
     for (; it < itmax;) {
         Step cur{-1, 0};
         const bool check_this = residual_mode && (it + 1 >= plan.next || it + 1 == itmax);
+        // plain Gauss-Seidel results for the first sweep, the last and every checked one
+        const float beta = (mom > 0.f && it > 0 && it + 1 < itmax && !check_this) ? mom : 0.f;
         for (;;) {
             const Step nxt = step_after(cur), nnx = step_after(nxt);
             const bool interior = cur.c < 0;
@@ -960,7 +1015,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                 }
             } else if (has_next) {
                 if (!staged) {
-                    relax_desc(A, next);
+                    relax_desc(A, next, beta);
                 } else if (A.poison_stage ? mbar_wait(&s_mbar[3], 0, &dc->err, 16)
                                           : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
                     const float4 *buf = xbuf + (q & 1) * (S.chunk_cap * 8);
@@ -973,30 +1028,25 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
+            float prev[GB_STAGED_ROWS];
+            load_prev(A, xout, nout, beta, prev);
             const bool sweep_end = last_wave && nxt.c < 0;
             if (!last_wave) {
-#pragma unroll
-                for (int k = 0; k < GB_STAGED_ROWS; k++)
-                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                store_staged(A, xout, lout, nout, beta, prev);
                 fetch(nnx);
                 __syncthreads();
                 if (s_abort) { drain(); return; }
             } else {
                 const bool check_next = check_this && sweep_end;
-                if (check_next) {
-#pragma unroll
-                    for (int k = 0; k < GB_STAGED_ROWS; k++)
-                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
-                }
+                if (check_next) store_staged(A, xout, lout, nout, beta, prev);
                 unsigned target = 0;
                 if (nbr) nbr_release();
                 else grid_arrive(&dc->gsync, gen, target);
                 if (threadIdx.x == 0) issue(nxt);
-                if (!check_next) {
-#pragma unroll
-                    for (int k = 0; k < GB_STAGED_ROWS; k++)
-                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
-                }
+                if (!check_next) store_staged(A, xout, lout, nout, beta, prev);
+                // the interior multipliers move on while the other blocks
+                // finish the step (read again only in the next interior phase)
+                if (interior && mom > 0.f) interior_momentum(beta);
                 fetch(nnx);
                 // the next step: a cross colour this block has groups in, or
                 // the next sweep's interior phase (its accumulators are read
@@ -1009,7 +1059,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     grid_arrive(&dc->gsync, gen, target);
                     ok = grid_wait(&dc->gsync, &dc->err, gen, target);
                 } else {
-                    ok = nbr_wait(sweep_end ? (nsplit ? s_nb > 0 : s_ng > 0) : s_xn[nxt.c] > 0);
+                    ok = nbr_wait(sweep_end ? ((nsplit || mom > 0.f) ? s_nb > 0 : s_ng > 0) : s_xn[nxt.c] > 0);
                 }
                 if (!ok || s_abort) { drain(); return; }
             }
@@ -1040,6 +1090,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                 if (!form_fc(true) || !residual_rel(rel)) { drain(); return; }
             }
             if (rel <= A.target) break;
+            if (mom > 0.f && plan.s_prev >= 0 && rel > plan.r_prev) mom = mom_halved(mom, A.momentum);
             plan.after(it, rel, A.target, A.check_every, A.predict_checks);
         }
         // every block's cross updates of the part's bodies are out (the last
@@ -1047,9 +1098,10 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         // the accumulators come back
         if (nsplit) {
             if (s_nb > 0) fold_part();
-        } else if (s_ng > 0) {
+        } else if (s_ng > 0 || mom > 0.f) {
             load_part(false);
         }
+        if (mom > 0.f && it < itmax) part_momentum(beta);
         __syncthreads();
     }
     // The global accumulators are current here (read back after the last
@@ -1057,5 +1109,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     // interior multipliers go out for the integration and the warm-start store.
     publish_lambda();
     drain();
-    if (tid == 0) dc->iterations = it;
+    if (tid == 0) {
+        dc->iterations = it;
+        dc->mom_final = mom;
+    }
 }

@@ -1104,6 +1104,9 @@ struct PgsArgs {
     int passes;       // passes over a manifold's rows each time it is relaxed (>= 1)
     int poison_stage; // error-path tests: the staging waits name a copy that is never issued
     int chunk_cap;    // staged rows per shared-memory buffer (the waves were cut to it)
+    float momentum;   // momentum between sweeps (used when lprev is set)
+    float *lprev;     // [rows]: every multiplier as the previous sweep left it (null: no momentum)
+    float4 *fcprev;   // [2 * bodies]: every body's accumulators as the previous sweep left them
 };
 
 // Manifold descriptors in colour-slot order: the solver reads one int4 per
@@ -1238,11 +1241,57 @@ __device__ __forceinline__ void relax_row_local(const Rows &Rw, int r, float &la
     }
 }
 
+// Momentum between sweeps (PgsArgs::momentum = beta, lprev set): after sweep k
+// every multiplier moves on from that sweep's projected Gauss-Seidel result
+// y_k to y_k + beta (y_k - y_{k-1}) before sweep k + 1 starts from it, and every
+// body's accumulators fc = M^-1 J^T lambda by the same rule, which keeps fc and
+// the multipliers consistent (the map is linear).  This is the extrapolation
+// step of Nesterov's accelerated gradient method with a fixed coefficient
+// (Y. Nesterov, "A method for solving the convex programming problem with
+// convergence rate O(1/k^2)", 1983), applied to the iterates of the projected
+// Gauss-Seidel sweep, as nonsmooth nonlinear conjugate gradient methods apply
+// their direction to them (M. Silcowitz, S. Niebe, K. Erleben, "A nonsmooth
+// nonlinear conjugate gradient method for interactive contact force
+// problems", The Visual Computer 26, 2010).  The limit is the same LCP
+// solution: a fixed point of the sweep is one of the extrapolation.  A sweep
+// that ends in a residual check, the first and the last sweep use beta = 0,
+// so every check and the final multipliers are plain Gauss-Seidel results; a
+// check whose residual rose halves beta for the rest of the solve, and below
+// an eighth of the value set the sweeps go on without momentum (letting beta
+// grow back after a falling check let cyclic states recur).  A row's
+// multiplier is moved on by the thread that relaxed it, right after it stores
+// the result; a body's accumulators at the end of the sweep.
+__device__ __forceinline__ float mom_halved(float mom, float set) { return 0.5f * mom < 0.125f * set ? 0.f : 0.5f * mom; }
+__device__ __forceinline__ void store_lambda(const PgsArgs &A, int r, float out, float beta) {
+    if (A.lprev) {
+        float v = out;
+        if (beta > 0.f) v = fmaf(beta, out - __ldcg(&A.lprev[r]), out);
+        __stcg(&A.lprev[r], out);
+        A.Rw.lambda[r] = v;
+    } else {
+        A.Rw.lambda[r] = out;
+    }
+}
+// body b's accumulators (l, a) as the sweep left them: kept in fcprev, and
+// moved on by beta times their change over the sweep
+__device__ __forceinline__ void body_momentum(const PgsArgs &A, int b, float4 &l, float4 &a, float beta) {
+    if (beta > 0.f) {
+        const float4 pl = ldcg4(&A.fcprev[2 * b]), pa = ldcg4(&A.fcprev[2 * b + 1]);
+        stcg4(&A.fcprev[2 * b], l);
+        stcg4(&A.fcprev[2 * b + 1], a);
+        l = make_float4(fmaf(beta, l.x - pl.x, l.x), fmaf(beta, l.y - pl.y, l.y), fmaf(beta, l.z - pl.z, l.z), l.w);
+        a = make_float4(fmaf(beta, a.x - pa.x, a.x), fmaf(beta, a.y - pa.y, a.y), fmaf(beta, a.z - pa.z, a.z), a.w);
+    } else {
+        stcg4(&A.fcprev[2 * b], l);
+        stcg4(&A.fcprev[2 * b + 1], a);
+    }
+}
+
 // One manifold by one thread: the normal (findex < 0) rows of all its
 // contacts first, then the friction rows, mirroring the reference's findex
 // partition (quickstep.cpp:2329-2355).  lambda of a manifold is read and
 // written only by the thread that owns the manifold's slot.
-__device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
+__device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d, float beta = 0.f) {
     const int r0 = d.x, n = desc_rows(d), r1 = d.x + n;
     const bool two = d.w >= 0;
     float4 f1l = ldcg4(&A.fc[2 * d.z]), f1a = ldcg4(&A.fc[2 * d.z + 1]);
@@ -1267,12 +1316,14 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
                 relax_row_local(A.Rw, r0 + k, lam[k], lf, true, f1l, f1a, f2l, f2a, two);
             }
         }
-        for (int k = 0; k < n; k++) A.Rw.lambda[r0 + k] = lam[k];
+        for (int k = 0; k < n; k++) store_lambda(A, r0 + k, lam[k], beta);
     } else {
         for (int r = r0; r < r1; r++)
             if (A.Rw.findex[r] < 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
         for (int r = r0; r < r1; r++)
             if (A.Rw.findex[r] >= 0) relax_row(A.Rw, r, f1l, f1a, f2l, f2a, two);
+        if (A.lprev)
+            for (int r = r0; r < r1; r++) store_lambda(A, r, A.Rw.lambda[r], beta);
     }
     stcg4(&A.fc[2 * d.z], f1l); stcg4(&A.fc[2 * d.z + 1], f1a);
     if (two) { stcg4(&A.fc[2 * d.w], f2l); stcg4(&A.fc[2 * d.w + 1], f2a); }
@@ -1298,6 +1349,31 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d) {
 // of its descriptor's y.
 #define GB_PGS_THREADS 256  // threads a block of the sweep kernels by default (128 is the other instance)
 #define GB_STAGED_ROWS 12  // rows of a staged slot at most (4 contacts x 3, or a plain group)
+
+// a staged slot's relaxed multipliers out to global memory.  With momentum
+// the previous sweep's results are loaded together, right after the
+// relaxation (one round trip to L2 that the block's arrival covers), and used
+// when the multipliers are stored.
+__device__ __forceinline__ void load_prev(const PgsArgs &A, int x, int n, float beta, float (&prev)[GB_STAGED_ROWS]) {
+#pragma unroll
+    for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = (beta > 0.f && k < n) ? __ldcg(&A.lprev[x + k]) : 0.f;
+}
+__device__ __forceinline__ void store_staged(const PgsArgs &A, int x, const float (&lout)[GB_STAGED_ROWS], int n,
+                                             float beta, const float (&prev)[GB_STAGED_ROWS]) {
+    if (!A.lprev) {
+#pragma unroll
+        for (int k = 0; k < GB_STAGED_ROWS; k++)
+            if (k < n) A.Rw.lambda[x + k] = lout[k];
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < GB_STAGED_ROWS; k++)
+        if (k < n) {
+            const float out = lout[k];
+            A.Rw.lambda[x + k] = beta > 0.f ? fmaf(beta, out - prev[k], out) : out;
+            __stcg(&A.lprev[x + k], out);
+        }
+}
 #define GB_CHUNK_ROWS 800  // staged rows per buffer by default: 2 x 100 KB of shared memory (at most)
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
@@ -1725,6 +1801,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
     int it = 0, check = 0, last_reform = 0;
     CheckPlan plan;
     plan.init(A.check_every);
+    float mom = A.lprev ? A.momentum : 0.f;  // momentum between sweeps (halved when a check's residual rises)
     float *slots = dc->racc;  // [2][2]: residual, max|lambda| per check parity
     // fc = M^-1 J^T lambda, colour by colour so no two manifolds of a pass touch one body
     auto form_fc = [&](bool zero) -> bool {
@@ -1867,6 +1944,9 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
     }
     for (; it < itmax && ncol > 0;) {
         Step cur{0, 0};
+        // plain Gauss-Seidel results for the first sweep, the last and every checked one
+        const bool check_this = residual_mode && (it + 1 >= plan.next || it + 1 == itmax);
+        const float beta = (mom > 0.f && it > 0 && it + 1 < itmax && !check_this) ? mom : 0.f;
         for (;;) {
             const Step nxt = step_after(cur), nnx = step_after(nxt);
             const bool last_wave = cur.w + 1 == s_wcount[cur.c];
@@ -1878,7 +1958,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             int nout = 0, xout = 0;
             if (has_next) {
                 if (!staged) {
-                    relax_desc(A, next);
+                    relax_desc(A, next, beta);
                 } else if (A.poison_stage ? mbar_wait(&s_mbar[2], 0, &dc->err, 16)
                                           : mbar_wait(&s_mbar[q & 1], (q >> 1) & 1, &dc->err)) {
                     const float4 *buf = pgs_smem + (q & 1) * (A.chunk_cap * 8);
@@ -1890,13 +1970,13 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
                     s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
+            float prev[GB_STAGED_ROWS];
+            load_prev(A, xout, nout, beta, prev);
             const bool sweep_end = last_wave && cur.c == ncol - 1;
             if (!last_wave) {
                 // another wave of this colour follows: a block barrier (the
                 // colour's slots share no body, so no other block waits on these)
-#pragma unroll
-                for (int k = 0; k < GB_STAGED_ROWS; k++)
-                    if (k < nout) A.Rw.lambda[xout + k] = lout[k];
+                store_staged(A, xout, lout, nout, beta, prev);
                 fetch(nnx);
                 __syncthreads();
                 if (s_abort) { drain(); return; }
@@ -1907,20 +1987,12 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
                 // prefetch the next slot while the other blocks arrive.  Before a
                 // residual check (which reads every multiplier right after this
                 // barrier) they go out before the arrival.
-                const bool check_next = residual_mode && sweep_end && (it + 1 >= plan.next || it + 1 == itmax);
-                if (check_next) {
-#pragma unroll
-                    for (int k = 0; k < GB_STAGED_ROWS; k++)
-                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
-                }
+                const bool check_next = check_this && sweep_end;
+                if (check_next) store_staged(A, xout, lout, nout, beta, prev);
                 unsigned target = 0;
                 grid_arrive(&dc->gsync, gen, target);
                 if (threadIdx.x == 0) issue(nxt);
-                if (!check_next) {
-#pragma unroll
-                    for (int k = 0; k < GB_STAGED_ROWS; k++)
-                        if (k < nout) A.Rw.lambda[xout + k] = lout[k];
-                }
+                if (!check_next) store_staged(A, xout, lout, nout, beta, prev);
                 fetch(nnx);
                 if (!grid_wait(&dc->gsync, &dc->err, gen, target) || s_abort) { drain(); return; }
             }
@@ -1932,7 +2004,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             cur = nxt;
         }
         ++it;
-        if (residual_mode && (it >= plan.next || it == itmax)) {
+        if (check_this) {
             // Re-form fc = M^-1 J^T lambda from lambda every reform_every sweeps:
             // thousands of incremental FP32 updates let fc drift from the
             // multipliers it stands for, and relaxation against a drifted fc
@@ -1953,11 +2025,29 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
                 if (!form_fc(true) || !residual_rel(rel)) { drain(); return; }
             }
             if (rel <= A.target) break;
+            if (mom > 0.f && plan.s_prev >= 0 && rel > plan.r_prev) mom = mom_halved(mom, A.momentum);
             plan.after(it, rel, A.target, A.check_every, A.predict_checks);
+        }
+        if (mom > 0.f && it < itmax) {
+            // momentum: the bodies' accumulators after the sweep (the rows'
+            // multipliers moved on when they were stored); the barrier keeps
+            // the next sweep's updates out of what this pass reads
+            for (int b = tid; b < A.nb; b += nth) {
+                float4 l = ldcg4(&A.fc[2 * b]), a = ldcg4(&A.fc[2 * b + 1]);
+                body_momentum(A, b, l, a, beta);
+                if (beta > 0.f) {
+                    stcg4(&A.fc[2 * b], l);
+                    stcg4(&A.fc[2 * b + 1], a);
+                }
+            }
+            if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
         }
     }
     drain();  // the copy issued for the colour after the last one relaxed
-    if (tid == 0) dc->iterations = it;
+    if (tid == 0) {
+        dc->iterations = it;
+        dc->mom_final = mom;
+    }
 }
 
 #include "pgs_slab.cuh"
@@ -2521,6 +2611,9 @@ static bool reserve_step(Workspace &ws, int nb, const SolverParams &P, bool colo
     if (coloured) {
         const ColouredPlan c = plan_coloured(ws, P);
         if (!ensure_coloured(ws, nb, c)) return false;
+        if (P.momentum > 0.f &&
+            !(ws.m_lprev.ensure((size_t)ws.row_cap * 4) && ws.b_fcprev.ensure((size_t)(nb > 0 ? nb : 1) * 32)))
+            return false;
         nscan = std::max(nscan, std::max((size_t)c.ncb, c.wave_cap));
         nscan = std::max(nscan, std::max((size_t)c.pgs_blocks * GB_SLAB_COLOURS, c.ngroups));
     }
@@ -2707,6 +2800,13 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         k_split_mask<<<grid, 256, 0, s>>>(ws.dc, ws.x_nsplit.as<int>(), nb, ws.x_smask.as<int>());
         count_launch(5);
     }
+    // momentum between sweeps on the two-level sweep: every body a crossing group touches is in a column's list
+    cudaMemsetAsync(&ws.dc->mom_off, 0, 4, s);
+    if (slab && P.momentum > 0.f) {
+        k_mom_check<<<grid, 256, 0, s>>>(ws.dc, ws.m_colour.as<int>(), ws.grp_body.as<int2>(), ws.s_part.as<int>(),
+                                         ws.s_blocal.as<int>(), caps.bcap);
+        count_launch();
+    }
     cudaMemsetAsync(ws.col_count.p, 0, GB_MAX_COLOURS * 4, s);
     cudaMemsetAsync(ws.col_fill.p, 0, GB_MAX_COLOURS * 4, s);
     k_colour_count<<<grid, 256, 0, s>>>(ws.m_colour.as<int>(), ws.dc, ws.col_count.as<int>());
@@ -2804,6 +2904,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
     cudaMemsetAsync(ws.dc->racc, 0, 4 * sizeof(float), s);
     cudaMemsetAsync(&ws.dc->iterations, 0, 4, s);
     cudaMemsetAsync(&ws.dc->nhist, 0, 4, s);
+    cudaMemsetAsync(&ws.dc->mom_final, 0, 4, s);
     if (ev0) cudaEventRecord(ev0, s);
     {
         PgsArgs A;
@@ -2833,6 +2934,9 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.wbase = ws.wv_base.as<int>();
         A.sched = ws.wv_sched.as<int>();
         A.chunk_cap = chunk_cap;
+        A.momentum = P.momentum;
+        A.lprev = P.momentum > 0.f ? ws.m_lprev.as<float>() : nullptr;
+        A.fcprev = P.momentum > 0.f ? ws.b_fcprev.as<float4>() : nullptr;
         // one block per SM (the grid barrier's cost grows with the block count;
         // the chunk packing above assumes exactly pgs_blocks blocks)
         const size_t smem = (size_t)2 * chunk_cap * 128;  // two chunk buffers

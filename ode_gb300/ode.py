@@ -52,7 +52,7 @@ class dJointFeedback(ctypes.Structure):
 class gbodeTuning(ctypes.Structure):
     _fields_ = [("blocks", ctypes.c_int), ("passes", ctypes.c_int), ("check_every", ctypes.c_int),
                 ("ms_per_step", ctypes.c_float), ("candidates", ctypes.c_int), ("threads", ctypes.c_int),
-                ("chunk_rows", ctypes.c_int), ("two_level", ctypes.c_int)]
+                ("chunk_rows", ctypes.c_int), ("two_level", ctypes.c_int), ("momentum", ctypes.c_float)]
 
 
 class gbodeStepStats(ctypes.Structure):
@@ -60,7 +60,8 @@ class gbodeStepStats(ctypes.Structure):
                 ("iterations", ctypes.c_int), ("residual", ctypes.c_float), ("pairs", ctypes.c_int),
                 ("solve_ms", ctypes.c_float), ("step_ms", ctypes.c_float), ("sleeping", ctypes.c_int),
                 ("interior_colours", ctypes.c_int), ("interior_rows", ctypes.c_int),
-                ("neighbour_waits", ctypes.c_int), ("cross_classes", ctypes.c_int)]
+                ("neighbour_waits", ctypes.c_int), ("cross_classes", ctypes.c_int),
+                ("momentum", ctypes.c_float)]
 
 
 dNearCallback = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ID, ID)
@@ -164,6 +165,7 @@ _PROTOS = [
     ("gbodeWorldSetSweepSync", None, [ID, ctypes.c_int]), ("gbodeWorldGetSweepSync", ctypes.c_int, [ID]),
     ("gbodeWorldSetResidualChecks", None, [ID, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetCrossClasses", None, [ID, ctypes.c_int]), ("gbodeWorldGetCrossClasses", ctypes.c_int, [ID]),
+    ("gbodeWorldSetSweepMomentum", None, [ID, ctypes.c_float]), ("gbodeWorldGetSweepMomentum", ctypes.c_float, [ID]),
     ("gbodeTestInject", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldSetSolverTiles", None, [ID, ctypes.c_int, ctypes.c_int]),
     ("gbodeWorldGetSolverTiles", None, [ID, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
