@@ -1375,6 +1375,7 @@ __device__ __forceinline__ void store_staged(const PgsArgs &A, int x, const floa
         }
 }
 #define GB_CHUNK_ROWS 800  // staged rows per buffer by default: 2 x 100 KB of shared memory (at most)
+#define GB_CHUNK_ROWS_MOM 792  // at most, with momentum (room for 12 floats a thread beside the buffers)
 __device__ __forceinline__ int desc_chunk_off(int4 d) { return (d.y >> 16) & 0xfff; }
 __device__ __forceinline__ int swz(int row, int a) { return row * 8 + (a ^ (row & 7)); }
 
@@ -1906,6 +1907,9 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             while (nwaited < nissued) retire();
     };
     float *my_lam = s_lam + threadIdx.x * 13;
+    // with momentum: the next slot's previous-sweep results, copied beside its
+    // multipliers (after the two chunk buffers), so storing needs no load
+    float *my_lp = A.lprev ? (float *)(pgs_smem + (size_t)2 * A.chunk_cap * 8) + threadIdx.x * GB_STAGED_ROWS : nullptr;
     // Two-deep descriptor pipeline: `ahead` (the slot of the step after the
     // next one) is loaded a step early, so the multiplier copies for `next`
     // can be issued at once, without waiting for a descriptor load.
@@ -1928,6 +1932,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             staged = (next.y & GB_DESC_STAGED) && desc_chunk_off(next) + n <= A.chunk_cap;
             if (staged) {
                 for (int k = 0; k < n; k++) cp_async4(&my_lam[k], &A.Rw.lambda[next.x + k]);
+                if (my_lp)
+                    for (int k = 0; k < n; k++) cp_async4(&my_lp[k], &A.lprev[next.x + k]);
                 cp_async_commit();
             }
         }
@@ -1970,8 +1976,9 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
                     s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
-            float prev[GB_STAGED_ROWS];
-            load_prev(A, xout, nout, beta, prev);
+            float prev[GB_STAGED_ROWS];  // (a staged slot's copy arrived before its relaxation)
+#pragma unroll
+            for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = (beta > 0.f && k < nout) ? my_lp[k] : 0.f;
             const bool sweep_end = last_wave && cur.c == ncol - 1;
             if (!last_wave) {
                 // another wave of this colour follows: a block barrier (the
@@ -2032,12 +2039,35 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             // momentum: the bodies' accumulators after the sweep (the rows'
             // multipliers moved on when they were stored); the barrier keeps
             // the next sweep's updates out of what this pass reads
-            for (int b = tid; b < A.nb; b += nth) {
-                float4 l = ldcg4(&A.fc[2 * b]), a = ldcg4(&A.fc[2 * b + 1]);
-                body_momentum(A, b, l, a, beta);
-                if (beta > 0.f) {
-                    stcg4(&A.fc[2 * b], l);
-                    stcg4(&A.fc[2 * b + 1], a);
+            // (four bodies a thread at a time, their loads issued together)
+            for (int b0 = tid; b0 < A.nb; b0 += 4 * nth) {
+                float4 l[4], a[4], pl[4], pa[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int b = b0 + j * nth;
+                    if (b < A.nb) {
+                        l[j] = ldcg4(&A.fc[2 * b]);
+                        a[j] = ldcg4(&A.fc[2 * b + 1]);
+                        if (beta > 0.f) {
+                            pl[j] = ldcg4(&A.fcprev[2 * b]);
+                            pa[j] = ldcg4(&A.fcprev[2 * b + 1]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int b = b0 + j * nth;
+                    if (b >= A.nb) continue;
+                    stcg4(&A.fcprev[2 * b], l[j]);
+                    stcg4(&A.fcprev[2 * b + 1], a[j]);
+                    if (beta > 0.f) {
+                        const float4 x = l[j], y = a[j];
+                        stcg4(&A.fc[2 * b], make_float4(fmaf(beta, x.x - pl[j].x, x.x), fmaf(beta, x.y - pl[j].y, x.y),
+                                                        fmaf(beta, x.z - pl[j].z, x.z), x.w));
+                        stcg4(&A.fc[2 * b + 1], make_float4(fmaf(beta, y.x - pa[j].x, y.x),
+                                                            fmaf(beta, y.y - pa[j].y, y.y),
+                                                            fmaf(beta, y.z - pa[j].z, y.z), y.w));
+                    }
                 }
             }
             if (!grid_sync(&dc->gsync, &dc->err, gen)) { drain(); return; }
@@ -2485,7 +2515,9 @@ template <int T>
 static int pgs_per_sm() {
     static const int v = []() {
         const size_t smem = (size_t)2 * GB_CHUNK_ROWS * 128;
-        cudaFuncSetAttribute((const void *)k_pgs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const size_t smem_mom = (size_t)2 * GB_CHUNK_ROWS_MOM * 128 + (size_t)T * GB_STAGED_ROWS * 4;
+        cudaFuncSetAttribute((const void *)k_pgs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(smem > smem_mom ? smem : smem_mom));
         int n = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&n, (const void *)k_pgs<T>, T, smem, 0);
         return n;
@@ -2559,6 +2591,9 @@ static ColouredPlan plan_coloured(const Workspace &ws, const SolverParams &P) {
     const int chunk = P.pgs_chunk > 0 ? (P.pgs_chunk < 64 ? 64 : (P.pgs_chunk > GB_CHUNK_ROWS ? GB_CHUNK_ROWS : P.pgs_chunk))
                                       : GB_CHUNK_ROWS;
     c.chunk_cap = c.slab ? GB_SLAB_XCHUNK : chunk;
+    // momentum on the one-level sweep stages each thread's previous-sweep
+    // results beside the chunk buffers (GB_STAGED_ROWS floats a thread)
+    if (!c.slab && P.momentum > 0.f && c.chunk_cap > GB_CHUNK_ROWS_MOM) c.chunk_cap = GB_CHUNK_ROWS_MOM;
     // waves: one per (colour, block) at least, plus one per T slots and per chunk_cap - 12 staged rows
     c.wave_cap = 2 * (size_t)c.ncb + c.ngroups / c.threads + (size_t)ws.row_cap / (c.chunk_cap - 12) + 16;
     return c;
@@ -2939,7 +2974,8 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
         A.fcprev = P.momentum > 0.f ? ws.b_fcprev.as<float4>() : nullptr;
         // one block per SM (the grid barrier's cost grows with the block count;
         // the chunk packing above assumes exactly pgs_blocks blocks)
-        const size_t smem = (size_t)2 * chunk_cap * 128;  // two chunk buffers
+        // two chunk buffers, and with momentum the threads' previous-sweep results
+        const size_t smem = (size_t)2 * chunk_cap * 128 + (A.lprev ? (size_t)threads * GB_STAGED_ROWS * 4 : 0);
         const int per_sm = threads == 128 ? pgs_per_sm<128>() : pgs_per_sm<256>();
         if (per_sm < 1) return false;
         const int blocks = pgs_blocks;

