@@ -22,7 +22,8 @@ def _rank(rank, world, port, out):
     import torch
     import torch.distributed as dist
     import bench
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import datetime
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=60))
     dev = torch.device("cpu")
     t = bench.dist_max(10.0 + rank, world, dev)
     n = bench.dist_sum(100.0 * (rank + 1), world, dev)
