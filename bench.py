@@ -83,6 +83,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0, help="run N steps only (for ncu), no JSON")
+    ap.add_argument("--curve", action="store_true",
+                    help="after the warm-up, one step from the same state with and without momentum: print the "
+                         "residual at each check and the sweeps done by then (one JSON line each), no bench line")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched capsule-chain leg")
     ap.add_argument("--chains", type=int, default=8192, help="batched leg: independent capsule chains")
@@ -364,6 +367,9 @@ def run_gbode(args, ws, rank, local):
         np.savez_compressed(args.save_settled, pos=settled[:, 0:3], q=settled[:, 3:7], lvel=settled[:, 19:22],
                             avel=settled[:, 22:25], seed=1 + rank, settle=args.settle + args.warmup)
         return
+    if args.curve:
+        residual_curves(args, L, w)
+        return
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     peak, peak_kind = measured_peak()
     launches0 = L.gbodeKernelLaunchCount()
@@ -482,6 +488,25 @@ def run_gbode(args, ws, rank, local):
         "batched": batched,
     }
     print(json.dumps(line))
+
+
+def residual_curves(args, L, w):
+    """One step from the saved state with the configured solver, with and
+    without momentum: the FP32 residual at every check and the sweeps done by
+    then (gbodeWorldGetResidualHistory / gbodeWorldGetResidualSweeps)."""
+    hist = np.zeros(256, np.float32)
+    at = np.zeros(256, np.int32)
+    for beta in sorted({0.0, args.momentum}):
+        restore_snapshot(L, w)
+        L.gbodeWorldSetSweepMomentum(w.w, beta)
+        w.step_fused()
+        w.sync()
+        st = w.stats()
+        n = L.gbodeWorldGetResidualHistory(w.w, hist.ctypes.data_as(ode_f32p()), 256)
+        L.gbodeWorldGetResidualSweeps(w.w, at.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), 256)
+        print(json.dumps({"momentum": beta, "two_level": args.two_level, "cross_classes": args.cross_classes,
+                          "sweeps": st.iterations, "residual": st.residual, "momentum_at_end": st.momentum,
+                          "checks": [[int(a), float(h)] for a, h in zip(at[:n], hist[:n])]}))
 
 
 def restore_snapshot(L, w):

@@ -607,6 +607,9 @@ int gbodeWorldGetContacts(dWorldID w, float *out, int cap);
  * (residual-target mode), oldest first.  Returns the number of checks (at
  * most 256 are kept).  Synchronises the stream. */
 int gbodeWorldGetResidualHistory(dWorldID w, float *out, int cap);
+/* The sweeps done at each of those checks (0 for the checks of the start),
+ * oldest first; returns the number of checks.  Synchronises the stream. */
+int gbodeWorldGetResidualSweeps(dWorldID w, int *out, int cap);
 
 /* Last error message ("" if none) and clear. */
 const char *gbodeGetLastError(void);

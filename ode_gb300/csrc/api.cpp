@@ -2573,6 +2573,15 @@ int gbodeWorldGetResidualHistory(dWorldID w, float *out, int cap) {
     return n;
 }
 
+int gbodeWorldGetResidualSweeps(dWorldID w, int *out, int cap) {
+    if (!w->ws.dc) return 0;
+    cudaMemcpyAsync(w->ws.hc, w->ws.dc, sizeof(DevCounters), cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    int n = w->ws.hc->nhist;
+    if (out) for (int i = 0; i < n && i < cap; i++) out[i] = w->ws.hc->rsweep[i];
+    return n;
+}
+
 int gbodeWorldGetContacts(dWorldID w, float *out, int cap) {
     if (!w->ws.dc) return 0;
     int n = 0;

@@ -97,6 +97,7 @@ struct DevCounters {
     int split_k;           // two-level sweep: classes of the last solve's cross phase with mass splitting (0: off)
     int mom_off;           // two-level sweep: a group touches a body outside the columns' lists (no momentum)
     float mom_final;       // momentum of the last solve's last sweeps (0: off)
+    int rsweep[256];       // sweeps done at each residual check of the last solve (rhist's checks)
 };
 
 // auto-disable state per body, int4: x flags, y idle steps, z steps left,

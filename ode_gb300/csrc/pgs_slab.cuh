@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
             float *other = slots + 2 * ((check + 1) & 1);
             other[0] = 0.f; other[1] = 0.f;
             dc->resid = rel; dc->maxlam = ll;
-            if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
+            if (check < 256) { dc->rhist[check] = rel; dc->rsweep[check] = it; dc->nhist = check + 1; }
         }
         ++check;
         return true;
@@ -1028,8 +1028,14 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
+            // momentum: the slot's previous-sweep results, loaded together right
+            // after the relaxation (the block's release covers part of the
+            // round trip); staging them beside the multipliers would take
+            // shared memory from the interior rows or the chunk buffers, and
+            // with 80-row chunks the extra waves cost more than the loads
             float prev[GB_STAGED_ROWS];
-            load_prev(A, xout, nout, beta, prev);
+#pragma unroll
+            for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = (beta > 0.f && k < nout) ? __ldcg(&A.lprev[xout + k]) : 0.f;
             const bool sweep_end = last_wave && nxt.c < 0;
             if (!last_wave) {
                 store_staged(A, xout, lout, nout, beta, prev);

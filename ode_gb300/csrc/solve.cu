@@ -1350,14 +1350,10 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d, float beta 
 #define GB_PGS_THREADS 256  // threads a block of the sweep kernels by default (128 is the other instance)
 #define GB_STAGED_ROWS 12  // rows of a staged slot at most (4 contacts x 3, or a plain group)
 
-// a staged slot's relaxed multipliers out to global memory.  With momentum
-// the previous sweep's results are loaded together, right after the
-// relaxation (one round trip to L2 that the block's arrival covers), and used
-// when the multipliers are stored.
-__device__ __forceinline__ void load_prev(const PgsArgs &A, int x, int n, float beta, float (&prev)[GB_STAGED_ROWS]) {
-#pragma unroll
-    for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = (beta > 0.f && k < n) ? __ldcg(&A.lprev[x + k]) : 0.f;
-}
+// a staged slot's relaxed multipliers out to global memory; with momentum
+// `prev` holds the slot's previous-sweep results (staged beside the
+// multipliers by the one-level sweep, loaded after the relaxation by the
+// two-level sweep)
 __device__ __forceinline__ void store_staged(const PgsArgs &A, int x, const float (&lout)[GB_STAGED_ROWS], int n,
                                              float beta, const float (&prev)[GB_STAGED_ROWS]) {
     if (!A.lprev) {
@@ -1839,7 +1835,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs(PgsArgs A) {
             float *other = slots + 2 * ((check + 1) & 1);
             other[0] = 0.f; other[1] = 0.f;
             dc->resid = rel; dc->maxlam = ll;
-            if (check < 256) { dc->rhist[check] = rel; dc->nhist = check + 1; }
+            if (check < 256) { dc->rhist[check] = rel; dc->rsweep[check] = it; dc->nhist = check + 1; }
         }
         ++check;
         return true;

@@ -187,6 +187,7 @@ _PROTOS = [
     ("gbodeWorldGetLastRows", ctypes.c_int, [ID, _F, ctypes.c_int]),
     ("gbodeWorldGetContacts", ctypes.c_int, [ID, _F, ctypes.c_int]),
     ("gbodeWorldGetResidualHistory", ctypes.c_int, [ID, _F, ctypes.c_int]),
+    ("gbodeWorldGetResidualSweeps", ctypes.c_int, [ID, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     ("gbodeGetLastError", ctypes.c_char_p, []), ("gbodeKernelLaunchCount", ctypes.c_longlong, []),
     ("gbodeWorldGetBodyCount", ctypes.c_int, [ID]), ("gbodeWorldGetState", None, [ID, _F]),
     ("gbodeWorldSetState", None, [ID, _F]),

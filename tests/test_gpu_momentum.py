@@ -72,6 +72,13 @@ def test_momentum_on_a_pile(gblib, two_level, classes, beta):
         sweeps[1].append(st[1].iterations)
         if step == 0:
             dpos = float(np.abs(worlds[0].state()[:, 0:3] - a[:, 0:3]).max())
+    # the residual checks of the last step: the sweeps done at each, in order, the last at the solve's end
+    import ctypes
+    hist = np.zeros(256, np.float32)
+    at = np.zeros(256, np.int32)
+    n = L.gbodeWorldGetResidualHistory(worlds[1].w, hist.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 256)
+    assert L.gbodeWorldGetResidualSweeps(worlds[1].w, at.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), 256) == n > 0
+    assert np.all(np.diff(at[:n]) >= 0) and at[n - 1] == st[1].iterations and hist[n - 1] <= 1e-4
     r64, _, ml = worlds[1].last_residual()
     print(f"{'two' if two_level else 'one'}-level: sweeps plain {np.mean(sweeps[0]):.1f}, momentum "
           f"{np.mean(sweeps[1]):.1f} (beta at the end {st[1].momentum}); FP64 residual {r64 / max(1.0, ml):.2e}; "
