@@ -963,7 +963,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         for (int i = threadIdx.x; i < s_ng; i += blockDim.x) {
             const int4 d = idesc[i];
             const int n = desc_rows(d);
-            float prev[GB_STAGED_ROWS];
+            float prev[GB_STAGED_ROWS] = {};
             if (beta > 0.f) {
 #pragma unroll
                 for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = k < n ? __ldcg(&A.lprev[d.x + k]) : 0.f;
@@ -1001,6 +1001,7 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
             const bool last_wave = interior || cur.w + 1 == s_wcount[cur.c];
             if (threadIdx.x == 0 && !last_wave) issue(nxt);
             float lout[GB_STAGED_ROWS];
+            float prev[GB_STAGED_ROWS] = {};
             int nout = 0, xout = 0;
             if (interior) {
                 if (s_ng > 0) {  // a part without interior groups leaves its bodies' accumulators alone
@@ -1014,6 +1015,12 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     if (check_this) publish_lambda();
                 }
             } else if (has_next) {
+                // momentum: the slot's previous-sweep results, loaded together
+                // before the relaxation (in flight while the rows arrive and
+                // are relaxed)
+#pragma unroll
+                for (int k = 0; k < GB_STAGED_ROWS; k++)
+                    prev[k] = (beta > 0.f && staged && k < desc_rows(next)) ? __ldcg(&A.lprev[next.x + k]) : 0.f;
                 if (!staged) {
                     relax_desc(A, next, beta);
                 } else if (A.poison_stage ? mbar_wait(&s_mbar[3], 0, &dc->err, 16)
@@ -1028,14 +1035,6 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
                     s_abort = 1;  // the whole block leaves after the next block barrier
                 }
             }
-            // momentum: the slot's previous-sweep results, loaded together right
-            // after the relaxation (the block's release covers part of the
-            // round trip); staging them beside the multipliers would take
-            // shared memory from the interior rows or the chunk buffers, and
-            // with 80-row chunks the extra waves cost more than the loads
-            float prev[GB_STAGED_ROWS];
-#pragma unroll
-            for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = (beta > 0.f && k < nout) ? __ldcg(&A.lprev[xout + k]) : 0.f;
             const bool sweep_end = last_wave && nxt.c < 0;
             if (!last_wave) {
                 store_staged(A, xout, lout, nout, beta, prev);
