@@ -959,32 +959,53 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     // momentum: the part's interior multipliers and listed bodies after a sweep
     // (interior groups are triplet manifolds: at most 12 rows; the previous
     // results of a group are loaded together)
+    // (a thread's groups two at a time, their loads issued together)
     auto interior_momentum = [&](float beta) {
-        for (int i = threadIdx.x; i < s_ng; i += blockDim.x) {
+        for (int i = threadIdx.x; i < s_ng; i += 2 * blockDim.x) {
+            const int i2 = i + blockDim.x;
             const int4 d = idesc[i];
-            const int n = desc_rows(d);
-            float prev[GB_STAGED_ROWS] = {};
+            const int4 e = i2 < s_ng ? idesc[i2] : make_int4(0, 0, 0, 0);  // rows 0: nothing
+            const int n = desc_rows(d), m = desc_rows(e);
+            float p[GB_STAGED_ROWS] = {}, q[GB_STAGED_ROWS] = {};
             if (beta > 0.f) {
 #pragma unroll
-                for (int k = 0; k < GB_STAGED_ROWS; k++) prev[k] = k < n ? __ldcg(&A.lprev[d.x + k]) : 0.f;
+                for (int k = 0; k < GB_STAGED_ROWS; k++) {
+                    p[k] = k < n ? __ldcg(&A.lprev[d.x + k]) : 0.f;
+                    q[k] = k < m ? __ldcg(&A.lprev[e.x + k]) : 0.f;
+                }
             }
 #pragma unroll
-            for (int k = 0; k < GB_STAGED_ROWS; k++)
+            for (int k = 0; k < GB_STAGED_ROWS; k++) {
                 if (k < n) {
                     const float out = ilam[d.w + k];
-                    if (beta > 0.f) ilam[d.w + k] = fmaf(beta, out - prev[k], out);
+                    if (beta > 0.f) ilam[d.w + k] = fmaf(beta, out - p[k], out);
                     __stcg(&A.lprev[d.x + k], out);
                 }
+                if (k < m) {
+                    const float out = ilam[e.w + k];
+                    if (beta > 0.f) ilam[e.w + k] = fmaf(beta, out - q[k], out);
+                    __stcg(&A.lprev[e.x + k], out);
+                }
+            }
         }
     };
-    auto part_momentum = [&](float beta) {
+    // (from_global: the accumulators come from global memory, loaded together
+    // with the previous values; otherwise from the part's copies)
+    auto part_momentum = [&](float beta, bool from_global) {
         for (int l = threadIdx.x; l < s_nb; l += blockDim.x) {
             const int b = ibid[l];
-            float4 fl = ifc[2 * l], fa = ifc[2 * l + 1];
+            float4 fl, fa;
+            if (from_global) {
+                fl = ldcg4(&A.fc[2 * b]);
+                fa = ldcg4(&A.fc[2 * b + 1]);
+            } else {
+                fl = ifc[2 * l];
+                fa = ifc[2 * l + 1];
+            }
             body_momentum(A, b, fl, fa, beta);
+            ifc[2 * l] = fl;
+            ifc[2 * l + 1] = fa;
             if (beta > 0.f) {
-                ifc[2 * l] = fl;
-                ifc[2 * l + 1] = fa;
                 stcg4(&A.fc[2 * b], fl);
                 stcg4(&A.fc[2 * b + 1], fa);
             }
@@ -1103,10 +1124,12 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         // the accumulators come back
         if (nsplit) {
             if (s_nb > 0) fold_part();
-        } else if (s_ng > 0 || mom > 0.f) {
+            if (mom > 0.f && it < itmax) part_momentum(beta, false);
+        } else if (mom > 0.f && it < itmax) {
+            part_momentum(beta, true);  // reads the accumulators back as load_part does
+        } else if (s_ng > 0) {
             load_part(false);
         }
-        if (mom > 0.f && it < itmax) part_momentum(beta);
         __syncthreads();
     }
     // The global accumulators are current here (read back after the last
