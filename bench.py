@@ -421,6 +421,8 @@ def run_gbode(args, ws, rank, local):
         e2e_s = dist_max(time.perf_counter() - t0, ws, dev)
         e2e = {"value": dist_sum(sc.nb * n_ok, ws, dev) / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
+    # the same steps without momentum between sweeps
+    no_mom = no_momentum_leg(args, w, L, stream, flush, sc.nb, ws, dev) if args.momentum > 0 else None
     # learned warm start: the same settled state, the same timed loop
     learned = None
     if not args.no_learned:
@@ -484,6 +486,7 @@ def run_gbode(args, ws, rank, local):
         "gpu_launches": launches,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "without_momentum": no_mom,
         "learned": learned,
         "batched": batched,
     }
@@ -722,6 +725,25 @@ def learned_leg(args, w, L, stream, flush, plain, nb, ws, dev):
             "start_residual_mlp": float(np.median(r_mlp)), "start_residual_plain": float(np.median(r_plain)),
             "weights": os.path.relpath(path, ROOT),
             "note": "the network's start is used only when its residual beats the previous-step start's"}
+
+
+def no_momentum_leg(args, w, L, stream, flush, nb, ws, dev):
+    """The pile's timed steps again without momentum between sweeps (the
+    same settings otherwise): W untimed steps, the snapshot of the plain leg's
+    start restored, the same timed loop and counting rules."""
+    restore_snapshot(L, w)
+    L.gbodeWorldSetSweepMomentum(w.w, 0.0)
+    for _ in range(args.warmup):
+        w.step_fused()
+    w.sync()
+    restore_snapshot(L, w)
+    T = timed_steps(w, stream, flush, args.steps)
+    L.gbodeWorldSetSweepMomentum(w.w, args.momentum)
+    total_ms_max = dist_max(sum(T["step_ms"]), ws, dev)
+    ok = sum(1 for r in T["resid"] if r <= args.target)
+    return {"value": dist_sum(nb * ok, ws, dev) / (total_ms_max / 1e3), "unit": "body-steps/s",
+            "ms_per_step": total_ms_max / args.steps, "sweeps_per_step": float(np.mean(T["sweeps"])),
+            "steps_at_target": ok}
 
 
 def cpu_baseline(sc, w, args, threads):
