@@ -603,7 +603,9 @@ struct SlabArgs {
     unsigned *xprog;       // [blocks]: steps each block has finished
     // split classes (the cross phase's steps are the classes: k_split_*)
     int split;             // classes asked for (the solve uses dc->split_k: 0 exact colours)
-    long long *dacc;       // [bodies * split * 6]: class accumulators (zero between sweeps)
+    int dstride;           // classes a body's slots hold in dacc (split, or 1 without split classes)
+    long long *dacc;       // [bodies * dstride * 6]: class accumulators (zero between sweeps); class 0 also
+                           // re-forms the accumulators from the multipliers
     const int *smask;      // [bodies]: the classes whose groups share the body (bit c)
 };
 
@@ -700,23 +702,24 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
     float *slots = dc->racc;
     // fc = M^-1 J^T lambda over every group (cross colours, then interior colours), from global lambda
     auto form_fc = [&](bool zero) -> bool {
-        if (nsplit) {
-            // a split class's groups may share a body: every group's share
-            // goes into class 0's integer accumulators (any order gives the
-            // same sums), which then replace (or are added to) fc; the class
-            // accumulators are zero here (folded before every check)
+        if (S.dacc) {
+            // every group's share goes into its bodies' class-0 integer
+            // accumulators (2^-32 units: any order gives the same sums, so no
+            // barrier per colour, and a split class's groups may share a
+            // body), which then replace (or are added to) fc; the slots are
+            // zero here (folded before every check, cleared after each use)
             for (int cc = 0; cc < ncol + nicol; cc++) {
                 const int c = cc < ncol ? cc : 64 + (cc - ncol);
                 for (int k = tid; k < s_ccount[c]; k += nth)
-                    apply_desc_fix(A, __ldg(&A.desc[s_cstart[c] + k]), S.dacc, S.split);
+                    apply_desc_fix(A, __ldg(&A.desc[s_cstart[c] + k]), S.dacc, S.dstride);
             }
             if (!grid_sync(&dc->gsync, &dc->err, gen)) return false;
             for (int b = tid; b < A.nb; b += nth) {
                 float4 fl = make_float4(0.f, 0.f, 0.f, 0.f), fa = fl;
                 if (!zero) { fl = ldcg4(&A.fc[2 * b]); fa = ldcg4(&A.fc[2 * b + 1]); }
                 float4 gl = make_float4(0.f, 0.f, 0.f, 0.f), ga = gl;
-                split_sum(S.dacc, S.split, b, 1, gl, ga);  // the class-0 slot
-                longlong2 *p = (longlong2 *)split_slot(S.dacc, S.split, b, 0);
+                split_sum(S.dacc, S.dstride, b, 1, gl, ga);  // the class-0 slot
+                longlong2 *p = (longlong2 *)split_slot(S.dacc, S.dstride, b, 0);
                 const longlong2 zz = make_longlong2(0, 0);
                 __stcg(p, zz); __stcg(p + 1, zz); __stcg(p + 2, zz);
                 fl.x += gl.x; fl.y += gl.y; fl.z += gl.z;

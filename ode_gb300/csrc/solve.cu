@@ -2615,8 +2615,8 @@ static bool ensure_coloured(Workspace &ws, int nb, const ColouredPlan &c) {
            ws.x_fill.ensure((size_t)64 * c.pgs_blocks * 4) && ws.x_accn.ensure(nbb * 4) &&
            ws.x_acc.ensure(nbb * GB_XACC * 4) && ws.x_adj.ensure((size_t)c.pgs_blocks * GB_XADJ_WORDS * 4) &&
            ws.x_prog.ensure((size_t)c.pgs_blocks * 4) &&
-           (!c.split || (ws.x_nsplit.ensure((size_t)c.split * nbb * 4) && ws.x_dacc.ensure((size_t)c.split * nbb * 48) &&
-                         ws.x_smask.ensure(nbb * 4)));
+           ws.x_dacc.ensure((size_t)(c.split > 0 ? c.split : 1) * nbb * 48) &&
+           (!c.split || (ws.x_nsplit.ensure((size_t)c.split * nbb * 4) && ws.x_smask.ensure(nbb * 4)));
 }
 
 // Every device buffer a step writes, allocated before its first kernel: an
@@ -2920,8 +2920,10 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             cudaMemsetAsync(ws.x_prog.p, 0, (size_t)pgs_blocks * 4, s);
             count_launch();
         }
-        if (nsplit) cudaMemsetAsync(ws.x_dacc.p, 0, (size_t)nsplit * nbb * 48, s);
     }
+    // the two-level sweep re-forms the accumulators in fixed-point integer
+    // slots (one per body and class; class 0 without split classes)
+    if (slab) cudaMemsetAsync(ws.x_dacc.p, 0, (size_t)(nsplit > 0 ? nsplit : 1) * (nb > 0 ? nb : 1) * 48, s);
     // solve
     cudaMemsetAsync(&ws.dc->gsync, 0, sizeof(GridSync), s);
     if (g_test.barrier) {
@@ -2993,6 +2995,7 @@ bool launch_quickstep(Workspace &ws, int nb, int, const SolverParams &P, cudaStr
             SA.xadj = ws.x_adj.as<unsigned>();
             SA.xprog = ws.x_prog.as<unsigned>();
             SA.split = nsplit;
+            SA.dstride = nsplit > 0 ? nsplit : 1;
             SA.dacc = ws.x_dacc.as<long long>();
             SA.smask = ws.x_smask.as<int>();
             void *args[] = {(void *)&SA};

@@ -64,7 +64,7 @@ def test_momentum_on_a_pile(gblib, two_level, classes, beta):
         st = [w.stats() for w in worlds]
         for s in st:
             assert s.residual <= 1e-4, (step, s.residual, s.iterations)
-        assert st[0].momentum == 0.0 and 0.0 <= st[1].momentum <= beta
+        assert st[0].momentum == 0.0 and 0.0 <= st[1].momentum <= np.float32(beta)
         assert len({(s.iterations, s.rows, s.momentum) for s in st[1:]}) == 1, step
         a, b, c = (w.state() for w in worlds[1:])
         assert np.array_equal(a, b) and np.array_equal(a, c), step
