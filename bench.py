@@ -421,12 +421,19 @@ def run_gbode(args, ws, rank, local):
         e2e_s = dist_max(time.perf_counter() - t0, ws, dev)
         e2e = {"value": dist_sum(sc.nb * n_ok, ws, dev) / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
-    # the same steps without momentum between sweeps
-    no_mom = no_momentum_leg(args, w, L, stream, flush, sc.nb, ws, dev) if args.momentum > 0 else None
+    # the same steps without momentum between sweeps, and with the library's
+    # defaults (one-level sweep, no momentum): the plain drop-in at the target
+    no_mom = rerun_leg(args, w, L, stream, flush, sc.nb, ws, dev, args.two_level, 0.0) if args.momentum > 0 else None
+    dropin = rerun_leg(args, w, L, stream, flush, sc.nb, ws, dev, 0, 0.0)
+    dropin["settings"] = ("the library's default sweep (one-level coloured, no two-level sweep, no momentum) at the "
+                          "residual target, with the other legs' previous-step warm start, W and check schedule")
     # learned warm start: the same settled state, the same timed loop
     learned = None
     if not args.no_learned:
         learned = learned_leg(args, w, L, stream, flush, T, sc.nb, ws, dev)
+        if "value" in learned and dropin["value"] > 0:
+            # the learned form against the plain drop-in at the same residual
+            learned["vs_dropin_defaults"] = learned["value"] / dropin["value"]
     # batched independent worlds: capsule chains with hinge/ball joints
     batched = None
     if not args.no_batched and ws == 1:
@@ -487,6 +494,7 @@ def run_gbode(args, ws, rank, local):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "without_momentum": no_mom,
+        "dropin_defaults": dropin,
         "learned": learned,
         "batched": batched,
     }
@@ -727,17 +735,21 @@ def learned_leg(args, w, L, stream, flush, plain, nb, ws, dev):
             "note": "the network's start is used only when its residual beats the previous-step start's"}
 
 
-def no_momentum_leg(args, w, L, stream, flush, nb, ws, dev):
-    """The pile's timed steps again without momentum between sweeps (the
-    same settings otherwise): W untimed steps, the snapshot of the plain leg's
-    start restored, the same timed loop and counting rules."""
+def rerun_leg(args, w, L, stream, flush, nb, ws, dev, two_level, momentum):
+    """The pile's timed steps again with other solver settings (the two-level
+    sweep's interior phases, momentum between sweeps; everything else as the
+    plain leg): W untimed steps, the snapshot of the plain leg's start
+    restored, the same timed loop and counting rules; the plain leg's
+    settings are put back afterwards."""
+    L.gbodeWorldSetTwoLevelSweep(w.w, two_level)
+    L.gbodeWorldSetSweepMomentum(w.w, momentum)
     restore_snapshot(L, w)
-    L.gbodeWorldSetSweepMomentum(w.w, 0.0)
     for _ in range(args.warmup):
         w.step_fused()
     w.sync()
     restore_snapshot(L, w)
     T = timed_steps(w, stream, flush, args.steps)
+    L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
     L.gbodeWorldSetSweepMomentum(w.w, args.momentum)
     total_ms_max = dist_max(sum(T["step_ms"]), ws, dev)
     ok = sum(1 for r in T["resid"] if r <= args.target)
