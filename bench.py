@@ -9,16 +9,22 @@ grid into an open box of 5 static planes; dt 1/120, mu 0.6, dContactApprox1,
 configured 30 sweeps per step (untimed), then W warm-up and K timed steps run.
 
 A step is the fused path: gbodeSpaceCollideContacts (broad phase, narrow
-phase, contact joints on the device) + dWorldQuickStep with the coloured PGS,
-warm-started from the previous step's multipliers (contact cache keyed by geom
-pair and slot), W = 1.0, iterating until the natural-map LCP residual
-(relative to max(1, max|lambda|)) is <= 1e-4, checked every 5 sweeps, or 3000
-sweeps.  `value` counts only
+phase, contact joints on the device) + dWorldQuickStep with the coloured PGS
+(two-level sweep: column interiors in shared memory, crossing manifolds in
+global colours; momentum 0.8 between sweeps), warm-started from the previous
+step's multipliers (contact cache keyed by geom pair and slot), W = 1.0,
+iterating until the natural-map LCP residual (relative to max(1,
+max|lambda|)) is <= 1e-4 -- checks at least 5 sweeps apart, at half the
+predicted distance to the target -- or 3000 sweeps.  `value` counts only
 steps that reached the target.  Timing: CUDA events on the world's stream
 around each step, an L2 flush (256 MB write) before every timed step, outside
 the events.  `e2e` runs the same steps through the C ABI with host buffers:
 the full body state is set from host memory before and read back after every
-step, wall-clock timed.
+step, wall-clock timed.  The line also carries the same steps rerun without
+momentum (`without_momentum`) and with the library's default sweep
+(`dropin_defaults`), the learned warm start on them (`learned`), the batched
+capsule-chain and vehicle worlds (`batched`), the CPU baseline, the roofline
+of the sweep kernel and the SM clocks sampled during the timed steps.
 
 --impl reference times the reference algorithm on the host CPU (the oracle
 port of ODE's dSpaceCollide + dWorldQuickStep: random row reordering every 8
