@@ -960,9 +960,8 @@ __global__ void __launch_bounds__(T, 1) k_pgs_slab(SlabArgs S) {
         fetch(step_after(s0));
     }
     // momentum: the part's interior multipliers and listed bodies after a sweep
-    // (interior groups are triplet manifolds: at most 12 rows; the previous
-    // results of a group are loaded together)
-    // (a thread's groups two at a time, their loads issued together)
+    // (interior groups are triplet manifolds, at most 12 rows; a thread takes
+    // its groups two at a time and issues their previous results' loads together)
     auto interior_momentum = [&](float beta) {
         for (int i = threadIdx.x; i < s_ng; i += 2 * blockDim.x) {
             const int i2 = i + blockDim.x;

@@ -1259,8 +1259,8 @@ __device__ __forceinline__ void relax_row_local(const Rows &Rw, int r, float &la
 // check whose residual rose halves beta for the rest of the solve, and below
 // an eighth of the value set the sweeps go on without momentum (letting beta
 // grow back after a falling check let cyclic states recur).  A row's
-// multiplier is moved on by the thread that relaxed it, right after it stores
-// the result; a body's accumulators at the end of the sweep.
+// multiplier is moved on by the thread that relaxed it, when it stores the
+// result; a body's accumulators at the end of the sweep.
 __device__ __forceinline__ float mom_halved(float mom, float set) { return 0.5f * mom < 0.125f * set ? 0.f : 0.5f * mom; }
 __device__ __forceinline__ void store_lambda(const PgsArgs &A, int r, float out, float beta) {
     if (A.lprev) {
@@ -1352,7 +1352,7 @@ __device__ __forceinline__ void relax_desc(const PgsArgs &A, int4 d, float beta 
 
 // a staged slot's relaxed multipliers out to global memory; with momentum
 // `prev` holds the slot's previous-sweep results (staged beside the
-// multipliers by the one-level sweep, loaded after the relaxation by the
+// multipliers by the one-level sweep, loaded before the relaxation by the
 // two-level sweep)
 __device__ __forceinline__ void store_staged(const PgsArgs &A, int x, const float (&lout)[GB_STAGED_ROWS], int n,
                                              float beta, const float (&prev)[GB_STAGED_ROWS]) {
