@@ -80,7 +80,8 @@ void Workspace::release() {
                    &w_keys_prev, &w_lambda_prev, &res_f, &res_v, &scan_tmp, &s_bw, &s_part, &s_blocal, &s_pbcount,
                    &s_pbody, &s_prow, &s_pgrp, &s_gpart, &s_gdesc, &s_pccount, &s_pcstart, &s_pcfill, &s_ilist,
                    &s_irown, &s_irowoff, &s_idesc, &s_ipack, &s_hist, &s_binpart, &n_perm, &n_key, &x_cnt,
-                   &x_start, &x_fill, &x_accn, &x_acc, &x_adj, &x_prog, &x_nsplit, &x_dacc, &x_smask};
+                   &x_start, &x_fill, &x_accn, &x_acc, &x_adj, &x_prog, &x_nsplit, &x_dacc, &x_smask, &m_lprev,
+                   &b_fcprev, &p_cache};
     for (DBuf *b : all) b->release();
     if (dc) cudaFree(dc);
     if (hc) cudaFreeHost(hc);

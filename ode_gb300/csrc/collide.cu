@@ -180,17 +180,27 @@ __device__ __forceinline__ bool aabb_pair_ok(const Geoms &G, int a, int b) {
     return true;
 }
 
-// pass 0 counts, pass 1 writes (then sorts each geom's partners ascending)
+// pass 0 counts (and keeps each geom's first GB_BP_CACHE partners, in the
+// order found), pass 1 writes: a geom whose partners all fit the cache copies
+// them, the others search again; then each geom's partners are sorted
+// ascending.  Either way the pairs and their order are the same.
+#define GB_BP_CACHE 8
 template <int PASS>
 __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mask, const int *start, const int *count,
                            const int *members, const int *big_list, int *pcount, const int *pstart, int2 *pairs,
-                           int pair_cap, DevCounters *dc, int exact) {
+                           int pair_cap, DevCounters *dc, int exact, int *cache) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= G.n) return;
     int la = G.level[a];
     int n = 0;
     int base = PASS ? pstart[a] : 0;
-    if (la != BIG_LEVEL) {
+    const bool cached = PASS && pcount[a] <= GB_BP_CACHE;
+    if (cached) {
+        // partners copied from pass 0's cache (no search)
+        n = pcount[a];
+        for (int i = 0; i < n; i++)
+            if (base + i < pair_cap) pairs[base + i] = make_int2(a, cache[(size_t)a * GB_BP_CACHE + i]);
+    } else if (la != BIG_LEVEL) {
         int maxlevel = dc->maxlevel;
         int4 lo = G.dblo[a], hi = G.dbhi[a];
         for (int L = la; L <= maxlevel; L++) {
@@ -228,6 +238,8 @@ __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mas
                             if (PASS) {
                                 int idx = base + n;
                                 if (idx < pair_cap) pairs[idx] = make_int2(a, b);
+                            } else if (n < GB_BP_CACHE) {
+                                cache[(size_t)a * GB_BP_CACHE + n] = b;
                             }
                             n++;
                         }
@@ -240,6 +252,8 @@ __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mas
             if (PASS) {
                 int idx = base + n;
                 if (idx < pair_cap) pairs[idx] = make_int2(a, b);
+            } else if (n < GB_BP_CACHE) {
+                cache[(size_t)a * GB_BP_CACHE + n] = b;
             }
             n++;
         }
@@ -252,6 +266,8 @@ __global__ void k_bp_pairs(Geoms G, const unsigned long long *keys, unsigned mas
             if (PASS) {
                 int idx = base + n;
                 if (idx < pair_cap) pairs[idx] = make_int2(a, b);
+            } else if (n < GB_BP_CACHE) {
+                cache[(size_t)a * GB_BP_CACHE + n] = b;
             }
             n++;
         }
@@ -487,7 +503,7 @@ bool launch_broadphase(Workspace &ws, int ng, int exact, cudaStream_t s) {
     size_t nge = ng > 0 ? ng : 1;
     if (!(ws.h_keys.ensure(tsz * 8) && ws.h_count.ensure(tsz * 4) && ws.h_start.ensure(tsz * 4) &&
           ws.h_fill.ensure(tsz * 4) && ws.h_members.ensure(nge * 8 * 4) && ws.h_entry.ensure(nge * 8 * 4) &&
-          ws.p_count.ensure(nge * 4) && ws.p_start.ensure(nge * 4)))
+          ws.p_count.ensure(nge * 4) && ws.p_start.ensure(nge * 4) && ws.p_cache.ensure(nge * GB_BP_CACHE * 4)))
         return false;
     if (ws.pair_cap < 16 * (int)nge) {
         int cap = 16 * (int)nge;
@@ -505,12 +521,13 @@ bool launch_broadphase(Workspace &ws, int ng, int exact, cudaStream_t s) {
                                                     ws.h_members.as<int>());
     k_bp_pairs<0><<<grid_for(ng, 128), 128, 0, s>>>(G, ws.h_keys.as<unsigned long long>(), mask, ws.h_start.as<int>(),
                                                     ws.h_count.as<int>(), ws.h_members.as<int>(), ws.g_big.as<int>(),
-                                                    ws.p_count.as<int>(), nullptr, nullptr, 0, ws.dc, exact);
+                                                    ws.p_count.as<int>(), nullptr, nullptr, 0, ws.dc, exact,
+                                                    ws.p_cache.as<int>());
     scan_exclusive(ws.p_count.as<int>(), ws.p_start.as<int>(), nullptr, ng, &ws.dc->npairs, ws, s);
     k_bp_pairs<1><<<grid_for(ng, 128), 128, 0, s>>>(G, ws.h_keys.as<unsigned long long>(), mask, ws.h_start.as<int>(),
                                                     ws.h_count.as<int>(), ws.h_members.as<int>(), ws.g_big.as<int>(),
-                                                    nullptr, ws.p_start.as<int>(), ws.pairs.as<int2>(), ws.pair_cap, ws.dc,
-                                                    exact);
+                                                    ws.p_count.as<int>(), ws.p_start.as<int>(), ws.pairs.as<int2>(),
+                                                    ws.pair_cap, ws.dc, exact, ws.p_cache.as<int>());
     k_bp_finish<<<1, 1, 0, s>>>(ws.dc, ws.pair_cap);
     count_launch(5);
     return cudaGetLastError() == cudaSuccess;

@@ -113,6 +113,7 @@ struct Workspace {
     DBuf g_cls, g_body, g_dims, g_spos, g_sR, g_pos, g_R, g_amin, g_amax, g_level, g_dblo, g_dbhi, g_big;
     // broad phase
     DBuf h_keys, h_count, h_start, h_fill, h_members, h_entry, p_count, p_start, pairs;
+    DBuf p_cache;  // broad phase: each geom's first partners, kept by the counting pass
     // narrow phase
     DBuf c_slots, c_count, c_start, contacts, surfaces, c_mcount, c_rstart, c_code;
     DBuf n_perm, n_key;  // narrow phase: pairs grouped by collider class, counts and fills per class
