@@ -57,11 +57,11 @@ B_ROW_MOM = 8      # momentum between sweeps: a row's previous result read and w
 B_BODY_MOM = 128   # momentum between sweeps: a body's accumulators and their previous values, read and written
 # DRAM bytes (read + write) per launch of the sweep kernel on the settled 32,768-body pile,
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches):
-# k_pgs_slab (two-level sweep, exact crossing colours, momentum 0.8, kernel of commit 8963173):
-# 78.7 and 77.1 MB; k_pgs (one-level, no momentum): 240.4 and 204.2 MB.  The rows stay in L2 /
+# k_pgs_slab (two-level sweep, exact crossing colours, momentum 0.8, kernel of commit 4fcd219):
+# 80.0 and 79.0 MB; k_pgs (one-level, no momentum): 240.4 and 204.2 MB.  The rows stay in L2 /
 # shared memory across sweeps.
-PGS_TRAFFIC = {"gb::k_pgs_slab": 7.791e7, "gb::k_pgs": 2.223e8}
-PGS_TRAFFIC_SOURCE = {"gb::k_pgs_slab": "kernel of commit 8963173, momentum 0.8, exact crossing colours",
+PGS_TRAFFIC = {"gb::k_pgs_slab": 7.953e7, "gb::k_pgs": 2.223e8}
+PGS_TRAFFIC_SOURCE = {"gb::k_pgs_slab": "kernel of commit 4fcd219, momentum 0.8, exact crossing colours",
                       "gb::k_pgs": "kernel of commit 53e9ef8, one-level sweep without momentum"}
 
 
