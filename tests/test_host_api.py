@@ -396,3 +396,14 @@ def test_body_quaternion_is_normalised(L):
     R = np.array(L.dBodyGetRotation(b)[:12]).reshape(3, 4)[:, :3]
     assert np.allclose(R, np.diag([-1.0, -1.0, 1.0]), atol=1e-7)
     L.dWorldDestroy(w)
+
+
+def test_sweep_momentum_setting(L):
+    """gbodeWorldSetSweepMomentum: off by default, negative values read 0,
+    values above 0.95 are clamped to 0.95; the setting needs no device."""
+    w = L.dWorldCreate()
+    assert L.gbodeWorldGetSweepMomentum(w) == 0.0
+    for value, expect in ((0.8, 0.8), (-1.0, 0.0), (2.0, 0.95), (0.0, 0.0)):
+        L.gbodeWorldSetSweepMomentum(w, value)
+        assert L.gbodeWorldGetSweepMomentum(w) == pytest.approx(expect)
+    L.dWorldDestroy(w)
