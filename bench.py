@@ -429,15 +429,22 @@ def run_gbode(args, ws, rank, local):
                "d2h_bytes_per_step": d2h}
     # the same steps without momentum between sweeps, and with the library's
     # defaults (one-level sweep, no momentum): the plain drop-in at the target
-    no_mom = rerun_leg(args, w, L, stream, flush, sc.nb, ws, dev, args.two_level, 0.0) if args.momentum > 0 else None
-    dropin = rerun_leg(args, w, L, stream, flush, sc.nb, ws, dev, 0, 0.0)
+    def guarded(two_level, momentum):
+        try:
+            return rerun_leg(args, w, L, stream, flush, sc.nb, ws, dev, two_level, momentum)
+        except RuntimeError as e:  # a failed step: the leg is reported, the bench line still printed
+            L.gbodeWorldSetTwoLevelSweep(w.w, args.two_level)
+            L.gbodeWorldSetSweepMomentum(w.w, args.momentum)
+            return {"unavailable": str(e)}
+    no_mom = guarded(args.two_level, 0.0) if args.momentum > 0 else None
+    dropin = guarded(0, 0.0)
     dropin["settings"] = ("the library's default sweep (one-level coloured, no two-level sweep, no momentum) at the "
                           "residual target, with the other legs' previous-step warm start, W and check schedule")
     # learned warm start: the same settled state, the same timed loop
     learned = None
     if not args.no_learned:
         learned = learned_leg(args, w, L, stream, flush, T, sc.nb, ws, dev)
-        if "value" in learned and dropin["value"] > 0:
+        if "value" in learned and dropin.get("value", 0) > 0:
             # the learned form against the plain drop-in at the same residual
             learned["vs_dropin_defaults"] = learned["value"] / dropin["value"]
     # batched independent worlds: capsule chains with hinge/ball joints
